@@ -1,0 +1,172 @@
+/*
+ * nebula.h — C ABI of libnebula.so, the GB300 (sm_103a) implementation of the
+ * NebulaViewer simulation step: isothermal-Euler MUSCL + HLL/Rusanov RK2 hydro with the
+ * ionized-fraction sound-speed mix, the ray-cast Stromgren ionization front, the
+ * dust-attenuated FUV field and the wind / jet sources.
+ *
+ * The reference exposes this path as a Python class, `Sim` (sim.py:543-1222), whose
+ * methods launch NVIDIA-Warp kernels; it has no FFI of its own.  Each entry point below
+ * names the reference method or kernel it replaces.  The Python drop-in
+ * (nebulaviewer_gb300.Sim) binds them with ctypes.
+ *
+ * Conventions
+ *   - Every call returns 0 (NB_OK) or a negative NB_ERR_* code and never aborts or traps;
+ *     nb_last_error() describes the last failure of a handle (thread-local text for
+ *     calls made without a handle).
+ *   - Field buffers are CALLER-OWNED device memory (float32, C-order [i][j][k], k
+ *     fastest, shape (nx, ny, nz)); the library owns its scratch (ray-front tables, the
+ *     FUV attenuation grid, tensor maps, the per-instance control block) and its CUDA
+ *     graphs.  Device pointers must be 16-byte aligned and nz a multiple of 4 (the
+ *     reference's grid_shape rounds every axis to a multiple of 8).
+ *   - A handle is used from one host thread at a time; work is enqueued on the stream
+ *     given to nb_create (0 = the legacy default stream) and is asynchronous unless
+ *     the call says otherwise.
+ *   - The simulation clock (t, dt, it) lives in device memory: nothing in a step waits
+ *     for the host, so steps can be captured and replayed as CUDA graphs.
+ */
+#ifndef NEBULA_GB300_H
+#define NEBULA_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define NB_ABI_VERSION 1
+
+enum {
+    NB_OK = 0,
+    NB_ERR_ARG = -1,        /* bad argument (null pointer, size, alignment) */
+    NB_ERR_CUDA = -2,       /* a CUDA runtime call failed */
+    NB_ERR_STATE = -3,      /* call not valid in the handle's current state */
+    NB_ERR_LIMIT = -4,      /* a stated maximum was exceeded */
+    NB_ERR_TIMEOUT = -5,    /* a bounded device-side wait gave up (see nb_device_status) */
+    NB_ERR_NOMEM = -6       /* device allocation refused */
+};
+
+enum { NB_SOLVER_RUSANOV = 0, NB_SOLVER_HLL = 1 };
+enum { NB_LIM_MINMOD = 0, NB_LIM_VANLEER = 1, NB_LIM_MC = 2 };
+enum { NB_STAR_MAIN = 0, NB_STAR_ABS = 1 };                   /* sim.py:652 star kinds */
+enum { NB_JET_JET = 0, NB_JET_PROTO = 1, NB_JET_NONE = 2 };   /* sim.py:653 jet kinds */
+
+typedef struct nb_instance* nb_handle;
+
+/* Fields of one simulation instance (all caller-owned device memory, nx*ny*nz cells).
+ * The 40 B/cell layout of sim.py:718-735: rho, mx, my, mz, xi (float32), stage
+ * (4 float32 planes: the RK2 stage between the two hydro kernels, scratch between steps),
+ * dfront and g0 (float16, or float32 when fields_fp32 != 0). */
+typedef struct nb_fields {
+    float* rho;
+    float* mx;
+    float* my;
+    float* mz;
+    float* xi;
+    float* stage;           /* 4 * nx*ny*nz floats */
+    void* dfront;           /* __half, or float when fields_fp32 */
+    void* g0;               /* __half, or float when fields_fp32 */
+} nb_fields;
+
+/* Static description of an instance: the values sim.py:Sim.reset computes (sim.py:591-795). */
+typedef struct nb_desc {
+    int abi_version;        /* NB_ABI_VERSION */
+    int nx, ny, nz;
+    double dx;              /* cell size; cell centres at (i + 1/2) dx from the origin */
+    double cn2, ci2;        /* neutral / ionized sound speed squared (sim.py:740-741) */
+    double floor_rho;       /* density floor (nebula3d.py:591) */
+    double vmax;            /* velocity cap (sim.py:1020) */
+    double cfl;             /* CFL number (nebula3d.py:589) */
+    int solver;             /* NB_SOLVER_* (sim.py:1016) */
+    int limiter;            /* NB_LIM_* (sim.py:1022); Rusanov always uses minmod */
+    /* ionizing rays (sim.py:743-755) */
+    int nu, nphi;
+    double dr;              /* ray step: dx (fast) or dx/2 (bake) */
+    int nsteps;             /* int(diag / dr) + 1 */
+    double diag;            /* |L| + 0.6: the no-front radius rcap */
+    /* FUV grid (sim.py:756-757) */
+    int fnr, fnu, fnphi;
+    int fields_fp32;        /* P['fp32_fields']: dfront / g0 stored as float32 */
+    int max_stars;          /* star table capacity (sim.py:745 cap) */
+    nb_fields f;
+    void* stream;           /* cudaStream_t; 0 = legacy default stream */
+} nb_desc;
+
+/* Live parameters (sim.py:82-83 LIVE + the fixed jet geometry), read on device every step. */
+typedef struct nb_live {
+    double q_main, wind, jet, jet_proto, jet_pulse, jet_period, kappa_fuv, q_ramp;
+    double jet_angle_deg, jet_r;
+    double dt_cap;          /* Sim.dt_cap (bake.py:113); <= 0 means none */
+    int phase_main;         /* 1 once the main phase started (sim.py:786, 816) */
+} nb_live;
+
+/* One star: sim.py Sim.stars entry (x, y, z, qf, t_on) with its kind, and its jet axis. */
+typedef struct nb_star {
+    double x, y, z;
+    double qf;              /* Q / q_main for NB_STAR_MAIN, absolute Q for NB_STAR_ABS */
+    double t_on;
+    double ax, ay, az;      /* jet axis (sim.py:713, Sim.jets) */
+    int kind;               /* NB_STAR_* */
+    int jkind;              /* NB_JET_* */
+} nb_star;
+
+/* Simulation clock (device-resident; sim.py Sim.t / Sim.dt / Sim.it). */
+typedef struct nb_clock {
+    double t;
+    double dt;
+    int64_t it;
+} nb_clock;
+
+/* ---------------------------------------------------------------- lifetime */
+/* Replaces Sim.__init__/reset's buffer set-up (sim.py:718-759). */
+int nb_create(const nb_desc* desc, nb_handle* out);
+/* Releases library scratch and graphs (never the caller's fields). */
+void nb_destroy(nb_handle h);
+const char* nb_last_error(nb_handle h);
+int nb_device_status(nb_handle h, int* status);     /* bounded-wait failures seen on device */
+
+/* ---------------------------------------------------------------- configuration */
+/* Sim.P live parameters; replaces set_param's effect on the next step (sim.py:1154-1166). */
+int nb_set_live(nb_handle h, const nb_live* live);
+/* Star list; replaces replace_stars / the star part of reset (sim.py:1120-1133, 710-714).
+ * The per-step weights of _set_star_weights (sim.py:914-925) are computed on device. */
+int nb_set_stars(nb_handle h, const nb_star* stars, int n);
+/* Sim.t / dt / it, as written by set_state_meta (sim.py:1185-1211). */
+int nb_set_clock(nb_handle h, const nb_clock* c);
+int nb_get_clock(nb_handle h, nb_clock* c);          /* synchronizes the stream */
+
+/* ---------------------------------------------------------------- the step */
+/* k main-phase steps of Sim.step (sim.py:1141-1152 -> _main_step sim.py:1099-1114):
+ * ionize when it % ion_every == 0, dt from the CFL max speed on device, the two RK2
+ * hydro stages, t += dt.  Asynchronous. */
+int nb_step(nb_handle h, int k, int ion_every);
+/* Sim.ionize (sim.py:927-947): rays per active star, front apply, smoothing, fp16 dfront. */
+int nb_ionize(nb_handle h);
+/* Sim.fuv_field (sim.py:949-985): FUV rays per active star, G0 into g0. */
+int nb_fuv(nb_handle h);
+/* Marks the CFL max speed stale after the caller rewrote rho/m/xi (timeline restore). */
+int nb_invalidate(nb_handle h);
+
+/* ---------------------------------------------------------------- single kernels
+ * Parity and benchmarking entry points for one reference kernel launch each. */
+/* One RK2 stage: nebula3d.py:76-151 hydro_stage / sim.py:423-498 hydro_stage_hll, launched
+ * as in sim.py:1025/1028 (in -> out with out = a*U0 + b*(in + dt L(in))).  in/U0/out are
+ * 4-plane (rho, mx, my, mz) pointers; out may alias U0 (stage 2 in place).  dt and pulse
+ * are given explicitly; the star/jet weights are those of the handle's current clock. */
+int nb_hydro_stage(nb_handle h, const float* const in4[4], const float* const u0_4[4], float* const out4[4],
+                   float a, float b, float dt, float pulse);
+/* nebula3d.py:154-162 max_speed over the handle's current fields (synchronizes). */
+int nb_max_speed(nb_handle h, float* smax_out);
+/* nebula3d.py:247-270 cast_rays for one star into rfront_out (device, nu*nphi floats). */
+int nb_cast_rays(nb_handle h, const double star_xyz[3], double Q, float* rfront_out);
+/* nebula3d.py:320-352 cast_fuv for one star into att_out (device, fnr*fnu*fnphi floats,
+ * reference layout [b][iu][ip]). */
+int nb_cast_fuv(nb_handle h, const double star_xyz[3], float* att_out);
+
+/* ---------------------------------------------------------------- diagnostics */
+/* FP64 conservation totals: sum rho, sum mx, sum my, sum mz (times dx^3 = mass/momentum). */
+int nb_reduce_fp64(nb_handle h, double out[4]);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* NEBULA_GB300_H */

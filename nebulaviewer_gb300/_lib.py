@@ -1,0 +1,107 @@
+"""ctypes binding of libnebula.so (include/nebula.h).
+
+The library is built in-tree by `nebulaviewer_gb300.build.build()`; importing this module
+without it raises immediately: there is no CPU or PyTorch fallback for the simulation step.
+"""
+import ctypes as C
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libnebula.so")
+
+NB_ABI_VERSION = 1
+NB_OK = 0
+ERRORS = {-1: "NB_ERR_ARG", -2: "NB_ERR_CUDA", -3: "NB_ERR_STATE", -4: "NB_ERR_LIMIT", -5: "NB_ERR_TIMEOUT",
+          -6: "NB_ERR_NOMEM"}
+SOLVERS = {"rusanov": 0, "hll": 1}
+LIMITERS = {"minmod": 0, "vanleer": 1, "mc": 2}
+STAR_KINDS = {"main": 0, "abs": 1}
+JET_KINDS = {"jet": 0, "proto": 1, "none": 2}
+
+
+class NbFields(C.Structure):
+    _fields_ = [("rho", C.c_void_p), ("mx", C.c_void_p), ("my", C.c_void_p), ("mz", C.c_void_p),
+                ("xi", C.c_void_p), ("stage", C.c_void_p), ("dfront", C.c_void_p), ("g0", C.c_void_p)]
+
+
+class NbDesc(C.Structure):
+    _fields_ = [("abi_version", C.c_int), ("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int),
+                ("dx", C.c_double), ("cn2", C.c_double), ("ci2", C.c_double), ("floor_rho", C.c_double),
+                ("vmax", C.c_double), ("cfl", C.c_double), ("solver", C.c_int), ("limiter", C.c_int),
+                ("nu", C.c_int), ("nphi", C.c_int), ("dr", C.c_double), ("nsteps", C.c_int), ("diag", C.c_double),
+                ("fnr", C.c_int), ("fnu", C.c_int), ("fnphi", C.c_int), ("fields_fp32", C.c_int),
+                ("max_stars", C.c_int), ("f", NbFields), ("stream", C.c_void_p)]
+
+
+class NbLive(C.Structure):
+    _fields_ = [("q_main", C.c_double), ("wind", C.c_double), ("jet", C.c_double), ("jet_proto", C.c_double),
+                ("jet_pulse", C.c_double), ("jet_period", C.c_double), ("kappa_fuv", C.c_double),
+                ("q_ramp", C.c_double), ("jet_angle_deg", C.c_double), ("jet_r", C.c_double),
+                ("dt_cap", C.c_double), ("phase_main", C.c_int)]
+
+
+class NbStar(C.Structure):
+    _fields_ = [("x", C.c_double), ("y", C.c_double), ("z", C.c_double), ("qf", C.c_double), ("t_on", C.c_double),
+                ("ax", C.c_double), ("ay", C.c_double), ("az", C.c_double), ("kind", C.c_int), ("jkind", C.c_int)]
+
+
+class NbClock(C.Structure):
+    _fields_ = [("t", C.c_double), ("dt", C.c_double), ("it", C.c_int64)]
+
+
+# name -> (restype, argtypes): every symbol include/nebula.h declares
+_P = C.c_void_p
+_F4 = C.c_void_p * 4
+SIGNATURES = {
+    "nb_create": (C.c_int, [C.POINTER(NbDesc), C.POINTER(_P)]),
+    "nb_destroy": (None, [_P]),
+    "nb_last_error": (C.c_char_p, [_P]),
+    "nb_device_status": (C.c_int, [_P, C.POINTER(C.c_int)]),
+    "nb_set_live": (C.c_int, [_P, C.POINTER(NbLive)]),
+    "nb_set_stars": (C.c_int, [_P, C.POINTER(NbStar), C.c_int]),
+    "nb_set_clock": (C.c_int, [_P, C.POINTER(NbClock)]),
+    "nb_get_clock": (C.c_int, [_P, C.POINTER(NbClock)]),
+    "nb_step": (C.c_int, [_P, C.c_int, C.c_int]),
+    "nb_ionize": (C.c_int, [_P]),
+    "nb_fuv": (C.c_int, [_P]),
+    "nb_invalidate": (C.c_int, [_P]),
+    "nb_hydro_stage": (C.c_int, [_P, _F4, _F4, _F4, C.c_float, C.c_float, C.c_float, C.c_float]),
+    "nb_max_speed": (C.c_int, [_P, C.POINTER(C.c_float)]),
+    "nb_cast_rays": (C.c_int, [_P, C.c_double * 3, C.c_double, _P]),
+    "nb_cast_fuv": (C.c_int, [_P, C.c_double * 3, _P]),
+    "nb_reduce_fp64": (C.c_int, [_P, C.c_double * 4]),
+}
+
+_lib = None
+
+
+class NebulaError(RuntimeError):
+    pass
+
+
+def load(path=LIB_PATH):
+    """Load libnebula.so (once).  Raises if it is missing: build it first."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise NebulaError(f"{path} is missing: run nebulaviewer_gb300.build.build() (nvcc, sm_103a) first")
+    lib = C.CDLL(path)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def check(rc, handle=None, what=""):
+    if rc != NB_OK:
+        lib = load()
+        msg = lib.nb_last_error(handle).decode(errors="replace")
+        raise NebulaError(f"{what}: {ERRORS.get(rc, rc)}: {msg}")
+    return rc
+
+
+def f4(ptrs):
+    return _F4(*[C.c_void_p(int(p)) for p in ptrs])

@@ -1,0 +1,454 @@
+// The C ABI of include/nebula.h: instance set-up, the step sequencing of sim.py (_main_step,
+// ionize, fuv_field) over the device kernels, and single-kernel entry points for parity.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+
+#include "nb_internal.cuh"
+
+#define NB_EXPORT extern "C" __attribute__((visibility("default")))
+
+struct nb_instance {
+    nb_desc d{};
+    cudaStream_t stream = nullptr;
+    NbConst hc{};                       // host copy of the device constants
+    NbConst* c = nullptr;
+    NbState* st = nullptr;
+    NbStarDev* stars = nullptr;
+    NbStarW* sw = nullptr;
+    CUtensorMap* maps = nullptr;        // NB_NMAPS maps of the instance's planes
+    CUtensorMap* tmp_maps = nullptr;    // maps for nb_hydro_stage on foreign planes
+    float4* dirs = nullptr;             // ionizing-ray directions (nu * nphi)
+    float4* dirs_fuv = nullptr;         // FUV-ray directions (fnu * fnphi)
+    float* rfront = nullptr;            // [star][nu][nphi]
+    float* att = nullptr;               // [star][fnu][fnphi][fnr]
+    float* scratch3 = nullptr;          // 3 floats: a single star position for the one-star kernels
+    double* red = nullptr;              // FP64 reduction partials
+    int nstars = 0, star_alloc = 0;
+    long long host_it = 0;
+    int smax_valid = 0;
+    int chunk_i = 64, ray_group = 32, fuv_group = 32;
+    long long ncell = 0;
+    std::string err;
+};
+
+static thread_local std::string g_err;
+
+namespace {
+
+int fail(nb_instance* h, int code, const std::string& msg) {
+    if (h) h->err = msg; else g_err = msg;
+    return code;
+}
+int cuda_fail(nb_instance* h, cudaError_t e, const char* what) {
+    return fail(h, NB_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+#define CK(h, call)                                                          \
+    do {                                                                     \
+        cudaError_t e_ = (call);                                             \
+        if (e_ != cudaSuccess) return cuda_fail((h), e_, #call);             \
+    } while (0)
+
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no -lcuda needed)
+using EncodeFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                              const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                              CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+EncodeFn encode_fn() {
+    static EncodeFn fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<EncodeFn>(p);
+    });
+    return fn;
+}
+
+// A (nx, ny, nz) float32 plane, k fastest, read as (40 x (TJ+4) x 1) boxes.
+bool encode_plane(CUtensorMap* m, const float* ptr, int nx, int ny, int nz) {
+    EncodeFn fn = encode_fn();
+    if (!fn) return false;
+    const int tj = nb_hydro_tile_j();
+    cuuint64_t dims[3] = {(cuuint64_t)nz, (cuuint64_t)ny, (cuuint64_t)nx};
+    cuuint64_t strides[2] = {(cuuint64_t)nz * 4, (cuuint64_t)ny * nz * 4};
+    cuuint32_t box[3] = {40, (cuuint32_t)(tj + 4), 1};
+    cuuint32_t es[3] = {1, 1, 1};
+    return fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float*>(ptr), dims, strides, box, es,
+              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
+
+bool is_pow2(double x) {
+    int e;
+    return x > 0.0 && std::frexp(x, &e) == 0.5;
+}
+
+int upload_const(nb_instance* h) {
+    CK(h, cudaMemcpyAsync(h->c, &h->hc, sizeof(NbConst), cudaMemcpyHostToDevice, h->stream));
+    return NB_OK;
+}
+
+float* plane(nb_instance* h, int p) { return h->d.f.stage + (long long)p * h->ncell; }
+
+int launch_stage(nb_instance* h, const float* const in[4], const float* const u0[4], float* const out[4], int map_in,
+                 const CUtensorMap* maps, float a, float b, bool override_, float dt, float pulse, bool smax) {
+    HydroLaunch L{};
+    L.c = h->c;
+    L.st = h->st;
+    L.sw = h->sw;
+    L.maps = maps;
+    L.map_in = map_in;
+    for (int f = 0; f < 4; ++f) {
+        L.in[f] = in[f];
+        L.u0[f] = u0[f];
+        L.out[f] = out[f];
+    }
+    L.xi = h->d.f.xi;
+    L.a = a;
+    L.b = b;
+    L.use_override = override_ ? 1 : 0;
+    L.dt_override = dt;
+    L.pulse_override = pulse;
+    L.smax_bits = smax ? &h->st->smax_bits : nullptr;
+    L.status = &h->st->status;
+    const int tj = nb_hydro_tile_j();
+    L.tiles_k = (h->d.nz + 31) / 32;
+    L.tiles_j = (h->d.ny + tj - 1) / tj;
+    L.chunk_i = h->chunk_i < h->d.nx ? h->chunk_i : h->d.nx;
+    L.n_chunks = (h->d.nx + L.chunk_i - 1) / L.chunk_i;
+    L.nstars_host = h->nstars;
+    CK(h, nb_launch_hydro(L, h->d.solver, h->d.limiter, h->stream));
+    return NB_OK;
+}
+
+int do_ionize(nb_instance* h) {
+    const nb_fields& f = h->d.f;
+    CK(h, nb_launch_weights(h->c, h->st, h->stars, h->sw, h->nstars, h->stream));
+    if (h->nstars > 0)
+        CK(h, nb_launch_cast_rays(h->c, h->sw, h->dirs, f.rho, h->rfront, h->nstars, h->ray_group, nullptr, 0.0f,
+                                  h->stream, h->d.nu, h->d.nphi));
+    float* xi_raw = plane(h, 0);            // sim.py:928-941: xi_tmp lives in the stage block
+    CK(h, nb_launch_apply_front(h->c, h->sw, h->rfront, h->nstars, xi_raw, f.dfront, &h->st->smax_bits, h->stream,
+                                h->ncell, h->d.fields_fp32 ? 0 : 1));
+    CK(h, nb_launch_smooth(h->c, xi_raw, f.xi, f.rho, f.mx, f.my, f.mz, &h->st->smax_bits, h->stream, h->ncell));
+    h->smax_valid = 1;
+    return NB_OK;
+}
+
+int do_step(nb_instance* h, int ion_every) {
+    const nb_fields& f = h->d.f;
+    int rc;
+    if (ion_every > 0 && h->host_it % ion_every == 0) {           // sim.py:1102-1103
+        if ((rc = do_ionize(h)) != NB_OK) return rc;
+    } else if (!h->smax_valid) {
+        CK(h, nb_launch_max_speed(h->c, f.rho, f.mx, f.my, f.mz, f.xi, &h->st->smax_bits, h->ncell, h->stream));
+    }
+    // sim.py:1104-1108: star weights at t, dt from the max speed (dt_cap), pulse; t += dt
+    CK(h, nb_launch_ctrl(h->c, h->st, h->stars, h->sw, h->nstars, 1, h->stream));
+    const float* U[4] = {f.rho, f.mx, f.my, f.mz};
+    float* Uw[4] = {f.rho, f.mx, f.my, f.mz};
+    float* S[4] = {plane(h, 0), plane(h, 1), plane(h, 2), plane(h, 3)};
+    const float* Sc[4] = {S[0], S[1], S[2], S[3]};
+    // sim.py:1025: U -> U1 (a = 0, b = 1);  sim.py:1028: U1 -> U in place (a = b = 1/2) + max speed
+    if ((rc = launch_stage(h, U, U, S, NB_MAP_RHO, h->maps, 0.0f, 1.0f, false, 0.f, 0.f, false)) != NB_OK) return rc;
+    if ((rc = launch_stage(h, Sc, U, Uw, NB_MAP_S0, h->maps, 0.5f, 0.5f, false, 0.f, 0.f, true)) != NB_OK) return rc;
+    h->host_it += 1;
+    h->smax_valid = 1;
+    return NB_OK;
+}
+
+}  // namespace
+
+// ============================================================================ C ABI
+NB_EXPORT const char* nb_last_error(nb_handle h) { return h ? h->err.c_str() : g_err.c_str(); }
+
+NB_EXPORT int nb_create(const nb_desc* d, nb_handle* out) {
+    if (!d || !out) return fail(nullptr, NB_ERR_ARG, "null argument");
+    *out = nullptr;
+    if (d->abi_version != NB_ABI_VERSION) return fail(nullptr, NB_ERR_ARG, "abi_version mismatch");
+    if (d->nx < 1 || d->ny < 1 || d->nz < 4 || d->nz % 4 != 0)
+        return fail(nullptr, NB_ERR_ARG, "grid must be nx, ny >= 1 and nz a positive multiple of 4");
+    if (!(d->dx > 0.0) || d->nu < 1 || d->nphi < 1 || d->fnr < 1 || d->fnu < 1 || d->fnphi < 1 || d->nsteps < 1 ||
+        !(d->dr > 0.0))
+        return fail(nullptr, NB_ERR_ARG, "bad geometry / ray budget");
+    if (d->max_stars < 1 || d->max_stars > NB_MAX_STARS)
+        return fail(nullptr, NB_ERR_LIMIT, "max_stars must be in [1, 256]");
+    const nb_fields& f = d->f;
+    const void* ptrs[] = {f.rho, f.mx, f.my, f.mz, f.xi, f.stage, f.dfront, f.g0};
+    for (const void* p : ptrs)
+        if (!p || !aligned16(p)) return fail(nullptr, NB_ERR_ARG, "field pointers must be non-null and 16-byte aligned");
+    if (d->solver != NB_SOLVER_RUSANOV && d->solver != NB_SOLVER_HLL) return fail(nullptr, NB_ERR_ARG, "bad solver");
+    if (d->limiter < 0 || d->limiter > 2) return fail(nullptr, NB_ERR_ARG, "bad limiter");
+    if (!encode_fn()) return fail(nullptr, NB_ERR_CUDA, "cuTensorMapEncodeTiled unavailable");
+
+    nb_instance* h = new nb_instance();
+    h->d = *d;
+    h->stream = static_cast<cudaStream_t>(d->stream);
+    h->ncell = (long long)d->nx * d->ny * d->nz;
+    if (h->ncell * 4 > (1LL << 62)) { delete h; return fail(nullptr, NB_ERR_LIMIT, "grid too large"); }
+    NbConst& c = h->hc;
+    c.nx = d->nx; c.ny = d->ny; c.nz = d->nz; c.nstars = 0;
+    c.dx_pow2 = is_pow2(d->dx) ? 1 : 0;
+    c.solver = d->solver; c.limiter = d->limiter; c.fields_fp32 = d->fields_fp32;
+    c.dx = (float)d->dx;
+    c.inv_dx = (float)(1.0 / d->dx);
+    c.floor_ = (float)d->floor_rho;
+    c.cn2 = (float)d->cn2;
+    c.ci2 = (float)d->ci2;
+    c.vmax = (float)d->vmax;
+    c.width = (float)(1.2 * d->dx);                               // sim.py:939
+    c.bmax[0] = (float)(d->nx * d->dx);                           // sim.py:621, 750
+    c.bmax[1] = (float)(d->ny * d->dx);
+    c.bmax[2] = (float)(d->nz * d->dx);
+    c.diag_f = (float)d->diag;
+    c.dr_f = (float)d->dr;
+    c.binr_f = (float)(d->diag / d->fnr);                         // sim.py:958
+    c.nu = d->nu; c.nphi = d->nphi; c.nsteps = d->nsteps;
+    c.fnr = d->fnr; c.fnu = d->fnu; c.fnphi = d->fnphi;
+    c.dx_d = d->dx; c.cfl = d->cfl; c.diag_d = d->diag;
+    c.q_main = 1.0; c.jet_period = 1.0; c.phase_main = 1;
+    c.jet_cos = 1.0; c.jet_cos_f = 1.0f;
+
+    auto bail = [&](int rc) { nb_destroy(h); return rc; };
+    cudaError_t e;
+#define CKC(call)                                                          \
+    do {                                                                   \
+        e = (call);                                                        \
+        if (e != cudaSuccess) {                                            \
+            g_err = std::string(#call) + ": " + cudaGetErrorString(e);     \
+            return bail(e == cudaErrorMemoryAllocation ? NB_ERR_NOMEM : NB_ERR_CUDA); \
+        }                                                                  \
+    } while (0)
+    CKC(cudaMalloc(&h->c, sizeof(NbConst)));
+    CKC(cudaMalloc(&h->st, sizeof(NbState)));
+    CKC(cudaMalloc(&h->stars, sizeof(NbStarDev) * d->max_stars));
+    CKC(cudaMalloc(&h->sw, sizeof(NbStarW) * d->max_stars));
+    CKC(cudaMalloc(&h->maps, sizeof(CUtensorMap) * NB_NMAPS));
+    CKC(cudaMalloc(&h->tmp_maps, sizeof(CUtensorMap) * NB_NMAPS));
+    CKC(cudaMalloc(&h->dirs, sizeof(float4) * (size_t)d->nu * d->nphi));
+    CKC(cudaMalloc(&h->dirs_fuv, sizeof(float4) * (size_t)d->fnu * d->fnphi));
+    CKC(cudaMalloc(&h->scratch3, 4 * sizeof(float)));
+    CKC(cudaMalloc(&h->red, sizeof(double) * nb_reduce_scratch_doubles()));
+    CKC(cudaMemsetAsync(h->st, 0, sizeof(NbState), h->stream));
+    CKC(cudaMemsetAsync(h->sw, 0, sizeof(NbStarW) * d->max_stars, h->stream));
+    CUtensorMap hm[NB_NMAPS];
+    const float* planes[NB_NMAPS] = {f.rho, f.mx, f.my, f.mz, f.xi, f.stage, f.stage + h->ncell,
+                                     f.stage + 2 * h->ncell, f.stage + 3 * h->ncell};
+    for (int m = 0; m < NB_NMAPS; ++m)
+        if (!encode_plane(&hm[m], planes[m], d->nx, d->ny, d->nz)) {
+            g_err = "cuTensorMapEncodeTiled failed";
+            return bail(NB_ERR_CUDA);
+        }
+    CKC(cudaMemcpyAsync(h->maps, hm, sizeof(hm), cudaMemcpyHostToDevice, h->stream));
+    CKC(nb_launch_ray_dirs(d->nu, d->nphi, h->dirs, h->stream));
+    CKC(nb_launch_ray_dirs(d->fnu, d->fnphi, h->dirs_fuv, h->stream));
+    CKC(cudaMemcpyAsync(h->c, &h->hc, sizeof(NbConst), cudaMemcpyHostToDevice, h->stream));
+    CKC(cudaStreamSynchronize(h->stream));
+#undef CKC
+    *out = h;
+    return NB_OK;
+}
+
+NB_EXPORT void nb_destroy(nb_handle h) {
+    if (!h) return;
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    else cudaDeviceSynchronize();
+    void* ps[] = {h->c, h->st, h->stars, h->sw, h->maps, h->tmp_maps, h->dirs, h->dirs_fuv,
+                  h->rfront, h->att, h->scratch3, h->red};
+    for (void* p : ps)
+        if (p) cudaFree(p);
+    delete h;
+}
+
+NB_EXPORT int nb_set_live(nb_handle h, const nb_live* L) {
+    if (!h || !L) return fail(h, NB_ERR_ARG, "null argument");
+    NbConst& c = h->hc;
+    c.q_main = L->q_main;
+    c.wind = L->wind;
+    c.jet = L->jet;
+    c.jet_proto = L->jet_proto;
+    c.jet_pulse = L->jet_pulse;
+    c.jet_period = L->jet_period;
+    c.kappa_fuv = L->kappa_fuv;
+    c.q_ramp = L->q_ramp;
+    c.jet_r = L->jet_r;
+    c.jet_cos = std::cos(L->jet_angle_deg * (3.141592653589793 / 180.0));   // sim.py:1018 math.cos(math.radians(.))
+    c.dt_cap = L->dt_cap;
+    c.phase_main = L->phase_main;
+    c.wind_f = (float)L->wind;
+    c.jet_cos_f = (float)c.jet_cos;
+    c.jet_r_f = (float)L->jet_r;
+    c.kappa_f = (float)L->kappa_fuv;
+    return upload_const(h);
+}
+
+NB_EXPORT int nb_set_stars(nb_handle h, const nb_star* s, int n) {
+    if (!h || (n > 0 && !s)) return fail(h, NB_ERR_ARG, "null argument");
+    if (n < 0 || n > h->d.max_stars) return fail(h, NB_ERR_LIMIT, "more stars than max_stars");
+    if (n > h->star_alloc) {
+        CK(h, cudaStreamSynchronize(h->stream));
+        if (h->rfront) cudaFree(h->rfront);
+        if (h->att) cudaFree(h->att);
+        h->rfront = nullptr;
+        h->att = nullptr;
+        h->star_alloc = 0;
+        const size_t rf = sizeof(float) * (size_t)n * h->d.nu * h->d.nphi;
+        const size_t at = sizeof(float) * (size_t)n * h->d.fnr * h->d.fnu * h->d.fnphi;
+        if (cudaMalloc(&h->rfront, rf) != cudaSuccess || cudaMalloc(&h->att, at) != cudaSuccess) {
+            cudaGetLastError();
+            return fail(h, NB_ERR_NOMEM, "ray scratch allocation refused");
+        }
+        h->star_alloc = n;
+    }
+    NbStarDev tmp[NB_MAX_STARS];
+    for (int i = 0; i < n; ++i) {
+        tmp[i].x = s[i].x; tmp[i].y = s[i].y; tmp[i].z = s[i].z;
+        tmp[i].qf = s[i].qf; tmp[i].t_on = s[i].t_on;
+        tmp[i].ax = s[i].ax; tmp[i].ay = s[i].ay; tmp[i].az = s[i].az;
+        tmp[i].kind = s[i].kind; tmp[i].jkind = s[i].jkind;
+    }
+    if (n > 0) CK(h, cudaMemcpyAsync(h->stars, tmp, sizeof(NbStarDev) * n, cudaMemcpyHostToDevice, h->stream));
+    h->nstars = n;
+    h->hc.nstars = n;
+    return upload_const(h);
+}
+
+NB_EXPORT int nb_set_clock(nb_handle h, const nb_clock* c) {
+    if (!h || !c) return fail(h, NB_ERR_ARG, "null argument");
+    NbState s{};
+    CK(h, cudaMemcpyAsync(&s, h->st, sizeof(NbState), cudaMemcpyDeviceToHost, h->stream));
+    CK(h, cudaStreamSynchronize(h->stream));
+    s.t = c->t;
+    s.dt = c->dt;
+    s.it = c->it;
+    CK(h, cudaMemcpyAsync(h->st, &s, sizeof(NbState), cudaMemcpyHostToDevice, h->stream));
+    CK(h, cudaStreamSynchronize(h->stream));
+    h->host_it = c->it;
+    h->smax_valid = 0;
+    return NB_OK;
+}
+
+NB_EXPORT int nb_get_clock(nb_handle h, nb_clock* c) {
+    if (!h || !c) return fail(h, NB_ERR_ARG, "null argument");
+    NbState s{};
+    CK(h, cudaMemcpyAsync(&s, h->st, sizeof(NbState), cudaMemcpyDeviceToHost, h->stream));
+    CK(h, cudaStreamSynchronize(h->stream));
+    c->t = s.t;
+    c->dt = s.dt;
+    c->it = s.it;
+    return NB_OK;
+}
+
+NB_EXPORT int nb_device_status(nb_handle h, int* status) {
+    if (!h || !status) return fail(h, NB_ERR_ARG, "null argument");
+    NbState s{};
+    CK(h, cudaMemcpyAsync(&s, h->st, sizeof(NbState), cudaMemcpyDeviceToHost, h->stream));
+    CK(h, cudaStreamSynchronize(h->stream));
+    *status = (int)s.status;
+    return NB_OK;
+}
+
+NB_EXPORT int nb_invalidate(nb_handle h) {
+    if (!h) return fail(h, NB_ERR_ARG, "null handle");
+    h->smax_valid = 0;
+    return NB_OK;
+}
+
+NB_EXPORT int nb_step(nb_handle h, int k, int ion_every) {
+    if (!h) return fail(h, NB_ERR_ARG, "null handle");
+    if (k < 0 || ion_every < 1) return fail(h, NB_ERR_ARG, "k >= 0 and ion_every >= 1 required");
+    if (!h->hc.phase_main) return fail(h, NB_ERR_STATE, "the main phase has not started");
+    for (int s = 0; s < k; ++s) {
+        int rc = do_step(h, ion_every);
+        if (rc != NB_OK) return rc;
+    }
+    return NB_OK;
+}
+
+NB_EXPORT int nb_ionize(nb_handle h) {
+    if (!h) return fail(h, NB_ERR_ARG, "null handle");
+    return do_ionize(h);
+}
+
+NB_EXPORT int nb_fuv(nb_handle h) {
+    if (!h) return fail(h, NB_ERR_ARG, "null handle");
+    const size_t es = h->d.fields_fp32 ? 4 : 2;
+    if (!h->hc.phase_main) {                                         // sim.py:952-954
+        CK(h, cudaMemsetAsync(h->d.f.g0, 0, es * h->ncell, h->stream));
+        return NB_OK;
+    }
+    CK(h, nb_launch_weights(h->c, h->st, h->stars, h->sw, h->nstars, h->stream));
+    if (h->nstars > 0)
+        CK(h, nb_launch_cast_fuv(h->c, h->sw, h->dirs_fuv, h->d.f.rho, h->d.f.xi, h->att, h->nstars, h->fuv_group,
+                                 nullptr, 0, h->stream, h->d.fnu, h->d.fnphi));
+    CK(h, nb_launch_apply_fuv(h->c, h->sw, h->att, h->nstars, h->d.f.g0, h->stream, h->ncell,
+                              h->d.fields_fp32 ? 0 : 1));
+    return NB_OK;
+}
+
+NB_EXPORT int nb_hydro_stage(nb_handle h, const float* const in4[4], const float* const u0_4[4],
+                             float* const out4[4], float a, float b, float dt, float pulse) {
+    if (!h || !in4 || !u0_4 || !out4) return fail(h, NB_ERR_ARG, "null argument");
+    for (int f = 0; f < 4; ++f)
+        if (!in4[f] || !u0_4[f] || !out4[f] || !aligned16(in4[f]))
+            return fail(h, NB_ERR_ARG, "plane pointers must be non-null (inputs 16-byte aligned)");
+    CUtensorMap hm[NB_NMAPS];
+    for (int f = 0; f < 4; ++f)
+        if (!encode_plane(&hm[f], in4[f], h->d.nx, h->d.ny, h->d.nz)) return fail(h, NB_ERR_CUDA, "tensor map");
+    if (!encode_plane(&hm[NB_MAP_XI], h->d.f.xi, h->d.nx, h->d.ny, h->d.nz)) return fail(h, NB_ERR_CUDA, "tensor map");
+    CK(h, cudaMemcpyAsync(h->tmp_maps, hm, sizeof(CUtensorMap) * 5, cudaMemcpyHostToDevice, h->stream));
+    CK(h, nb_launch_weights(h->c, h->st, h->stars, h->sw, h->nstars, h->stream));
+    int rc = launch_stage(h, in4, u0_4, out4, 0, h->tmp_maps, a, b, true, dt, pulse, false);
+    if (rc != NB_OK) return rc;
+    CK(h, cudaStreamSynchronize(h->stream));        // tmp_maps is reused by the next call
+    return NB_OK;
+}
+
+NB_EXPORT int nb_max_speed(nb_handle h, float* smax_out) {
+    if (!h || !smax_out) return fail(h, NB_ERR_ARG, "null argument");
+    const nb_fields& f = h->d.f;
+    CK(h, nb_launch_max_speed(h->c, f.rho, f.mx, f.my, f.mz, f.xi, &h->st->smax_bits, h->ncell, h->stream));
+    unsigned bits = 0;
+    CK(h, cudaMemcpyAsync(&bits, &h->st->smax_bits, 4, cudaMemcpyDeviceToHost, h->stream));
+    CK(h, cudaStreamSynchronize(h->stream));
+    std::memcpy(smax_out, &bits, 4);
+    h->smax_valid = 1;
+    return NB_OK;
+}
+
+NB_EXPORT int nb_cast_rays(nb_handle h, const double xyz[3], double Q, float* rfront_out) {
+    if (!h || !xyz || !rfront_out) return fail(h, NB_ERR_ARG, "null argument");
+    float s3[4] = {(float)xyz[0], (float)xyz[1], (float)xyz[2], 0.f};
+    CK(h, cudaMemcpyAsync(h->scratch3, s3, sizeof(s3), cudaMemcpyHostToDevice, h->stream));
+    CK(h, nb_launch_cast_rays(h->c, h->sw, h->dirs, h->d.f.rho, rfront_out, 1, h->ray_group, h->scratch3, (float)Q,
+                              h->stream, h->d.nu, h->d.nphi));
+    CK(h, cudaStreamSynchronize(h->stream));
+    return NB_OK;
+}
+
+NB_EXPORT int nb_cast_fuv(nb_handle h, const double xyz[3], float* att_out) {
+    if (!h || !xyz || !att_out) return fail(h, NB_ERR_ARG, "null argument");
+    float s3[4] = {(float)xyz[0], (float)xyz[1], (float)xyz[2], 0.f};
+    CK(h, cudaMemcpyAsync(h->scratch3, s3, sizeof(s3), cudaMemcpyHostToDevice, h->stream));
+    CK(h, nb_launch_cast_fuv(h->c, h->sw, h->dirs_fuv, h->d.f.rho, h->d.f.xi, att_out, 1, 32, h->scratch3, 1,
+                             h->stream, h->d.fnu, h->d.fnphi));
+    CK(h, cudaStreamSynchronize(h->stream));
+    return NB_OK;
+}
+
+NB_EXPORT int nb_reduce_fp64(nb_handle h, double out[4]) {
+    if (!h || !out) return fail(h, NB_ERR_ARG, "null argument");
+    const nb_fields& f = h->d.f;
+    CK(h, nb_launch_reduce_fp64(f.rho, f.mx, f.my, f.mz, h->ncell, h->red, h->stream));
+    CK(h, cudaMemcpyAsync(out, h->red + nb_reduce_scratch_doubles() - 4, 4 * sizeof(double), cudaMemcpyDeviceToHost,
+                          h->stream));
+    CK(h, cudaStreamSynchronize(h->stream));
+    return NB_OK;
+}

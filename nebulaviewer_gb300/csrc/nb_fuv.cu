@@ -1,0 +1,198 @@
+// Dust-attenuated FUV field G0 = sum_star L exp(-tau_FUV) / r^2.  Follows
+// nebula3d.py:320-352 (cast_fuv: per-ray dust optical depth binned on a coarse spherical
+// grid att[r, u, phi]) and nebula3d.py:355-388 (apply_fuv: trilinear att / r^2 per cell),
+// as driven by sim.py:949-985 (fuv_field, fp16 store of G0).
+//
+// GB300 design: cast_fuv marches a ray with a group of G lanes, the optical depth being an
+// inclusive group scan over a Kahan-compensated carry; a lane that crosses into new radial
+// bins writes them.  All rays of all active stars are one launch, into one attenuation grid
+// per star laid out [star][u][phi][r] (r fastest: a ray's bins are contiguous).  apply_fuv
+// then accumulates every active star for a cell in one register, in the reference's star
+// order (so the float32 sum is the reference's), and stores G0 once as fp16.
+#include "nb_rayutil.cuh"
+
+namespace {
+
+template <int G, bool REF_LAYOUT>
+__global__ void __launch_bounds__(256) cast_fuv_kernel(const NbConst* __restrict__ c, const NbStarW* __restrict__ sw,
+                                                       const float4* __restrict__ dirs,
+                                                       const float* __restrict__ rho, const float* __restrict__ xi,
+                                                       float* __restrict__ att, int nstars,
+                                                       const float* star_override) {
+    const int nr = c->fnr, nu = c->fnu, nphi = c->fnphi, nray = nu * nphi;
+    const long long gid = (blockIdx.x * (long long)blockDim.x + threadIdx.x) / G;
+    const int lane = threadIdx.x % G;
+    const unsigned gmask = G == 32 ? 0xffffffffu : (((1u << G) - 1u) << ((threadIdx.x & 31) / G * G));
+    if (gid >= (long long)nray * nstars) return;
+    const int s = (int)(gid / nray), ray = (int)(gid % nray);
+    float sx, sy, sz;
+    if (star_override) {
+        sx = star_override[0]; sy = star_override[1]; sz = star_override[2];
+    } else {
+        const NbStarW w = sw[s];
+        if (!w.active) return;
+        sx = w.w.x; sy = w.w.y; sz = w.w.z;
+    }
+    const int iu = ray / nphi, ip = ray % nphi;
+    // bin b of this ray
+    auto at = [&](int b) -> float& {
+        return REF_LAYOUT ? att[((long long)b * nu + iu) * nphi + ip]
+                          : att[((long long)s * nray + ray) * nr + b];
+    };
+    const int nx = c->nx, ny = c->ny, nz = c->nz;
+    const float dx = c->dx, inv_dx = c->inv_dx, dr = c->dr_f, binr = c->binr_f, kappa = c->kappa_f;
+    const bool pow2 = c->dx_pow2 != 0;
+    const float4 d = dirs[ray];
+    float t0, t1;
+    nb_box_range(sx, sy, sz, d.x, d.y, d.z, c->bmax, t0, t1);
+    const int n0 = trunc_i(t0 / dr);
+    const int n1 = min(c->nsteps, trunc_i(t1 / dr) + 2);
+    float hi = 0.0f, comp = 0.0f;      // Kahan-compensated optical depth carried between segments
+    int ib = 0;                        // first bin not yet written
+    bool stopped = false;
+    for (int base = n0; base < n1; base += G) {
+        const int n = base + lane;
+        const bool valid = n < n1;
+        const float r = ((float)n + 0.5f) * dr;
+        float dtau = 0.0f;
+        int nb = ib;
+        if (valid) {
+            const float qx = sx + d.x * r, qy = sy + d.y * r, qz = sz + d.z * r;
+            const float n_tot = sample_n(rho, nx, ny, nz, qx, qy, qz, dx, inv_dx, pow2);
+            const float x_i = sample_n(xi, nx, ny, nz, qx, qy, qz, dx, inv_dx, pow2);
+            dtau = kappa * n_tot * (1.0f - 0.92f * x_i) * dr;
+            nb = trunc_i(r / binr);
+        }
+        float incl = dtau;
+#pragma unroll
+        for (int o = 1; o < G; o <<= 1) {
+            const float v = __shfl_up_sync(gmask, incl, o, G);
+            if (lane >= o) incl = incl + v;
+        }
+        const float tau = hi + (incl - comp);
+        // bins [prev, min(nb, nr)) take exp(-tau) of this sample (nb never decreases along a ray)
+        int prev = __shfl_up_sync(gmask, nb, 1, G);
+        if (lane == 0) prev = ib;
+        const bool stop = valid && nb >= nr;
+        const unsigned bal = __ballot_sync(gmask, stop);
+        const unsigned mine = G == 32 ? bal : (bal >> ((threadIdx.x & 31) / G * G)) & ((1u << G) - 1u);
+        const int first_stop = mine ? __ffs(mine) - 1 : G;
+        if (valid && lane <= first_stop && nb > prev) {
+            const float v = expf(-tau);
+            const int e = min(nb, nr);
+            for (int b = prev; b < e; ++b) at(b) = v;
+        }
+        if (mine) {
+            stopped = true;
+            break;
+        }
+        const int last = min(G, n1 - base) - 1;
+        ib = __shfl_sync(gmask, nb, last, G);
+        const float total = __shfl_sync(gmask, incl, G - 1, G);
+        const float y = total - comp;
+        const float tsum = hi + y;
+        comp = (tsum - hi) - y;
+        hi = tsum;
+    }
+    if (!stopped) {
+        const float v = expf(-(hi - comp));
+        for (int b = ib + lane; b < nr; b += G) at(b) = v;
+    }
+}
+
+template <bool HALF>
+__global__ void __launch_bounds__(256) apply_fuv_kernel(const NbConst* __restrict__ c, const NbStarW* __restrict__ sw,
+                                                        const float* __restrict__ att, int nstars,
+                                                        void* __restrict__ g0) {
+    __shared__ float4 st[NB_MAX_STARS];
+    __shared__ float lum[NB_MAX_STARS];
+    __shared__ int act[NB_MAX_STARS];
+    for (int s = threadIdx.x; s < nstars; s += blockDim.x) {
+        st[s] = sw[s].w;
+        lum[s] = sw[s].lum_f;
+        act[s] = sw[s].active;
+    }
+    __syncthreads();
+    const int nx = c->nx, ny = c->ny, nz = c->nz, nr = c->fnr, nu = c->fnu, nphi = c->fnphi;
+    const long long n = (long long)nx * ny * nz;
+    const float dx = c->dx, binr = c->binr_f;
+    const float two_pi = 2.0f * pi_f();
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
+        const int k = (int)(q % nz);
+        const long long t = q / nz;
+        const int j = (int)(t % ny), i = (int)(t / ny);
+        const float px = ((float)i + 0.5f) * dx, py = ((float)j + 0.5f) * dx, pz = ((float)k + 0.5f) * dx;
+        float g = 0.0f;
+        for (int s = 0; s < nstars; ++s) {
+            if (!act[s]) continue;
+            const float4 sp = st[s];
+            const float rx = px - sp.x, ry = py - sp.y, rz = pz - sp.z;
+            const float r = fmaxr(sqrtf(((0.0f + rx * rx) + ry * ry) + rz * rz), 1e-6f);
+            const float u = rz / r;
+            float phi = atan2f(ry, rx);
+            if (phi < 0.0f) phi = phi + two_pi;
+            const float fr = r / binr - 0.5f;
+            const float fu = (u + 1.0f) * 0.5f * (float)nu - 0.5f;
+            const float fp = phi / two_pi * (float)nphi - 0.5f;
+            const int ir = (int)floorf(fr), iu = (int)floorf(fu), ip = (int)floorf(fp);
+            const float tr = fr - (float)ir, tu = fu - (float)iu, tp = fp - (float)ip;
+            const float* as = att + (long long)s * nu * nphi * nr;
+            float acc = 0.0f;
+#pragma unroll
+            for (int aa = 0; aa < 2; ++aa)
+#pragma unroll
+                for (int bb = 0; bb < 2; ++bb)
+#pragma unroll
+                    for (int cc = 0; cc < 2; ++cc) {
+                        const float w = (aa == 0 ? 1.0f - tr : tr) * (bb == 0 ? 1.0f - tu : tu) * (cc == 0 ? 1.0f - tp : tp);
+                        const int rr = iclampd(ir + aa, 0, nr - 1);
+                        const int uu = iclampd(iu + bb, 0, nu - 1);
+                        const int pp = (((ip + cc) % nphi) + nphi) % nphi;
+                        acc = acc + w * __ldg(as + ((long long)uu * nphi + pp) * nr + rr);
+                    }
+            const float r2 = fmaxr(r * r, 0.0004f);
+            g = g + lum[s] * acc / r2;
+        }
+        if (HALF)
+            reinterpret_cast<__half*>(g0)[q] = __float2half_rn(g);
+        else
+            reinterpret_cast<float*>(g0)[q] = g;
+    }
+}
+
+int grid_for(long long n, int threads) {
+    long long b = (n + threads - 1) / threads;
+    const long long cap = 152LL * 16;
+    return (int)(b < cap ? (b < 1 ? 1 : b) : cap);
+}
+
+}  // namespace
+
+cudaError_t nb_launch_cast_fuv(const NbConst* c, const NbStarW* sw, const float4* dirs, const float* rho,
+                               const float* xi, float* att, int nstars, int group, const float* star_override,
+                               int ref_layout, cudaStream_t s, int fnu, int fnphi) {
+    const long long threads = (long long)fnu * fnphi * nstars * group;
+    const int blocks = (int)((threads + 255) / 256);
+#define NB_FUV_LAUNCH(G, R) cast_fuv_kernel<G, R><<<blocks, 256, 0, s>>>(c, sw, dirs, rho, xi, att, nstars, star_override)
+    if (ref_layout) {
+        NB_FUV_LAUNCH(32, true);
+    } else {
+        switch (group) {
+            case 8: NB_FUV_LAUNCH(8, false); break;
+            case 16: NB_FUV_LAUNCH(16, false); break;
+            default: NB_FUV_LAUNCH(32, false); break;
+        }
+    }
+#undef NB_FUV_LAUNCH
+    return cudaGetLastError();
+}
+
+cudaError_t nb_launch_apply_fuv(const NbConst* c, const NbStarW* sw, const float* att, int nstars, void* g0,
+                                cudaStream_t s, long long ncell, int half) {
+    const int blocks = grid_for(ncell, 256);
+    if (half)
+        apply_fuv_kernel<true><<<blocks, 256, 0, s>>>(c, sw, att, nstars, g0);
+    else
+        apply_fuv_kernel<false><<<blocks, 256, 0, s>>>(c, sw, att, nstars, g0);
+    return cudaGetLastError();
+}

@@ -1,0 +1,396 @@
+// One RK2 stage of the isothermal-Euler update: MUSCL reconstruction (minmod / van Leer /
+// MC) + HLL or Rusanov face flux, unsplit x->y->z divergence, wind and jet sources, the
+// convex RK combination a*U0 + b*(U + dt*dU), density floor and velocity cap.
+//
+// Follows nebula3d.py:76-151 (hydro_stage, Rusanov) and sim.py:423-498 (hydro_stage_hll)
+// with the face fluxes of nebula3d.py:54-72 / sim.py:397-420.  Every float operation is
+// the reference's, in the reference's order (the library is built with -fmad=false), so a
+// stage is bit-identical to the float32 oracle.
+//
+// GB300 layout: a block owns a 32 (k) x TJ (j) column of cells and marches along i.  Each
+// (j,k) plane tile with a 2-cell halo is brought into shared memory by TMA (five 3-D tiled
+// loads: rho, mx, my, mz, xi; double-buffered, mbarrier-tracked) while the previous plane
+// is computed.  A plane is converted once to primitives (rho, u, v, w) and (c^2, c) in
+// shared memory; every face flux is then evaluated once (the reference evaluates each face
+// twice) and shared through shared memory (y, z faces) or registers (x faces).  Stage 2
+// also reduces the CFL max speed of the new state (nebula3d.py:154-162) into one atomic.
+#include "nb_internal.cuh"
+
+namespace {
+
+constexpr int TK = 32;            // cells per tile along k (one warp)
+constexpr int RAWW = 40;          // raw tile width along k: [k0-4, k0+36), 16-byte aligned start
+constexpr int PW = 36;            // primitive tile width along k: [k0-2, k0+34)
+
+template <int LIM>
+__device__ __forceinline__ float slope_lim(float a, float b) {
+    if (a * b <= 0.0f) return 0.0f;
+    if (LIM == 2) {                                           // sim.py:366-372 mc_lim
+        float s = a > 0.0f ? 1.0f : -1.0f;
+        return s * fminr(fminr(2.0f * fabsf(a), 2.0f * fabsf(b)), 0.5f * fabsf(a + b));
+    }
+    if (LIM == 1) return 2.0f * a * b / (a + b);              // sim.py:375-380 vl_lim
+    if (fabsf(a) < fabsf(b)) return a;                        // nebula3d.py:40-46 minmod
+    return b;
+}
+
+__device__ __forceinline__ float comp(const float4& v, int c) {
+    return c == 0 ? v.x : (c == 1 ? v.y : (c == 2 ? v.z : v.w));
+}
+
+// Face flux between cells b and c along axis AX (1 = x, 2 = y, 3 = z: the velocity
+// component normal to the face).  cs = (c^2, c) of a cell.
+//   dot((0, L1, L2, L3), e_AX) == 0 + L_AX exactly (the other products are +-0 and the
+//   velocities are finite), and e_c * (rho c^2) == +0 for c != AX.
+template <int SOLVER, int LIM, int AX>
+__device__ __forceinline__ float4 face_flux(const float4 qa, const float4 qb, const float4 qc, const float4 qd,
+                                            const float2 csb, const float2 csc, const float floor_) {
+    constexpr int LM = SOLVER == NB_SOLVER_HLL ? LIM : 0;
+    float L[4], R[4];
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+        const float a = comp(qa, c), b = comp(qb, c), cc = comp(qc, c), d = comp(qd, c);
+        const float d1 = b - a, d2 = cc - b, d3 = d - cc;
+        L[c] = b + 0.5f * slope_lim<LM>(d1, d2);
+        R[c] = cc - 0.5f * slope_lim<LM>(d2, d3);
+    }
+    const float rL = fmaxr(L[0], floor_), rR = fmaxr(R[0], floor_);
+    const float unL = 0.0f + L[AX], unR = 0.0f + R[AX];
+    const float UL[4] = {rL, rL * L[1], rL * L[2], rL * L[3]};
+    const float UR[4] = {rR, rR * R[1], rR * R[2], rR * R[3]};
+    const float pL = rL * csb.x, pR = rR * csc.x;
+    float FL[4], FR[4], F[4];
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+        FL[c] = UL[c] * unL + (c == AX ? pL : 0.0f);
+        FR[c] = UR[c] * unR + (c == AX ? pR : 0.0f);
+    }
+    if (SOLVER == NB_SOLVER_RUSANOV) {
+        const float amax = fmaxr(fabsf(unL) + csb.y, fabsf(unR) + csc.y);
+        const float ha = 0.5f * amax;
+#pragma unroll
+        for (int c = 0; c < 4; ++c) F[c] = 0.5f * (FL[c] + FR[c]) - ha * (UR[c] - UL[c]);
+        return make_float4(F[0], F[1], F[2], F[3]);
+    }
+    const float SL = fminr(unL - csb.y, unR - csc.y);
+    const float SR = fmaxr(unL + csb.y, unR + csc.y);
+    if (SL >= 0.0f) return make_float4(FL[0], FL[1], FL[2], FL[3]);
+    if (SR <= 0.0f) return make_float4(FR[0], FR[1], FR[2], FR[3]);
+    const float slsr = SL * SR, den = SR - SL;
+#pragma unroll
+    for (int c = 0; c < 4; ++c) F[c] = (SR * FL[c] - SL * FR[c] + slsr * (UR[c] - UL[c])) / den;
+    return make_float4(F[0], F[1], F[2], F[3]);
+}
+
+struct Raw5 {
+    float r, mx, my, mz, xi;
+};
+
+template <int TJ>
+struct HydroSmem {
+    static constexpr int RAW_FIELD = (TJ + 4) * RAWW;                     // floats per field per slot
+    static constexpr int RAW_BYTES = 2 * 5 * RAW_FIELD * 4;
+    static constexpr int PRIM_BYTES = 3 * (TJ + 4) * PW * 16;
+    static constexpr int CS_BYTES = 3 * (TJ + 4) * PW * 8;
+    static constexpr int FACE_BYTES = ((TJ + 1) * TK + TJ * (TK + 1)) * 16;
+    static constexpr int BAR_BYTES = 64;
+    static constexpr int FIXED = RAW_BYTES + PRIM_BYTES + CS_BYTES + FACE_BYTES + BAR_BYTES;
+    static int bytes(int nstars) { return FIXED + nstars * 32; }
+};
+
+template <int SOLVER, int LIM, int TJ, bool STAGE2>
+__global__ void __launch_bounds__(TK * TJ, (TJ <= 8 ? 2 : 1))
+hydro_stage_kernel(const HydroLaunch L) {
+    using SM = HydroSmem<TJ>;
+    extern __shared__ __align__(128) unsigned char smem[];
+    float* raw = reinterpret_cast<float*>(smem);                                   // [2][5][TJ+4][40]
+    float4* prim = reinterpret_cast<float4*>(smem + SM::RAW_BYTES);                // [3][TJ+4][36]
+    float2* cs = reinterpret_cast<float2*>(smem + SM::RAW_BYTES + SM::PRIM_BYTES); // [3][TJ+4][36]
+    float4* fy = reinterpret_cast<float4*>(smem + SM::RAW_BYTES + SM::PRIM_BYTES + SM::CS_BYTES);  // [TJ+1][32]
+    float4* fz = fy + (TJ + 1) * TK;                                               // [TJ][33]
+    uint64_t* bar = reinterpret_cast<uint64_t*>(smem + SM::FIXED - SM::BAR_BYTES);
+    float4* sw_w = reinterpret_cast<float4*>(smem + SM::FIXED);
+    const NbConst& C = *L.c;
+    const int nx = C.nx, ny = C.ny, nz = C.nz, nstars = C.nstars;
+    float4* sw_j = sw_w + nstars;
+
+    const int tid = threadIdx.x, tk = tid & 31, tj = tid >> 5;
+    int tile = blockIdx.x;
+    const int kt = tile % L.tiles_k;
+    tile /= L.tiles_k;
+    const int jt = tile % L.tiles_j;
+    const int ci = tile / L.tiles_j;
+    const int k0 = kt * TK, j0 = jt * TJ;
+    const int i0 = ci * L.chunk_i;
+    const int i_end = min(nx, i0 + L.chunk_i);
+    const int P0 = i0 - 2, P1 = i_end + 1;
+
+    const float floor_ = C.floor_, cn2 = C.cn2, ci2 = C.ci2, vmax = C.vmax, dx = C.dx;
+    const float dt = L.use_override ? L.dt_override : L.st->dt_f;
+    const float pulse = L.use_override ? L.pulse_override : L.st->pulse_f;
+    const float wind = C.wind_f, jet_cos = C.jet_cos_f, jet_r = C.jet_r_f;
+    const float a = L.a, b = L.b;
+
+    for (int s = tid; s < nstars; s += blockDim.x) {
+        sw_w[s] = L.sw[s].w;
+        sw_j[s] = L.sw[s].jet;
+    }
+    constexpr unsigned TX_BYTES = 5u * SM::RAW_FIELD * 4u;
+    auto issue = [&](int p, int slot) {
+        const int pc = iclampd(p, 0, nx - 1);
+        float* dst = raw + slot * 5 * SM::RAW_FIELD;
+        fence_proxy_async();
+        mbar_expect_tx(&bar[slot], TX_BYTES);
+#pragma unroll
+        for (int f = 0; f < 4; ++f)
+            tma_load_3d(dst + f * SM::RAW_FIELD, &L.maps[L.map_in + f], k0 - 4, j0 - 2, pc, &bar[slot]);
+        tma_load_3d(dst + 4 * SM::RAW_FIELD, &L.maps[NB_MAP_XI], k0 - 4, j0 - 2, pc, &bar[slot]);
+    };
+    if (tid == 0) {
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    if (tid == 0) {
+        issue(P0, 0);
+        issue(P0 + 1, 1);
+    }
+
+    // own-column windows: q for planes p-3..p, (c^2, c) and raw values for planes p-2..p
+    float4 qw0 = make_float4(0.f, 0.f, 0.f, 0.f), qw1 = qw0, qw2 = qw0, qw3 = qw0;
+    float2 cw0 = make_float2(0.f, 0.f), cw1 = cw0, cw2 = cw0;
+    Raw5 rw0{}, rw1{}, rw2{};
+    float4 fx_prev = qw0;
+    float vmax_local = 0.0f;
+    unsigned ph0 = 0, ph1 = 0;
+    bool failed = false;
+
+    // clamped global -> raw-tile coordinates
+    auto raw_at = [&](const float* base, int jj, int kk) {      // jj, kk: prim-tile coords
+        const int jc = iclampd(j0 - 2 + jj, 0, ny - 1) - (j0 - 2);
+        const int kc = iclampd(k0 - 2 + kk, 0, nz - 1) - (k0 - 4);
+        return jc * RAWW + kc;
+    };
+
+    for (int p = P0; p <= P1; ++p) {
+        const int rs = (p - P0) & 1;
+        const int ps = (p - P0) % 3;
+        bool ok = mbar_wait_bounded(&bar[rs], rs ? ph1 : ph0);
+        if (rs) ph1 ^= 1u; else ph0 ^= 1u;
+        if (__syncthreads_or(!ok)) { failed = true; break; }
+        const float* rb = raw + rs * 5 * SM::RAW_FIELD;
+        float4* pp = prim + ps * (TJ + 4) * PW;
+        float2* cp = cs + ps * (TJ + 4) * PW;
+        // ---- convert plane p: own cell, then the halo strips (corners are never read)
+        Raw5 own;
+        {
+            const int jj = tj + 2, kk = tk + 2;
+            const int o = raw_at(rb, jj, kk);
+            own.r = rb[o];
+            own.mx = rb[SM::RAW_FIELD + o];
+            own.my = rb[2 * SM::RAW_FIELD + o];
+            own.mz = rb[3 * SM::RAW_FIELD + o];
+            own.xi = rb[4 * SM::RAW_FIELD + o];
+            const float r = fmaxr(own.r, floor_);
+            const float c2 = cn2 + own.xi * (ci2 - cn2);
+            pp[jj * PW + kk] = make_float4(r, own.mx / r, own.my / r, own.mz / r);
+            cp[jj * PW + kk] = make_float2(c2, sqrtf(c2));
+        }
+        for (int h = tid; h < 4 * TK + 4 * TJ; h += TK * TJ) {
+            int jj, kk;
+            if (h < 4 * TK) {
+                const int rr = h >> 5;
+                jj = rr < 2 ? rr : TJ + rr;
+                kk = 2 + (h & 31);
+            } else {
+                const int hh = h - 4 * TK;
+                jj = 2 + (hh >> 2);
+                const int q = hh & 3;
+                kk = q < 2 ? q : 32 + q;
+            }
+            const int o = raw_at(rb, jj, kk);
+            const float r = fmaxr(rb[o], floor_);
+            const float xv = rb[4 * SM::RAW_FIELD + o];
+            const float c2 = cn2 + xv * (ci2 - cn2);
+            pp[jj * PW + kk] = make_float4(r, rb[SM::RAW_FIELD + o] / r, rb[2 * SM::RAW_FIELD + o] / r,
+                                           rb[3 * SM::RAW_FIELD + o] / r);
+            cp[jj * PW + kk] = make_float2(c2, sqrtf(c2));
+        }
+        __syncthreads();
+        if (tid == 0 && p + 2 <= P1) issue(p + 2, rs);
+        // ---- shift the own-column windows
+        qw0 = qw1; qw1 = qw2; qw2 = qw3;
+        qw3 = pp[(tj + 2) * PW + tk + 2];
+        cw0 = cw1; cw1 = cw2;
+        cw2 = cp[(tj + 2) * PW + tk + 2];
+        rw0 = rw1; rw1 = rw2; rw2 = own;
+        if (p < P0 + 3) continue;
+        // x face (p-2)+1/2 from planes p-3..p
+        const float4 fx_new = face_flux<SOLVER, LIM, 1>(qw0, qw1, qw2, qw3, cw0, cw1, floor_);
+        if (p < i0 + 2) { fx_prev = fx_new; continue; }
+        // ---- cell plane i = p - 2 (prim slot of plane i)
+        const int i = p - 2;
+        const int si = (i - P0) % 3;
+        const float4* q = prim + si * (TJ + 4) * PW;
+        const float2* c = cs + si * (TJ + 4) * PW;
+        const int jj = tj + 2, kk = tk + 2;
+        const float4 fyp = face_flux<SOLVER, LIM, 2>(q[(jj - 1) * PW + kk], q[jj * PW + kk], q[(jj + 1) * PW + kk],
+                                                     q[(jj + 2) * PW + kk], c[jj * PW + kk], c[(jj + 1) * PW + kk],
+                                                     floor_);
+        const float4 fzp = face_flux<SOLVER, LIM, 3>(q[jj * PW + kk - 1], q[jj * PW + kk], q[jj * PW + kk + 1],
+                                                     q[jj * PW + kk + 2], c[jj * PW + kk], c[jj * PW + kk + 1],
+                                                     floor_);
+        fy[(tj + 1) * TK + tk] = fyp;
+        fz[tj * (TK + 1) + tk + 1] = fzp;
+        if (tj == 0) {                          // the y face below the tile: (j0-1)+1/2
+            fy[tk] = face_flux<SOLVER, LIM, 2>(q[0 * PW + kk], q[1 * PW + kk], q[2 * PW + kk], q[3 * PW + kk],
+                                               c[1 * PW + kk], c[2 * PW + kk], floor_);
+        } else if (tj == 1 && tk < TJ) {        // the z face before the tile in row tk: (k0-1)+1/2
+            const int r2 = (tk + 2) * PW;
+            fz[tk * (TK + 1)] = face_flux<SOLVER, LIM, 3>(q[r2 + 0], q[r2 + 1], q[r2 + 2], q[r2 + 3], c[r2 + 1],
+                                                          c[r2 + 2], floor_);
+        }
+        __syncthreads();
+        const float4 fym = fy[tj * TK + tk];
+        const float4 fzm = fz[tj * (TK + 1) + tk];
+        const float4 fxp = fx_new, fxm = fx_prev;
+        fx_prev = fx_new;
+        // div = 0 + (fR-fL)_x, then += (fR-fL)_y, then += (fR-fL)_z  (nebula3d.py:87-109)
+        float d0 = 0.0f + (fxp.x - fxm.x), d1 = 0.0f + (fxp.y - fxm.y);
+        float d2 = 0.0f + (fxp.z - fxm.z), d3 = 0.0f + (fxp.w - fxm.w);
+        d0 = d0 + (fyp.x - fym.x); d1 = d1 + (fyp.y - fym.y); d2 = d2 + (fyp.z - fym.z); d3 = d3 + (fyp.w - fym.w);
+        d0 = d0 + (fzp.x - fzm.x); d1 = d1 + (fzp.y - fzm.y); d2 = d2 + (fzp.z - fzm.z); d3 = d3 + (fzp.w - fzm.w);
+        const int j = j0 + tj, k = k0 + tk;
+        const bool inside = j < ny && k < nz;
+        // ---- sources and RK combination (nebula3d.py:111-151)
+        const Raw5 U = rw0;
+        float du0, du1, du2, du3;
+        if (C.dx_pow2) {
+            const float s = C.inv_dx;
+            du0 = -d0 * s; du1 = -d1 * s; du2 = -d2 * s; du3 = -d3 * s;
+        } else {
+            du0 = -d0 / dx; du1 = -d1 / dx; du2 = -d2 / dx; du3 = -d3 / dx;
+        }
+        const float px = ((float)i + 0.5f) * dx, py = ((float)j + 0.5f) * dx, pz = ((float)k + 0.5f) * dx;
+        const float x_ion = U.xi;
+        if (wind > 0.0f && x_ion > 0.01f) {
+            float ax = 0.0f, ay = 0.0f, az = 0.0f;
+            for (int s = 0; s < nstars; ++s) {
+                const float4 st = sw_w[s];
+                if (st.w > 0.0f) {
+                    const float rx = px - st.x, ry = py - st.y, rz = pz - st.z;
+                    const float r2 = ((0.0f + rx * rx) + ry * ry) + rz * rz + 0.0004f;
+                    const float f = st.w / (r2 * sqrtf(r2));
+                    ax = ax + rx * f; ay = ay + ry * f; az = az + rz * f;
+                }
+            }
+            const float wx = wind * x_ion;
+            ax = ax * wx; ay = ay * wx; az = az * wx;
+            du0 = du0 + 0.0f;
+            du1 = du1 + U.r * ax; du2 = du2 + U.r * ay; du3 = du3 + U.r * az;
+        }
+        float jx = 0.0f, jy = 0.0f, jz = 0.0f;
+        for (int s = 0; s < nstars; ++s) {
+            const float4 jt = sw_j[s];
+            const float4 st = sw_w[s];
+            if (jt.w > 0.0f && st.w > 0.0f) {
+                const float rx = px - st.x, ry = py - st.y, rz = pz - st.z;
+                const float r = sqrtf(((0.0f + rx * rx) + ry * ry) + rz * rz);
+                if (r < jet_r && r > 1e-6f) {
+                    const float cth = (((0.0f + rx * jt.x) + ry * jt.y) + rz * jt.z) / r;
+                    if (fabsf(cth) > jet_cos) {
+                        const float f = (cth > 0.0f ? 1.0f : -1.0f) * jt.w * pulse / (r * r + 0.0004f);
+                        jx = jx + jt.x * f; jy = jy + jt.y * f; jz = jz + jt.z * f;
+                    }
+                }
+            }
+        }
+        du0 = du0 + 0.0f;
+        du1 = du1 + U.r * jx; du2 = du2 + U.r * jy; du3 = du3 + U.r * jz;
+        const float un0 = U.r + dt * du0, un1 = U.mx + dt * du1, un2 = U.my + dt * du2, un3 = U.mz + dt * du3;
+        const long long cell = ((long long)i * ny + j) * nz + k;
+        float u00, u01, u02, u03;
+        if (STAGE2) {
+            if (inside) {
+                u00 = L.u0[0][cell]; u01 = L.u0[1][cell]; u02 = L.u0[2][cell]; u03 = L.u0[3][cell];
+            } else {
+                u00 = u01 = u02 = u03 = 0.0f;
+            }
+        } else {
+            u00 = U.r; u01 = U.mx; u02 = U.my; u03 = U.mz;
+        }
+        const float o0 = a * u00 + b * un0, o1 = a * u01 + b * un1, o2 = a * u02 + b * un2, o3 = a * u03 + b * un3;
+        const float r = fmaxr(o0, floor_);
+        float vx = o1 / r, vy = o2 / r, vz = o3 / r;
+        const float sp = sqrtf(((0.0f + vx * vx) + vy * vy) + vz * vz);
+        if (sp > vmax) {
+            const float f = vmax / sp;
+            vx = vx * f; vy = vy * f; vz = vz * f;
+        }
+        const float m1 = r * vx, m2 = r * vy, m3 = r * vz;
+        if (inside) {
+            L.out[0][cell] = r;
+            L.out[1][cell] = m1;
+            L.out[2][cell] = m2;
+            L.out[3][cell] = m3;
+            if (STAGE2 && L.smax_bits) {         // nebula3d.py:158-162 on the new state
+                const float v = fabsf(m1 / r) + fabsf(m2 / r) + fabsf(m3 / r) + cw0.y;
+                vmax_local = fmaxr(v, vmax_local);
+            }
+        }
+    }
+    if (__syncthreads_or(failed)) {
+        // a TMA wait gave up: record it, let the other slot's copy land (bounded), and leave
+        if (tid == 0) {
+            atomicOr(L.status, NB_DEV_TMA_TIMEOUT);
+            mbar_wait_bounded(&bar[0], ph0);
+            mbar_wait_bounded(&bar[1], ph1);
+        }
+        __syncthreads();
+        return;
+    }
+    if (STAGE2 && L.smax_bits) {
+        for (int o = 16; o > 0; o >>= 1) vmax_local = fmaxr(vmax_local, __shfl_xor_sync(0xffffffffu, vmax_local, o));
+        float* red = reinterpret_cast<float*>(fy);
+        __syncthreads();
+        if (tk == 0) red[tj] = vmax_local;
+        __syncthreads();
+        if (tid == 0) {
+            float m = 0.0f;
+            for (int w = 0; w < TJ; ++w) m = fmaxr(m, red[w]);
+            atomicMax(L.smax_bits, __float_as_uint(m));
+        }
+    }
+}
+
+template <int SOLVER, int LIM, int TJ, bool STAGE2>
+cudaError_t run_kernel(const HydroLaunch& L, cudaStream_t s) {
+    auto kern = hydro_stage_kernel<SOLVER, LIM, TJ, STAGE2>;
+    const int smem = HydroSmem<TJ>::bytes(L.nstars_host);
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e != cudaSuccess) return e;
+    const int blocks = L.tiles_k * L.tiles_j * L.n_chunks;
+    kern<<<blocks, TK * TJ, smem, s>>>(L);
+    return cudaGetLastError();
+}
+
+template <int SOLVER, int LIM, int TJ>
+cudaError_t run_stage(const HydroLaunch& L, cudaStream_t s) {
+    return L.smax_bits || L.u0[0] != L.in[0] ? run_kernel<SOLVER, LIM, TJ, true>(L, s)
+                                             : run_kernel<SOLVER, LIM, TJ, false>(L, s);
+}
+
+}  // namespace
+
+int nb_hydro_tile_j() { return 8; }
+
+cudaError_t nb_launch_hydro(const HydroLaunch& L, int solver, int limiter, cudaStream_t s) {
+    constexpr int TJ = 8;
+    if (solver == NB_SOLVER_RUSANOV) return run_stage<NB_SOLVER_RUSANOV, 0, TJ>(L, s);
+    switch (limiter) {
+        case NB_LIM_VANLEER: return run_stage<NB_SOLVER_HLL, NB_LIM_VANLEER, TJ>(L, s);
+        case NB_LIM_MC: return run_stage<NB_SOLVER_HLL, NB_LIM_MC, TJ>(L, s);
+        default: return run_stage<NB_SOLVER_HLL, NB_LIM_MINMOD, TJ>(L, s);
+    }
+}

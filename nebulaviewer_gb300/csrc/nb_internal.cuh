@@ -1,0 +1,155 @@
+// Internal declarations shared by the libnebula translation units.
+#pragma once
+#include <cuda.h>
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/nebula.h"
+
+#define NB_MAX_STARS 256          // star-table capacity limit (smem-resident in the kernels)
+#define NB_WAIT_LIMIT (1u << 22)  // iteration cap of every device-side spin wait
+
+// Device-status bits (NbState::status), reported by nb_device_status.
+#define NB_DEV_TMA_TIMEOUT 1u
+
+// ------------------------------------------------------------------ device-resident data
+// Scalars written by the host (geometry, physics, live parameters).  float copies are the
+// float32 kernel arguments the reference passes to Warp (Python double -> float32).
+struct NbConst {
+    int nx, ny, nz, nstars;
+    int dx_pow2;                 // dx == 2^-m: x / dx == x * (1/dx) exactly
+    int solver, limiter, fields_fp32;
+    float dx, inv_dx, floor_, cn2, ci2, vmax;
+    float width;                 // 1.2 * dx (sim.py:939)
+    float bmax[3];               // box extent (sim.py:750)
+    float diag_f, dr_f, binr_f;  // rcap, ray step, FUV bin width (sim.py:742-744, 958)
+    int nu, nphi, nsteps, fnr, fnu, fnphi;
+    double dx_d, cfl, diag_d;
+    // live parameters (sim.py:82-83)
+    double q_main, wind, jet, jet_proto, jet_pulse, jet_period, kappa_fuv, q_ramp, jet_r, jet_cos, dt_cap;
+    int phase_main;
+    float wind_f, jet_cos_f, jet_r_f, kappa_f;
+};
+
+// Written by device kernels every step.
+struct NbState {
+    double t, dt;
+    long long it;
+    float dt_f, pulse_f;         // float32 arguments of the step's hydro stages
+    unsigned smax_bits;          // CFL max speed (non-negative float bits; atomicMax on uint)
+    unsigned status;             // NB_DEV_* failure bits
+};
+
+struct NbStarDev {
+    double x, y, z, qf, t_on, ax, ay, az;
+    int kind, jkind;
+};
+
+// Weights of one star for the hydro sources and the ray kernels (computed on device at t).
+struct NbStarW {
+    float4 w;      // (x, y, z, q_eff / q_main or 0 before t_on)   sim.py:916
+    float4 jet;    // (ax, ay, az, strength)                       sim.py:923
+    float q_f;     // q_eff as float32 (cast_rays Q, sim.py:937)
+    float lum_f;   // q_eff / q_main as float32 (apply_fuv lum, sim.py:965)
+    int active;    // t >= t_on (sim.py:934)
+    int pad;
+};
+
+// Tensor maps of an instance's planes (device global memory, 64-byte aligned).
+enum { NB_MAP_RHO = 0, NB_MAP_MX, NB_MAP_MY, NB_MAP_MZ, NB_MAP_XI, NB_MAP_S0, NB_MAP_S1, NB_MAP_S2, NB_MAP_S3,
+       NB_NMAPS };
+
+// ------------------------------------------------------------------ kernel argument packs
+struct HydroLaunch {
+    const NbConst* c;
+    const NbState* st;
+    const NbStarW* sw;
+    const CUtensorMap* maps;     // device array of NB_NMAPS maps
+    int map_in;                  // NB_MAP_RHO (stage 1) or NB_MAP_S0 (stage 2)
+    const float* in[4];
+    const float* u0[4];
+    float* out[4];
+    const float* xi;
+    float a, b;
+    float dt_override, pulse_override;   // used when use_override (single-stage entry point)
+    int use_override;
+    unsigned* smax_bits;         // non-null: accumulate the CFL max speed of `out`
+    unsigned* status;
+    int tiles_k, tiles_j, chunk_i, n_chunks;
+    int nstars_host;             // == c->nstars (sizes the dynamic shared memory)
+};
+
+// ------------------------------------------------------------------ helpers
+__device__ __forceinline__ unsigned smem_u32(const void* p) {
+    return static_cast<unsigned>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ float fmaxr(float a, float b) { return a > b ? a : b; }   // Warp max
+__device__ __forceinline__ float fminr(float a, float b) { return a < b ? a : b; }   // Warp min
+__device__ __forceinline__ int iclampd(int x, int lo, int hi) { return x < lo ? lo : (x > hi ? hi : x); }
+
+// ---- mbarrier / TMA (sm_90+ PTX; every wait is bounded)
+__device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ bool mbar_test(uint64_t* bar, unsigned parity) {
+    unsigned ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// Returns false when the wait gave up after NB_WAIT_LIMIT polls.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, unsigned parity) {
+    for (unsigned n = 0; n < NB_WAIT_LIMIT; ++n)
+        if (mbar_test(bar, parity)) return true;
+    return false;
+}
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+
+// 3D tiled TMA load (non-multicast, this GPU's own memory).  c0 is the innermost (k)
+// coordinate and must be a multiple of 4 floats (16 bytes).
+__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, int c0, int c1, int c2,
+                                            uint64_t* bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+        " [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(smem_u32(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(smem_u32(bar))
+        : "memory");
+}
+
+// ------------------------------------------------------------------ launchers (nb_*.cu)
+cudaError_t nb_launch_hydro(const HydroLaunch& L, int solver, int limiter, cudaStream_t s);
+int nb_hydro_tile_j();
+cudaError_t nb_launch_ctrl(const NbConst* c, NbState* st, const NbStarDev* stars, NbStarW* sw, int nstars,
+                           int advance, cudaStream_t s);
+cudaError_t nb_launch_weights(const NbConst* c, const NbState* st, const NbStarDev* stars, NbStarW* sw,
+                              int nstars, cudaStream_t s);
+cudaError_t nb_launch_max_speed(const NbConst* c, const float* rho, const float* mx, const float* my,
+                                const float* mz, const float* xi, unsigned* smax_bits, long n, cudaStream_t s);
+cudaError_t nb_launch_ray_dirs(int nu, int nphi, float4* dirs, cudaStream_t s);
+cudaError_t nb_launch_cast_rays(const NbConst* c, const NbStarW* sw, const float4* dirs, const float* rho,
+                                float* rfront, int nstars, int group, const float* star_override, float q_override,
+                                cudaStream_t s, int nu, int nphi);
+cudaError_t nb_launch_apply_front(const NbConst* c, const NbStarW* sw, const float* rfront, int nstars,
+                                  float* xi_raw, void* dfront, unsigned* smax_reset, cudaStream_t s, long long ncell,
+                                  int half);
+cudaError_t nb_launch_smooth(const NbConst* c, const float* xi_raw, float* xi, const float* rho, const float* mx,
+                             const float* my, const float* mz, unsigned* smax_bits, cudaStream_t s, long long ncell);
+cudaError_t nb_launch_cast_fuv(const NbConst* c, const NbStarW* sw, const float4* dirs, const float* rho,
+                               const float* xi, float* att, int nstars, int group, const float* star_override,
+                               int ref_layout, cudaStream_t s, int fnu, int fnphi);
+cudaError_t nb_launch_apply_fuv(const NbConst* c, const NbStarW* sw, const float* att, int nstars, void* g0,
+                                cudaStream_t s, long long ncell, int half);
+cudaError_t nb_launch_reduce_fp64(const float* rho, const float* mx, const float* my, const float* mz, long n,
+                                  double* scratch, cudaStream_t s);   // totals at scratch[4*608 .. +4)
+int nb_reduce_scratch_doubles();

@@ -1,0 +1,57 @@
+// Device helpers shared by the ray kernels (ionizing rays and FUV rays).
+#pragma once
+#include "nb_internal.cuh"
+
+__device__ __forceinline__ float pi_f() { return 3.14159265358979323846f; }
+
+// nebula3d.py:195-226 sample_n (trilinear, 0 outside the domain).  With dx == 2^-m the
+// division p / dx is the exact multiplication p * 2^m.
+__device__ __forceinline__ float sample_n(const float* __restrict__ a, int nx, int ny, int nz, float px, float py,
+                                          float pz, float dx, float inv_dx, bool pow2) {
+    const float gx = (pow2 ? px * inv_dx : px / dx) - 0.5f;
+    const float gy = (pow2 ? py * inv_dx : py / dx) - 0.5f;
+    const float gz = (pow2 ? pz * inv_dx : pz / dx) - 0.5f;
+    if (gx < -0.5f || gy < -0.5f || gz < -0.5f) return 0.0f;
+    if (gx > (float)nx - 0.5f || gy > (float)ny - 0.5f || gz > (float)nz - 0.5f) return 0.0f;
+    const int i0 = (int)floorf(gx), j0 = (int)floorf(gy), k0 = (int)floorf(gz);
+    const float fx = gx - (float)i0, fy = gy - (float)j0, fz = gz - (float)k0;
+    const int ia = iclampd(i0, 0, nx - 1), ib = iclampd(i0 + 1, 0, nx - 1);
+    const int ja = iclampd(j0, 0, ny - 1), jb = iclampd(j0 + 1, 0, ny - 1);
+    const int ka = iclampd(k0, 0, nz - 1), kb = iclampd(k0 + 1, 0, nz - 1);
+    const long long sa = (long long)ia * ny, sb = (long long)ib * ny;
+    const float c000 = __ldg(a + (sa + ja) * nz + ka), c100 = __ldg(a + (sb + ja) * nz + ka);
+    const float c010 = __ldg(a + (sa + jb) * nz + ka), c110 = __ldg(a + (sb + jb) * nz + ka);
+    const float c001 = __ldg(a + (sa + ja) * nz + kb), c101 = __ldg(a + (sb + ja) * nz + kb);
+    const float c011 = __ldg(a + (sa + jb) * nz + kb), c111 = __ldg(a + (sb + jb) * nz + kb);
+    const float c00 = c000 + (c100 - c000) * fx;
+    const float c10 = c010 + (c110 - c010) * fx;
+    const float c01 = c001 + (c101 - c001) * fx;
+    const float c11 = c011 + (c111 - c011) * fx;
+    const float c0 = c00 + (c10 - c00) * fy;
+    const float c1 = c01 + (c11 - c01) * fy;
+    return c0 + (c1 - c0) * fz;
+}
+
+// nebula3d.py:229-244 box_range
+__device__ __forceinline__ void nb_box_range(float ox, float oy, float oz, float dxr, float dyr, float dzr, const float* bmax,
+                             float& t0, float& t1) {
+    t0 = 0.0f;
+    t1 = 1e9f;
+    const float o[3] = {ox, oy, oz}, d[3] = {dxr, dyr, dzr};
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        if (fabsf(d[a]) < 1e-9f) {
+            if (o[a] < 0.0f || o[a] > bmax[a]) t1 = -1.0f;
+        } else {
+            const float ta = (0.0f - o[a]) / d[a];
+            const float tb = (bmax[a] - o[a]) / d[a];
+            t0 = fmaxr(t0, fminr(ta, tb));
+            t1 = fminr(t1, fmaxr(ta, tb));
+        }
+    }
+}
+
+// Python int() of a float32 (truncation), kept inside the int range
+__device__ __forceinline__ int trunc_i(float x) {
+    return x > 2e9f ? 2000000000 : (x < -2e9f ? -2000000000 : (int)x);
+}

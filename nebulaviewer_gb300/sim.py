@@ -1,0 +1,503 @@
+"""`Sim`: the drop-in for the reference's GPU-resident simulation class (sim.py:543-1222)
+on the simulation-step path, backed by libnebula.so (hand-written sm_103a kernels).
+
+Same call surface as the reference for what viewer.py / bake.py / bench.py use on this
+path: step(k), ionize(), fuv_field(), update_render_fields(force), set_param(), replace_stars(),
+stars_absolute(), active_stars(), get_state_meta() / set_state_meta(), tau(), time_label(),
+stats(), render_scratch(); attributes rho, mx, my, mz, xi, dfront, g0, stage, shape, dx, L,
+t, it, dt, phase, P, prof, profile, dt_cap, version, rf_version, stars, kinds, jets, jkinds,
+events, ion_every, fuv_every.  Fields are device buffers with the wp.array surface the
+callers use (.numpy(), .shape, .dtype, .ptr, .fill_, .zero_, .assign, __cuda_array_interface__).
+
+What differs by design: the clock (t, dt, it) lives on the device, so step(k) enqueues k
+steps without a host round trip per step (the reference blocks on a max-speed read every
+step, sim.py:1012); reading `t` synchronizes.  The pre-turbulence (stirring) phase, the
+triggered star formation and cropped domains are outside this package's scope: a
+parameter set that asks for them is rejected.
+"""
+import ctypes as C
+import math
+import time
+
+import numpy as np
+import torch
+
+from . import _lib
+from . import ics as _ics
+from .params import LIVE, make_params, sound_speeds
+
+
+class Field:
+    """A device buffer (torch tensor) with the wp.array methods the reference's callers use."""
+
+    def __init__(self, t):
+        self.t = t
+
+    @property
+    def shape(self):
+        return tuple(self.t.shape)
+
+    @property
+    def dtype(self):
+        return np.dtype(str(self.t.dtype).replace("torch.", ""))
+
+    @property
+    def ptr(self):
+        return self.t.data_ptr()
+
+    @property
+    def __cuda_array_interface__(self):
+        return self.t.__cuda_array_interface__
+
+    def numpy(self):
+        return self.t.detach().cpu().numpy()
+
+    def torch(self):
+        return self.t
+
+    def fill_(self, v):
+        self.t.fill_(v)
+
+    def zero_(self):
+        self.t.zero_()
+
+    def assign(self, x):
+        self.t.copy_(torch.as_tensor(np.asarray(x)).reshape(self.t.shape).to(self.t.dtype))
+
+    def __getitem__(self, k):
+        return Field(self.t[k])
+
+    def __repr__(self):
+        return f"Field({self.shape}, {self.dtype}, {self.t.device})"
+
+
+class _Shape:
+    def __init__(self, shape):
+        self.shape = tuple(shape)
+
+
+def _ray_budget(nz, fast, rays, fuv_grid):
+    nu = rays[0] if rays else (512 if nz <= 256 else 1024)                       # sim.py:753-754
+    nphi = rays[1] if rays else 2 * nu
+    fg = tuple(fuv_grid) if fuv_grid else \
+        ((128, 128, 256) if nz <= 192 else ((160, 160, 320) if nz <= 256 else (256, 256, 512)))   # sim.py:756
+    return (int(nu), int(nphi)), tuple(int(v) for v in fg)
+
+
+class Sim:
+    """GPU-resident simulation on the GB300 kernels.
+
+    Sim("sheet", res=256); sim.step(4); sim.update_render_fields()
+    """
+
+    profile = False
+
+    def __init__(self, scenario="torus", res=None, params=None, ic_mode="synthetic", rays=None, fuv_grid=None,
+                 ion_every=None, device="cuda:0", verbose=True, fast=True, seed=None):
+        self.device = torch.device(device)
+        self.fast = fast
+        self.verbose = verbose
+        self.ic_mode = ic_mode
+        self.rays_override = rays
+        self.fuv_override = fuv_grid
+        self.ion_every_override = ion_every
+        self.prof = {}
+        self._h = None
+        self.reset(scenario, res, params, seed=seed)
+
+    # ------------------------------------------------------------------ construction
+    @classmethod
+    def from_state(cls, shape, dx, rho, stars, kinds, jets, jkinds, P, mom=None, rays=None, fuv_grid=None,
+                   ion_every=None, fast=True, device="cuda:0", verbose=False, start_main=True):
+        """An instance from explicit fields and star lists (what the reference's reset() leaves
+        behind, sim.py:710-795), e.g. initial conditions built by the reference's own IC code."""
+        self = cls.__new__(cls)
+        self.device = torch.device(device)
+        self.fast = fast
+        self.verbose = verbose
+        self.ic_mode = "state"
+        self.rays_override = rays
+        self.fuv_override = fuv_grid
+        self.ion_every_override = ion_every
+        self.prof = {}
+        self._h = None
+        self.scenario = "state"
+        self.res = None
+        ic = dict(shape=tuple(shape), dx=float(dx), rho=rho, mom=mom, stars=stars, kinds=kinds, jets=jets,
+                  jkinds=jkinds, P={})
+        self._setup(ic, dict(P), start_main=start_main)
+        return self
+
+    def reset(self, scenario=None, res=None, params=None, seed=None):
+        if scenario is not None:
+            self.scenario = scenario
+        if self.scenario not in _ics.SCENARIOS:
+            raise ValueError(f"unknown scenario {self.scenario!r}; synthetic scenarios: {sorted(_ics.SCENARIOS)}")
+        gen = _ics.SCENARIOS[self.scenario]
+        kw = {"device": self.device}
+        if res is not None:
+            kw["res"] = int(res)
+        if seed is not None:
+            kw["seed"] = int(seed)
+        ic = gen(**kw)
+        self.res = kw.get("res")
+        self._setup(ic, dict(params or {}))
+
+    def _setup(self, ic, overrides, start_main=True):
+        t_setup = time.perf_counter()
+        self.close()
+        P = make_params(overrides, base=ic["P"])
+        for key, what in (("pre_t", "the pre-turbulence (stirring) phase"), ("trigger", "triggered star formation"),
+                          ("drive_main", "main-phase stirring")):
+            if float(P.get(key, 0.0) or 0.0) > 0.0:
+                raise NotImplementedError(f"{what} ({key} > 0) is outside this package's simulation step")
+        if P.get("crop"):
+            raise NotImplementedError("cropped domains are outside this package's simulation step")
+        self.P = P
+        self.shape = tuple(int(v) for v in ic["shape"])
+        nx, ny, nz = self.shape
+        if nz % 4:
+            raise ValueError("nz must be a multiple of 4 (16-byte rows for the TMA tiles)")
+        self.dx = float(ic["dx"])
+        self.L = (nx * self.dx, ny * self.dx, nz * self.dx)
+        dev = self.device
+        f32 = dict(device=dev, dtype=torch.float32)
+        self._rho = torch.as_tensor(ic["rho"]).to(**f32).contiguous().clone()
+        if ic.get("mom") is None:
+            m = [torch.zeros(self.shape, **f32) for _ in range(3)]
+        else:
+            m = [torch.as_tensor(v).to(**f32).contiguous().clone() for v in ic["mom"]]
+        self._mx, self._my, self._mz = m
+        self._xi = torch.zeros(self.shape, **f32)
+        self._stage = torch.zeros((4,) + self.shape, **f32)
+        hdt = torch.float32 if P.get("fp32_fields") else torch.float16
+        self._dfront = torch.full(self.shape, 1e3, device=dev, dtype=hdt)
+        self._g0 = torch.zeros(self.shape, device=dev, dtype=hdt)
+        self.stars = [tuple(float(v) for v in s) for s in ic["stars"]]
+        self.kinds = list(ic["kinds"])
+        self.jets = [tuple(float(v) for v in j[:3]) for j in ic["jets"]]
+        self.jkinds = list(ic["jkinds"])
+        self.cn2, self.ci2, self.vmax = sound_speeds(P)
+        Lx, Ly, Lz = self.L
+        self.diag = math.sqrt(Lx ** 2 + Ly ** 2 + Lz ** 2) + 0.6                    # sim.py:742
+        self.dr = (1.0 if self.fast else 0.5) * self.dx                             # sim.py:743
+        self.nsteps = int(self.diag / self.dr) + 1                                  # sim.py:744
+        self.cap = max(len(self.stars), int(P["max_stars"]))                        # sim.py:745
+        rays, fuv = _ray_budget(nz, self.fast, self.rays_override, self.fuv_override)
+        self.rfront = _Shape(rays)
+        self.att = _Shape(fuv)
+        self.ion_every = self.ion_every_override or (max(P["ion_every"], 3) if self.fast else P["ion_every"])
+        self.fuv_every = (8 if nz <= 160 else 16) if self.fast else 8               # sim.py:759
+        self._stream = torch.cuda.current_stream(dev) if dev.type == "cuda" else None
+        lib = _lib.load()
+        d = _lib.NbDesc()
+        d.abi_version = _lib.NB_ABI_VERSION
+        d.nx, d.ny, d.nz = nx, ny, nz
+        d.dx = self.dx
+        d.cn2, d.ci2, d.vmax = self.cn2, self.ci2, self.vmax
+        d.floor_rho = float(P["floor"])
+        d.cfl = float(P["cfl"])
+        d.solver = _lib.SOLVERS[P.get("solver", "rusanov")]
+        d.limiter = _lib.LIMITERS[P.get("limiter", "minmod")]
+        d.nu, d.nphi = rays
+        d.dr = self.dr
+        d.nsteps = self.nsteps
+        d.diag = self.diag
+        d.fnr, d.fnu, d.fnphi = fuv
+        d.fields_fp32 = 1 if P.get("fp32_fields") else 0
+        d.max_stars = min(256, max(self.cap, 1))
+        st = self._stage
+        n = nx * ny * nz
+        d.f = _lib.NbFields(self._rho.data_ptr(), self._mx.data_ptr(), self._my.data_ptr(), self._mz.data_ptr(),
+                            self._xi.data_ptr(), st.data_ptr(), self._dfront.data_ptr(), self._g0.data_ptr())
+        d.stream = self._stream.cuda_stream if self._stream is not None else None
+        h = C.c_void_p()
+        _lib.check(lib.nb_create(C.byref(d), C.byref(h)), None, "nb_create")
+        self._h = h
+        self._lib = lib
+        self._n = n
+        self._live_key = None
+        self._stars_key = None
+        self._dt_cap = None
+        self._it = 0
+        self.version = 0
+        self.rf_version = -1
+        self.fuv_version = -10 ** 9
+        self.generation = getattr(self, "generation", 0) + 1
+        self.events = []
+        self.births = []
+        self.n_born = 0
+        self.last_birth = -1e9
+        self.mach = None
+        self.sm0 = None
+        self.tp, self.ip = 0.0, 0
+        self.P_reset = dict(P)
+        self.q_main0 = P["q_main"]
+        self.phase = "main"
+        self._push(force=True)
+        if start_main:
+            self.ionize()                                                           # sim.py:806-818
+        self._sync()
+        self.setup_s = time.perf_counter() - t_setup
+        self.log(f"{self.scenario} grid {nx}x{ny}x{nz} ({n / 1e6:.1f}M cells) rays {rays[0]}x{rays[1]} "
+                 f"fuv {fuv} solver {P.get('solver')} setup {self.setup_s:.2f}s, {len(self.stars)} stars")
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._sync()
+            self._lib.nb_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # ------------------------------------------------------------------ helpers
+    def log(self, *a):
+        if self.verbose:
+            print("[sim]", *a, flush=True)
+
+    def _sync(self):
+        if self._stream is not None:
+            self._stream.synchronize()
+
+    def _tick(self, key, t0):
+        self.prof[key] = self.prof.get(key, 0.0) + (time.perf_counter() - t0)
+
+    def _chk(self, rc, what):
+        _lib.check(rc, self._h, what)
+
+    def _push(self, force=False):
+        """upload live parameters / the star table when they changed (P may be edited directly,
+        as bake.py does, sim.py:88-93 there)"""
+        P = self.P
+        cap = self._dt_cap if self._dt_cap is not None else -1.0
+        live = (float(P["q_main"]), float(P["wind"]), float(P["jet"]), float(P["jet_proto"]), float(P["jet_pulse"]),
+                float(P["jet_period"]), float(P["kappa_fuv"]), float(P.get("q_ramp", 0.0)), float(P["jet_angle"]),
+                float(P["jet_r"]), float(cap), 1 if self.phase == "main" else 0)
+        if force or live != self._live_key:
+            L = _lib.NbLive(*live)
+            self._chk(self._lib.nb_set_live(self._h, C.byref(L)), "nb_set_live")
+            self._live_key = live
+        skey = (tuple(self.stars), tuple(self.kinds), tuple(self.jets), tuple(self.jkinds))
+        if force or skey != self._stars_key:
+            n = len(self.stars)
+            arr = (_lib.NbStar * max(n, 1))()
+            for i, s in enumerate(self.stars):
+                a = self.jets[i] if i < len(self.jets) else (0.0, 0.0, 1.0)
+                jk = self.jkinds[i] if i < len(self.jkinds) else "none"
+                arr[i] = _lib.NbStar(s[0], s[1], s[2], s[3], s[4], a[0], a[1], a[2], _lib.STAR_KINDS[self.kinds[i]],
+                                     _lib.JET_KINDS[jk])
+            self._chk(self._lib.nb_set_stars(self._h, arr, n), "nb_set_stars")
+            self._stars_key = skey
+
+    # ------------------------------------------------------------------ fields
+    rho = property(lambda self: Field(self._rho))
+    mx = property(lambda self: Field(self._mx))
+    my = property(lambda self: Field(self._my))
+    mz = property(lambda self: Field(self._mz))
+    xi = property(lambda self: Field(self._xi))
+    stage = property(lambda self: Field(self._stage))
+    dfront = property(lambda self: Field(self._dfront))
+    g0 = property(lambda self: Field(self._g0))
+    r1 = property(lambda self: Field(self._stage[0]))
+    mx1 = property(lambda self: Field(self._stage[1]))
+    my1 = property(lambda self: Field(self._stage[2]))
+    mz1 = property(lambda self: Field(self._stage[3]))
+    xi_tmp = property(lambda self: Field(self._stage[0]))
+
+    def render_scratch(self):
+        """two RGBA16F grids (half4 views of the stage block), free between steps (sim.py:821-825)"""
+        b = self._stage.view(torch.float16).reshape(-1)
+        n = self._n
+        return (Field(b[:4 * n].view(self.shape + (4,))), Field(b[4 * n:8 * n].view(self.shape + (4,))))
+
+    # ------------------------------------------------------------------ clock (device resident)
+    def _clock(self):
+        c = _lib.NbClock()
+        self._chk(self._lib.nb_get_clock(self._h, C.byref(c)), "nb_get_clock")
+        return c
+
+    def _set_clock(self, t=None, dt=None, it=None):
+        c = self._clock()
+        c.t = c.t if t is None else float(t)
+        c.dt = c.dt if dt is None else float(dt)
+        c.it = c.it if it is None else int(it)
+        self._chk(self._lib.nb_set_clock(self._h, C.byref(c)), "nb_set_clock")
+        self._it = int(c.it)
+
+    t = property(lambda self: self._clock().t, lambda self, v: self._set_clock(t=v))
+    dt = property(lambda self: self._clock().dt, lambda self, v: self._set_clock(dt=v))
+    it = property(lambda self: self._it, lambda self, v: self._set_clock(it=v))
+
+    @property
+    def dt_cap(self):
+        return self._dt_cap
+
+    @dt_cap.setter
+    def dt_cap(self, v):
+        self._dt_cap = None if v is None else float(v)
+
+    # ------------------------------------------------------------------ physics pieces (host views)
+    def q_of(self, i):
+        s = self.stars[i]
+        return s[3] * self.P["q_main"] if self.kinds[i] == "main" else s[3]
+
+    def ramp(self, i, t=None):
+        t = self.t if t is None else t
+        age = t - self.stars[i][4]
+        if self.phase != "main" or age < 0.0:
+            return 0.0
+        tr = float(self.P.get("q_ramp", 0.0))
+        if tr <= 0.0 or age >= tr:
+            return 1.0
+        x = age / tr
+        s = x * x * (3.0 - 2.0 * x)
+        return max(s * s * s, 1e-4)
+
+    def q_eff(self, i, t=None):
+        return self.q_of(i) * self.ramp(i, t)
+
+    def jet_of(self, i):
+        k = self.jkinds[i]
+        return self.P["jet"] if k == "jet" else (self.P["jet_proto"] if k == "proto" else 0.0)
+
+    def active_stars(self):
+        if self.phase != "main":
+            return []
+        t = self.t
+        return [(s[0], s[1], s[2], self.q_eff(i, t) / self.P["q_main"], t - s[4]) for i, s in enumerate(self.stars)
+                if t >= s[4]]
+
+    # ------------------------------------------------------------------ the step
+    def ionize(self):
+        """sim.py:927-947: rays of every active star, front apply, smoothing, fp16 dfront"""
+        t0 = time.perf_counter()
+        self._push()
+        self._chk(self._lib.nb_ionize(self._h), "nb_ionize")
+        if self.profile:
+            self._sync()
+            self._tick("ionize", t0)
+
+    def fuv_field(self):
+        """sim.py:949-985: G0 of every active star into g0"""
+        self._push()
+        self._chk(self._lib.nb_fuv(self._h), "nb_fuv")
+
+    fuv_every = 8
+
+    def update_render_fields(self, force=False):
+        """sim.py:989-1007: recompute G0 when the simulation advanced, on the reference's cadence"""
+        if self.rf_version == self.version and not force:
+            return False
+        t0 = time.perf_counter()
+        t = self.t
+        n_on = sum(1 for s in self.stars if t >= s[4])
+        tr = float(self.P.get("q_ramp", 0.0))
+        ramping = tr > 0 and any(0.0 <= t - s[4] < tr for s in self.stars)
+        if ramping and self.version - self.fuv_version >= max(2, self.fuv_every // 4):
+            force = True
+        if (force or self.version - self.fuv_version >= self.fuv_every
+                or n_on != getattr(self, "fuv_nstars", -1) or self.phase != getattr(self, "fuv_phase", None)):
+            self.fuv_field()
+            self.fuv_version, self.fuv_nstars, self.fuv_phase = self.version, n_on, self.phase
+        self.rf_version = self.version
+        if self.profile:
+            self._sync()
+            self._tick("render_fields", t0)
+        return True
+
+    def step(self, k=1, sync=True):
+        """advance k main-phase steps (sim.py:1141-1152).  Returns wall seconds.  With sync=False
+        the steps are only enqueued on the stream."""
+        t0 = time.perf_counter()
+        self._push()
+        self._chk(self._lib.nb_step(self._h, int(k), int(self.ion_every)), "nb_step")
+        self._it += int(k)
+        self.version += int(k)
+        if sync:
+            self._sync()
+        self._tick("step", t0)
+        self.prof["n_steps"] = self.prof.get("n_steps", 0) + k
+        return time.perf_counter() - t0
+
+    def set_param(self, name, value):
+        """sim.py:1154-1166: live parameters take effect on the next step and are logged"""
+        old = self.P.get(name)
+        if isinstance(old, int) and not isinstance(old, bool):
+            value = int(round(value))
+        self.P[name] = value
+        if name in LIVE:
+            self.events.append((float(self.t if self.phase == "main" else 0.0), name, value))
+        return value
+
+    def replace_stars(self, stars, kinds, jets, jkinds):
+        """sim.py:1120-1133: an explicit star list (bake.py replays the preview's)"""
+        self.stars = [tuple(float(v) for v in s) for s in stars]
+        self.kinds = list(kinds)
+        self.jets = [tuple(float(v) for v in j[:3]) for j in jets]
+        self.jkinds = list(jkinds)
+        if len(self.stars) > self.cap:
+            self.cap = len(self.stars)
+            if self.cap > 256:
+                raise _lib.NebulaError("more than 256 stars")
+            self.close()
+            raise _lib.NebulaError("the star table grew past max_stars; rebuild the Sim with a larger max_stars")
+        if self.phase == "main":
+            self.ionize()
+
+    def stars_absolute(self):
+        st = [(s[0], s[1], s[2], self.q_of(i), s[4]) for i, s in enumerate(self.stars)]
+        jt = [(j[0], j[1], j[2], self.jet_of(i)) for i, j in enumerate(self.jets)]
+        return st, jt
+
+    # ------------------------------------------------------------------ timeline (snapshots)
+    def tau(self):
+        return self.t if self.phase == "main" else self.tp - self.P["pre_t"]
+
+    def get_state_meta(self):
+        """sim.py:1173-1183: everything but the big fields needed to resume from this moment"""
+        c = self._clock()
+        return dict(t=c.t, it=int(c.it), tp=self.tp, ip=self.ip, dt=c.dt, phase=self.phase, mach=self.mach,
+                    stars=list(self.stars), kinds=list(self.kinds), jets=list(self.jets), jkinds=list(self.jkinds),
+                    births=list(self.births), n_born=self.n_born, last_birth=self.last_birth, P=dict(self.P),
+                    n_events=len(self.events), sm0=self.sm0, drv=None, rng=None, noise_calls=0)
+
+    def set_state_meta(self, m):
+        """sim.py:1185-1211: after the fields were restored"""
+        for k in ("tp", "ip", "phase", "mach", "n_born", "last_birth", "sm0"):
+            setattr(self, k, m[k])
+        self.stars, self.kinds = list(m["stars"]), list(m["kinds"])
+        self.jets, self.jkinds = list(m["jets"]), list(m["jkinds"])
+        self.births = list(m["births"])
+        self.P = dict(m["P"])
+        self.events = self.events[:m["n_events"]]
+        self._set_clock(t=m["t"], dt=m["dt"], it=m["it"])
+        self._chk(self._lib.nb_invalidate(self._h), "nb_invalidate")
+        self._push(force=True)
+        self.version += 1
+        self.rf_version = self.version
+        self.fuv_version = self.version
+        self.fuv_nstars = sum(1 for s in self.stars if m["t"] >= s[4])
+        self.fuv_phase = self.phase
+
+    def time_label(self):
+        return f"t={self.t:.4f}"
+
+    def stats(self):
+        xi = self._xi
+        r = self._rho
+        return dict(ion=float(xi.double().mean()), rho_max=float(r.max()), rho_min=float(r.min()))
+
+    def conservation(self):
+        """FP64 totals (mass, x/y/z momentum) of the current state, times the cell volume."""
+        out = (C.c_double * 4)()
+        self._chk(self._lib.nb_reduce_fp64(self._h, out), "nb_reduce_fp64")
+        v = self.dx ** 3
+        return tuple(float(x) * v for x in out)
+
+    def invalidate(self):
+        """call after writing rho / m / xi directly: the next step recomputes the CFL max speed"""
+        self._chk(self._lib.nb_invalidate(self._h), "nb_invalidate")

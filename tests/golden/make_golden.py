@@ -1,0 +1,237 @@
+"""Generate the golden fixtures under tests/golden/ by running the REFERENCE's own
+kernel source and its `Sim` driver on small seeded inputs.
+
+    python tests/golden/make_golden.py [--ref /root/reference]
+
+The reference is NVIDIA-Warp Python; `warp` is absent here, so `warp_stub` supplies
+a float32 restatement of the Warp builtins its kernels call (see that module's
+docstring for exactly what it does and does not reproduce).  Everything else —
+the kernel bodies, `Sim.reset/_start_main/step/ionize/fuv_field/_compute_dt/
+_hydro/_set_star_weights`, the initial conditions — is the reference's code,
+imported unmodified from the reference checkout.
+
+Fixtures (all small, committed):
+  kernels.npz      per-kernel inputs/outputs: hydro_stage (Rusanov), hydro_stage_hll
+                   (minmod / van Leer / MC) for both RK2 stages, max_speed, cast_rays,
+                   apply_front, smooth_xi, cast_fuv, apply_fuv, to_half.
+  sim_<name>.npz   end-to-end reference `Sim` runs: the state after reset (first
+                   ionization included) and after every step, clocks, the FUV field.
+Test infrastructure only: nothing in the product reads these files.
+"""
+import argparse
+import json
+import math
+import os
+import sys
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+import warp_stub  # noqa: E402
+
+warp_stub.install()
+
+
+def import_reference(ref):
+    sys.path.insert(0, ref)
+    sys.dont_write_bytecode = True
+    import nebula3d  # noqa: F401
+    import sim as refsim
+    return sys.modules["nebula3d"], refsim
+
+
+def f32(x):
+    return np.asarray(x, np.float32)
+
+
+# ----------------------------------------------------------------------------- per-kernel cases
+def kernel_cases(N, S, rng):
+    wp = warp_stub
+    out = {}
+    nx, ny, nz = 10, 9, 8
+    dx = 1.0 / nz
+    shape = (nx, ny, nz)
+    rho = np.exp(rng.normal(0.0, 1.2, shape)).astype(np.float32)
+    rho[rng.random(shape) < 0.06] = 1e-3               # below the floor (2e-3): exercises max(rho, floor)
+    vel = rng.normal(0.0, 1.5, (3,) + shape).astype(np.float32)
+    vel[:, rng.random(shape) < 0.05] *= 8.0            # a few cells above vmax = 6
+    mom = (vel * rho).astype(np.float32)
+    xi = rng.random(shape).astype(np.float32)
+    xi[rng.random(shape) < 0.2] = 0.0
+    xi[rng.random(shape) < 0.1] = 1.0
+    L = np.array(shape) * dx
+    stars = np.array([[0.45 * L[0], 0.55 * L[1], 0.5 * L[2], 1.0],
+                      [0.2 * L[0], 0.3 * L[1], 0.7 * L[2], 0.4],
+                      [0.8 * L[0], 0.7 * L[1], 0.2 * L[2], 0.0]], np.float32)       # last one off
+    ax = rng.normal(size=(3, 3))
+    ax /= np.linalg.norm(ax, axis=1, keepdims=True)
+    jets = np.concatenate([ax, np.array([[3.0], [0.0], [2.0]])], 1).astype(np.float32)
+    cn2, ci2, floor, vmax = (1.0 / 12.0) ** 2, 1.0, 2e-3, 6.0
+    jet_cos, jet_r, pulse, wind = math.cos(math.radians(30.0)), 0.3, 1.3, 0.5
+    smax = np.zeros(1, np.float32)
+    N.max_speed.run(shape, [rho, mom[0], mom[1], mom[2], xi, cn2, ci2, smax])
+    dt = 0.3 * dx / float(smax[0])
+    out.update(k_rho=rho, k_mom=mom, k_xi=xi, k_stars=stars, k_jets=jets, k_smax=smax.copy(),
+               k_scalars=np.array([dx, cn2, ci2, floor, vmax, jet_cos, jet_r, pulse, wind, dt], np.float64))
+    sv = [wp.vec4(*s) for s in stars]
+    jv = [wp.vec4(*j) for j in jets]
+    for name, kern, lim in (("rus", N.hydro_stage, None), ("hll0", S.hydro_stage_hll, 0),
+                            ("hll1", S.hydro_stage_hll, 1), ("hll2", S.hydro_stage_hll, 2)):
+        t0 = time.time()
+        o1 = np.zeros((4,) + shape, np.float32)
+        common = [sv, len(sv), wind, jv, jet_cos, jet_r, pulse, dt, dx]
+        tail = [floor, cn2, ci2, vmax] + ([lim] if lim is not None else [])
+        kern.run(shape, [rho, mom[0], mom[1], mom[2], xi, rho, mom[0], mom[1], mom[2],
+                         o1[0], o1[1], o1[2], o1[3]] + common + [0.0, 1.0] + tail)
+        o2 = np.zeros((4,) + shape, np.float32)
+        kern.run(shape, [o1[0], o1[1], o1[2], o1[3], xi, rho, mom[0], mom[1], mom[2],
+                         o2[0], o2[1], o2[2], o2[3]] + common + [0.5, 0.5] + tail)
+        out[f"k_{name}_s1"] = o1
+        out[f"k_{name}_s2"] = o2
+        print(f"  hydro {name}: {time.time() - t0:.1f}s", flush=True)
+
+    # ---- ionization: a dense blob so some rays stop and some reach rcap
+    g = (np.indices(shape).transpose(1, 2, 3, 0) + 0.5) * dx
+    blob = 30.0 * np.exp(-np.sum((g - np.array([0.6, 0.5, 0.45]) * L) ** 2, -1) / (2 * 0.12 ** 2))
+    rrho = (rho * 0.5 + blob).astype(np.float32)
+    diag = float(math.sqrt(float(np.sum(L ** 2))) + 0.6)
+    bmax = wp.vec3(*L)
+    ray_stars = [(0.45 * L[0], 0.55 * L[1], 0.5 * L[2], 2e-2),
+                 (0.15 * L[0], 0.8 * L[1], 0.3 * L[2], 4e-1),
+                 (-0.3, 0.4 * L[1], 0.5 * L[2], 3.0)]          # outside the box: t_in > 0
+    nu, nphi = 6, 12
+    out["r_rho"] = rrho
+    out["r_stars"] = np.array(ray_stars, np.float64)
+    out["r_meta"] = np.array([nu, nphi, diag], np.float64)
+    for tag, drf in (("full", 1.0), ("half", 0.5)):
+        dr = drf * dx
+        nsteps = int(diag / dr) + 1
+        xi_a = np.zeros(shape, np.float32)
+        df_a = np.full(shape, 1e3, np.float32)
+        rfs = []
+        for (sx, sy, sz, Q) in ray_stars:
+            rf = np.zeros((nu, nphi), np.float32)
+            svec = wp.vec3(sx, sy, sz)
+            N.cast_rays.run((nu, nphi), [rrho, svec, Q, dr, nsteps, dx, diag, bmax, rf])
+            N.apply_front.run(shape, [rf, svec, dx, 1.2 * dx, xi_a, df_a])
+            rfs.append(rf)
+        xi_raw = xi_a.copy()
+        xs = np.zeros(shape, np.float32)
+        N.smooth_xi.run(shape, [xi_a, xs])
+        out[f"r_{tag}_rfront"] = np.stack(rfs)
+        out[f"r_{tag}_xi_raw"] = xi_raw
+        out[f"r_{tag}_df"] = df_a
+        out[f"r_{tag}_xi"] = xs
+        out[f"r_{tag}_nsteps"] = np.array([nsteps])
+    print("  rays done", flush=True)
+
+    # ---- FUV: reuse the smoothed xi from the full-step ionization
+    fnr, fnu, fnp = 5, 4, 8
+    binr = diag / fnr
+    kappa = 10.0
+    g0 = np.zeros(shape, np.float32)
+    atts = []
+    dr = dx
+    nsteps = int(diag / dr) + 1
+    for (sx, sy, sz, Q) in ray_stars:
+        att = np.zeros((fnr, fnu, fnp), np.float32)
+        svec = wp.vec3(sx, sy, sz)
+        N.cast_fuv.run((fnu, fnp), [rrho, out["r_full_xi"], svec, kappa, dr, nsteps, dx, binr, bmax, att])
+        N.apply_fuv.run(shape, [att, svec, Q / 0.1, dx, binr, g0])
+        atts.append(att)
+    out["f_att"] = np.stack(atts)
+    out["f_g0"] = g0
+    out["f_meta"] = np.array([fnr, fnu, fnp, kappa, binr, nsteps], np.float64)
+    h = np.array([0.0, -0.0, 1e-8, 3.14159, 65504.0, 65519.0, 65520.0, 1e6, -2.5e-5, 1000.0, 0.1],
+                 np.float32).reshape(1, 1, 11)
+    ho = np.zeros(h.shape, np.float16)
+    S.to_half.run(h.shape, [h, ho])
+    out["h_in"], out["h_out"] = h, ho
+    print("  fuv / to_half done", flush=True)
+    return out
+
+
+# ----------------------------------------------------------------------------- reference Sim runs
+def sim_case(S, scenario, res, overrides, nsteps, fast, rays, fuv, ion_every=None, dt_cap_at=None):
+    P = S.make_params(scenario, overrides)
+    t0 = time.time()
+    sim = S.Sim(scenario, res=res, params=P, ic_mode="matched", rays=rays, fuv_grid=fuv,
+                ion_every=ion_every, device="cpu", verbose=False, fast=fast)
+    print(f"  {scenario} {sim.shape} reset {time.time() - t0:.1f}s, {len(sim.stars)} stars", flush=True)
+
+    def snap():
+        return dict(rho=sim.rho.numpy(), mx=sim.mx.numpy(), my=sim.my.numpy(), mz=sim.mz.numpy(),
+                    xi=sim.xi.numpy(), dfront=sim.dfront.numpy())
+
+    s0 = snap()
+    rho0 = s0["rho"]
+    meta = dict(scenario=scenario, res=res, shape=list(sim.shape), dx=sim.dx, L=list(sim.L), fast=fast,
+                rays=list(rays), fuv=list(fuv), ion_every=sim.ion_every, fuv_every=sim.fuv_every,
+                stars=[list(map(float, s)) for s in sim.stars], kinds=list(sim.kinds),
+                jets=[list(map(float, j)) for j in sim.jets], jkinds=list(sim.jkinds),
+                P={k: v for k, v in sim.P.items() if isinstance(v, (int, float, str, bool, type(None), list))},
+                dr=sim.dr, nsteps=sim.nsteps, diag=sim.diag, cap=sim.cap, cn2=sim.cn2, ci2=sim.ci2,
+                dt_caps=[])
+    steps = []
+    for n in range(nsteps):
+        cap = None
+        if dt_cap_at is not None and n == dt_cap_at:
+            cap = 0.5 * sim.P["cfl"] * sim.dx / 12.0
+        sim.dt_cap = cap
+        meta["dt_caps"].append(cap)
+        t1 = time.time()
+        sim.step(1)
+        st = snap()
+        st.update(t=sim.t, dt=sim.dt, it=sim.it)
+        steps.append(st)
+        print(f"    step {n}: t={sim.t:.6g} dt={sim.dt:.6g} ({time.time() - t1:.1f}s)", flush=True)
+    sim.dt_cap = None
+    sim.update_render_fields(force=True)
+    g0 = sim.g0.numpy()
+    out = {"meta": np.array(json.dumps(meta)), "rho_ic": rho0}
+    # the state right after reset (includes _start_main's first ionization)
+    for k, v in s0.items():
+        out[f"s0_{k}"] = v
+    for n, st in enumerate(steps):
+        for k, v in st.items():
+            out[f"s{n + 1}_{k}"] = np.asarray(v)
+    out["g0"] = g0
+    return out
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--only", default=None)
+    a = ap.parse_args()
+    N, S = import_reference(a.ref)
+    rng = np.random.default_rng(20261203)
+    if a.only in (None, "kernels"):
+        print("kernels:", flush=True)
+        np.savez_compressed(os.path.join(HERE, "kernels.npz"), **kernel_cases(N, S, rng))
+    cases = {
+        # bubbles: 6 stars, wind, HLL + minmod, fast-mode budgets (dr = dx, ionize every 3 steps)
+        "bubbles": dict(scenario="bubbles", res=8, overrides=dict(pre_t=0.0, trigger=0.0, seed=5, min_sep=0.2),
+                        nsteps=6, fast=True, rays=(8, 16), fuv=(6, 8, 16)),
+        # bipolar: jets (cone widened to reach cell centres at this resolution), wind, q ramp, MC limiter,
+        # bake-mode budgets (dr = dx/2, ionize every 2 steps), and one dt_cap step
+        "bipolar": dict(scenario="bipolar", res=8, overrides=dict(pre_t=0.0, seed=7, jet_r=0.35, jet_angle=35.0,
+                                                                  limiter="mc", clumps=0),
+                        nsteps=3, fast=False, rays=(8, 16), fuv=(6, 8, 16), dt_cap_at=1),
+        # cliff: Rusanov solver, embedded stars that switch on later, van Leer is ignored by Rusanov
+        "cliff": dict(scenario="cliff", res=8, overrides=dict(pre_t=0.0, seed=11, solver="rusanov", n_embedded=2,
+                                                              globules=10),
+                      nsteps=3, fast=True, rays=(8, 16), fuv=(6, 8, 16), ion_every=2),
+    }
+    for name, c in cases.items():
+        if a.only not in (None, name):
+            continue
+        print(f"sim {name}:", flush=True)
+        np.savez_compressed(os.path.join(HERE, f"sim_{name}.npz"), **sim_case(S, **c))
+    print("done")
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,91 @@
+"""CPU tests: the C-ABI library loads and exports every symbol include/nebula.h declares;
+host-side logic (parameters, ray budgets, initial conditions, ctypes layouts)."""
+import ctypes as C
+import os
+import re
+
+import numpy as np
+import pytest
+
+from conftest import ROOT
+
+
+def header_symbols():
+    src = open(os.path.join(ROOT, "include", "nebula.h")).read()
+    return sorted(set(re.findall(r"^\s*(?:int|void|const char\*)\s+(nb_\w+)\s*\(", src, re.M)))
+
+
+def test_library_exports_every_declared_symbol(lib_built):
+    from nebulaviewer_gb300 import _lib
+    names = header_symbols()
+    assert len(names) >= 17
+    for n in names:
+        assert hasattr(lib_built, n), n
+    assert set(names) == set(_lib.SIGNATURES), "ctypes signatures must cover the header exactly"
+
+
+def test_struct_layouts_match_header():
+    """field order / sizes of the ctypes mirrors (x86-64 and aarch64 share this ABI)"""
+    from nebulaviewer_gb300 import _lib
+    assert C.sizeof(_lib.NbStar) == 8 * 8 + 2 * 4
+    assert C.sizeof(_lib.NbClock) == 24
+    assert _lib.NbDesc.f.offset % 8 == 0
+    assert C.sizeof(_lib.NbLive) == 11 * 8 + 8
+
+
+def test_null_handle_errors_without_gpu(lib_built):
+    from nebulaviewer_gb300 import _lib
+    lib = _lib.load()
+    assert lib.nb_step(None, 1, 1) == -1
+    assert b"null" in lib.nb_last_error(None)
+    d = _lib.NbDesc()
+    d.abi_version = 999
+    h = C.c_void_p()
+    assert lib.nb_create(C.byref(d), C.byref(h)) == -1
+    assert b"abi" in lib.nb_last_error(None)
+    d.abi_version = _lib.NB_ABI_VERSION
+    d.nx, d.ny, d.nz = 8, 8, 6           # nz not a multiple of 4
+    assert lib.nb_create(C.byref(d), C.byref(h)) == -1
+
+
+def test_params_defaults_and_sound_speeds():
+    from nebulaviewer_gb300.params import make_params, sound_speeds
+    P = make_params()
+    assert P["cfl"] == 0.3 and P["floor"] == 2e-3 and P["solver"] == "hll" and P["q_ramp"] == 0.02
+    assert sound_speeds(P) == ((1 / 12.0) ** 2, 1.0, 6.0)
+    assert sound_speeds(dict(P, cn2=1.0, ci2=144.0, vmax=72.0)) == (1.0, 144.0, 72.0)
+
+
+def test_ray_budget_matches_reference_rule():
+    from nebulaviewer_gb300.sim import _ray_budget
+    assert _ray_budget(256, True, None, None) == ((512, 1024), (160, 160, 320))
+    assert _ray_budget(128, True, None, None) == ((512, 1024), (128, 128, 256))
+    assert _ray_budget(512, True, None, None) == ((1024, 2048), (256, 256, 512))
+    assert _ray_budget(64, False, (8, 16), (4, 8, 16)) == ((8, 16), (4, 8, 16))
+
+
+def test_synthetic_ics_are_seeded_and_shaped():
+    from nebulaviewer_gb300 import ics
+    a = ics.torus(res=8)
+    b = ics.torus(res=8)
+    assert a["rho"].shape == (16, 16, 16)
+    assert np.array_equal(a["rho"].numpy(), b["rho"].numpy())
+    assert abs(a["stars"][0][0] - 1.0) < 1e-12 and abs(a["P"]["q_main"] - 0.25 ** 3 / 3) < 1e-15
+    s = ics.sheet(res=32)
+    assert s["rho"].shape == (32, 32, 32) and len(s["stars"]) == 6
+    v = np.stack([m.numpy() / s["rho"].numpy() for m in s["mom"]])
+    assert 2.0 < np.sqrt((v ** 2).sum(0).mean()) < 8.0          # rms Mach ~5 at cs_n = 1
+    c = ics.cliffwall(res=32, nclumps=4)
+    r = c["rho"].numpy()
+    assert r[:4].max() < 3.0 and r[-4:].min() > 150.0
+
+
+def test_product_path_does_not_import_the_oracle():
+    """the package must never route through the CPU oracle"""
+    pkg = os.path.join(ROOT, "nebulaviewer_gb300")
+    for dirpath, _, files in os.walk(pkg):
+        for f in files:
+            if f.endswith((".py", ".cu", ".cuh", ".h")):
+                src = open(os.path.join(dirpath, f)).read()
+                assert not re.search(r"^\s*(import|from)\s+oracle\b", src, re.M), f
+                assert "liboracle" not in src and "ref_cpu" not in src, f
