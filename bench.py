@@ -1,0 +1,366 @@
+"""Benchmark of the simulation step: Gcell-updates/s (hydro + ionization) on one GB300,
+the HBM-roofline fraction of the dominant kernel, and the CPU baseline beside it.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+Workload (one "step" = one main-phase simulation step, sim.py:1099-1114, plus the FUV field
+on the viewer's cadence): the turbulent sheet at 256^3 FP32 (Gaussian slab n = 50, k^-4
+velocity field of rms Mach 5, log-normal density sigma 0.5), six stars with log-uniform
+photon rates, winds on, ionization every 3 steps with 512 x 1024 rays (dr = dx), FUV every
+16 steps on a 160 x 160 x 320 grid -- the reference Sim's fast-mode budgets for this grid
+(sim.py:753-759).  HLL + minmod, RK2, CFL 0.3, cs_n = 1, cs_i = 12.  Synthetic seeded data.
+
+--impl reference times the reference scheme's CPU implementation (the CPU restatement of its
+kernels in oracle/, all host threads) on the same workload and metric.
+Under torchrun (N > 1) every rank advances its own independent instance (replicas; the path
+does not shard) and the job throughput is N x cells x steps / max-over-ranks time.
+"""
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Gcell-updates/s (hydro+ion)"
+UNIT = "Gcell-updates/s"
+RES = 256
+
+
+def workload(res):
+    rays = "512x1024" if res <= 256 else "1024x2048"
+    fuv = "128x128x256" if res <= 192 else ("160x160x320" if res <= 256 else "256x256x512")
+    return (f"turbulent sheet {res}^3 fp32, 6 stars, wind on, ionization every 3 steps ({rays} rays, dr=dx), "
+            f"FUV every {8 if res <= 160 else 16} steps ({fuv} grid), HLL+minmod RK2 CFL 0.3")
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def ncu_traffic():
+    """per-launch DRAM bytes of kernels at this workload, from the committed ncu summary"""
+    p = os.path.join(ROOT, "profiles", "traffic_sheet256.txt")   # per-launch DRAM bytes at 256^3
+    out = {}
+    if os.path.exists(p):
+        for line in open(p):
+            parts = line.split()
+            if len(parts) >= 2 and not line.startswith("#"):
+                try:
+                    out[parts[0]] = float(parts[1])
+                except ValueError:
+                    pass
+    return out
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms during the timed region"""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.p = None
+
+    def __enter__(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.p = None
+        return self
+
+    def __exit__(self, *a):
+        self.lines = []
+        if self.p is not None:
+            self.p.terminate()
+            try:
+                out, _ = self.p.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.p.kill()
+                out, _ = self.p.communicate()
+            self.lines = [ln for ln in out.splitlines() if ln.strip()]
+
+    def summary(self):
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in getattr(self, "lines", []):
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = max(mx, float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def algorithmic_bytes(kind, ncell, nstars):
+    """compulsory HBM bytes of one launch of each kernel kind (per cell: float32 state)"""
+    per = {"stage1": 36, "stage2": 52, "cast_rays": 4 * nstars, "apply_front": 6, "smooth": 24,
+           "cast_fuv": 8 * nstars, "apply_fuv": 2, "max_speed": 20, "ctrl": 0}
+    return per.get(kind, 0) * ncell
+
+
+def cpu_sample(ic_host, steps=3):
+    """the oracle (reference scheme, CPU restatement) on a bounded sample of the workload"""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    from nebulaviewer_gb300.params import make_params, sound_speeds
+    P = make_params(base=ic_host["P"])
+    cn2, ci2, vmax = sound_speeds(P)
+    o = O.OracleSim(ic_host["shape"], ic_host["dx"], ic_host["rho"], ic_host["stars"], ic_host["kinds"],
+                    ic_host["jets"], ic_host["jkinds"], P, mom=ic_host["mom"], cn2=cn2, ci2=ci2, vmax=vmax)
+    t0 = time.perf_counter()
+    o.step(steps)
+    t1 = time.perf_counter()
+    o.fuv_field()
+    t2 = time.perf_counter()
+    # per step: the steps (1 ionization in 3) plus the FUV field amortized on its 16-step cadence
+    per_step = (t1 - t0) / steps + (t2 - t1) / o.fuv_every
+    ncell = math.prod(ic_host["shape"])
+    return ncell / per_step / 1e9, O.threads(), per_step, o
+
+
+def host_ic(sim):
+    """the instance's initial state on the host (the CPU arm starts from the same fields)"""
+    import numpy as np
+    return dict(shape=sim.shape, dx=sim.dx, rho=sim.rho.numpy().astype(np.float32),
+                mom=[sim.mx.numpy(), sim.my.numpy(), sim.mz.numpy()], stars=list(sim.stars),
+                kinds=list(sim.kinds), jets=list(sim.jets), jkinds=list(sim.jkinds), P=dict(sim.P))
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    import torch
+    from nebulaviewer_gb300 import ics
+    dev = "cuda" if torch.cuda.is_available() else "cpu"
+    ic = ics.sheet(res=args.res, device=dev)
+    import numpy as np
+    ic_host = dict(ic, rho=ic["rho"].cpu().numpy(), mom=[m.cpu().numpy() for m in ic["mom"]])
+    del ic
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    from nebulaviewer_gb300.params import make_params, sound_speeds
+    P = make_params(base=ic_host["P"])
+    cn2, ci2, vmax = sound_speeds(P)
+    o = O.OracleSim(ic_host["shape"], ic_host["dx"], ic_host["rho"], ic_host["stars"], ic_host["kinds"],
+                    ic_host["jets"], ic_host["jkinds"], P, mom=ic_host["mom"], cn2=cn2, ci2=ci2, vmax=vmax)
+    for _ in range(min(args.warmup, 1)):
+        o.step(1)
+    budget = 150.0
+    t0 = time.perf_counter()
+    done = 0
+    for n in range(args.steps):
+        o.step(1)
+        if o.version % o.fuv_every == 0:
+            o.fuv_field()
+        done += 1
+        if time.perf_counter() - t0 > budget:
+            break
+    el = time.perf_counter() - t0
+    ncell = math.prod(ic_host["shape"])
+    val = ncell * done / el / 1e9
+    cores = O.threads()
+    sample = f"{done} of {args.steps} requested steps of the {workload(args.res)} (bounded to {budget:.0f} s)"
+    line = {"impl": "reference", "metric": METRIC, "value": val, "unit": UNIT, "n_gpus": ws, "steps": done,
+            "warmup": min(args.warmup, 1), "ms_per_step": el / done * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": workload(args.res), "grid": [args.res] * 3, "parallelism": "cpu threads"},
+            "cpu_baseline": {"value": val, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
+            "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_gb300(args):
+    import ctypes as C
+    import torch
+    ws, rank, local = dist_env()
+    from nebulaviewer_gb300 import build as nb_build
+    if rank == 0:
+        nb_build.build(verbose=False)
+    dist = None
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+        dist.barrier()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    from nebulaviewer_gb300 import _lib
+    from nebulaviewer_gb300.sim import Sim
+    lib = _lib.load()
+    sim = Sim("sheet", res=args.res, device=dev, verbose=False)
+    ncell = sim._n
+    nstars = len(sim.stars)
+    ic_host = host_ic(sim) if (rank == 0 and ws == 1 and not args.no_cpu_baseline) else None
+    pinned0 = [t.detach().to("cpu").pin_memory() for t in (sim._rho, sim._mx, sim._my, sim._mz)]
+    stream = torch.cuda.current_stream(dev)
+
+    def device_steps(k):
+        for _ in range(k):
+            sim.step(1, sync=False)
+            if sim.version % sim.fuv_every == 0:          # the render-field cadence (sim.py:997-1002)
+                sim.fuv_field()
+
+    device_steps(args.warmup)
+    torch.cuda.synchronize(dev)
+    # ---------------- device-resident throughput (the metric's value)
+    lib.nb_profile(sim._h, 1)
+    prof_ms = (C.c_double * 16)()
+    prof_n = (C.c_longlong * 16)()
+    lib.nb_profile_read(sim._h, prof_ms, prof_n)          # discard the warm-up records
+    l0 = C.c_longlong()
+    lib.nb_counters(sim._h, C.byref(l0))
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize(dev)
+    with ClockSampler(local) as clk:
+        ev0.record(stream)
+        device_steps(args.steps)
+        ev1.record(stream)
+        torch.cuda.synchronize(dev)
+    if dist:
+        dist.barrier()
+    el_ms = ev0.elapsed_time(ev1)
+    lib.nb_profile_read(sim._h, prof_ms, prof_n)
+    lib.nb_profile(sim._h, 0)
+    l1 = C.c_longlong()
+    lib.nb_counters(sim._h, C.byref(l1))
+    launches = int(l1.value - l0.value)
+    t_max = el_ms
+    if dist:
+        t = torch.tensor([el_ms], device=dev, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_max = float(t.item())
+    value = ws * ncell * args.steps / (t_max * 1e-3) / 1e9
+    # ---------------- end to end through the public API with host buffers
+    # every step: sim.step(1) (returns after the step finished), the live-parameter block
+    # pushed H2D as a caller that edits P each step does (bake.py), and the clock read D2H
+    # (sim.t, as bake.py reads it every step); around the steps: the initial state uploaded
+    # from pinned host memory and the result fields (rho, xi) read back to pinned memory.
+    out_host = [torch.empty(sim.shape, dtype=torch.float32).pin_memory() for _ in range(2)]
+    e2e_steps = args.steps
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    for dst, src in zip((sim._rho, sim._mx, sim._my, sim._mz), pinned0):
+        dst.copy_(src, non_blocking=True)
+    sim.invalidate()
+    h2d_live = C.sizeof(_lib.NbLive)
+    for _ in range(e2e_steps):
+        sim._live_key = None                               # force the H2D push of the live block
+        sim.step(1)
+        sim.update_render_fields()
+        _ = sim.t
+    out_host[0].copy_(sim._rho, non_blocking=True)
+    out_host[1].copy_(sim._xi, non_blocking=True)
+    torch.cuda.synchronize(dev)
+    e2e_s = time.perf_counter() - t0
+    if dist:
+        t = torch.tensor([e2e_s], device=dev, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e_val = ws * ncell * e2e_steps / e2e_s / 1e9
+    h2d = (16 * ncell) / e2e_steps + h2d_live
+    d2h = (8 * ncell) / e2e_steps + C.sizeof(_lib.NbClock)
+    # ---------------- roofline of the dominant kernel
+    peak, peak_kind = measured_peaks()
+    kinds = {}
+    for i, name in enumerate(_lib.PROF_KINDS):
+        if prof_n[i]:
+            kinds[name] = (prof_ms[i], int(prof_n[i]))
+    dom = max(kinds, key=lambda k: kinds[k][0])
+    dom_ms, dom_n = kinds[dom]
+    dom_bytes = algorithmic_bytes(dom, ncell, nstars)
+    achieved = dom_bytes / (dom_ms / dom_n * 1e-3) / 1e9
+    traffic = ncu_traffic().get(dom) if args.res == RES else None
+    ion_every, fuv_every = sim.ion_every, sim.fuv_every
+    b_step = 108 + (4 * nstars + 14) / ion_every + (8 * nstars + 2) / fuv_every
+    step_gbs = b_step * ncell * args.steps / (el_ms * 1e-3) / 1e9
+    clocks = clk.summary()
+    res = None
+    if rank == 0:
+        res = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": workload(args.res), "grid": list(sim.shape), "stars": nstars, "ion_every": ion_every,
+                       "fuv_every": fuv_every, "rays": list(sim.rfront.shape), "fuv_grid": list(sim.att.shape),
+                       "parallelism": f"replicas x{ws}", "l2": f"state {40 * ncell / 1e9:.2f} GB vs 129 MB L2 (no flush)"},
+            "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "peak_source": peak_kind,
+                         "traffic": traffic, "algorithmic_bytes_per_launch": dom_bytes,
+                         "avg_launch_ms": dom_ms / dom_n},
+            "step_roofline": {"bytes_per_cell_step": b_step, "achieved": step_gbs, "peak": peak, "unit": "GB/s",
+                              "frac": step_gbs / peak},
+            "kernels_ms": {k: {"ms_total": v[0], "launches": v[1], "share": v[0] / sum(x[0] for x in kinds.values())}
+                           for k, v in kinds.items()},
+            "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                    "how": "Sim.step(1) + update_render_fields + clock read per step; state upload from pinned "
+                           "host memory and rho/xi read-back inside the timed region"},
+            "gpu_launches": launches,
+            "clocks": clocks,
+        }
+    sim.close()
+    if rank == 0 and ic_host is not None:
+        cv, cores, per_step, _ = cpu_sample(ic_host, steps=3)
+        res["cpu_baseline"] = {"value": cv, "unit": UNIT, "cores": cores, "kind": "port",
+                               "sample": f"3 steps (1 ionization) + 1 FUV field amortized over 16 steps of the same "
+                                         f"{args.res}^3 workload, oracle/ref_cpu.cpp with OpenMP ({per_step:.2f} s/step)"}
+    if rank == 0:
+        print(json.dumps(res), flush=True)
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=96)
+    ap.add_argument("--warmup", type=int, default=6)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--res", type=int, default=RES, help="grid size (the workload is defined at 256)")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gb300(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

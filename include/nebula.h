@@ -163,6 +163,26 @@ int nb_cast_rays(nb_handle h, const double star_xyz[3], double Q, float* rfront_
 int nb_cast_fuv(nb_handle h, const double star_xyz[3], float* att_out);
 
 /* ---------------------------------------------------------------- diagnostics */
+/* Kernel kinds timed by nb_profile (CUDA events on the handle's stream around each launch). */
+enum {
+    NB_PROF_CTRL = 0,         /* star weights / dt / pulse (sim.py:914-925, 1009-1012, 1108) */
+    NB_PROF_STAGE1 = 1,       /* hydro RK2 stage 1 */
+    NB_PROF_STAGE2 = 2,       /* hydro RK2 stage 2 (+ CFL max speed) */
+    NB_PROF_CAST_RAYS = 3,    /* nebula3d.py:247-270 */
+    NB_PROF_APPLY_FRONT = 4,  /* nebula3d.py:281-307, all stars */
+    NB_PROF_SMOOTH = 5,       /* nebula3d.py:310-315 (+ CFL max speed) */
+    NB_PROF_CAST_FUV = 6,     /* nebula3d.py:320-352 */
+    NB_PROF_APPLY_FUV = 7,    /* nebula3d.py:355-388, all stars */
+    NB_PROF_MAX_SPEED = 8,    /* nebula3d.py:154-162 stand-alone */
+    NB_PROF_KINDS = 16
+};
+/* No reference counterpart (the reference times whole calls with perf_counter, sim.py:578-579):
+ * enable / disable per-kernel CUDA-event timing; nb_profile_read synchronizes, returns the
+ * summed milliseconds and launch counts per kind since the last read, and resets them. */
+int nb_profile(nb_handle h, int enable);
+int nb_profile_read(nb_handle h, double ms[NB_PROF_KINDS], long long count[NB_PROF_KINDS]);
+/* Number of kernels the handle has launched (a claim the benchmark reports). */
+int nb_counters(nb_handle h, long long* launches);
 /* FP64 conservation totals: sum rho, sum mx, sum my, sum mz (times dx^3 = mass/momentum). */
 int nb_reduce_fp64(nb_handle h, double out[4]);
 

@@ -70,7 +70,11 @@ SIGNATURES = {
     "nb_cast_rays": (C.c_int, [_P, C.c_double * 3, C.c_double, _P]),
     "nb_cast_fuv": (C.c_int, [_P, C.c_double * 3, _P]),
     "nb_reduce_fp64": (C.c_int, [_P, C.c_double * 4]),
+    "nb_profile": (C.c_int, [_P, C.c_int]),
+    "nb_profile_read": (C.c_int, [_P, C.c_double * 16, C.c_longlong * 16]),
+    "nb_counters": (C.c_int, [_P, C.POINTER(C.c_longlong)]),
 }
+PROF_KINDS = ["ctrl", "stage1", "stage2", "cast_rays", "apply_front", "smooth", "cast_fuv", "apply_fuv", "max_speed"]
 
 _lib = None
 

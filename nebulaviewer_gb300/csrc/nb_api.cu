@@ -5,6 +5,7 @@
 #include <cstring>
 #include <mutex>
 #include <string>
+#include <vector>
 
 #include "nb_internal.cuh"
 
@@ -31,6 +32,11 @@ struct nb_instance {
     int smax_valid = 0;
     int chunk_i = 64, ray_group = 32, fuv_group = 32;
     long long ncell = 0;
+    long long launches = 0;             // kernels this handle launched (nb_counters)
+    int profiling = 0;                  // CUDA-event timing per kernel kind (nb_profile)
+    struct ProfRec { int kind; cudaEvent_t a, b; };
+    std::vector<ProfRec> recs;
+    std::vector<cudaEvent_t> pool;
     std::string err;
 };
 
@@ -83,6 +89,38 @@ bool encode_plane(CUtensorMap* m, const float* ptr, int nx, int ny, int nz) {
               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
+cudaEvent_t ev_get(nb_instance* h) {
+    if (!h->pool.empty()) {
+        cudaEvent_t e = h->pool.back();
+        h->pool.pop_back();
+        return e;
+    }
+    cudaEvent_t e = nullptr;
+    cudaEventCreate(&e);
+    return e;
+}
+
+// Brackets the launches of one kernel kind with CUDA events on the handle's stream.
+struct Prof {
+    nb_instance* h;
+    int kind;
+    cudaEvent_t a = nullptr;
+    Prof(nb_instance* h_, int kind_, int nlaunch) : h(h_), kind(kind_) {
+        h->launches += nlaunch;
+        if (h->profiling) {
+            a = ev_get(h);
+            cudaEventRecord(a, h->stream);
+        }
+    }
+    ~Prof() {
+        if (a) {
+            cudaEvent_t b = ev_get(h);
+            cudaEventRecord(b, h->stream);
+            h->recs.push_back({kind, a, b});
+        }
+    }
+};
+
 bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
 
 bool is_pow2(double x) {
@@ -124,20 +162,32 @@ int launch_stage(nb_instance* h, const float* const in[4], const float* const u0
     L.chunk_i = h->chunk_i < h->d.nx ? h->chunk_i : h->d.nx;
     L.n_chunks = (h->d.nx + L.chunk_i - 1) / L.chunk_i;
     L.nstars_host = h->nstars;
+    Prof pf(h, smax ? NB_PROF_STAGE2 : NB_PROF_STAGE1, 1);
     CK(h, nb_launch_hydro(L, h->d.solver, h->d.limiter, h->stream));
     return NB_OK;
 }
 
 int do_ionize(nb_instance* h) {
     const nb_fields& f = h->d.f;
-    CK(h, nb_launch_weights(h->c, h->st, h->stars, h->sw, h->nstars, h->stream));
-    if (h->nstars > 0)
+    {
+        Prof pf(h, NB_PROF_CTRL, 1);
+        CK(h, nb_launch_weights(h->c, h->st, h->stars, h->sw, h->nstars, h->stream));
+    }
+    if (h->nstars > 0) {
+        Prof pf(h, NB_PROF_CAST_RAYS, 1);
         CK(h, nb_launch_cast_rays(h->c, h->sw, h->dirs, f.rho, h->rfront, h->nstars, h->ray_group, nullptr, 0.0f,
                                   h->stream, h->d.nu, h->d.nphi));
+    }
     float* xi_raw = plane(h, 0);            // sim.py:928-941: xi_tmp lives in the stage block
-    CK(h, nb_launch_apply_front(h->c, h->sw, h->rfront, h->nstars, xi_raw, f.dfront, &h->st->smax_bits, h->stream,
-                                h->ncell, h->d.fields_fp32 ? 0 : 1));
-    CK(h, nb_launch_smooth(h->c, xi_raw, f.xi, f.rho, f.mx, f.my, f.mz, &h->st->smax_bits, h->stream, h->ncell));
+    {
+        Prof pf(h, NB_PROF_APPLY_FRONT, 1);
+        CK(h, nb_launch_apply_front(h->c, h->sw, h->rfront, h->nstars, xi_raw, f.dfront, &h->st->smax_bits,
+                                    h->stream, h->ncell, h->d.fields_fp32 ? 0 : 1));
+    }
+    {
+        Prof pf(h, NB_PROF_SMOOTH, 1);
+        CK(h, nb_launch_smooth(h->c, xi_raw, f.xi, f.rho, f.mx, f.my, f.mz, &h->st->smax_bits, h->stream, h->ncell));
+    }
     h->smax_valid = 1;
     return NB_OK;
 }
@@ -148,10 +198,14 @@ int do_step(nb_instance* h, int ion_every) {
     if (ion_every > 0 && h->host_it % ion_every == 0) {           // sim.py:1102-1103
         if ((rc = do_ionize(h)) != NB_OK) return rc;
     } else if (!h->smax_valid) {
+        Prof pf(h, NB_PROF_MAX_SPEED, 2);
         CK(h, nb_launch_max_speed(h->c, f.rho, f.mx, f.my, f.mz, f.xi, &h->st->smax_bits, h->ncell, h->stream));
     }
     // sim.py:1104-1108: star weights at t, dt from the max speed (dt_cap), pulse; t += dt
-    CK(h, nb_launch_ctrl(h->c, h->st, h->stars, h->sw, h->nstars, 1, h->stream));
+    {
+        Prof pf(h, NB_PROF_CTRL, 1);
+        CK(h, nb_launch_ctrl(h->c, h->st, h->stars, h->sw, h->nstars, 1, h->stream));
+    }
     const float* U[4] = {f.rho, f.mx, f.my, f.mz};
     float* Uw[4] = {f.rho, f.mx, f.my, f.mz};
     float* S[4] = {plane(h, 0), plane(h, 1), plane(h, 2), plane(h, 3)};
@@ -264,6 +318,11 @@ NB_EXPORT void nb_destroy(nb_handle h) {
                   h->rfront, h->att, h->scratch3, h->red};
     for (void* p : ps)
         if (p) cudaFree(p);
+    for (auto& r : h->recs) {
+        cudaEventDestroy(r.a);
+        cudaEventDestroy(r.b);
+    }
+    for (cudaEvent_t e : h->pool) cudaEventDestroy(e);
     delete h;
 }
 
@@ -384,12 +443,20 @@ NB_EXPORT int nb_fuv(nb_handle h) {
         CK(h, cudaMemsetAsync(h->d.f.g0, 0, es * h->ncell, h->stream));
         return NB_OK;
     }
-    CK(h, nb_launch_weights(h->c, h->st, h->stars, h->sw, h->nstars, h->stream));
-    if (h->nstars > 0)
+    {
+        Prof pf(h, NB_PROF_CTRL, 1);
+        CK(h, nb_launch_weights(h->c, h->st, h->stars, h->sw, h->nstars, h->stream));
+    }
+    if (h->nstars > 0) {
+        Prof pf(h, NB_PROF_CAST_FUV, 1);
         CK(h, nb_launch_cast_fuv(h->c, h->sw, h->dirs_fuv, h->d.f.rho, h->d.f.xi, h->att, h->nstars, h->fuv_group,
                                  nullptr, 0, h->stream, h->d.fnu, h->d.fnphi));
-    CK(h, nb_launch_apply_fuv(h->c, h->sw, h->att, h->nstars, h->d.f.g0, h->stream, h->ncell,
-                              h->d.fields_fp32 ? 0 : 1));
+    }
+    {
+        Prof pf(h, NB_PROF_APPLY_FUV, 1);
+        CK(h, nb_launch_apply_fuv(h->c, h->sw, h->att, h->nstars, h->d.f.g0, h->stream, h->ncell,
+                                  h->d.fields_fp32 ? 0 : 1));
+    }
     return NB_OK;
 }
 
@@ -450,5 +517,38 @@ NB_EXPORT int nb_reduce_fp64(nb_handle h, double out[4]) {
     CK(h, cudaMemcpyAsync(out, h->red + nb_reduce_scratch_doubles() - 4, 4 * sizeof(double), cudaMemcpyDeviceToHost,
                           h->stream));
     CK(h, cudaStreamSynchronize(h->stream));
+    return NB_OK;
+}
+
+NB_EXPORT int nb_profile(nb_handle h, int enable) {
+    if (!h) return fail(h, NB_ERR_ARG, "null handle");
+    h->profiling = enable ? 1 : 0;
+    return NB_OK;
+}
+
+NB_EXPORT int nb_profile_read(nb_handle h, double ms[NB_PROF_KINDS], long long count[NB_PROF_KINDS]) {
+    if (!h || !ms || !count) return fail(h, NB_ERR_ARG, "null argument");
+    CK(h, cudaStreamSynchronize(h->stream));
+    for (int k = 0; k < NB_PROF_KINDS; ++k) {
+        ms[k] = 0.0;
+        count[k] = 0;
+    }
+    for (auto& r : h->recs) {
+        float t = 0.0f;
+        CK(h, cudaEventElapsedTime(&t, r.a, r.b));
+        if (r.kind >= 0 && r.kind < NB_PROF_KINDS) {
+            ms[r.kind] += t;
+            count[r.kind] += 1;
+        }
+        h->pool.push_back(r.a);
+        h->pool.push_back(r.b);
+    }
+    h->recs.clear();
+    return NB_OK;
+}
+
+NB_EXPORT int nb_counters(nb_handle h, long long* launches) {
+    if (!h || !launches) return fail(h, NB_ERR_ARG, "null argument");
+    *launches = h->launches;
     return NB_OK;
 }
