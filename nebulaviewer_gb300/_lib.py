@@ -73,7 +73,9 @@ SIGNATURES = {
     "nb_profile": (C.c_int, [_P, C.c_int]),
     "nb_profile_read": (C.c_int, [_P, C.c_double * 16, C.c_longlong * 16]),
     "nb_counters": (C.c_int, [_P, C.POINTER(C.c_longlong)]),
+    "nb_set_tuning": (C.c_int, [_P, C.c_int, C.c_int]),
 }
+TUNE = {"chunk_i": 0, "ray_group": 1, "fuv_group": 2}
 PROF_KINDS = ["ctrl", "stage1", "stage2", "cast_rays", "apply_front", "smooth", "cast_fuv", "apply_fuv", "max_speed"]
 
 _lib = None

@@ -552,3 +552,20 @@ NB_EXPORT int nb_counters(nb_handle h, long long* launches) {
     *launches = h->launches;
     return NB_OK;
 }
+
+NB_EXPORT int nb_set_tuning(nb_handle h, int key, int value) {
+    if (!h) return fail(h, NB_ERR_ARG, "null handle");
+    switch (key) {
+        case NB_TUNE_CHUNK_I:
+            if (value < 1) return fail(h, NB_ERR_ARG, "chunk_i must be >= 1");
+            h->chunk_i = value;
+            return NB_OK;
+        case NB_TUNE_RAY_GROUP:
+        case NB_TUNE_FUV_GROUP:
+            if (value != 8 && value != 16 && value != 32) return fail(h, NB_ERR_ARG, "group must be 8, 16 or 32");
+            (key == NB_TUNE_RAY_GROUP ? h->ray_group : h->fuv_group) = value;
+            return NB_OK;
+        default:
+            return fail(h, NB_ERR_ARG, "unknown tuning key");
+    }
+}

@@ -98,8 +98,12 @@ struct HydroSmem {
     static int bytes(int nstars) { return FIXED + nstars * 32; }
 };
 
+#ifndef NB_HYDRO_MINB
+#define NB_HYDRO_MINB 2               // resident blocks per SM the register budget is sized for
+#endif
+
 template <int SOLVER, int LIM, int TJ, bool STAGE2>
-__global__ void __launch_bounds__(TK * TJ, (TJ <= 8 ? 2 : 1))
+__global__ void __launch_bounds__(TK * TJ, NB_HYDRO_MINB)
 hydro_stage_kernel(const HydroLaunch L) {
     using SM = HydroSmem<TJ>;
     extern __shared__ __align__(128) unsigned char smem[];
@@ -231,6 +235,13 @@ hydro_stage_kernel(const HydroLaunch L) {
         if (p < i0 + 2) { fx_prev = fx_new; continue; }
         // ---- cell plane i = p - 2 (prim slot of plane i)
         const int i = p - 2;
+        const int j = j0 + tj, k = k0 + tk;
+        const bool inside = j < ny && k < nz;
+        const long long cell = ((long long)i * ny + j) * nz + k;
+        float u00 = 0.0f, u01 = 0.0f, u02 = 0.0f, u03 = 0.0f;
+        if (STAGE2 && inside) {                 // own-cell U^n, issued before the flux work
+            u00 = L.u0[0][cell]; u01 = L.u0[1][cell]; u02 = L.u0[2][cell]; u03 = L.u0[3][cell];
+        }
         const int si = (i - P0) % 3;
         const float4* q = prim + si * (TJ + 4) * PW;
         const float2* c = cs + si * (TJ + 4) * PW;
@@ -261,8 +272,6 @@ hydro_stage_kernel(const HydroLaunch L) {
         float d2 = 0.0f + (fxp.z - fxm.z), d3 = 0.0f + (fxp.w - fxm.w);
         d0 = d0 + (fyp.x - fym.x); d1 = d1 + (fyp.y - fym.y); d2 = d2 + (fyp.z - fym.z); d3 = d3 + (fyp.w - fym.w);
         d0 = d0 + (fzp.x - fzm.x); d1 = d1 + (fzp.y - fzm.y); d2 = d2 + (fzp.z - fzm.z); d3 = d3 + (fzp.w - fzm.w);
-        const int j = j0 + tj, k = k0 + tk;
-        const bool inside = j < ny && k < nz;
         // ---- sources and RK combination (nebula3d.py:111-151)
         const Raw5 U = rw0;
         float du0, du1, du2, du3;
@@ -280,7 +289,7 @@ hydro_stage_kernel(const HydroLaunch L) {
                 const float4 st = sw_w[s];
                 if (st.w > 0.0f) {
                     const float rx = px - st.x, ry = py - st.y, rz = pz - st.z;
-                    const float r2 = ((0.0f + rx * rx) + ry * ry) + rz * rz + 0.0004f;
+                    const float r2 = ((rx * rx + ry * ry) + rz * rz) + 0.0004f;     // 0 + x*x == x*x
                     const float f = st.w / (r2 * sqrtf(r2));
                     ax = ax + rx * f; ay = ay + ry * f; az = az + rz * f;
                 }
@@ -296,7 +305,7 @@ hydro_stage_kernel(const HydroLaunch L) {
             const float4 st = sw_w[s];
             if (jt.w > 0.0f && st.w > 0.0f) {
                 const float rx = px - st.x, ry = py - st.y, rz = pz - st.z;
-                const float r = sqrtf(((0.0f + rx * rx) + ry * ry) + rz * rz);
+                const float r = sqrtf((rx * rx + ry * ry) + rz * rz);
                 if (r < jet_r && r > 1e-6f) {
                     const float cth = (((0.0f + rx * jt.x) + ry * jt.y) + rz * jt.z) / r;
                     if (fabsf(cth) > jet_cos) {
@@ -309,21 +318,13 @@ hydro_stage_kernel(const HydroLaunch L) {
         du0 = du0 + 0.0f;
         du1 = du1 + U.r * jx; du2 = du2 + U.r * jy; du3 = du3 + U.r * jz;
         const float un0 = U.r + dt * du0, un1 = U.mx + dt * du1, un2 = U.my + dt * du2, un3 = U.mz + dt * du3;
-        const long long cell = ((long long)i * ny + j) * nz + k;
-        float u00, u01, u02, u03;
-        if (STAGE2) {
-            if (inside) {
-                u00 = L.u0[0][cell]; u01 = L.u0[1][cell]; u02 = L.u0[2][cell]; u03 = L.u0[3][cell];
-            } else {
-                u00 = u01 = u02 = u03 = 0.0f;
-            }
-        } else {
+        if (!STAGE2) {
             u00 = U.r; u01 = U.mx; u02 = U.my; u03 = U.mz;
         }
         const float o0 = a * u00 + b * un0, o1 = a * u01 + b * un1, o2 = a * u02 + b * un2, o3 = a * u03 + b * un3;
         const float r = fmaxr(o0, floor_);
         float vx = o1 / r, vy = o2 / r, vz = o3 / r;
-        const float sp = sqrtf(((0.0f + vx * vx) + vy * vy) + vz * vz);
+        const float sp = sqrtf((vx * vx + vy * vy) + vz * vz);
         if (sp > vmax) {
             const float f = vmax / sp;
             vx = vx * f; vy = vy * f; vz = vz * f;

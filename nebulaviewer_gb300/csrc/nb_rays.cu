@@ -127,7 +127,7 @@ __global__ void __launch_bounds__(256) apply_front_kernel(const NbConst* __restr
             if (!act[s]) continue;
             const float4 sp = st[s];
             const float rx = px - sp.x, ry = py - sp.y, rz = pz - sp.z;
-            const float r = fmaxr(sqrtf(((0.0f + rx * rx) + ry * ry) + rz * rz), 1e-6f);
+            const float r = fmaxr(sqrtf((rx * rx + ry * ry) + rz * rz), 1e-6f);     // 0 + x*x == x*x
             const float u = rz / r;
             float phi = atan2f(ry, rx);
             if (phi < 0.0f) phi = phi + two_pi;
