@@ -189,6 +189,22 @@ int nb_set_tuning(nb_handle h, int key, int value);
 /* Number of kernels the handle has launched (a claim the benchmark reports). */
 int nb_counters(nb_handle h, long long* launches);
 
+/* ---------------------------------------------------------------- allocation-free entry point
+ * No counterpart in the reference.  The FP64 totals of nb_reduce_fp64 (sum rho, mx, my, mz
+ * over n cells) for callers that cannot allocate device memory -- e.g. a serving process whose
+ * device memory all belongs to a pre-sized pool, or code that must not call cudaMalloc while
+ * another thread captures work into a CUDA graph.  It needs no handle: the caller passes the
+ * four input planes (device) and out4 (device, 4 doubles); the per-block partial sums live in
+ * a library-owned static device array of 512 KiB (held by every GPU that loads the library
+ * until the process exits), which caps n at 2^30 cells: larger n returns NB_ERR_LIMIT with a
+ * message in nb_static_last_error().  It calls no cudaMalloc / cudaFree.  The first call on a
+ * device looks up that array's device address (cudaGetSymbolAddress, with the device current);
+ * make that first call before any stream capture.  Every call shares the one array: calls
+ * that overlap on the GPU (different streams without ordering) race.  Asynchronous on
+ * `stream` (0 = legacy default stream). */
+int nb_reduce_fp64_static(const float* rho, const float* mx, const float* my, const float* mz, long long n,
+                          double* out4, void* stream);
+const char* nb_static_last_error(void);
 /* FP64 conservation totals: sum rho, sum mx, sum my, sum mz (times dx^3 = mass/momentum). */
 int nb_reduce_fp64(nb_handle h, double out[4]);
 

@@ -5,6 +5,9 @@
 // device->host read of the reference (sim.py:1012), so a whole step can be replayed as a
 // CUDA graph.  Also: the stand-alone CFL max-speed reduction (nebula3d.py:154-162) and the
 // deterministic FP64 conservation totals.
+#include <mutex>
+#include <string>
+
 #include "nb_internal.cuh"
 
 namespace {
@@ -152,4 +155,74 @@ cudaError_t nb_launch_reduce_fp64(const float* rho, const float* mx, const float
     reduce_partials<<<RED_BLOCKS, RED_THREADS, 0, s>>>(rho, mx, my, mz, n, scratch);
     reduce_final<<<1, 32, 0, s>>>(scratch, RED_BLOCKS, scratch + RED_BLOCKS * 4);
     return cudaGetLastError();
+}
+
+// ============================================================================ allocation-free totals
+// nb_reduce_fp64_static: the FP64 conservation totals for callers that cannot allocate device
+// memory (a process whose allocations all come from a pre-sized pool or arena owned by someone
+// else, or code that must not call cudaMalloc while other work is being captured into a CUDA
+// graph).  The per-block partial sums live in this file-scope device array instead of handle
+// scratch, so the caller passes only the input planes and a device output.
+#define NB_STATIC_RED_CELLS_PER_BLOCK (1LL << 16)          // cells summed by one block
+#define NB_STATIC_RED_MAX_BLOCKS (1 << 14)                  // 16384 blocks -> n <= 2^30 cells
+static __device__ __align__(256) double g_static_red[NB_STATIC_RED_MAX_BLOCKS * 4 + 4];   // 512 KiB + 32 B
+
+namespace {
+
+#define NB_MAX_DEVICES 64
+std::mutex g_static_mu;
+double* g_static_ptr[NB_MAX_DEVICES];     // device address of g_static_red, per device (set up once)
+
+thread_local std::string g_static_err;
+
+}  // namespace
+
+extern "C" __attribute__((visibility("default"))) const char* nb_static_last_error(void) {
+    return g_static_err.c_str();
+}
+
+extern "C" __attribute__((visibility("default"))) int nb_reduce_fp64_static(const float* rho, const float* mx,
+                                                                         const float* my, const float* mz,
+                                                                         long long n, double* out4, void* stream) {
+    if (!rho || !mx || !my || !mz || !out4) {
+        g_static_err = "nb_reduce_fp64_static: null pointer";
+        return NB_ERR_ARG;
+    }
+    if (n < 1 || n > (long long)NB_STATIC_RED_MAX_BLOCKS * NB_STATIC_RED_CELLS_PER_BLOCK) {
+        g_static_err = "nb_reduce_fp64_static: n must be in [1, 2^30] cells (the static scratch holds 16384 "
+                       "block partials of 65536 cells each)";
+        return NB_ERR_LIMIT;
+    }
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess || dev < 0 || dev >= NB_MAX_DEVICES) {
+        g_static_err = std::string("nb_reduce_fp64_static: cudaGetDevice: ") + cudaGetErrorString(e);
+        return NB_ERR_CUDA;
+    }
+    double* part = nullptr;
+    {
+        // set-up, once per device, with that device current: the device address of the array
+        std::lock_guard<std::mutex> lock(g_static_mu);
+        if (!g_static_ptr[dev]) {
+            void* p = nullptr;
+            e = cudaGetSymbolAddress(&p, g_static_red);
+            if (e != cudaSuccess || !p) {
+                g_static_err = std::string("nb_reduce_fp64_static: cudaGetSymbolAddress: ") + cudaGetErrorString(e);
+                return NB_ERR_CUDA;
+            }
+            g_static_ptr[dev] = static_cast<double*>(p);
+        }
+        part = g_static_ptr[dev];
+    }
+    const int blocks = (int)((n + NB_STATIC_RED_CELLS_PER_BLOCK - 1) / NB_STATIC_RED_CELLS_PER_BLOCK);
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    // every partial the final pass reads is written by this call's first pass: nothing to clear
+    reduce_partials<<<blocks, RED_THREADS, 0, s>>>(rho, mx, my, mz, n, part);
+    reduce_final<<<1, 32, 0, s>>>(part, blocks, out4);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        g_static_err = std::string("nb_reduce_fp64_static: launch: ") + cudaGetErrorString(e);
+        return NB_ERR_CUDA;
+    }
+    return NB_OK;
 }
