@@ -182,7 +182,7 @@ enum {
 int nb_profile(nb_handle h, int enable);
 int nb_profile_read(nb_handle h, double ms[NB_PROF_KINDS], long long count[NB_PROF_KINDS]);
 /* Launch-shape knobs picked by the package's autotuner (no reference counterpart): the i-chunk
- * of the hydro march, and the lanes per ray (8, 16, 32) of the ionizing / FUV ray kernels.
+ * of the hydro march, and the lanes per ray (4, 8, 16, 32 ionizing; 8, 16, 32 FUV) of the ray kernels.
  * Results do not depend on them except through the rounding of the ray sums. */
 enum { NB_TUNE_CHUNK_I = 0, NB_TUNE_RAY_GROUP = 1, NB_TUNE_FUV_GROUP = 2 };
 int nb_set_tuning(nb_handle h, int key, int value);

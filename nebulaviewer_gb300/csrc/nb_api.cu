@@ -30,7 +30,7 @@ struct nb_instance {
     int nstars = 0, star_alloc = 0;
     long long host_it = 0;
     int smax_valid = 0;
-    int chunk_i = 64, ray_group = 32, fuv_group = 32;
+    int chunk_i = 32, ray_group = 4, fuv_group = 16;      // measured best at 256^3 (nb_set_tuning)
     long long ncell = 0;
     long long launches = 0;             // kernels this handle launched (nb_counters)
     int profiling = 0;                  // CUDA-event timing per kernel kind (nb_profile)
@@ -182,11 +182,11 @@ int do_ionize(nb_instance* h) {
     {
         Prof pf(h, NB_PROF_APPLY_FRONT, 1);
         CK(h, nb_launch_apply_front(h->c, h->sw, h->rfront, h->nstars, xi_raw, f.dfront, &h->st->smax_bits,
-                                    h->stream, h->ncell, h->d.fields_fp32 ? 0 : 1));
+                                    h->stream, h->d.nx, h->d.ny, h->d.fields_fp32 ? 0 : 1));
     }
     {
         Prof pf(h, NB_PROF_SMOOTH, 1);
-        CK(h, nb_launch_smooth(h->c, xi_raw, f.xi, f.rho, f.mx, f.my, f.mz, &h->st->smax_bits, h->stream, h->ncell));
+        CK(h, nb_launch_smooth(h->c, xi_raw, f.xi, f.rho, f.mx, f.my, f.mz, &h->st->smax_bits, h->stream, h->d.nx, h->d.ny));
     }
     h->smax_valid = 1;
     return NB_OK;
@@ -454,8 +454,8 @@ NB_EXPORT int nb_fuv(nb_handle h) {
     }
     {
         Prof pf(h, NB_PROF_APPLY_FUV, 1);
-        CK(h, nb_launch_apply_fuv(h->c, h->sw, h->att, h->nstars, h->d.f.g0, h->stream, h->ncell,
-                                  h->d.fields_fp32 ? 0 : 1));
+        CK(h, nb_launch_apply_fuv(h->c, h->sw, h->att, h->nstars, h->d.f.g0, h->stream, h->d.nx,
+                                  h->d.ny, h->d.fields_fp32 ? 0 : 1));
     }
     return NB_OK;
 }
@@ -562,7 +562,8 @@ NB_EXPORT int nb_set_tuning(nb_handle h, int key, int value) {
             return NB_OK;
         case NB_TUNE_RAY_GROUP:
         case NB_TUNE_FUV_GROUP:
-            if (value != 8 && value != 16 && value != 32) return fail(h, NB_ERR_ARG, "group must be 8, 16 or 32");
+            if (value != 8 && value != 16 && value != 32 && !(value == 4 && key == NB_TUNE_RAY_GROUP))
+                return fail(h, NB_ERR_ARG, "lanes per ray must be 4 (ionizing rays only), 8, 16 or 32");
             (key == NB_TUNE_RAY_GROUP ? h->ray_group : h->fuv_group) = value;
             return NB_OK;
         default:

@@ -107,21 +107,21 @@ __global__ void __launch_bounds__(256) apply_fuv_kernel(const NbConst* __restric
     __shared__ float4 st[NB_MAX_STARS];
     __shared__ float lum[NB_MAX_STARS];
     __shared__ int act[NB_MAX_STARS];
-    for (int s = threadIdx.x; s < nstars; s += blockDim.x) {
+    for (int s = threadIdx.y * blockDim.x + threadIdx.x; s < nstars; s += blockDim.x * blockDim.y) {
         st[s] = sw[s].w;
         lum[s] = sw[s].lum_f;
         act[s] = sw[s].active;
     }
     __syncthreads();
     const int nx = c->nx, ny = c->ny, nz = c->nz, nr = c->fnr, nu = c->fnu, nphi = c->fnphi;
-    const long long n = (long long)nx * ny * nz;
     const float dx = c->dx, binr = c->binr_f;
     const float two_pi = 2.0f * pi_f();
-    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
-        const int k = (int)(q % nz);
-        const long long t = q / nz;
-        const int j = (int)(t % ny), i = (int)(t / ny);
-        const float px = ((float)i + 0.5f) * dx, py = ((float)j + 0.5f) * dx, pz = ((float)k + 0.5f) * dx;
+    const RowWalk w(nx, ny, nz);
+    if (!w.valid) return;
+    const float px = ((float)w.i + 0.5f) * dx, py = ((float)w.j + 0.5f) * dx;
+    for (int k = w.k0; k < nz; k += 32) {
+        const long long q = w.base + k;
+        const float pz = ((float)k + 0.5f) * dx;
         float g = 0.0f;
         for (int s = 0; s < nstars; ++s) {
             if (!act[s]) continue;
@@ -137,6 +137,7 @@ __global__ void __launch_bounds__(256) apply_fuv_kernel(const NbConst* __restric
             const int ir = (int)floorf(fr), iu = (int)floorf(fu), ip = (int)floorf(fp);
             const float tr = fr - (float)ir, tu = fu - (float)iu, tp = fp - (float)ip;
             const float* as = att + (long long)s * nu * nphi * nr;
+            const int pw[2] = {wrap_index(ip, nphi), wrap_index(ip + 1, nphi)};
             float acc = 0.0f;
 #pragma unroll
             for (int aa = 0; aa < 2; ++aa)
@@ -144,11 +145,10 @@ __global__ void __launch_bounds__(256) apply_fuv_kernel(const NbConst* __restric
                 for (int bb = 0; bb < 2; ++bb)
 #pragma unroll
                     for (int cc = 0; cc < 2; ++cc) {
-                        const float w = (aa == 0 ? 1.0f - tr : tr) * (bb == 0 ? 1.0f - tu : tu) * (cc == 0 ? 1.0f - tp : tp);
+                        const float wgt = (aa == 0 ? 1.0f - tr : tr) * (bb == 0 ? 1.0f - tu : tu) * (cc == 0 ? 1.0f - tp : tp);
                         const int rr = iclampd(ir + aa, 0, nr - 1);
                         const int uu = iclampd(iu + bb, 0, nu - 1);
-                        const int pp = (((ip + cc) % nphi) + nphi) % nphi;
-                        acc = acc + w * __ldg(as + ((long long)uu * nphi + pp) * nr + rr);
+                        acc = acc + wgt * __ldg(as + ((long long)uu * nphi + pw[cc]) * nr + rr);
                     }
             const float r2 = fmaxr(r * r, 0.0004f);
             g = g + lum[s] * acc / r2;
@@ -158,12 +158,6 @@ __global__ void __launch_bounds__(256) apply_fuv_kernel(const NbConst* __restric
         else
             reinterpret_cast<float*>(g0)[q] = g;
     }
-}
-
-int grid_for(long long n, int threads) {
-    long long b = (n + threads - 1) / threads;
-    const long long cap = 152LL * 16;
-    return (int)(b < cap ? (b < 1 ? 1 : b) : cap);
 }
 
 }  // namespace
@@ -188,11 +182,11 @@ cudaError_t nb_launch_cast_fuv(const NbConst* c, const NbStarW* sw, const float4
 }
 
 cudaError_t nb_launch_apply_fuv(const NbConst* c, const NbStarW* sw, const float* att, int nstars, void* g0,
-                                cudaStream_t s, long long ncell, int half) {
-    const int blocks = grid_for(ncell, 256);
+                                cudaStream_t s, int nx, int ny, int half) {
+    const int blocks = rowwalk_blocks(nx, ny);
     if (half)
-        apply_fuv_kernel<true><<<blocks, 256, 0, s>>>(c, sw, att, nstars, g0);
+        apply_fuv_kernel<true><<<blocks, dim3(32, 8), 0, s>>>(c, sw, att, nstars, g0);
     else
-        apply_fuv_kernel<false><<<blocks, 256, 0, s>>>(c, sw, att, nstars, g0);
+        apply_fuv_kernel<false><<<blocks, dim3(32, 8), 0, s>>>(c, sw, att, nstars, g0);
     return cudaGetLastError();
 }

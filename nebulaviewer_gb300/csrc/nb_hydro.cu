@@ -82,15 +82,11 @@ __device__ __forceinline__ float4 face_flux(const float4 qa, const float4 qb, co
     return make_float4(F[0], F[1], F[2], F[3]);
 }
 
-struct Raw5 {
-    float r, mx, my, mz, xi;
-};
-
 template <int TJ>
 struct HydroSmem {
     static constexpr int RAW_FIELD = (TJ + 4) * RAWW;                     // floats per field per slot
     static constexpr int RAW_BYTES = 2 * 5 * RAW_FIELD * 4;
-    static constexpr int PRIM_BYTES = 3 * (TJ + 4) * PW * 16;
+    static constexpr int PRIM_BYTES = 4 * (TJ + 4) * PW * 16;
     static constexpr int CS_BYTES = 3 * (TJ + 4) * PW * 8;
     static constexpr int FACE_BYTES = ((TJ + 1) * TK + TJ * (TK + 1)) * 16;
     static constexpr int BAR_BYTES = 64;
@@ -99,7 +95,7 @@ struct HydroSmem {
 };
 
 #ifndef NB_HYDRO_MINB
-#define NB_HYDRO_MINB 2               // resident blocks per SM the register budget is sized for
+#define NB_HYDRO_MINB 3               // resident blocks per SM the register budget is sized for
 #endif
 
 template <int SOLVER, int LIM, int TJ, bool STAGE2>
@@ -108,7 +104,7 @@ hydro_stage_kernel(const HydroLaunch L) {
     using SM = HydroSmem<TJ>;
     extern __shared__ __align__(128) unsigned char smem[];
     float* raw = reinterpret_cast<float*>(smem);                                   // [2][5][TJ+4][40]
-    float4* prim = reinterpret_cast<float4*>(smem + SM::RAW_BYTES);                // [3][TJ+4][36]
+    float4* prim = reinterpret_cast<float4*>(smem + SM::RAW_BYTES);                // [4][TJ+4][36]
     float2* cs = reinterpret_cast<float2*>(smem + SM::RAW_BYTES + SM::PRIM_BYTES); // [3][TJ+4][36]
     float4* fy = reinterpret_cast<float4*>(smem + SM::RAW_BYTES + SM::PRIM_BYTES + SM::CS_BYTES);  // [TJ+1][32]
     float4* fz = fy + (TJ + 1) * TK;                                               // [TJ][33]
@@ -161,49 +157,51 @@ hydro_stage_kernel(const HydroLaunch L) {
         issue(P0 + 1, 1);
     }
 
-    // own-column windows: q for planes p-3..p, (c^2, c) and raw values for planes p-2..p
-    float4 qw0 = make_float4(0.f, 0.f, 0.f, 0.f), qw1 = qw0, qw2 = qw0, qw3 = qw0;
-    float2 cw0 = make_float2(0.f, 0.f), cw1 = cw0, cw2 = cw0;
-    Raw5 rw0{}, rw1{}, rw2{};
-    float4 fx_prev = qw0;
+    float4 fx_prev = make_float4(0.f, 0.f, 0.f, 0.f);
     float vmax_local = 0.0f;
     unsigned ph0 = 0, ph1 = 0;
     bool failed = false;
 
     // clamped global -> raw-tile coordinates
-    auto raw_at = [&](const float* base, int jj, int kk) {      // jj, kk: prim-tile coords
+    auto raw_at = [&](int jj, int kk) {      // jj, kk: prim-tile coords
         const int jc = iclampd(j0 - 2 + jj, 0, ny - 1) - (j0 - 2);
         const int kc = iclampd(k0 - 2 + kk, 0, nz - 1) - (k0 - 4);
         return jc * RAWW + kc;
     };
+    const int own = (tj + 2) * PW + tk + 2;          // this thread's cell in a prim / cs tile
+    const int j = j0 + tj, k = k0 + tk;
+    const bool inside = j < ny && k < nz;
+    constexpr int PSLOT = (TJ + 4) * PW;
 
     for (int p = P0; p <= P1; ++p) {
         const int rs = (p - P0) & 1;
-        const int ps = (p - P0) % 3;
+        const int ps = (p - P0) & 3;                 // prim slot of plane p (4 slots: p-3..p)
+        const int cq = (p - P0) % 3;                 // cs slot of plane p (3 slots: p-2..p)
+        // own-cell values of plane i = p - 2 the epilogue needs, issued before the flux work
+        const int i = p - 2;
+        const long long cell = ((long long)i * ny + j) * nz + k;
+        const bool work = p >= i0 + 2;
+        float u00 = 0.f, u01 = 0.f, u02 = 0.f, u03 = 0.f, ur = 0.f, umx = 0.f, umy = 0.f, umz = 0.f, uxi = 0.f;
+        if (work && inside) {
+            ur = L.in[0][cell]; umx = L.in[1][cell]; umy = L.in[2][cell]; umz = L.in[3][cell];
+            uxi = L.xi[cell];
+            if (STAGE2) {
+                u00 = L.u0[0][cell]; u01 = L.u0[1][cell]; u02 = L.u0[2][cell]; u03 = L.u0[3][cell];
+            }
+        }
         bool ok = mbar_wait_bounded(&bar[rs], rs ? ph1 : ph0);
         if (rs) ph1 ^= 1u; else ph0 ^= 1u;
         if (__syncthreads_or(!ok)) { failed = true; break; }
         const float* rb = raw + rs * 5 * SM::RAW_FIELD;
-        float4* pp = prim + ps * (TJ + 4) * PW;
-        float2* cp = cs + ps * (TJ + 4) * PW;
+        float4* pp = prim + ps * PSLOT;
+        float2* cp = cs + cq * PSLOT;
         // ---- convert plane p: own cell, then the halo strips (corners are never read)
-        Raw5 own;
-        {
-            const int jj = tj + 2, kk = tk + 2;
-            const int o = raw_at(rb, jj, kk);
-            own.r = rb[o];
-            own.mx = rb[SM::RAW_FIELD + o];
-            own.my = rb[2 * SM::RAW_FIELD + o];
-            own.mz = rb[3 * SM::RAW_FIELD + o];
-            own.xi = rb[4 * SM::RAW_FIELD + o];
-            const float r = fmaxr(own.r, floor_);
-            const float c2 = cn2 + own.xi * (ci2 - cn2);
-            pp[jj * PW + kk] = make_float4(r, own.mx / r, own.my / r, own.mz / r);
-            cp[jj * PW + kk] = make_float2(c2, sqrtf(c2));
-        }
-        for (int h = tid; h < 4 * TK + 4 * TJ; h += TK * TJ) {
+        for (int h = tid - TK * TJ; h < 4 * TK + 4 * TJ; h += TK * TJ) {
             int jj, kk;
-            if (h < 4 * TK) {
+            if (h < 0) {
+                jj = tj + 2;
+                kk = tk + 2;
+            } else if (h < 4 * TK) {
                 const int rr = h >> 5;
                 jj = rr < 2 ? rr : TJ + rr;
                 kk = 2 + (h & 31);
@@ -213,7 +211,7 @@ hydro_stage_kernel(const HydroLaunch L) {
                 const int q = hh & 3;
                 kk = q < 2 ? q : 32 + q;
             }
-            const int o = raw_at(rb, jj, kk);
+            const int o = raw_at(jj, kk);
             const float r = fmaxr(rb[o], floor_);
             const float xv = rb[4 * SM::RAW_FIELD + o];
             const float c2 = cn2 + xv * (ci2 - cn2);
@@ -223,28 +221,18 @@ hydro_stage_kernel(const HydroLaunch L) {
         }
         __syncthreads();
         if (tid == 0 && p + 2 <= P1) issue(p + 2, rs);
-        // ---- shift the own-column windows
-        qw0 = qw1; qw1 = qw2; qw2 = qw3;
-        qw3 = pp[(tj + 2) * PW + tk + 2];
-        cw0 = cw1; cw1 = cw2;
-        cw2 = cp[(tj + 2) * PW + tk + 2];
-        rw0 = rw1; rw1 = rw2; rw2 = own;
         if (p < P0 + 3) continue;
-        // x face (p-2)+1/2 from planes p-3..p
-        const float4 fx_new = face_flux<SOLVER, LIM, 1>(qw0, qw1, qw2, qw3, cw0, cw1, floor_);
-        if (p < i0 + 2) { fx_prev = fx_new; continue; }
-        // ---- cell plane i = p - 2 (prim slot of plane i)
-        const int i = p - 2;
-        const int j = j0 + tj, k = k0 + tk;
-        const bool inside = j < ny && k < nz;
-        const long long cell = ((long long)i * ny + j) * nz + k;
-        float u00 = 0.0f, u01 = 0.0f, u02 = 0.0f, u03 = 0.0f;
-        if (STAGE2 && inside) {                 // own-cell U^n, issued before the flux work
-            u00 = L.u0[0][cell]; u01 = L.u0[1][cell]; u02 = L.u0[2][cell]; u03 = L.u0[3][cell];
-        }
-        const int si = (i - P0) % 3;
-        const float4* q = prim + si * (TJ + 4) * PW;
-        const float2* c = cs + si * (TJ + 4) * PW;
+        // x face (p-2)+1/2 from the own column of planes p-3..p
+        const float4 fx_new = face_flux<SOLVER, LIM, 1>(prim[((p - 3 - P0) & 3) * PSLOT + own],
+                                                        prim[((p - 2 - P0) & 3) * PSLOT + own],
+                                                        prim[((p - 1 - P0) & 3) * PSLOT + own], pp[own],
+                                                        cs[((p - 2 - P0) % 3) * PSLOT + own],
+                                                        cs[((p - 1 - P0) % 3) * PSLOT + own], floor_);
+        if (!work) { fx_prev = fx_new; continue; }
+        // ---- cell plane i = p - 2
+        const int si = (i - P0) & 3;
+        const float4* q = prim + si * PSLOT;
+        const float2* c = cs + ((i - P0) % 3) * PSLOT;
         const int jj = tj + 2, kk = tk + 2;
         const float4 fyp = face_flux<SOLVER, LIM, 2>(q[(jj - 1) * PW + kk], q[jj * PW + kk], q[(jj + 1) * PW + kk],
                                                      q[(jj + 2) * PW + kk], c[jj * PW + kk], c[(jj + 1) * PW + kk],
@@ -273,16 +261,15 @@ hydro_stage_kernel(const HydroLaunch L) {
         d0 = d0 + (fyp.x - fym.x); d1 = d1 + (fyp.y - fym.y); d2 = d2 + (fyp.z - fym.z); d3 = d3 + (fyp.w - fym.w);
         d0 = d0 + (fzp.x - fzm.x); d1 = d1 + (fzp.y - fzm.y); d2 = d2 + (fzp.z - fzm.z); d3 = d3 + (fzp.w - fzm.w);
         // ---- sources and RK combination (nebula3d.py:111-151)
-        const Raw5 U = rw0;
         float du0, du1, du2, du3;
         if (C.dx_pow2) {
-            const float s = C.inv_dx;
-            du0 = -d0 * s; du1 = -d1 * s; du2 = -d2 * s; du3 = -d3 * s;
+            const float sc = C.inv_dx;
+            du0 = -d0 * sc; du1 = -d1 * sc; du2 = -d2 * sc; du3 = -d3 * sc;
         } else {
             du0 = -d0 / dx; du1 = -d1 / dx; du2 = -d2 / dx; du3 = -d3 / dx;
         }
         const float px = ((float)i + 0.5f) * dx, py = ((float)j + 0.5f) * dx, pz = ((float)k + 0.5f) * dx;
-        const float x_ion = U.xi;
+        const float x_ion = uxi;
         if (wind > 0.0f && x_ion > 0.01f) {
             float ax = 0.0f, ay = 0.0f, az = 0.0f;
             for (int s = 0; s < nstars; ++s) {
@@ -297,7 +284,7 @@ hydro_stage_kernel(const HydroLaunch L) {
             const float wx = wind * x_ion;
             ax = ax * wx; ay = ay * wx; az = az * wx;
             du0 = du0 + 0.0f;
-            du1 = du1 + U.r * ax; du2 = du2 + U.r * ay; du3 = du3 + U.r * az;
+            du1 = du1 + ur * ax; du2 = du2 + ur * ay; du3 = du3 + ur * az;
         }
         float jx = 0.0f, jy = 0.0f, jz = 0.0f;
         for (int s = 0; s < nstars; ++s) {
@@ -316,10 +303,10 @@ hydro_stage_kernel(const HydroLaunch L) {
             }
         }
         du0 = du0 + 0.0f;
-        du1 = du1 + U.r * jx; du2 = du2 + U.r * jy; du3 = du3 + U.r * jz;
-        const float un0 = U.r + dt * du0, un1 = U.mx + dt * du1, un2 = U.my + dt * du2, un3 = U.mz + dt * du3;
+        du1 = du1 + ur * jx; du2 = du2 + ur * jy; du3 = du3 + ur * jz;
+        const float un0 = ur + dt * du0, un1 = umx + dt * du1, un2 = umy + dt * du2, un3 = umz + dt * du3;
         if (!STAGE2) {
-            u00 = U.r; u01 = U.mx; u02 = U.my; u03 = U.mz;
+            u00 = ur; u01 = umx; u02 = umy; u03 = umz;
         }
         const float o0 = a * u00 + b * un0, o1 = a * u01 + b * un1, o2 = a * u02 + b * un2, o3 = a * u03 + b * un3;
         const float r = fmaxr(o0, floor_);
@@ -336,7 +323,7 @@ hydro_stage_kernel(const HydroLaunch L) {
             L.out[2][cell] = m2;
             L.out[3][cell] = m3;
             if (STAGE2 && L.smax_bits) {         // nebula3d.py:158-162 on the new state
-                const float v = fabsf(m1 / r) + fabsf(m2 / r) + fabsf(m3 / r) + cw0.y;
+                const float v = fabsf(m1 / r) + fabsf(m2 / r) + fabsf(m3 / r) + c[own].y;
                 vmax_local = fmaxr(v, vmax_local);
             }
         }

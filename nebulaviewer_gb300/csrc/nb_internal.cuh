@@ -141,15 +141,15 @@ cudaError_t nb_launch_cast_rays(const NbConst* c, const NbStarW* sw, const float
                                 float* rfront, int nstars, int group, const float* star_override, float q_override,
                                 cudaStream_t s, int nu, int nphi);
 cudaError_t nb_launch_apply_front(const NbConst* c, const NbStarW* sw, const float* rfront, int nstars,
-                                  float* xi_raw, void* dfront, unsigned* smax_reset, cudaStream_t s, long long ncell,
+                                  float* xi_raw, void* dfront, unsigned* smax_reset, cudaStream_t s, int nx, int ny,
                                   int half);
 cudaError_t nb_launch_smooth(const NbConst* c, const float* xi_raw, float* xi, const float* rho, const float* mx,
-                             const float* my, const float* mz, unsigned* smax_bits, cudaStream_t s, long long ncell);
+                             const float* my, const float* mz, unsigned* smax_bits, cudaStream_t s, int nx, int ny);
 cudaError_t nb_launch_cast_fuv(const NbConst* c, const NbStarW* sw, const float4* dirs, const float* rho,
                                const float* xi, float* att, int nstars, int group, const float* star_override,
                                int ref_layout, cudaStream_t s, int fnu, int fnphi);
 cudaError_t nb_launch_apply_fuv(const NbConst* c, const NbStarW* sw, const float* att, int nstars, void* g0,
-                                cudaStream_t s, long long ncell, int half);
+                                cudaStream_t s, int nx, int ny, int half);
 cudaError_t nb_launch_reduce_fp64(const float* rho, const float* mx, const float* my, const float* mz, long n,
                                   double* scratch, cudaStream_t s);   // totals at scratch[4*608 .. +4)
 int nb_reduce_scratch_doubles();

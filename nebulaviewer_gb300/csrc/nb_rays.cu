@@ -107,21 +107,22 @@ __global__ void __launch_bounds__(256) apply_front_kernel(const NbConst* __restr
                                                           unsigned* smax_reset) {
     __shared__ float4 st[NB_MAX_STARS];
     __shared__ int act[NB_MAX_STARS];
-    for (int s = threadIdx.x; s < nstars; s += blockDim.x) {
+    const int tlin = threadIdx.y * blockDim.x + threadIdx.x;
+    for (int s = tlin; s < nstars; s += blockDim.x * blockDim.y) {
         st[s] = sw[s].w;
         act[s] = sw[s].active;
     }
     __syncthreads();
-    if (smax_reset && blockIdx.x == 0 && threadIdx.x == 0) *smax_reset = 0u;
+    if (smax_reset && blockIdx.x == 0 && tlin == 0) *smax_reset = 0u;
     const int nx = c->nx, ny = c->ny, nz = c->nz, nu = c->nu, nphi = c->nphi;
-    const long long n = (long long)nx * ny * nz;
     const float dx = c->dx, width = c->width;
     const float two_pi = 2.0f * pi_f();
-    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
-        const int k = (int)(q % nz);
-        const long long t = q / nz;
-        const int j = (int)(t % ny), i = (int)(t / ny);
-        const float px = ((float)i + 0.5f) * dx, py = ((float)j + 0.5f) * dx, pz = ((float)k + 0.5f) * dx;
+    const RowWalk w(nx, ny, nz);
+    if (!w.valid) return;
+    const float px = ((float)w.i + 0.5f) * dx, py = ((float)w.j + 0.5f) * dx;
+    for (int k = w.k0; k < nz; k += 32) {
+        const long long q = w.base + k;
+        const float pz = ((float)k + 0.5f) * dx;
         float xi = 0.0f, df = 1e3f;
         for (int s = 0; s < nstars; ++s) {
             if (!act[s]) continue;
@@ -137,7 +138,7 @@ __global__ void __launch_bounds__(256) apply_front_kernel(const NbConst* __restr
             const float tu = fu - (float)iu, tp = fp - (float)ip;
             const float* rfs = rfront + (long long)s * nu * nphi;
             const int u0 = iclampd(iu, 0, nu - 1), u1 = iclampd(iu + 1, 0, nu - 1);
-            const int p0 = ((ip % nphi) + nphi) % nphi, p1 = (((ip + 1) % nphi) + nphi) % nphi;
+            const int p0 = wrap_index(ip, nphi), p1 = wrap_index(ip + 1, nphi);
             const float ra = __ldg(rfs + u0 * nphi + p0) * (1.0f - tp) + __ldg(rfs + u0 * nphi + p1) * tp;
             const float rb = __ldg(rfs + u1 * nphi + p0) * (1.0f - tp) + __ldg(rfs + u1 * nphi + p1) * tp;
             const float rf = ra * (1.0f - tu) + rb * tu;
@@ -160,42 +161,38 @@ __global__ void __launch_bounds__(256) smooth_kernel(const NbConst* __restrict__
                                                      const float* __restrict__ mx, const float* __restrict__ my,
                                                      const float* __restrict__ mz, unsigned* smax_bits) {
     const int nx = c->nx, ny = c->ny, nz = c->nz;
-    const long long n = (long long)nx * ny * nz;
     const float cn2 = c->cn2, ci2 = c->ci2;
     float m = 0.0f;
-    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
-        const int k = (int)(q % nz);
-        const long long t = q / nz;
-        const int j = (int)(t % ny), i = (int)(t / ny);
+    const RowWalk w(nx, ny, nz);
+    if (w.valid) {
         const long long sj = nz, si = (long long)ny * nz;
-        const float xm = __ldg(src + q - (i > 0 ? si : 0)), xp = __ldg(src + q + (i < nx - 1 ? si : 0));
-        const float ym = __ldg(src + q - (j > 0 ? sj : 0)), yp = __ldg(src + q + (j < ny - 1 ? sj : 0));
-        const float zm = __ldg(src + q - (k > 0 ? 1 : 0)), zp = __ldg(src + q + (k < nz - 1 ? 1 : 0));
-        const float mm = (xm + xp + ym + yp + zm + zp) / 6.0f;
-        const float x = 0.5f * __ldg(src + q) + 0.5f * mm;
-        xi[q] = x;
-        if (smax_bits) {
-            const float r = rho[q];
-            const float v = fabsf(mx[q] / r) + fabsf(my[q] / r) + fabsf(mz[q] / r) + sqrtf(cn2 + x * (ci2 - cn2));
-            m = fmaxr(v, m);
+        const long long dxm = w.i > 0 ? si : 0, dxp = w.i < nx - 1 ? si : 0;
+        const long long dym = w.j > 0 ? sj : 0, dyp = w.j < ny - 1 ? sj : 0;
+        for (int k = w.k0; k < nz; k += 32) {
+            const long long q = w.base + k;
+            const float xm = __ldg(src + q - dxm), xp = __ldg(src + q + dxp);
+            const float ym = __ldg(src + q - dym), yp = __ldg(src + q + dyp);
+            const float zm = __ldg(src + q - (k > 0 ? 1 : 0)), zp = __ldg(src + q + (k < nz - 1 ? 1 : 0));
+            const float mm = (xm + xp + ym + yp + zm + zp) / 6.0f;
+            const float x = 0.5f * __ldg(src + q) + 0.5f * mm;
+            xi[q] = x;
+            if (smax_bits) {
+                const float r = rho[q];
+                const float v = fabsf(mx[q] / r) + fabsf(my[q] / r) + fabsf(mz[q] / r) + sqrtf(cn2 + x * (ci2 - cn2));
+                m = fmaxr(v, m);
+            }
         }
     }
     if (!smax_bits) return;
     for (int o = 16; o > 0; o >>= 1) m = fmaxr(m, __shfl_xor_sync(0xffffffffu, m, o));
     __shared__ float red[32];
-    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+    if (threadIdx.x == 0) red[threadIdx.y] = m;
     __syncthreads();
-    if (threadIdx.x == 0) {
+    if (threadIdx.x == 0 && threadIdx.y == 0) {
         float b = 0.0f;
-        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) b = fmaxr(b, red[w]);
+        for (int w = 0; w < (int)blockDim.y; ++w) b = fmaxr(b, red[w]);
         atomicMax(smax_bits, __float_as_uint(b));
     }
-}
-
-int grid_for(long long n, int threads) {
-    long long b = (n + threads - 1) / threads;
-    const long long cap = 152LL * 16;
-    return (int)(b < cap ? (b < 1 ? 1 : b) : cap);
 }
 
 }  // namespace
@@ -212,6 +209,7 @@ cudaError_t nb_launch_cast_rays(const NbConst* c, const NbStarW* sw, const float
     const long long threads = (long long)nu * nphi * nstars * group;
     const int blocks = (int)((threads + 255) / 256);
     switch (group) {
+        case 4: cast_rays_kernel<4><<<blocks, 256, 0, s>>>(c, sw, dirs, rho, rfront, nstars, star_override, q_override); break;
         case 8: cast_rays_kernel<8><<<blocks, 256, 0, s>>>(c, sw, dirs, rho, rfront, nstars, star_override, q_override); break;
         case 16: cast_rays_kernel<16><<<blocks, 256, 0, s>>>(c, sw, dirs, rho, rfront, nstars, star_override, q_override); break;
         default: cast_rays_kernel<32><<<blocks, 256, 0, s>>>(c, sw, dirs, rho, rfront, nstars, star_override, q_override); break;
@@ -220,18 +218,19 @@ cudaError_t nb_launch_cast_rays(const NbConst* c, const NbStarW* sw, const float
 }
 
 cudaError_t nb_launch_apply_front(const NbConst* c, const NbStarW* sw, const float* rfront, int nstars,
-                                  float* xi_raw, void* dfront, unsigned* smax_reset, cudaStream_t s, long long ncell,
+                                  float* xi_raw, void* dfront, unsigned* smax_reset, cudaStream_t s, int nx, int ny,
                                   int half) {
-    const int blocks = grid_for(ncell, 256);
+    const dim3 blk(32, 8);
+    const int blocks = rowwalk_blocks(nx, ny);
     if (half)
-        apply_front_kernel<true><<<blocks, 256, 0, s>>>(c, sw, rfront, nstars, xi_raw, dfront, smax_reset);
+        apply_front_kernel<true><<<blocks, blk, 0, s>>>(c, sw, rfront, nstars, xi_raw, dfront, smax_reset);
     else
-        apply_front_kernel<false><<<blocks, 256, 0, s>>>(c, sw, rfront, nstars, xi_raw, dfront, smax_reset);
+        apply_front_kernel<false><<<blocks, blk, 0, s>>>(c, sw, rfront, nstars, xi_raw, dfront, smax_reset);
     return cudaGetLastError();
 }
 
 cudaError_t nb_launch_smooth(const NbConst* c, const float* xi_raw, float* xi, const float* rho, const float* mx,
-                             const float* my, const float* mz, unsigned* smax_bits, cudaStream_t s, long long ncell) {
-    smooth_kernel<<<grid_for(ncell, 256), 256, 0, s>>>(c, xi_raw, xi, rho, mx, my, mz, smax_bits);
+                             const float* my, const float* mz, unsigned* smax_bits, cudaStream_t s, int nx, int ny) {
+    smooth_kernel<<<rowwalk_blocks(nx, ny), dim3(32, 8), 0, s>>>(c, xi_raw, xi, rho, mx, my, mz, smax_bits);
     return cudaGetLastError();
 }

@@ -55,3 +55,30 @@ __device__ __forceinline__ void nb_box_range(float ox, float oy, float oz, float
 __device__ __forceinline__ int trunc_i(float x) {
     return x > 2e9f ? 2000000000 : (x < -2e9f ? -2000000000 : (int)x);
 }
+
+// Row-major cell walk for the per-cell kernels: blockDim = (32, 8); a thread owns row
+// r = blockIdx.x * 8 + threadIdx.y (r = i * ny + j) and cells k = threadIdx.x + 32 m.
+// One 32-bit division per thread instead of 64-bit divisions per cell.
+struct RowWalk {
+    int i, j, k0;
+    long long base;       // linear index of (i, j, 0)
+    bool valid;
+    __device__ __forceinline__ RowWalk(int nx, int ny, int nz) {
+        const int r = blockIdx.x * blockDim.y + threadIdx.y;
+        valid = r < nx * ny;
+        i = valid ? r / ny : 0;
+        j = valid ? r - i * ny : 0;
+        k0 = threadIdx.x;
+        base = (long long)r * nz;
+    }
+};
+__host__ __forceinline__ int rowwalk_blocks(int nx, int ny) { return (nx * ny + 7) / 8; }
+
+// ((ip % n) + n) % n for the ip in [-1, n] reachable from a float angle in [0, 2 pi]; the
+// general form only when ip falls outside (it cannot for finite inputs).
+__device__ __forceinline__ int wrap_index(int ip, int n) {
+    if (ip >= 0 && ip < n) return ip;
+    if (ip == -1) return n - 1;
+    if (ip == n) return 0;
+    return ((ip % n) + n) % n;
+}
