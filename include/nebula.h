@@ -162,6 +162,24 @@ int nb_cast_rays(nb_handle h, const double star_xyz[3], double Q, float* rfront_
  * reference layout [b][iu][ip]). */
 int nb_cast_fuv(nb_handle h, const double star_xyz[3], float* att_out);
 
+/* ---------------------------------------------------------------- batches
+ * No single reference counterpart: many Sim instances (sim.py:543) advanced together, each
+ * with its own clock, CFL dt, stars and ionization cadence (it % ion_every, sim.py:1102).
+ * A batch step = one control launch for every instance, the ionization of every instance due
+ * to ionize (3 launches), and one persistent launch per RK2 stage walking a tile work-list that
+ * spans all instances; the step is replayed as a CUDA graph when every instance or none
+ * ionizes.  The instances must share solver, limiter and stream; the batch works on its own
+ * stream, ordered after / before the instances' stream by events.  The instance handles stay
+ * valid and usable between batch steps (nb_step, nb_fuv, nb_get_clock ...). */
+typedef struct nb_batch_s* nb_batch;
+enum { NB_BATCH_GRAPHS = 0, NB_BATCH_GRID = 1, NB_BATCH_RAY_GROUP = 2 };
+int nb_batch_create(const nb_handle* instances, const int* ion_every, int n, nb_batch* out);
+int nb_batch_step(nb_batch b, int k);
+int nb_batch_set_option(nb_batch b, int key, int value);
+int nb_batch_counters(nb_batch b, long long* launches);
+void nb_batch_destroy(nb_batch b);
+const char* nb_batch_last_error(nb_batch b);
+
 /* ---------------------------------------------------------------- diagnostics */
 /* Kernel kinds timed by nb_profile (CUDA events on the handle's stream around each launch). */
 enum {

@@ -74,6 +74,12 @@ SIGNATURES = {
     "nb_profile_read": (C.c_int, [_P, C.c_double * 16, C.c_longlong * 16]),
     "nb_counters": (C.c_int, [_P, C.POINTER(C.c_longlong)]),
     "nb_set_tuning": (C.c_int, [_P, C.c_int, C.c_int]),
+    "nb_batch_create": (C.c_int, [C.POINTER(_P), C.POINTER(C.c_int), C.c_int, C.POINTER(_P)]),
+    "nb_batch_step": (C.c_int, [_P, C.c_int]),
+    "nb_batch_set_option": (C.c_int, [_P, C.c_int, C.c_int]),
+    "nb_batch_counters": (C.c_int, [_P, C.POINTER(C.c_longlong)]),
+    "nb_batch_destroy": (None, [_P]),
+    "nb_batch_last_error": (C.c_char_p, [_P]),
     "nb_reduce_fp64_static": (C.c_int, [_P, _P, _P, _P, C.c_longlong, _P, _P]),
     "nb_static_last_error": (C.c_char_p, []),
 }

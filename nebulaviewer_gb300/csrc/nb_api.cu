@@ -2,6 +2,7 @@
 // ionize, fuv_field) over the device kernels, and single-kernel entry points for parity.
 #include <cmath>
 #include <cstdio>
+#include <algorithm>
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -569,4 +570,336 @@ NB_EXPORT int nb_set_tuning(nb_handle h, int key, int value) {
         default:
             return fail(h, NB_ERR_ARG, "unknown tuning key");
     }
+}
+
+// ============================================================================ batches
+// Many instances advanced together: one persistent launch per RK2 stage over a tile work-list
+// spanning all of them (largest instances first), one launch for every instance's control
+// block, three launches for the ionization of every instance due to ionize, and each whole
+// step replayed as a CUDA graph.  Every instance keeps its own clock, CFL dt and cadence.
+struct nb_batch_s {
+    std::vector<nb_instance*> inst;
+    std::vector<int> ion_every;
+    cudaStream_t user = nullptr;        // the instances' stream
+    cudaStream_t bs = nullptr;          // the batch's own stream (capturable)
+    cudaEvent_t ev_in = nullptr, ev_out = nullptr;
+    int solver = 0, limiter = 0, max_stars = 1, grid = 0, ray_group = 4;
+    NbBatchInst* d_inst = nullptr;
+    HydroLaunch* d_L1 = nullptr;
+    HydroLaunch* d_L2 = nullptr;
+    int2* d_work = nullptr;
+    int n_work = 0;
+    unsigned* d_counters = nullptr;
+    NbRayJob* d_jobs_all = nullptr;     // every instance ionizes (the lockstep case)
+    long long all_groups = 0, all_blocks = 0;
+    NbRayJob* d_jobs = nullptr;         // a per-step subset
+    std::vector<NbRayJob> h_all;
+    std::vector<const float*> rfront0;  // each instance's ray scratch when the batch was built
+    std::vector<int> nstars0;
+    int use_graphs = 1;
+    cudaGraphExec_t g_plain = nullptr, g_ion = nullptr;
+    int warm_plain = 0, warm_ion = 0;
+    long long launches = 0;
+    std::string err;
+};
+
+namespace {
+
+int bfail(nb_batch_s* b, int code, const std::string& m) {
+    b->err = m;
+    return code;
+}
+#define BCK(b, call)                                                                        \
+    do {                                                                                    \
+        cudaError_t e_ = (call);                                                            \
+        if (e_ != cudaSuccess) return bfail((b), NB_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+HydroLaunch stage_desc(nb_instance* h, bool stage2) {
+    HydroLaunch L{};
+    const nb_fields& f = h->d.f;
+    L.c = h->c;
+    L.st = h->st;
+    L.sw = h->sw;
+    L.maps = h->maps;
+    L.map_in = stage2 ? NB_MAP_S0 : NB_MAP_RHO;
+    for (int c = 0; c < 4; ++c) {
+        float* S = plane(h, c);
+        float* U[4] = {f.rho, f.mx, f.my, f.mz};
+        L.in[c] = stage2 ? S : U[c];
+        L.u0[c] = U[c];
+        L.out[c] = stage2 ? U[c] : S;
+    }
+    L.xi = f.xi;
+    L.a = stage2 ? 0.5f : 0.0f;
+    L.b = stage2 ? 0.5f : 1.0f;
+    L.smax_bits = stage2 ? &h->st->smax_bits : nullptr;
+    L.status = &h->st->status;
+    const int tj = nb_hydro_tile_j();
+    L.tiles_k = (h->d.nz + 31) / 32;
+    L.tiles_j = (h->d.ny + tj - 1) / tj;
+    L.chunk_i = h->chunk_i < h->d.nx ? h->chunk_i : h->d.nx;
+    L.n_chunks = (h->d.nx + L.chunk_i - 1) / L.chunk_i;
+    L.nstars_host = h->nstars;
+    return L;
+}
+
+NbRayJob ray_job(nb_instance* h) {
+    NbRayJob J{};
+    const nb_fields& f = h->d.f;
+    J.c = h->c;
+    J.sw = h->sw;
+    J.dirs = h->dirs;
+    J.rho = f.rho;
+    J.mx = f.mx;
+    J.my = f.my;
+    J.mz = f.mz;
+    J.rfront = h->rfront;
+    J.xi_raw = plane(h, 0);
+    J.xi = f.xi;
+    J.dfront = f.dfront;
+    J.smax = &h->st->smax_bits;
+    J.nstars = h->nstars;
+    J.half = h->d.fields_fp32 ? 0 : 1;
+    return J;
+}
+
+// prefix sums of ray groups and row blocks over a job list; returns (groups, blocks)
+void job_prefix(std::vector<NbRayJob>& jobs, const std::vector<nb_instance*>& hs, long long& groups, long long& blocks) {
+    groups = 0;
+    blocks = 0;
+    for (size_t e = 0; e < jobs.size(); ++e) {
+        jobs[e].ray0 = groups;
+        jobs[e].blk0 = blocks;
+        groups += (long long)hs[e]->nstars * hs[e]->d.nu * hs[e]->d.nphi;
+        blocks += ((long long)hs[e]->d.nx * hs[e]->d.ny + 7) / 8;
+    }
+}
+
+int batch_hydro(nb_batch_s* b) {
+    b->launches += 3;
+    BCK(b, nb_launch_ctrl_batch(b->d_inst, (int)b->inst.size(), 1, b->d_counters, b->bs));
+    BCK(b, nb_launch_hydro_batch(b->d_L1, b->d_work, b->n_work, b->d_counters + 0, b->max_stars, 0, b->solver,
+                                 b->limiter, b->grid, b->bs));
+    BCK(b, nb_launch_hydro_batch(b->d_L2, b->d_work, b->n_work, b->d_counters + 1, b->max_stars, 1, b->solver,
+                                 b->limiter, b->grid, b->bs));
+    return NB_OK;
+}
+
+int batch_ionize(nb_batch_s* b, const NbRayJob* jobs, int n_jobs, long long groups, long long blocks) {
+    b->launches += 4;
+    BCK(b, nb_launch_ctrl_batch(b->d_inst, (int)b->inst.size(), 0, nullptr, b->bs));
+    BCK(b, nb_launch_ionize_batch(jobs, n_jobs, groups, blocks, b->ray_group, b->bs));
+    return NB_OK;
+}
+
+int batch_run_graph(nb_batch_s* b, cudaGraphExec_t* g, int ion) {
+    if (!*g) {
+        cudaGraph_t graph = nullptr;
+        BCK(b, cudaStreamBeginCapture(b->bs, cudaStreamCaptureModeRelaxed));
+        int rc = ion ? batch_ionize(b, b->d_jobs_all, (int)b->inst.size(), b->all_groups, b->all_blocks) : NB_OK;
+        if (rc == NB_OK) rc = batch_hydro(b);
+        cudaError_t e = cudaStreamEndCapture(b->bs, &graph);
+        if (rc != NB_OK) {
+            if (graph) cudaGraphDestroy(graph);
+            return rc;
+        }
+        if (e != cudaSuccess) return bfail(b, NB_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+        e = cudaGraphInstantiate(g, graph, 0);
+        cudaGraphDestroy(graph);
+        if (e != cudaSuccess) return bfail(b, NB_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
+        b->launches -= ion ? 7 : 3;       // captured, not launched
+    }
+    b->launches += ion ? 7 : 3;
+    BCK(b, cudaGraphLaunch(*g, b->bs));
+    return NB_OK;
+}
+
+}  // namespace
+
+NB_EXPORT const char* nb_batch_last_error(nb_batch b) { return b ? b->err.c_str() : g_err.c_str(); }
+
+NB_EXPORT int nb_batch_create(const nb_handle* hs, const int* ion_every, int n, nb_batch* out) {
+    if (!hs || !ion_every || !out || n < 1) return fail(nullptr, NB_ERR_ARG, "nb_batch_create: bad arguments");
+    *out = nullptr;
+    for (int i = 0; i < n; ++i) {
+        if (!hs[i] || ion_every[i] < 1) return fail(nullptr, NB_ERR_ARG, "nb_batch_create: null handle / ion_every < 1");
+        if (hs[i]->d.solver != hs[0]->d.solver || hs[i]->d.limiter != hs[0]->d.limiter)
+            return fail(nullptr, NB_ERR_ARG, "nb_batch_create: all instances need the same solver and limiter");
+        if (hs[i]->stream != hs[0]->stream)
+            return fail(nullptr, NB_ERR_ARG, "nb_batch_create: all instances need the same stream");
+        if (!hs[i]->hc.phase_main) return fail(nullptr, NB_ERR_STATE, "nb_batch_create: main phase not started");
+        for (int j = 0; j < i; ++j)
+            if (hs[j] == hs[i]) return fail(nullptr, NB_ERR_ARG, "nb_batch_create: an instance appears twice");
+    }
+    nb_batch_s* b = new nb_batch_s();
+    auto bail = [&](int rc, const std::string& m) {
+        g_err = m;
+        nb_batch_destroy(b);
+        return rc;
+    };
+    b->inst.assign(hs, hs + n);
+    b->ion_every.assign(ion_every, ion_every + n);
+    for (int i = 0; i < n; ++i) {
+        b->rfront0.push_back(hs[i]->rfront);
+        b->nstars0.push_back(hs[i]->nstars);
+    }
+    b->user = hs[0]->stream;
+    b->solver = hs[0]->d.solver;
+    b->limiter = hs[0]->d.limiter;
+    b->ray_group = hs[0]->ray_group;
+    for (auto* h : b->inst) b->max_stars = std::max(b->max_stars, h->nstars);
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    b->grid = (sms > 0 ? sms : 152) * 3;
+    if (cudaStreamCreateWithFlags(&b->bs, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&b->ev_in, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&b->ev_out, cudaEventDisableTiming) != cudaSuccess)
+        return bail(NB_ERR_CUDA, "nb_batch_create: stream / event creation failed");
+    // descriptors
+    std::vector<NbBatchInst> bi(n);
+    std::vector<HydroLaunch> L1(n), L2(n);
+    for (int i = 0; i < n; ++i) {
+        nb_instance* h = b->inst[i];
+        bi[i] = NbBatchInst{h->c, h->st, h->stars, h->sw, h->nstars, 0};
+        L1[i] = stage_desc(h, false);
+        L2[i] = stage_desc(h, true);
+    }
+    // work list: largest instances first, each instance's tiles in order
+    std::vector<int> order(n);
+    for (int i = 0; i < n; ++i) order[i] = i;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int c) { return b->inst[a]->ncell > b->inst[c]->ncell; });
+    std::vector<int2> work;
+    for (int i : order) {
+        const int tiles = L1[i].tiles_k * L1[i].tiles_j * L1[i].n_chunks;
+        for (int t = 0; t < tiles; ++t) work.push_back(make_int2(i, t));
+    }
+    b->n_work = (int)work.size();
+    b->h_all.resize(n);
+    for (int i = 0; i < n; ++i) b->h_all[i] = ray_job(b->inst[i]);
+    job_prefix(b->h_all, b->inst, b->all_groups, b->all_blocks);
+    if (cudaMalloc(&b->d_inst, sizeof(NbBatchInst) * n) != cudaSuccess ||
+        cudaMalloc(&b->d_L1, sizeof(HydroLaunch) * n) != cudaSuccess ||
+        cudaMalloc(&b->d_L2, sizeof(HydroLaunch) * n) != cudaSuccess ||
+        cudaMalloc(&b->d_work, sizeof(int2) * work.size()) != cudaSuccess ||
+        cudaMalloc(&b->d_counters, 2 * sizeof(unsigned)) != cudaSuccess ||
+        cudaMalloc(&b->d_jobs_all, sizeof(NbRayJob) * n) != cudaSuccess ||
+        cudaMalloc(&b->d_jobs, sizeof(NbRayJob) * n) != cudaSuccess) {
+        cudaGetLastError();
+        return bail(NB_ERR_NOMEM, "nb_batch_create: device allocation refused");
+    }
+    cudaStream_t s = b->bs;
+    if (cudaMemcpyAsync(b->d_inst, bi.data(), sizeof(NbBatchInst) * n, cudaMemcpyHostToDevice, s) != cudaSuccess ||
+        cudaMemcpyAsync(b->d_L1, L1.data(), sizeof(HydroLaunch) * n, cudaMemcpyHostToDevice, s) != cudaSuccess ||
+        cudaMemcpyAsync(b->d_L2, L2.data(), sizeof(HydroLaunch) * n, cudaMemcpyHostToDevice, s) != cudaSuccess ||
+        cudaMemcpyAsync(b->d_work, work.data(), sizeof(int2) * work.size(), cudaMemcpyHostToDevice, s) != cudaSuccess ||
+        cudaMemcpyAsync(b->d_jobs_all, b->h_all.data(), sizeof(NbRayJob) * n, cudaMemcpyHostToDevice, s) != cudaSuccess ||
+        cudaMemsetAsync(b->d_counters, 0, 2 * sizeof(unsigned), s) != cudaSuccess ||
+        cudaStreamSynchronize(s) != cudaSuccess)
+        return bail(NB_ERR_CUDA, "nb_batch_create: upload failed");
+    *out = b;
+    return NB_OK;
+}
+
+NB_EXPORT void nb_batch_destroy(nb_batch b) {
+    if (!b) return;
+    if (b->bs) cudaStreamSynchronize(b->bs);
+    if (b->g_plain) cudaGraphExecDestroy(b->g_plain);
+    if (b->g_ion) cudaGraphExecDestroy(b->g_ion);
+    void* ps[] = {b->d_inst, b->d_L1, b->d_L2, b->d_work, b->d_counters, b->d_jobs_all, b->d_jobs};
+    for (void* p : ps)
+        if (p) cudaFree(p);
+    if (b->ev_in) cudaEventDestroy(b->ev_in);
+    if (b->ev_out) cudaEventDestroy(b->ev_out);
+    if (b->bs) cudaStreamDestroy(b->bs);
+    delete b;
+}
+
+NB_EXPORT int nb_batch_set_option(nb_batch b, int key, int value) {
+    if (!b) return fail(nullptr, NB_ERR_ARG, "null batch");
+    switch (key) {
+        case NB_BATCH_GRAPHS: b->use_graphs = value ? 1 : 0; return NB_OK;
+        case NB_BATCH_GRID:
+            if (value < 1) return bfail(b, NB_ERR_ARG, "grid must be >= 1");
+            b->grid = value;
+            break;
+        case NB_BATCH_RAY_GROUP:
+            if (value != 4 && value != 8 && value != 16 && value != 32) return bfail(b, NB_ERR_ARG, "bad ray group");
+            b->ray_group = value;
+            break;
+        default: return bfail(b, NB_ERR_ARG, "unknown batch option");
+    }
+    // launch shapes are baked into captured graphs: drop them
+    if (b->bs) cudaStreamSynchronize(b->bs);
+    if (b->g_plain) cudaGraphExecDestroy(b->g_plain);
+    if (b->g_ion) cudaGraphExecDestroy(b->g_ion);
+    b->g_plain = b->g_ion = nullptr;
+    b->warm_plain = b->warm_ion = 0;
+    return NB_OK;
+}
+
+NB_EXPORT int nb_batch_step(nb_batch b, int k) {
+    if (!b) return fail(nullptr, NB_ERR_ARG, "null batch");
+    if (k < 0) return bfail(b, NB_ERR_ARG, "k >= 0 required");
+    const int n = (int)b->inst.size();
+    for (int i = 0; i < n; ++i)
+        if (b->inst[i]->rfront != b->rfront0[i] || b->inst[i]->nstars != b->nstars0[i])
+            return bfail(b, NB_ERR_STATE, "an instance's star table changed size since nb_batch_create: rebuild the batch");
+    BCK(b, cudaEventRecord(b->ev_in, b->user));
+    BCK(b, cudaStreamWaitEvent(b->bs, b->ev_in, 0));
+    // an instance whose CFL max speed is stale and that does not ionize first needs a fresh one
+    for (int i = 0; i < n; ++i) {
+        nb_instance* h = b->inst[i];
+        if (!h->smax_valid && h->host_it % b->ion_every[i] != 0) {
+            const nb_fields& f = h->d.f;
+            BCK(b, nb_launch_max_speed(h->c, f.rho, f.mx, f.my, f.mz, f.xi, &h->st->smax_bits, h->ncell, b->bs));
+            h->smax_valid = 1;
+            b->launches += 2;
+        }
+    }
+    for (int s = 0; s < k; ++s) {
+        std::vector<int> due;
+        for (int i = 0; i < n; ++i)
+            if (b->inst[i]->host_it % b->ion_every[i] == 0) due.push_back(i);
+        int rc = NB_OK;
+        const bool all = (int)due.size() == n, none = due.empty();
+        if (b->use_graphs && (all || none) && (all ? b->warm_ion : b->warm_plain)) {
+            rc = batch_run_graph(b, all ? &b->g_ion : &b->g_plain, all ? 1 : 0);
+        } else {
+            if (all) {
+                rc = batch_ionize(b, b->d_jobs_all, n, b->all_groups, b->all_blocks);
+                b->warm_ion = 1;
+            } else if (!none) {
+                std::vector<NbRayJob> jobs;
+                std::vector<nb_instance*> hs;
+                for (int i : due) {
+                    jobs.push_back(b->h_all[i]);
+                    hs.push_back(b->inst[i]);
+                }
+                long long groups = 0, blocks = 0;
+                job_prefix(jobs, hs, groups, blocks);
+                BCK(b, cudaMemcpyAsync(b->d_jobs, jobs.data(), sizeof(NbRayJob) * jobs.size(), cudaMemcpyHostToDevice,
+                                       b->bs));
+                rc = batch_ionize(b, b->d_jobs, (int)jobs.size(), groups, blocks);
+            } else {
+                b->warm_plain = 1;
+            }
+            if (rc == NB_OK) rc = batch_hydro(b);
+        }
+        if (rc != NB_OK) return rc;
+        for (auto* h : b->inst) {
+            h->host_it += 1;
+            h->smax_valid = 1;
+        }
+    }
+    BCK(b, cudaEventRecord(b->ev_out, b->bs));
+    BCK(b, cudaStreamWaitEvent(b->user, b->ev_out, 0));
+    return NB_OK;
+}
+
+NB_EXPORT int nb_batch_counters(nb_batch b, long long* launches) {
+    if (!b || !launches) return fail(nullptr, NB_ERR_ARG, "null argument");
+    *launches = b->launches;
+    return NB_OK;
 }

@@ -98,11 +98,13 @@ struct HydroSmem {
 #define NB_HYDRO_MINB 3               // resident blocks per SM the register budget is sized for
 #endif
 
+// One (j,k) tile column of one instance, marched over its i-chunk.  Called once per block by
+// the single-instance kernel and once per work item by the persistent batched kernel.  The
+// two mbarriers and their phases persist across calls: every load a call issues, it waits for.
 template <int SOLVER, int LIM, int TJ, bool STAGE2>
-__global__ void __launch_bounds__(TK * TJ, NB_HYDRO_MINB)
-hydro_stage_kernel(const HydroLaunch L) {
+__device__ __forceinline__ void hydro_tile(const HydroLaunch& L, int tile, unsigned char* smem, unsigned& ph0,
+                                           unsigned& ph1, bool& failed) {
     using SM = HydroSmem<TJ>;
-    extern __shared__ __align__(128) unsigned char smem[];
     float* raw = reinterpret_cast<float*>(smem);                                   // [2][5][TJ+4][40]
     float4* prim = reinterpret_cast<float4*>(smem + SM::RAW_BYTES);                // [4][TJ+4][36]
     float2* cs = reinterpret_cast<float2*>(smem + SM::RAW_BYTES + SM::PRIM_BYTES); // [3][TJ+4][36]
@@ -115,7 +117,6 @@ hydro_stage_kernel(const HydroLaunch L) {
     float4* sw_j = sw_w + nstars;
 
     const int tid = threadIdx.x, tk = tid & 31, tj = tid >> 5;
-    int tile = blockIdx.x;
     const int kt = tile % L.tiles_k;
     tile /= L.tiles_k;
     const int jt = tile % L.tiles_j;
@@ -147,20 +148,12 @@ hydro_stage_kernel(const HydroLaunch L) {
         tma_load_3d(dst + 4 * SM::RAW_FIELD, &L.maps[NB_MAP_XI], k0 - 4, j0 - 2, pc, &bar[slot]);
     };
     if (tid == 0) {
-        mbar_init(&bar[0], 1);
-        mbar_init(&bar[1], 1);
-        fence_mbar_init();
-    }
-    __syncthreads();
-    if (tid == 0) {
         issue(P0, 0);
         issue(P0 + 1, 1);
     }
 
     float4 fx_prev = make_float4(0.f, 0.f, 0.f, 0.f);
     float vmax_local = 0.0f;
-    unsigned ph0 = 0, ph1 = 0;
-    bool failed = false;
 
     // clamped global -> raw-tile coordinates
     auto raw_at = [&](int jj, int kk) {      // jj, kk: prim-tile coords
@@ -189,8 +182,10 @@ hydro_stage_kernel(const HydroLaunch L) {
                 u00 = L.u0[0][cell]; u01 = L.u0[1][cell]; u02 = L.u0[2][cell]; u03 = L.u0[3][cell];
             }
         }
-        bool ok = mbar_wait_bounded(&bar[rs], rs ? ph1 : ph0);
-        if (rs) ph1 ^= 1u; else ph0 ^= 1u;
+        const bool ok = mbar_wait_bounded(&bar[rs], rs ? ph1 : ph0);
+        if (ok) {                                // a timed-out slot keeps its parity for the abort wait
+            if (rs) ph1 ^= 1u; else ph0 ^= 1u;
+        }
         if (__syncthreads_or(!ok)) { failed = true; break; }
         const float* rb = raw + rs * 5 * SM::RAW_FIELD;
         float4* pp = prim + ps * PSLOT;
@@ -328,17 +323,8 @@ hydro_stage_kernel(const HydroLaunch L) {
             }
         }
     }
-    if (__syncthreads_or(failed)) {
-        // a TMA wait gave up: record it, let the other slot's copy land (bounded), and leave
-        if (tid == 0) {
-            atomicOr(L.status, NB_DEV_TMA_TIMEOUT);
-            mbar_wait_bounded(&bar[0], ph0);
-            mbar_wait_bounded(&bar[1], ph1);
-        }
-        __syncthreads();
-        return;
-    }
-    if (STAGE2 && L.smax_bits) {
+    if (failed) return;
+    if (STAGE2 && L.smax_bits) {                 // this tile's CFL max speed into its instance
         for (int o = 16; o > 0; o >>= 1) vmax_local = fmaxr(vmax_local, __shfl_xor_sync(0xffffffffu, vmax_local, o));
         float* red = reinterpret_cast<float*>(fy);
         __syncthreads();
@@ -350,6 +336,68 @@ hydro_stage_kernel(const HydroLaunch L) {
             atomicMax(L.smax_bits, __float_as_uint(m));
         }
     }
+}
+
+// a TMA wait gave up: record it, let both slots' copies land (bounded waits), leave
+template <int TJ>
+__device__ __forceinline__ void hydro_abort(unsigned char* smem, unsigned* status, unsigned ph0, unsigned ph1) {
+    using SM = HydroSmem<TJ>;
+    uint64_t* bar = reinterpret_cast<uint64_t*>(smem + SM::FIXED - SM::BAR_BYTES);
+    if (threadIdx.x == 0) {
+        atomicOr(status, NB_DEV_TMA_TIMEOUT);
+        mbar_wait_bounded(&bar[0], ph0);
+        mbar_wait_bounded(&bar[1], ph1);
+    }
+    __syncthreads();
+}
+
+template <int TJ>
+__device__ __forceinline__ void hydro_init_bars(unsigned char* smem) {
+    using SM = HydroSmem<TJ>;
+    uint64_t* bar = reinterpret_cast<uint64_t*>(smem + SM::FIXED - SM::BAR_BYTES);
+    if (threadIdx.x == 0) {
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+}
+
+template <int SOLVER, int LIM, int TJ, bool STAGE2>
+__global__ void __launch_bounds__(TK * TJ, NB_HYDRO_MINB) hydro_stage_kernel(const HydroLaunch L) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    hydro_init_bars<TJ>(smem);
+    unsigned ph0 = 0, ph1 = 0;
+    bool failed = false;
+    hydro_tile<SOLVER, LIM, TJ, STAGE2>(L, blockIdx.x, smem, ph0, ph1, failed);
+    if (failed) hydro_abort<TJ>(smem, L.status, ph0, ph1);
+}
+
+// Persistent batched stage: blocks take (instance, tile) work items from a list spanning many
+// instances of different sizes, in list order, through one atomic counter (reset by the
+// batched control kernel before every step).
+template <int SOLVER, int LIM, int TJ, bool STAGE2>
+__global__ void __launch_bounds__(TK * TJ, NB_HYDRO_MINB)
+hydro_batch_kernel(const HydroLaunch* __restrict__ Ls, const int2* __restrict__ work, int n_work,
+                   unsigned* counter) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    __shared__ int item;
+    hydro_init_bars<TJ>(smem);
+    unsigned ph0 = 0, ph1 = 0;
+    bool failed = false;
+    const HydroLaunch* last = nullptr;
+    for (;;) {
+        if (threadIdx.x == 0) item = (int)atomicAdd(counter, 1u);
+        __syncthreads();
+        const int it = item;
+        if (it >= n_work) break;
+        const int2 w = work[it];
+        last = &Ls[w.x];
+        hydro_tile<SOLVER, LIM, TJ, STAGE2>(*last, w.y, smem, ph0, ph1, failed);
+        if (failed) break;
+        __syncthreads();
+    }
+    if (failed && last) hydro_abort<TJ>(smem, last->status, ph0, ph1);
 }
 
 template <int SOLVER, int LIM, int TJ, bool STAGE2>
@@ -369,6 +417,24 @@ cudaError_t run_stage(const HydroLaunch& L, cudaStream_t s) {
                                              : run_kernel<SOLVER, LIM, TJ, false>(L, s);
 }
 
+template <int SOLVER, int LIM, int TJ, bool STAGE2>
+cudaError_t run_batch_kernel(const HydroLaunch* Ls, const int2* work, int n_work, unsigned* counter,
+                             int max_stars, int grid, cudaStream_t s) {
+    auto kern = hydro_batch_kernel<SOLVER, LIM, TJ, STAGE2>;
+    const int smem = HydroSmem<TJ>::bytes(max_stars);
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e != cudaSuccess) return e;
+    kern<<<grid, TK * TJ, smem, s>>>(Ls, work, n_work, counter);
+    return cudaGetLastError();
+}
+
+template <int SOLVER, int LIM, int TJ>
+cudaError_t run_batch(const HydroLaunch* Ls, const int2* work, int n_work, unsigned* counter, int max_stars,
+                      int stage2, int grid, cudaStream_t s) {
+    return stage2 ? run_batch_kernel<SOLVER, LIM, TJ, true>(Ls, work, n_work, counter, max_stars, grid, s)
+                  : run_batch_kernel<SOLVER, LIM, TJ, false>(Ls, work, n_work, counter, max_stars, grid, s);
+}
+
 }  // namespace
 
 int nb_hydro_tile_j() { return 8; }
@@ -380,5 +446,20 @@ cudaError_t nb_launch_hydro(const HydroLaunch& L, int solver, int limiter, cudaS
         case NB_LIM_VANLEER: return run_stage<NB_SOLVER_HLL, NB_LIM_VANLEER, TJ>(L, s);
         case NB_LIM_MC: return run_stage<NB_SOLVER_HLL, NB_LIM_MC, TJ>(L, s);
         default: return run_stage<NB_SOLVER_HLL, NB_LIM_MINMOD, TJ>(L, s);
+    }
+}
+
+cudaError_t nb_launch_hydro_batch(const HydroLaunch* Ls, const int2* work, int n_work, unsigned* counter,
+                                  int max_stars, int stage2, int solver, int limiter, int grid, cudaStream_t s) {
+    constexpr int TJ = 8;
+    if (solver == NB_SOLVER_RUSANOV)
+        return run_batch<NB_SOLVER_RUSANOV, 0, TJ>(Ls, work, n_work, counter, max_stars, stage2, grid, s);
+    switch (limiter) {
+        case NB_LIM_VANLEER:
+            return run_batch<NB_SOLVER_HLL, NB_LIM_VANLEER, TJ>(Ls, work, n_work, counter, max_stars, stage2, grid, s);
+        case NB_LIM_MC:
+            return run_batch<NB_SOLVER_HLL, NB_LIM_MC, TJ>(Ls, work, n_work, counter, max_stars, stage2, grid, s);
+        default:
+            return run_batch<NB_SOLVER_HLL, NB_LIM_MINMOD, TJ>(Ls, work, n_work, counter, max_stars, stage2, grid, s);
     }
 }

@@ -80,6 +80,36 @@ struct HydroLaunch {
     int nstars_host;             // == c->nstars (sizes the dynamic shared memory)
 };
 
+// One instance of a batch, as the batched control kernel sees it.
+struct NbBatchInst {
+    const NbConst* c;
+    NbState* st;
+    const NbStarDev* stars;
+    NbStarW* sw;
+    int nstars;
+    int pad;
+};
+
+// One instance of a batched ionization (nebula3d.py:247-315 over many instances in 3 launches).
+struct NbRayJob {
+    const NbConst* c;
+    const NbStarW* sw;
+    const float4* dirs;
+    const float* rho;
+    const float* mx;
+    const float* my;
+    const float* mz;
+    float* rfront;
+    float* xi_raw;
+    float* xi;
+    void* dfront;
+    unsigned* smax;
+    long long ray0;       // first ray group of this job (prefix over listed instances)
+    long long blk0;       // first row block of this job (8 rows per block)
+    int nstars;
+    int half;
+};
+
 // ------------------------------------------------------------------ helpers
 __device__ __forceinline__ unsigned smem_u32(const void* p) {
     return static_cast<unsigned>(__cvta_generic_to_shared(p));
@@ -130,8 +160,11 @@ __device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, i
 // ------------------------------------------------------------------ launchers (nb_*.cu)
 cudaError_t nb_launch_hydro(const HydroLaunch& L, int solver, int limiter, cudaStream_t s);
 int nb_hydro_tile_j();
+cudaError_t nb_launch_hydro_batch(const HydroLaunch* Ls, const int2* work, int n_work, unsigned* counter,
+                                  int max_stars, int stage2, int solver, int limiter, int grid, cudaStream_t s);
 cudaError_t nb_launch_ctrl(const NbConst* c, NbState* st, const NbStarDev* stars, NbStarW* sw, int nstars,
                            int advance, cudaStream_t s);
+cudaError_t nb_launch_ctrl_batch(const NbBatchInst* insts, int n, int advance, unsigned* counters, cudaStream_t s);
 cudaError_t nb_launch_weights(const NbConst* c, const NbState* st, const NbStarDev* stars, NbStarW* sw,
                               int nstars, cudaStream_t s);
 cudaError_t nb_launch_max_speed(const NbConst* c, const float* rho, const float* mx, const float* my,
@@ -145,6 +178,8 @@ cudaError_t nb_launch_apply_front(const NbConst* c, const NbStarW* sw, const flo
                                   int half);
 cudaError_t nb_launch_smooth(const NbConst* c, const float* xi_raw, float* xi, const float* rho, const float* mx,
                              const float* my, const float* mz, unsigned* smax_bits, cudaStream_t s, int nx, int ny);
+cudaError_t nb_launch_ionize_batch(const NbRayJob* jobs, int n_jobs, long long n_groups, long long n_blocks, int group,
+                                   cudaStream_t s);
 cudaError_t nb_launch_cast_fuv(const NbConst* c, const NbStarW* sw, const float4* dirs, const float* rho,
                                const float* xi, float* att, int nstars, int group, const float* star_override,
                                int ref_layout, cudaStream_t s, int fnu, int fnphi);

@@ -31,36 +31,21 @@ __global__ void ray_dirs_kernel(int nu, int nphi, float4* __restrict__ dirs) {
     dirs[id] = make_float4(s * cph, s * sph, u, 0.0f);
 }
 
-// nebula3d.py:247-270 cast_rays, G lanes per ray.
+// nebula3d.py:247-270 cast_rays: ray `ray` of star (sx, sy, sz, Q), G lanes per ray.
 template <int G>
-__global__ void __launch_bounds__(256) cast_rays_kernel(const NbConst* __restrict__ c, const NbStarW* __restrict__ sw,
-                                                        const float4* __restrict__ dirs,
-                                                        const float* __restrict__ rho, float* __restrict__ rfront,
-                                                        int nstars, const float* star_override, float q_override) {
-    const int nu = c->nu, nphi = c->nphi, nray = nu * nphi;
-    const long long gid = (blockIdx.x * (long long)blockDim.x + threadIdx.x) / G;
-    const int lane = threadIdx.x % G;
-    const unsigned gmask = G == 32 ? 0xffffffffu : (((1u << G) - 1u) << ((threadIdx.x & 31) / G * G));
-    if (gid >= (long long)nray * nstars) return;
-    const int s = (int)(gid / nray), ray = (int)(gid % nray);
-    float sx, sy, sz, Q;
-    if (star_override) {
-        sx = star_override[0]; sy = star_override[1]; sz = star_override[2]; Q = q_override;
-    } else {
-        const NbStarW w = sw[s];
-        if (!w.active) return;
-        sx = w.w.x; sy = w.w.y; sz = w.w.z; Q = w.q_f;
-    }
-    const int nx = c->nx, ny = c->ny, nz = c->nz;
-    const float dx = c->dx, inv_dx = c->inv_dx, dr = c->dr_f;
-    const bool pow2 = c->dx_pow2 != 0;
+__device__ __forceinline__ void cast_ray(const NbConst& C, const float4* __restrict__ dirs,
+                                         const float* __restrict__ rho, float* __restrict__ out, int ray, float sx,
+                                         float sy, float sz, float Q, int lane, unsigned gmask) {
+    const int nx = C.nx, ny = C.ny, nz = C.nz;
+    const float dx = C.dx, inv_dx = C.inv_dx, dr = C.dr_f;
+    const bool pow2 = C.dx_pow2 != 0;
     const float4 d = dirs[ray];
     float t0, t1;
-    nb_box_range(sx, sy, sz, d.x, d.y, d.z, c->bmax, t0, t1);
+    nb_box_range(sx, sy, sz, d.x, d.y, d.z, C.bmax, t0, t1);
     const int n0 = trunc_i(t0 / dr);
-    const int n1 = min(c->nsteps, trunc_i(t1 / dr) + 2);
+    const int n1 = min(C.nsteps, trunc_i(t1 / dr) + 2);
     float hi = 0.0f, comp = 0.0f;          // Kahan-compensated column carried between segments
-    float rf = c->diag_f;
+    float rf = C.diag_f;
     for (int base = n0; base < n1; base += G) {
         const int n = base + lane;
         const bool valid = n < n1;
@@ -94,34 +79,68 @@ __global__ void __launch_bounds__(256) cast_rays_kernel(const NbConst* __restric
         comp = (tsum - hi) - y;
         hi = tsum;
     }
-    if (lane == 0) rfront[(long long)s * nray + ray] = rf;
+    if (lane == 0) *out = rf;
 }
 
-// nebula3d.py:273-307 rf_at + apply_front, fused over the active stars, with the fp16
-// store of the front distance (sim.py:942, 980-985).
-template <bool HALF>
-__global__ void __launch_bounds__(256) apply_front_kernel(const NbConst* __restrict__ c,
-                                                          const NbStarW* __restrict__ sw,
-                                                          const float* __restrict__ rfront, int nstars,
-                                                          float* __restrict__ xi_raw, void* __restrict__ dfront,
-                                                          unsigned* smax_reset) {
-    __shared__ float4 st[NB_MAX_STARS];
-    __shared__ int act[NB_MAX_STARS];
-    const int tlin = threadIdx.y * blockDim.x + threadIdx.x;
-    for (int s = tlin; s < nstars; s += blockDim.x * blockDim.y) {
-        st[s] = sw[s].w;
-        act[s] = sw[s].active;
+template <int G>
+__global__ void __launch_bounds__(256) cast_rays_kernel(const NbConst* __restrict__ c, const NbStarW* __restrict__ sw,
+                                                        const float4* __restrict__ dirs,
+                                                        const float* __restrict__ rho, float* __restrict__ rfront,
+                                                        int nstars, const float* star_override, float q_override) {
+    const int nray = c->nu * c->nphi;
+    const long long gid = (blockIdx.x * (long long)blockDim.x + threadIdx.x) / G;
+    const int lane = threadIdx.x % G;
+    const unsigned gmask = G == 32 ? 0xffffffffu : (((1u << G) - 1u) << ((threadIdx.x & 31) / G * G));
+    if (gid >= (long long)nray * nstars) return;
+    const int s = (int)(gid / nray), ray = (int)(gid % nray);
+    if (star_override) {
+        cast_ray<G>(*c, dirs, rho, rfront + ray, ray, star_override[0], star_override[1], star_override[2],
+                    q_override, lane, gmask);
+        return;
     }
-    __syncthreads();
-    if (smax_reset && blockIdx.x == 0 && tlin == 0) *smax_reset = 0u;
-    const int nx = c->nx, ny = c->ny, nz = c->nz, nu = c->nu, nphi = c->nphi;
-    const float dx = c->dx, width = c->width;
+    const NbStarW w = sw[s];
+    if (!w.active) return;
+    cast_ray<G>(*c, dirs, rho, rfront + (long long)s * nray + ray, ray, w.w.x, w.w.y, w.w.z, w.q_f, lane, gmask);
+}
+
+// Rays of every star of every listed instance: job e owns groups [job[e].ray0, job[e+1].ray0).
+template <int G>
+__global__ void __launch_bounds__(256) cast_rays_batch_kernel(const NbRayJob* __restrict__ jobs, int n_jobs,
+                                                              long long n_groups) {
+    const long long gid = (blockIdx.x * (long long)blockDim.x + threadIdx.x) / G;
+    const int lane = threadIdx.x % G;
+    const unsigned gmask = G == 32 ? 0xffffffffu : (((1u << G) - 1u) << ((threadIdx.x & 31) / G * G));
+    if (gid >= n_groups) return;
+    int lo = 0, hi = n_jobs - 1;
+    while (lo < hi) {                          // last job with ray0 <= gid
+        const int mid = (lo + hi + 1) >> 1;
+        if (jobs[mid].ray0 <= gid) lo = mid; else hi = mid - 1;
+    }
+    const NbRayJob& J = jobs[lo];
+    const NbConst& C = *J.c;
+    const int nray = C.nu * C.nphi;
+    const long long local = gid - J.ray0;
+    const int s = (int)(local / nray), ray = (int)(local % nray);
+    if (s >= J.nstars) return;
+    const NbStarW w = J.sw[s];
+    if (!w.active) return;
+    cast_ray<G>(C, J.dirs, J.rho, J.rfront + (long long)s * nray + ray, ray, w.w.x, w.w.y, w.w.z, w.q_f, lane, gmask);
+}
+
+// nebula3d.py:273-307 rf_at + apply_front over one row (i, j), fused over the active stars,
+// with the fp16 store of the front distance (sim.py:942, 980-985).
+__device__ __forceinline__ void apply_front_row(const NbConst& C, const float4* st, const int* act, int nstars,
+                                                const float* __restrict__ rfront, float* __restrict__ xi_raw,
+                                                void* __restrict__ dfront, bool half, int row) {
+    const int nx = C.nx, ny = C.ny, nz = C.nz, nu = C.nu, nphi = C.nphi;
+    if (row >= nx * ny) return;
+    const int i = row / ny, j = row - (row / ny) * ny;
+    const long long base = (long long)row * nz;
+    const float dx = C.dx, width = C.width;
     const float two_pi = 2.0f * pi_f();
-    const RowWalk w(nx, ny, nz);
-    if (!w.valid) return;
-    const float px = ((float)w.i + 0.5f) * dx, py = ((float)w.j + 0.5f) * dx;
-    for (int k = w.k0; k < nz; k += 32) {
-        const long long q = w.base + k;
+    const float px = ((float)i + 0.5f) * dx, py = ((float)j + 0.5f) * dx;
+    for (int k = threadIdx.x; k < nz; k += 32) {
+        const long long q = base + k;
         const float pz = ((float)k + 0.5f) * dx;
         float xi = 0.0f, df = 1e3f;
         for (int s = 0; s < nstars; ++s) {
@@ -147,43 +166,85 @@ __global__ void __launch_bounds__(256) apply_front_kernel(const NbConst* __restr
             df = fminr(df, r - rf);
         }
         xi_raw[q] = xi;
-        if (HALF)
+        if (half)
             reinterpret_cast<__half*>(dfront)[q] = __float2half_rn(df);
         else
             reinterpret_cast<float*>(dfront)[q] = df;
     }
 }
 
-// nebula3d.py:310-315 smooth_xi (+ sim.py:941 copy back), then the CFL max speed
+__device__ __forceinline__ int load_stars(const NbStarW* sw, int nstars, float4* st, int* act) {
+    const int tlin = threadIdx.y * blockDim.x + threadIdx.x;
+    for (int s = tlin; s < nstars; s += blockDim.x * blockDim.y) {
+        st[s] = sw[s].w;
+        act[s] = sw[s].active;
+    }
+    __syncthreads();
+    return tlin;
+}
+
+template <bool HALF>
+__global__ void __launch_bounds__(256) apply_front_kernel(const NbConst* __restrict__ c,
+                                                          const NbStarW* __restrict__ sw,
+                                                          const float* __restrict__ rfront, int nstars,
+                                                          float* __restrict__ xi_raw, void* __restrict__ dfront,
+                                                          unsigned* smax_reset) {
+    __shared__ float4 st[NB_MAX_STARS];
+    __shared__ int act[NB_MAX_STARS];
+    const int tlin = load_stars(sw, nstars, st, act);
+    if (smax_reset && blockIdx.x == 0 && tlin == 0) *smax_reset = 0u;
+    apply_front_row(*c, st, act, nstars, rfront, xi_raw, dfront, HALF, blockIdx.x * blockDim.y + threadIdx.y);
+}
+
+// Rows of every listed instance; job e owns blocks [job[e].blk0, job[e+1].blk0) (8 rows each).
+__global__ void __launch_bounds__(256) apply_front_batch_kernel(const NbRayJob* __restrict__ jobs, int n_jobs) {
+    __shared__ float4 st[NB_MAX_STARS];
+    __shared__ int act[NB_MAX_STARS];
+    int lo = 0, hi = n_jobs - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (jobs[mid].blk0 <= (long long)blockIdx.x) lo = mid; else hi = mid - 1;
+    }
+    const NbRayJob& J = jobs[lo];
+    const int lb = (int)(blockIdx.x - J.blk0);
+    const int tlin = load_stars(J.sw, J.nstars, st, act);
+    if (lb == 0 && tlin == 0) *J.smax = 0u;
+    apply_front_row(*J.c, st, act, J.nstars, J.rfront, J.xi_raw, J.dfront, J.half != 0, lb * blockDim.y + threadIdx.y);
+}
+
+// nebula3d.py:310-315 smooth_xi (+ sim.py:941 copy back) of one row, then the CFL max speed
 // (nebula3d.py:154-162) of the state with the new xi.
-__global__ void __launch_bounds__(256) smooth_kernel(const NbConst* __restrict__ c, const float* __restrict__ src,
-                                                     float* __restrict__ xi, const float* __restrict__ rho,
-                                                     const float* __restrict__ mx, const float* __restrict__ my,
-                                                     const float* __restrict__ mz, unsigned* smax_bits) {
-    const int nx = c->nx, ny = c->ny, nz = c->nz;
-    const float cn2 = c->cn2, ci2 = c->ci2;
+__device__ __forceinline__ float smooth_row(const NbConst& C, const float* __restrict__ src, float* __restrict__ xi,
+                                            const float* __restrict__ rho, const float* __restrict__ mx,
+                                            const float* __restrict__ my, const float* __restrict__ mz, bool smax,
+                                            int row) {
+    const int nx = C.nx, ny = C.ny, nz = C.nz;
+    const float cn2 = C.cn2, ci2 = C.ci2;
     float m = 0.0f;
-    const RowWalk w(nx, ny, nz);
-    if (w.valid) {
-        const long long sj = nz, si = (long long)ny * nz;
-        const long long dxm = w.i > 0 ? si : 0, dxp = w.i < nx - 1 ? si : 0;
-        const long long dym = w.j > 0 ? sj : 0, dyp = w.j < ny - 1 ? sj : 0;
-        for (int k = w.k0; k < nz; k += 32) {
-            const long long q = w.base + k;
-            const float xm = __ldg(src + q - dxm), xp = __ldg(src + q + dxp);
-            const float ym = __ldg(src + q - dym), yp = __ldg(src + q + dyp);
-            const float zm = __ldg(src + q - (k > 0 ? 1 : 0)), zp = __ldg(src + q + (k < nz - 1 ? 1 : 0));
-            const float mm = (xm + xp + ym + yp + zm + zp) / 6.0f;
-            const float x = 0.5f * __ldg(src + q) + 0.5f * mm;
-            xi[q] = x;
-            if (smax_bits) {
-                const float r = rho[q];
-                const float v = fabsf(mx[q] / r) + fabsf(my[q] / r) + fabsf(mz[q] / r) + sqrtf(cn2 + x * (ci2 - cn2));
-                m = fmaxr(v, m);
-            }
+    if (row >= nx * ny) return m;
+    const int i = row / ny, j = row - (row / ny) * ny;
+    const long long base = (long long)row * nz;
+    const long long sj = nz, si = (long long)ny * nz;
+    const long long dxm = i > 0 ? si : 0, dxp = i < nx - 1 ? si : 0;
+    const long long dym = j > 0 ? sj : 0, dyp = j < ny - 1 ? sj : 0;
+    for (int k = threadIdx.x; k < nz; k += 32) {
+        const long long q = base + k;
+        const float xm = __ldg(src + q - dxm), xp = __ldg(src + q + dxp);
+        const float ym = __ldg(src + q - dym), yp = __ldg(src + q + dyp);
+        const float zm = __ldg(src + q - (k > 0 ? 1 : 0)), zp = __ldg(src + q + (k < nz - 1 ? 1 : 0));
+        const float mm = (xm + xp + ym + yp + zm + zp) / 6.0f;
+        const float x = 0.5f * __ldg(src + q) + 0.5f * mm;
+        xi[q] = x;
+        if (smax) {
+            const float r = rho[q];
+            const float v = fabsf(mx[q] / r) + fabsf(my[q] / r) + fabsf(mz[q] / r) + sqrtf(cn2 + x * (ci2 - cn2));
+            m = fmaxr(v, m);
         }
     }
-    if (!smax_bits) return;
+    return m;
+}
+
+__device__ __forceinline__ void block_max_to(float m, unsigned* smax_bits) {
     for (int o = 16; o > 0; o >>= 1) m = fmaxr(m, __shfl_xor_sync(0xffffffffu, m, o));
     __shared__ float red[32];
     if (threadIdx.x == 0) red[threadIdx.y] = m;
@@ -193,6 +254,27 @@ __global__ void __launch_bounds__(256) smooth_kernel(const NbConst* __restrict__
         for (int w = 0; w < (int)blockDim.y; ++w) b = fmaxr(b, red[w]);
         atomicMax(smax_bits, __float_as_uint(b));
     }
+}
+
+__global__ void __launch_bounds__(256) smooth_kernel(const NbConst* __restrict__ c, const float* __restrict__ src,
+                                                     float* __restrict__ xi, const float* __restrict__ rho,
+                                                     const float* __restrict__ mx, const float* __restrict__ my,
+                                                     const float* __restrict__ mz, unsigned* smax_bits) {
+    const float m = smooth_row(*c, src, xi, rho, mx, my, mz, smax_bits != nullptr,
+                               blockIdx.x * blockDim.y + threadIdx.y);
+    if (smax_bits) block_max_to(m, smax_bits);
+}
+
+__global__ void __launch_bounds__(256) smooth_batch_kernel(const NbRayJob* __restrict__ jobs, int n_jobs) {
+    int lo = 0, hi = n_jobs - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (jobs[mid].blk0 <= (long long)blockIdx.x) lo = mid; else hi = mid - 1;
+    }
+    const NbRayJob& J = jobs[lo];
+    const int lb = (int)(blockIdx.x - J.blk0);
+    const float m = smooth_row(*J.c, J.xi_raw, J.xi, J.rho, J.mx, J.my, J.mz, true, lb * blockDim.y + threadIdx.y);
+    block_max_to(m, J.smax);
 }
 
 }  // namespace
@@ -232,5 +314,23 @@ cudaError_t nb_launch_apply_front(const NbConst* c, const NbStarW* sw, const flo
 cudaError_t nb_launch_smooth(const NbConst* c, const float* xi_raw, float* xi, const float* rho, const float* mx,
                              const float* my, const float* mz, unsigned* smax_bits, cudaStream_t s, int nx, int ny) {
     smooth_kernel<<<rowwalk_blocks(nx, ny), dim3(32, 8), 0, s>>>(c, xi_raw, xi, rho, mx, my, mz, smax_bits);
+    return cudaGetLastError();
+}
+
+cudaError_t nb_launch_ionize_batch(const NbRayJob* jobs, int n_jobs, long long n_groups, long long n_blocks, int group,
+                                   cudaStream_t s) {
+    if (n_jobs <= 0) return cudaSuccess;
+    const long long threads = n_groups * group;
+    const long long blocks = (threads + 255) / 256;
+    if (blocks > 0) {
+        switch (group) {
+            case 4: cast_rays_batch_kernel<4><<<(unsigned)blocks, 256, 0, s>>>(jobs, n_jobs, n_groups); break;
+            case 8: cast_rays_batch_kernel<8><<<(unsigned)blocks, 256, 0, s>>>(jobs, n_jobs, n_groups); break;
+            case 16: cast_rays_batch_kernel<16><<<(unsigned)blocks, 256, 0, s>>>(jobs, n_jobs, n_groups); break;
+            default: cast_rays_batch_kernel<32><<<(unsigned)blocks, 256, 0, s>>>(jobs, n_jobs, n_groups); break;
+        }
+    }
+    apply_front_batch_kernel<<<(unsigned)n_blocks, dim3(32, 8), 0, s>>>(jobs, n_jobs);
+    smooth_batch_kernel<<<(unsigned)n_blocks, dim3(32, 8), 0, s>>>(jobs, n_jobs);
     return cudaGetLastError();
 }

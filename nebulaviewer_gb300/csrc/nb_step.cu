@@ -38,9 +38,9 @@ __device__ void star_weight(const NbConst& c, const NbStarDev& s, double t, NbSt
     w.pad = 0;
 }
 
-__global__ void ctrl_kernel(const NbConst* __restrict__ c, NbState* __restrict__ st,
-                            const NbStarDev* __restrict__ stars, NbStarW* __restrict__ sw, int nstars,
-                            int advance) {
+__device__ __forceinline__ void ctrl_body(const NbConst* __restrict__ c, NbState* __restrict__ st,
+                                          const NbStarDev* __restrict__ stars, NbStarW* __restrict__ sw, int nstars,
+                                          int advance) {
     const double t = st->t;
     for (int s = threadIdx.x; s < nstars; s += blockDim.x) star_weight(*c, stars[s], t, sw[s]);
     __syncthreads();                                      // every thread has read t before it moves
@@ -59,6 +59,22 @@ __global__ void ctrl_kernel(const NbConst* __restrict__ c, NbState* __restrict__
     st->smax_bits = 0u;                                   // the stage-2 epilogue accumulates the next max
     st->t = __dadd_rn(t, dt);                             // sim.py:1112-1113
     st->it = st->it + 1;
+}
+
+__global__ void ctrl_kernel(const NbConst* __restrict__ c, NbState* __restrict__ st,
+                            const NbStarDev* __restrict__ stars, NbStarW* __restrict__ sw, int nstars,
+                            int advance) {
+    ctrl_body(c, st, stars, sw, nstars, advance);
+}
+
+// one block per instance of a batch; block 0 also resets the persistent stage kernels' counters
+__global__ void ctrl_batch_kernel(const NbBatchInst* __restrict__ insts, int n, int advance, unsigned* counters) {
+    const NbBatchInst& I = insts[blockIdx.x];
+    if (counters && blockIdx.x == 0 && threadIdx.x == 0) {
+        counters[0] = 0u;
+        counters[1] = 0u;
+    }
+    ctrl_body(I.c, I.st, I.stars, I.sw, I.nstars, advance);
 }
 
 // nebula3d.py:154-162 max_speed, as an exact max reduction (atomicMax on the bits of a
@@ -145,6 +161,11 @@ cudaError_t nb_launch_max_speed(const NbConst* c, const float* rho, const float*
                                 const float* mz, const float* xi, unsigned* smax_bits, long n, cudaStream_t s) {
     zero_u32<<<1, 1, 0, s>>>(smax_bits);
     max_speed_kernel<<<1216, 256, 0, s>>>(c, rho, mx, my, mz, xi, smax_bits, n);
+    return cudaGetLastError();
+}
+
+cudaError_t nb_launch_ctrl_batch(const NbBatchInst* insts, int n, int advance, unsigned* counters, cudaStream_t s) {
+    if (n > 0) ctrl_batch_kernel<<<n, 128, 0, s>>>(insts, n, advance, counters);
     return cudaGetLastError();
 }
 

@@ -73,12 +73,18 @@ def solenoidal_velocity(shape, dx, seed, slope, rms, n=96, kmin=1.0, kmax=None, 
     return [s * _eval(shape, dx, kv, ph, amp, device, comp=e[:, c]) for c in range(3)]
 
 
-def torus(res=32, seed=1, device="cpu"):
-    n = 2 * res
-    dx = 1.0 / res
-    shape = (n, n, n)
-    ax = (torch.arange(n, device=device, dtype=torch.float64) + 0.5) * dx - 1.0
-    X, Y, Z = ax[:, None, None], ax[None, :, None], ax[None, None, :]
+def torus(res=32, seed=1, device="cpu", shape=None, nstars=1):
+    """the torus scene; `shape` gives a non-cubic box (dx = 2 / min(shape), torus at the centre),
+    `nstars` > 1 adds seeded weaker stars near the centre"""
+    if shape is None:
+        shape = (2 * res, 2 * res, 2 * res)
+        dx = 1.0 / res
+    else:
+        shape = tuple(int(v) for v in shape)
+        dx = 2.0 / min(shape)
+    c = [0.5 * s * dx for s in shape]
+    ax = [(torch.arange(s, device=device, dtype=torch.float64) + 0.5) * dx - cc for s, cc in zip(shape, c)]
+    X, Y, Z = ax[0][:, None, None], ax[1][None, :, None], ax[2][None, None, :]
     d = torch.sqrt((torch.sqrt(X * X + Y * Y) - 0.4) ** 2 + Z * Z)
     inside = 0.5 * (1.0 - torch.tanh((d - 0.15) / dx))
     sig = 0.3
@@ -87,9 +93,13 @@ def torus(res=32, seed=1, device="cpu"):
     Q = 0.25 ** 3 / 3.0                       # n^2 R^3 / 3 with n = 1, R = 0.25 (no 4 pi in cast_rays)
     P = dict(q_main=Q, wind=0.0, jet=0.0, q_ramp=0.0, kappa_fuv=10.0, cn2=1.0, ci2=144.0, vmax=72.0,
              solver="hll", limiter="minmod", cfl=0.3, floor=2e-3, seed=seed, ion_every=2)
-    stars = [(1.0, 1.0, 1.0, 1.0, 0.0)]
-    return dict(shape=shape, dx=dx, rho=rho, mom=None, stars=stars, kinds=["main"], jets=[(0.0, 0.0, 1.0)],
-                jkinds=["none"], P=P)
+    stars = [(c[0], c[1], c[2], 1.0, 0.0)]
+    rng = np.random.default_rng(seed + 3000)
+    for _ in range(nstars - 1):
+        off = rng.uniform(-0.3, 0.3, 3)
+        stars.append((c[0] + off[0], c[1] + off[1], c[2] + off[2], float(rng.uniform(0.1, 0.5)), 0.0))
+    return dict(shape=shape, dx=dx, rho=rho, mom=None, stars=stars, kinds=["main"] * nstars,
+                jets=[(0.0, 0.0, 1.0)] * nstars, jkinds=["none"] * nstars, P=P)
 
 
 def sheet(res=256, seed=2, nstars=6, device="cpu", shape=None):
@@ -155,3 +165,26 @@ def cliffwall(res=1024, seed=5, nclumps=40, device="cpu", shape=None):
 
 
 SCENARIOS = {"torus": torus, "sheet": sheet, "cliffwall": cliffwall}
+
+
+def batch_scenes(n=32, seed=7, device="cpu", lo=64, hi=192):
+    """The batched workload: n instances, cubes with edges drawn uniformly from [lo, hi]
+    (multiples of 8) plus cropped slabs such as 96 x 160 x 288 (every fourth instance), each
+    the torus or the sheet with its own seed and 1-8 stars."""
+    rng = np.random.default_rng(seed)
+    out = []
+    slabs = [(96, 160, 288), (160, 96, 224), (128, 192, 96)]
+    for m in range(n):
+        if m % 4 == 3:
+            shape = slabs[(m // 4) % len(slabs)]
+        else:
+            e = int(rng.integers(lo // 8, hi // 8 + 1)) * 8
+            shape = (e, e, e)
+        ns = int(rng.integers(1, 9))
+        s = int(rng.integers(1, 1 << 30))
+        if rng.random() < 0.5:
+            ic = torus(seed=s, device=device, shape=shape, nstars=ns)
+        else:
+            ic = sheet(res=min(shape), seed=s, nstars=ns, device=device, shape=shape)
+        out.append(ic)
+    return out
