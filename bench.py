@@ -397,6 +397,40 @@ def run_batch(args):
     return 0
 
 
+def run_served(args):
+    """Served: Poisson arrivals; each request branches from a device snapshot of a 96^3-320^3
+    instance, changes one star's photon rate or the wind by +-50% and runs 10-100 steps;
+    admission under a 150 GB HBM budget at 48 B/cell; continuous batching."""
+    import torch
+    from nebulaviewer_gb300 import build as nb_build
+    nb_build.build(verbose=False)
+    from nebulaviewer_gb300 import ics, serve
+    from nebulaviewer_gb300.sim import Sim
+    dev = torch.device("cuda", 0)
+    snaps = []
+    for m, e in enumerate((96, 160, 256, 320)):
+        ic = (ics.sheet(res=e, seed=40 + m, nstars=4, device=dev) if m % 2 == 0 else
+              ics.torus(seed=50 + m, device=dev, shape=(e, e, e), nstars=3))
+        s = Sim.from_state(ic["shape"], ic["dx"], ic["rho"], ic["stars"], ic["kinds"], ic["jets"], ic["jkinds"],
+                           ic["P"], mom=ic["mom"], device=dev)
+        s.step(8)
+        snaps.append(serve.Snapshot(s))
+        s.close()
+        del ic
+    torch.cuda.synchronize(dev)
+    reqs = serve.poisson_requests(snaps, args.requests, rate=args.rate, seed=1)
+    srv = serve.Server(snaps, budget_bytes=150e9, bytes_per_cell=48, max_slots=64)
+    stats, done = srv.run(reqs, realtime=True)
+    res = {"metric": "served p50/p99 latency and Gcell-updates/s", "value": stats["gcells_per_s"], "unit": UNIT,
+           "n_gpus": 1, "higher_is_better": True, "dtype": "f32", "data": "synthetic",
+           "p50_ms": stats["p50_ms"], "p99_ms": stats["p99_ms"],
+           "config": {"workload": f"{args.requests} requests, Poisson {args.rate:g}/s, snapshots 96^3/160^3/256^3/320^3, "
+                                  "+-50% on a star's Q or the wind, 10-100 steps, 150 GB budget at 48 B/cell"},
+           "stats": stats}
+    print(json.dumps(res), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -405,7 +439,9 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--res", type=int, default=RES, help="grid size (the workload is defined at 256)")
-    ap.add_argument("--workload", default="sheet256", choices=["sheet256", "batch32"])
+    ap.add_argument("--workload", default="sheet256", choices=["sheet256", "batch32", "served"])
+    ap.add_argument("--requests", type=int, default=100)
+    ap.add_argument("--rate", type=float, default=200.0)
     ap.add_argument("--instances", type=int, default=32)
     args = ap.parse_args()
     if args.warmup < 3:
@@ -414,6 +450,8 @@ def main():
         return run_reference(args)
     if args.workload == "batch32":
         return run_batch(args)
+    if args.workload == "served":
+        return run_served(args)
     return run_gb300(args)
 
 

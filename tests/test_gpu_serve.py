@@ -1,0 +1,50 @@
+"""Serving with continuous batching: requests branch from device snapshots, are admitted as
+slots / HBM budget free up, overlap on the device in one batch, and each result is the same
+(bit-identical) as running the request alone."""
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def env():
+    from nebulaviewer_gb300 import build
+    build.build(verbose=False)
+    from nebulaviewer_gb300 import ics, serve, sim
+    bases = [ics.torus(seed=3, device="cuda", shape=(32, 32, 32), nstars=2),
+             ics.sheet(res=24, seed=4, nstars=3, device="cuda", shape=(32, 40, 24))]
+    snaps = []
+    for ic in bases:
+        s = sim.Sim.from_state(ic["shape"], ic["dx"], ic["rho"], ic["stars"], ic["kinds"], ic["jets"], ic["jkinds"],
+                               ic["P"], mom=ic["mom"], rays=(64, 128), fuv_grid=(16, 16, 32))
+        s.step(4)
+        snaps.append(serve.Snapshot(s))
+        s.close()
+    return serve, snaps
+
+
+@pytest.mark.parametrize("slots,budget_cells", ((3, None), (8, 2 * 32 * 40 * 24)))
+def test_served_results_equal_alone(env, slots, budget_cells):
+    serve, snaps = env
+    reqs = serve.poisson_requests(snaps, 8, rate=1000.0, seed=slots, steps=(3, 9))
+    budget = 1e12 if budget_cells is None else 48.0 * budget_cells
+    srv = serve.Server(snaps, budget_bytes=budget, max_slots=slots, keep_state=True)
+    stats, done = srv.run(reqs, realtime=False)
+    assert stats["requests"] == 8 and stats["ticks"] >= max(r.nsteps for r in done)
+    assert stats["batch_rebuilds"] > 1                    # admissions happened while others ran
+    for r in done:
+        ref = serve.run_alone(snaps[r.snap], r)
+        assert r.result["t"] == ref["t"] and r.result["it"] == ref["it"]
+        for a, b in zip(r.result["state"], ref["state"]):
+            assert torch.equal(a, b)
+        assert r.result["totals"] == ref["totals"]
+
+
+def test_snapshot_branch_resumes_the_state(env):
+    serve, snaps = env
+    s = snaps[0].branch()
+    assert torch.equal(s._rho, snaps[0].fields["rho"]) and torch.equal(s._xi, snaps[0].fields["xi"])
+    assert s.it == snaps[0].meta["it"] and s.t == snaps[0].meta["t"]
+    s.close()
