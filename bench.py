@@ -431,6 +431,53 @@ def run_served(args):
     return 0
 
 
+def run_cliff(args):
+    """The large single instance: the 1024^3 ionized cloud wall (density step n = 1 -> 200, 40
+    clumps, the -x plane-parallel source + 3 stars, FUV on), FP64 conservation totals."""
+    import torch
+    from nebulaviewer_gb300 import build as nb_build
+    nb_build.build(verbose=False)
+    from nebulaviewer_gb300.sim import Sim
+    dev = torch.device("cuda", 0)
+    res = args.res if args.res != RES else 1024
+    sim = Sim("cliffwall", res=res, device=dev, verbose=False)
+    m0 = sim.conservation()
+    sim.step(args.warmup)
+    torch.cuda.synchronize(dev)
+    m1 = sim.conservation()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(0) as clk:
+        ev0.record()
+        for _ in range(args.steps):
+            sim.step(1, sync=False)
+            if sim.version % sim.fuv_every == 0:
+                sim.fuv_field()
+        ev1.record()
+        torch.cuda.synchronize(dev)
+    el = ev0.elapsed_time(ev1)
+    m2 = sim.conservation()
+    cells = sim._n
+    val = cells * args.steps / (el * 1e-3) / 1e9
+    peak, peak_kind = measured_peaks()
+    n = len(sim.stars)
+    b_step = 108 + (4 * n + 14 + 4) / sim.ion_every + (8 * n + 2 + 8) / sim.fuv_every
+    res_d = {"metric": METRIC + " 1024^3 cliff wall", "value": val, "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+             "warmup": args.warmup, "ms_per_step": el / args.steps, "higher_is_better": True, "dtype": "f32",
+             "data": "synthetic",
+             "config": {"workload": f"ionized cloud wall {res}^3 fp32 (step n=1->200, 40 clumps), -x plane-parallel "
+                                    f"source + 3 stars, FUV every {sim.fuv_every}", "grid": list(sim.shape),
+                        "state_gb": 40 * cells / 1e9},
+             "fp64_totals": {"mass_t0": m0[0], "mass_after_warmup": m1[0], "mass_end": m2[0],
+                             "rel_change_over_timed_steps": (m2[0] - m1[0]) / m1[0], "momentum_end": list(m2[1:]),
+                             "t_end": sim.t},
+             "step_roofline": {"bytes_per_cell_step": b_step, "achieved": b_step * val, "peak": peak, "unit": "GB/s",
+                               "frac": b_step * val / peak, "peak_source": peak_kind},
+             "clocks": clk.summary()}
+    sim.close()
+    print(json.dumps(res_d), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -439,7 +486,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--res", type=int, default=RES, help="grid size (the workload is defined at 256)")
-    ap.add_argument("--workload", default="sheet256", choices=["sheet256", "batch32", "served"])
+    ap.add_argument("--workload", default="sheet256", choices=["sheet256", "batch32", "served", "cliff1024"])
     ap.add_argument("--requests", type=int, default=100)
     ap.add_argument("--rate", type=float, default=200.0)
     ap.add_argument("--instances", type=int, default=32)
@@ -452,6 +499,8 @@ def main():
         return run_batch(args)
     if args.workload == "served":
         return run_served(args)
+    if args.workload == "cliff1024":
+        return run_cliff(args)
     return run_gb300(args)
 
 

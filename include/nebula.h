@@ -97,6 +97,9 @@ typedef struct nb_live {
     double jet_angle_deg, jet_r;
     double dt_cap;          /* Sim.dt_cap (bake.py:113); <= 0 means none */
     int phase_main;         /* 1 once the main phase started (sim.py:786, 816) */
+    /* plane-parallel source on the -x face (no reference counterpart; 0 = off): ionizing flux F
+     * against the column sum n^2 dx along +x, and FUV luminosity L giving G0 += L exp(-tau) */
+    double plane_flux, plane_fuv;
 } nb_live;
 
 /* One star: sim.py Sim.stars entry (x, y, z, qf, t_on) with its kind, and its jet axis. */

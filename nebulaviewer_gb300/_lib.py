@@ -37,7 +37,8 @@ class NbLive(C.Structure):
     _fields_ = [("q_main", C.c_double), ("wind", C.c_double), ("jet", C.c_double), ("jet_proto", C.c_double),
                 ("jet_pulse", C.c_double), ("jet_period", C.c_double), ("kappa_fuv", C.c_double),
                 ("q_ramp", C.c_double), ("jet_angle_deg", C.c_double), ("jet_r", C.c_double),
-                ("dt_cap", C.c_double), ("phase_main", C.c_int)]
+                ("dt_cap", C.c_double), ("phase_main", C.c_int), ("plane_flux", C.c_double),
+                ("plane_fuv", C.c_double)]
 
 
 class NbStar(C.Structure):

@@ -27,6 +27,7 @@ struct nb_instance {
     float* rfront = nullptr;            // [star][nu][nphi]
     float* att = nullptr;               // [star][fnu][fnphi][fnr]
     float* scratch3 = nullptr;          // 3 floats: a single star position for the one-star kernels
+    float* plane_xf = nullptr;          // [ny][nz] front of the -x plane source
     double* red = nullptr;              // FP64 reduction partials
     int nstars = 0, star_alloc = 0;
     long long host_it = 0;
@@ -179,6 +180,10 @@ int do_ionize(nb_instance* h) {
         CK(h, nb_launch_cast_rays(h->c, h->sw, h->dirs, f.rho, h->rfront, h->nstars, h->ray_group, nullptr, 0.0f,
                                   h->stream, h->d.nu, h->d.nphi));
     }
+    if (h->hc.plane_on) {
+        Prof pf(h, NB_PROF_CAST_RAYS, 1);
+        CK(h, nb_launch_plane_front(h->c, f.rho, h->plane_xf, h->d.ny, h->d.nz, h->stream));
+    }
     float* xi_raw = plane(h, 0);            // sim.py:928-941: xi_tmp lives in the stage block
     {
         Prof pf(h, NB_PROF_APPLY_FRONT, 1);
@@ -290,6 +295,9 @@ NB_EXPORT int nb_create(const nb_desc* d, nb_handle* out) {
     CKC(cudaMalloc(&h->dirs, sizeof(float4) * (size_t)d->nu * d->nphi));
     CKC(cudaMalloc(&h->dirs_fuv, sizeof(float4) * (size_t)d->fnu * d->fnphi));
     CKC(cudaMalloc(&h->scratch3, 4 * sizeof(float)));
+    CKC(cudaMalloc(&h->plane_xf, sizeof(float) * (size_t)d->ny * d->nz));
+    c.plane_xf = h->plane_xf;
+    c.plane_g0 = f.stage + 2 * h->ncell;
     CKC(cudaMalloc(&h->red, sizeof(double) * nb_reduce_scratch_doubles()));
     CKC(cudaMemsetAsync(h->st, 0, sizeof(NbState), h->stream));
     CKC(cudaMemsetAsync(h->sw, 0, sizeof(NbStarW) * d->max_stars, h->stream));
@@ -316,7 +324,7 @@ NB_EXPORT void nb_destroy(nb_handle h) {
     if (h->stream) cudaStreamSynchronize(h->stream);
     else cudaDeviceSynchronize();
     void* ps[] = {h->c, h->st, h->stars, h->sw, h->maps, h->tmp_maps, h->dirs, h->dirs_fuv,
-                  h->rfront, h->att, h->scratch3, h->red};
+                  h->rfront, h->att, h->scratch3, h->red, h->plane_xf};
     for (void* p : ps)
         if (p) cudaFree(p);
     for (auto& r : h->recs) {
@@ -346,6 +354,11 @@ NB_EXPORT int nb_set_live(nb_handle h, const nb_live* L) {
     c.jet_cos_f = (float)c.jet_cos;
     c.jet_r_f = (float)L->jet_r;
     c.kappa_f = (float)L->kappa_fuv;
+    c.plane_F = L->plane_flux;
+    c.plane_lum = L->plane_fuv;
+    c.plane_on = L->plane_flux > 0.0 ? 1 : 0;
+    c.plane_F_f = (float)L->plane_flux;
+    c.plane_lum_f = (float)L->plane_fuv;
     return upload_const(h);
 }
 
@@ -452,6 +465,10 @@ NB_EXPORT int nb_fuv(nb_handle h) {
         Prof pf(h, NB_PROF_CAST_FUV, 1);
         CK(h, nb_launch_cast_fuv(h->c, h->sw, h->dirs_fuv, h->d.f.rho, h->d.f.xi, h->att, h->nstars, h->fuv_group,
                                  nullptr, 0, h->stream, h->d.fnu, h->d.fnphi));
+    }
+    if (h->hc.plane_on) {
+        Prof pf(h, NB_PROF_CAST_FUV, 1);
+        CK(h, nb_launch_plane_fuv(h->c, h->d.f.rho, h->d.f.xi, plane(h, 2), h->d.ny, h->d.nz, h->stream));
     }
     {
         Prof pf(h, NB_PROF_APPLY_FUV, 1);
@@ -597,6 +614,7 @@ struct nb_batch_s {
     std::vector<const float*> rfront0;  // each instance's ray scratch when the batch was built
     std::vector<int> nstars0;
     int use_graphs = 1;
+    int n_plane = 0;                    // instances with the plane source (one extra launch each)
     cudaGraphExec_t g_plain = nullptr, g_ion = nullptr;
     int warm_plain = 0, warm_ion = 0;
     long long launches = 0;
@@ -686,9 +704,16 @@ int batch_hydro(nb_batch_s* b) {
     return NB_OK;
 }
 
-int batch_ionize(nb_batch_s* b, const NbRayJob* jobs, int n_jobs, long long groups, long long blocks) {
+int batch_ionize(nb_batch_s* b, const NbRayJob* jobs, int n_jobs, long long groups, long long blocks,
+                 const std::vector<int>& listed) {
     b->launches += 4;
     BCK(b, nb_launch_ctrl_batch(b->d_inst, (int)b->inst.size(), 0, nullptr, b->bs));
+    for (int i : listed) {
+        nb_instance* h = b->inst[i];
+        if (!h->hc.plane_on) continue;
+        b->launches += 1;
+        BCK(b, nb_launch_plane_front(h->c, h->d.f.rho, h->plane_xf, h->d.ny, h->d.nz, b->bs));
+    }
     BCK(b, nb_launch_ionize_batch(jobs, n_jobs, groups, blocks, b->ray_group, b->bs));
     return NB_OK;
 }
@@ -697,7 +722,9 @@ int batch_run_graph(nb_batch_s* b, cudaGraphExec_t* g, int ion) {
     if (!*g) {
         cudaGraph_t graph = nullptr;
         BCK(b, cudaStreamBeginCapture(b->bs, cudaStreamCaptureModeRelaxed));
-        int rc = ion ? batch_ionize(b, b->d_jobs_all, (int)b->inst.size(), b->all_groups, b->all_blocks) : NB_OK;
+        std::vector<int> all(b->inst.size());
+        for (size_t i = 0; i < all.size(); ++i) all[i] = (int)i;
+        int rc = ion ? batch_ionize(b, b->d_jobs_all, (int)b->inst.size(), b->all_groups, b->all_blocks, all) : NB_OK;
         if (rc == NB_OK) rc = batch_hydro(b);
         cudaError_t e = cudaStreamEndCapture(b->bs, &graph);
         if (rc != NB_OK) {
@@ -708,9 +735,9 @@ int batch_run_graph(nb_batch_s* b, cudaGraphExec_t* g, int ion) {
         e = cudaGraphInstantiate(g, graph, 0);
         cudaGraphDestroy(graph);
         if (e != cudaSuccess) return bfail(b, NB_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
-        b->launches -= ion ? 7 : 3;       // captured, not launched
+        b->launches -= ion ? 7 + b->n_plane : 3;       // captured, not launched
     }
-    b->launches += ion ? 7 : 3;
+    b->launches += ion ? 7 + b->n_plane : 3;
     BCK(b, cudaGraphLaunch(*g, b->bs));
     return NB_OK;
 }
@@ -748,7 +775,10 @@ NB_EXPORT int nb_batch_create(const nb_handle* hs, const int* ion_every, int n, 
     b->solver = hs[0]->d.solver;
     b->limiter = hs[0]->d.limiter;
     b->ray_group = hs[0]->ray_group;
-    for (auto* h : b->inst) b->max_stars = std::max(b->max_stars, h->nstars);
+    for (auto* h : b->inst) {
+        b->max_stars = std::max(b->max_stars, h->nstars);
+        b->n_plane += h->hc.plane_on ? 1 : 0;
+    }
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -868,7 +898,7 @@ NB_EXPORT int nb_batch_step(nb_batch b, int k) {
             rc = batch_run_graph(b, all ? &b->g_ion : &b->g_plain, all ? 1 : 0);
         } else {
             if (all) {
-                rc = batch_ionize(b, b->d_jobs_all, n, b->all_groups, b->all_blocks);
+                rc = batch_ionize(b, b->d_jobs_all, n, b->all_groups, b->all_blocks, due);
                 b->warm_ion = 1;
             } else if (!none) {
                 std::vector<NbRayJob> jobs;
@@ -881,7 +911,7 @@ NB_EXPORT int nb_batch_step(nb_batch b, int k) {
                 job_prefix(jobs, hs, groups, blocks);
                 BCK(b, cudaMemcpyAsync(b->d_jobs, jobs.data(), sizeof(NbRayJob) * jobs.size(), cudaMemcpyHostToDevice,
                                        b->bs));
-                rc = batch_ionize(b, b->d_jobs, (int)jobs.size(), groups, blocks);
+                rc = batch_ionize(b, b->d_jobs, (int)jobs.size(), groups, blocks, due);
             } else {
                 b->warm_plain = 1;
             }

@@ -116,6 +116,8 @@ __global__ void __launch_bounds__(256) apply_fuv_kernel(const NbConst* __restric
     const int nx = c->nx, ny = c->ny, nz = c->nz, nr = c->fnr, nu = c->fnu, nphi = c->fnphi;
     const float dx = c->dx, binr = c->binr_f;
     const float two_pi = 2.0f * pi_f();
+    const int C_plane_on = c->plane_on;
+    const float* C_plane_g0 = c->plane_g0;
     const RowWalk w(nx, ny, nz);
     if (!w.valid) return;
     const float px = ((float)w.i + 0.5f) * dx, py = ((float)w.j + 0.5f) * dx;
@@ -153,6 +155,7 @@ __global__ void __launch_bounds__(256) apply_fuv_kernel(const NbConst* __restric
             const float r2 = fmaxr(r * r, 0.0004f);
             g = g + lum[s] * acc / r2;
         }
+        if (C_plane_on) g = g + __ldg(C_plane_g0 + q);      // the -x plane source, after the stars
         if (HALF)
             reinterpret_cast<__half*>(g0)[q] = __float2half_rn(g);
         else
@@ -160,7 +163,32 @@ __global__ void __launch_bounds__(256) apply_fuv_kernel(const NbConst* __restric
     }
 }
 
+// FUV of the -x plane source (no reference counterpart): per column, the dust optical depth
+// of nebula3d.py:343 summed along +x to each cell centre; G0 term = L exp(-tau).
+__global__ void __launch_bounds__(256) plane_fuv_kernel(const NbConst* __restrict__ c, const float* __restrict__ rho,
+                                                        const float* __restrict__ xi, float* __restrict__ g) {
+    const int nx = c->nx, ny = c->ny, nz = c->nz;
+    const int col = blockIdx.x * blockDim.x + threadIdx.x;
+    if (col >= ny * nz) return;
+    const float kappa = c->kappa_f, dx = c->dx, lum = c->plane_lum_f;
+    const long long plane = (long long)ny * nz;
+    float tau = 0.0f;
+    for (int i = 0; i < nx; ++i) {
+        const long long q = i * plane + col;
+        const float dtau = kappa * __ldg(rho + q) * (1.0f - 0.92f * __ldg(xi + q)) * dx;
+        g[q] = lum * expf(-(tau + 0.5f * dtau));
+        tau = tau + dtau;
+    }
+}
+
 }  // namespace
+
+cudaError_t nb_launch_plane_fuv(const NbConst* c, const float* rho, const float* xi, float* g, int ny, int nz,
+                                cudaStream_t s) {
+    const int cols = ny * nz;
+    plane_fuv_kernel<<<(cols + 255) / 256, 256, 0, s>>>(c, rho, xi, g);
+    return cudaGetLastError();
+}
 
 cudaError_t nb_launch_cast_fuv(const NbConst* c, const NbStarW* sw, const float4* dirs, const float* rho,
                                const float* xi, float* att, int nstars, int group, const float* star_override,

@@ -30,6 +30,12 @@ struct NbConst {
     double q_main, wind, jet, jet_proto, jet_pulse, jet_period, kappa_fuv, q_ramp, jet_r, jet_cos, dt_cap;
     int phase_main;
     float wind_f, jet_cos_f, jet_r_f, kappa_f;
+    // plane-parallel ionizing / FUV source on the -x face (no reference counterpart)
+    int plane_on;
+    float plane_F_f, plane_lum_f;
+    double plane_F, plane_lum;
+    const float* plane_xf;      // [ny][nz] front position along +x per column
+    const float* plane_g0;      // [nx][ny][nz] plane FUV term (stage plane 2, written by the FUV pass)
 };
 
 // Written by device kernels every step.
@@ -180,6 +186,9 @@ cudaError_t nb_launch_smooth(const NbConst* c, const float* xi_raw, float* xi, c
                              const float* my, const float* mz, unsigned* smax_bits, cudaStream_t s, int nx, int ny);
 cudaError_t nb_launch_ionize_batch(const NbRayJob* jobs, int n_jobs, long long n_groups, long long n_blocks, int group,
                                    cudaStream_t s);
+cudaError_t nb_launch_plane_front(const NbConst* c, const float* rho, float* xf, int ny, int nz, cudaStream_t s);
+cudaError_t nb_launch_plane_fuv(const NbConst* c, const float* rho, const float* xi, float* g, int ny, int nz,
+                                cudaStream_t s);
 cudaError_t nb_launch_cast_fuv(const NbConst* c, const NbStarW* sw, const float4* dirs, const float* rho,
                                const float* xi, float* att, int nstars, int group, const float* star_override,
                                int ref_layout, cudaStream_t s, int fnu, int fnphi);

@@ -165,6 +165,12 @@ __device__ __forceinline__ void apply_front_row(const NbConst& C, const float4* 
             if (val > xi) xi = val;
             df = fminr(df, r - rf);
         }
+        if (C.plane_on) {                        // the -x plane-parallel source: same merge rules
+            const float xf = __ldg(C.plane_xf + (long long)j * nz + k);
+            const float val = fminr(fmaxr(0.0f, (xf - px) / width + 0.5f), 1.0f);
+            if (val > xi) xi = val;
+            df = fminr(df, px - xf);
+        }
         xi_raw[q] = xi;
         if (half)
             reinterpret_cast<__half*>(dfront)[q] = __float2half_rn(df);
@@ -277,7 +283,36 @@ __global__ void __launch_bounds__(256) smooth_batch_kernel(const NbRayJob* __res
     block_max_to(m, J.smax);
 }
 
+// Plane-parallel ionizing source on the -x face (no reference counterpart): per (j,k) column, the
+// recombination column sum n^2 dx along +x in cell order, the front where it passes the flux F,
+// interpolated inside the crossing cell as cast_rays does (nebula3d.py:262-268); no front: rcap.
+__global__ void __launch_bounds__(256) plane_front_kernel(const NbConst* __restrict__ c, const float* __restrict__ rho,
+                                                          float* __restrict__ xf) {
+    const int nx = c->nx, ny = c->ny, nz = c->nz;
+    const int col = blockIdx.x * blockDim.x + threadIdx.x;
+    if (col >= ny * nz) return;
+    const float F = c->plane_F_f, dx = c->dx;
+    float sum = 0.0f, x = c->diag_f;
+    const long long plane = (long long)ny * nz;
+    for (int i = 0; i < nx; ++i) {
+        const float n = __ldg(rho + i * plane + col);
+        const float inc = n * n * dx;
+        if (sum + inc > F) {
+            x = ((float)i + 0.5f) * dx - 0.5f * dx + dx * (F - sum) / fmaxr(inc, 1e-20f);
+            break;
+        }
+        sum = sum + inc;
+    }
+    xf[col] = x;
+}
+
 }  // namespace
+
+cudaError_t nb_launch_plane_front(const NbConst* c, const float* rho, float* xf, int ny, int nz, cudaStream_t s) {
+    const int cols = ny * nz;
+    plane_front_kernel<<<(cols + 255) / 256, 256, 0, s>>>(c, rho, xf);
+    return cudaGetLastError();
+}
 
 cudaError_t nb_launch_ray_dirs(int nu, int nphi, float4* dirs, cudaStream_t s) {
     const int n = nu * nphi;

@@ -158,8 +158,11 @@ def cliffwall(res=1024, seed=5, nclumps=40, device="cpu", shape=None):
     stars = [(0.25 * L[0], 0.5 * L[1], 0.5 * L[2], 1.0, 0.0),
              (0.15 * L[0], 0.3 * L[1], 0.65 * L[2], 0.5, 0.0),
              (0.3 * L[0], 0.7 * L[1], 0.35 * L[2], 0.4, 0.0)]
+    # plane-parallel source from -x: the flux ionizes the n = 1 side (column 0.5 x 1^2) and about
+    # 0.02 into the n = 200 wall (200^2 x 0.02 = 800)
     P = dict(q_main=5e-3, wind=0.0, jet=0.0, q_ramp=0.0, kappa_fuv=10.0, cn2=1.0, ci2=144.0, vmax=72.0,
-             solver="hll", limiter="minmod", cfl=0.3, floor=2e-3, seed=seed, ion_every=2)
+             solver="hll", limiter="minmod", cfl=0.3, floor=2e-3, seed=seed, ion_every=2,
+             plane_flux=0.5 * nx * dx + 200.0 ** 2 * 0.02, plane_fuv=5.0)
     return dict(shape=tuple(shape), dx=dx, rho=rho, mom=None, stars=stars, kinds=["main"] * 3,
                 jets=[(0.0, 0.0, 1.0)] * 3, jkinds=["none"] * 3, P=P)
 

@@ -276,7 +276,8 @@ class Sim:
         cap = self._dt_cap if self._dt_cap is not None else -1.0
         live = (float(P["q_main"]), float(P["wind"]), float(P["jet"]), float(P["jet_proto"]), float(P["jet_pulse"]),
                 float(P["jet_period"]), float(P["kappa_fuv"]), float(P.get("q_ramp", 0.0)), float(P["jet_angle"]),
-                float(P["jet_r"]), float(cap), 1 if self.phase == "main" else 0)
+                float(P["jet_r"]), float(cap), 1 if self.phase == "main" else 0,
+                float(P.get("plane_flux", 0.0) or 0.0), float(P.get("plane_fuv", 0.0) or 0.0))
         if force or live != self._live_key:
             L = _lib.NbLive(*live)
             self._chk(self._lib.nb_set_live(self._h, C.byref(L)), "nb_set_live")

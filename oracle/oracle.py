@@ -47,6 +47,9 @@ def lib():
                                                                            C.c_int, C.c_int, C.c_int, P]
             getattr(L, f"oracle_apply_fuv_{sfx}").argtypes = [C.c_int] * 3 + [P, C.c_int, C.c_int, C.c_int, P, T, T,
                                                                             T, P]
+            getattr(L, f"oracle_plane_front_{sfx}").argtypes = [C.c_int] * 3 + [P, T, T, T, P]
+            getattr(L, f"oracle_apply_plane_{sfx}").argtypes = [C.c_int] * 3 + [P, T, T, P, P]
+            getattr(L, f"oracle_plane_fuv_{sfx}").argtypes = [C.c_int] * 3 + [P, P, T, T, T, P]
         L.oracle_to_half.argtypes = [P, P, C.c_long]
         L.oracle_threads.restype = C.c_int
         _LIB = L
@@ -138,6 +141,28 @@ class Kernels:
         s = self._a(np.asarray(star, np.float64).astype(self.dt))
         assert g0.dtype == self.dt
         self._fn("apply_fuv")(nx, ny, nz, _p(a), a.shape[0], a.shape[1], a.shape[2], _p(s), lum, dx, binr, _p(g0))
+
+
+    # the -x plane-parallel source (no reference counterpart)
+    def plane_front(self, rho, F, dx, rcap):
+        nx, ny, nz = rho.shape
+        r = self._a(rho)
+        out = np.zeros((ny, nz), self.dt)
+        self._fn("plane_front")(nx, ny, nz, _p(r), F, dx, rcap, _p(out))
+        return out
+
+    def apply_plane(self, xf, dx, width, xi, dfront):
+        nx, ny, nz = xi.shape
+        x = self._a(xf)
+        assert xi.dtype == self.dt and dfront.dtype == self.dt
+        self._fn("apply_plane")(nx, ny, nz, _p(x), dx, width, _p(xi), _p(dfront))
+
+    def plane_fuv(self, rho, xi, kappa, lum, dx):
+        nx, ny, nz = rho.shape
+        r, x = self._a(rho), self._a(xi)
+        out = np.zeros(rho.shape, self.dt)
+        self._fn("plane_fuv")(nx, ny, nz, _p(r), _p(x), kappa, lum, dx, _p(out))
+        return out
 
 
 def to_half(x):
@@ -254,6 +279,10 @@ class OracleSim:
                                   self.bmax, nu, nphi)
             self.rfront = rf
             self.K.apply_front(rf, (sx, sy, sz), self.dx, 1.2 * self.dx, self.xi, df)
+        F = float(self.P.get("plane_flux", 0.0) or 0.0)
+        if F > 0.0:
+            xf = self.K.plane_front(self.rho, F, self.dx, self.diag)
+            self.K.apply_plane(xf, self.dx, 1.2 * self.dx, self.xi, df)
         self.xi[...] = self.K.smooth_xi(self.xi)
         self._store(df, self.dfront)
 
@@ -272,6 +301,9 @@ class OracleSim:
                                   self.dx, binr, self.bmax, fnr, fnu, fnp)
             self.att = att
             self.K.apply_fuv(att, (sx, sy, sz), self.q_eff(i) / self.P["q_main"], self.dx, binr, acc)
+        if float(self.P.get("plane_flux", 0.0) or 0.0) > 0.0:
+            acc += self.K.plane_fuv(self.rho, self.xi, self.P["kappa_fuv"], float(self.P.get("plane_fuv", 0.0)),
+                                    self.dx)
         self._store(acc, self.g0)
 
     def update_render_fields(self, force=False):                   # sim.py:989-1007

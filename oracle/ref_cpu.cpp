@@ -451,6 +451,61 @@ static void apply_fuv_t(int nx, int ny, int nz, const T* att, int nr, int nu, in
             }
 }
 
+// Plane-parallel source on the -x face (no reference counterpart; the CUDA path defines it the
+// same way): per (j,k) column the column sum n^2 dx along +x, the front interpolated in the
+// crossing cell as in nebula3d.py:262-268, rcap when the flux is never used up.
+template <class T>
+static void plane_front_t(int nx, int ny, int nz, const T* rho, T F, T dx, T rcap, T* xf) {
+    const long long plane = (long long)ny * nz;
+#pragma omp parallel for schedule(static)
+    for (long long col = 0; col < plane; ++col) {
+        T sum = T(0), x = rcap;
+        for (int i = 0; i < nx; ++i) {
+            const T n = rho[i * plane + col];
+            const T inc = n * n * dx;
+            if (sum + inc > F) {
+                x = (T(i) + T(0.5)) * dx - T(0.5) * dx + dx * (F - sum) / tmax(inc, T(1e-20));
+                break;
+            }
+            sum = sum + inc;
+        }
+        xf[col] = x;
+    }
+}
+
+// merge of the plane front into xi / dfront with nebula3d.py:303-307's rules
+template <class T>
+static void apply_plane_t(int nx, int ny, int nz, const T* xf, T dx, T width, T* xi, T* dfront) {
+    Grid g{nx, ny, nz};
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < nx; ++i)
+        for (int j = 0; j < ny; ++j)
+            for (int k = 0; k < nz; ++k) {
+                const T px = (T(i) + T(0.5)) * dx;
+                const T x = xf[(long long)j * nz + k];
+                const T val = tclamp((x - px) / width + T(0.5), T(0), T(1));
+                const long long q = g.idx(i, j, k);
+                if (val > xi[q]) xi[q] = val;
+                dfront[q] = tmin(dfront[q], px - x);
+            }
+}
+
+// FUV of the plane source: tau of nebula3d.py:343 summed along +x to each cell centre
+template <class T>
+static void plane_fuv_t(int nx, int ny, int nz, const T* rho, const T* xi, T kappa, T lum, T dx, T* g) {
+    const long long plane = (long long)ny * nz;
+#pragma omp parallel for schedule(static)
+    for (long long col = 0; col < plane; ++col) {
+        T tau = T(0);
+        for (int i = 0; i < nx; ++i) {
+            const long long q = i * plane + col;
+            const T dtau = kappa * rho[q] * (T(1) - T(0.92) * xi[q]) * dx;
+            g[q] = lum * std::exp(-(tau + T(0.5) * dtau));
+            tau = tau + dtau;
+        }
+    }
+}
+
 // float -> IEEE binary16 bits, round to nearest even (the conversion of sim.py:511-514 to_half)
 static inline uint16_t f32_to_f16_rne(float f) {
     uint32_t x;
@@ -514,6 +569,21 @@ static inline uint16_t f32_to_f16_rne(float f) {
                                                  const T* star, T lum, T dx, T binr, T* g0) {                       \
         apply_fuv_t<T>(nx, ny, nz, att, nr, nu, nphi, star, lum, dx, binr, g0);                                     \
     }
+
+#define INSTANTIATE_PLANE(T, SFX)                                                                           \
+    NB_ORACLE_EXPORT void oracle_plane_front_##SFX(int nx, int ny, int nz, const T* rho, T F, T dx, T rcap, T* xf) {  \
+        plane_front_t<T>(nx, ny, nz, rho, F, dx, rcap, xf);                                                      \
+    }                                                                                                         \
+    NB_ORACLE_EXPORT void oracle_apply_plane_##SFX(int nx, int ny, int nz, const T* xf, T dx, T width, T* xi,     \
+                                                   T* dfront) {                                               \
+        apply_plane_t<T>(nx, ny, nz, xf, dx, width, xi, dfront);                                              \
+    }                                                                                                         \
+    NB_ORACLE_EXPORT void oracle_plane_fuv_##SFX(int nx, int ny, int nz, const T* rho, const T* xi, T kappa, T lum, \
+                                                 T dx, T* g) {                                                \
+        plane_fuv_t<T>(nx, ny, nz, rho, xi, kappa, lum, dx, g);                                               \
+    }
+INSTANTIATE_PLANE(float, f32)
+INSTANTIATE_PLANE(double, f64)
 
 INSTANTIATE(float, f32)
 INSTANTIATE(double, f64)

@@ -30,7 +30,7 @@ def test_struct_layouts_match_header():
     assert C.sizeof(_lib.NbStar) == 8 * 8 + 2 * 4
     assert C.sizeof(_lib.NbClock) == 24
     assert _lib.NbDesc.f.offset % 8 == 0
-    assert C.sizeof(_lib.NbLive) == 11 * 8 + 8
+    assert C.sizeof(_lib.NbLive) == 11 * 8 + 8 + 2 * 8
 
 
 def test_null_handle_errors_without_gpu(lib_built):

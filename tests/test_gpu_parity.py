@@ -255,3 +255,30 @@ def test_sheet_256_deterministic_and_conserving(nb):
     assert torch.equal(a[0], b[0]) and torch.equal(a[1], b[1]) and torch.equal(a[2], b[2])
     assert a[3] == b[3] and a[4] == b[4]
     assert abs(a[4][0] - a[3][0]) / a[3][0] < 5e-3
+
+
+def test_cliffwall_plane_source_against_oracle(nb):
+    """the ionized cloud wall: a density step with clumps, 3 stars and the -x plane-parallel
+    source (no reference counterpart: checked against the oracle's FP32 and FP64 restatement)"""
+    import oracle as O
+    g, o = _oracle_pair(nb, "cliffwall", 64, rays=(128, 256), fuv=(32, 32, 64), nclumps=8)
+    from nebulaviewer_gb300 import ics
+    from nebulaviewer_gb300.params import make_params, sound_speeds
+    ic = ics.cliffwall(res=64, nclumps=8)
+    P = make_params(base=ic["P"])
+    cn2, ci2, vmax = sound_speeds(P)
+    o64 = O.OracleSim(ic["shape"], ic["dx"], ic["rho"].numpy(), ic["stars"], ic["kinds"], ic["jets"], ic["jkinds"],
+                      P, rays=(128, 256), fuv_grid=(32, 32, 64), cn2=cn2, ci2=ci2, vmax=vmax, dtype=np.float64)
+    assert 0.3 < float((g.xi.numpy() > 0.5).mean()) < 0.8        # the plane source ionizes the n = 1 side
+    _compare(g, o, 1e-6)
+    for n in range(6):
+        g.step(1)
+        o.step(1)
+        o64.step(1)
+        _compare(g, o, 1e-5)
+    g.update_render_fields(force=True)
+    o.update_render_fields(force=True)
+    assert rel_linf(g.g0.numpy().astype(np.float32), o.g0.astype(np.float32)) < 5e-3
+    for k in ("rho", "mx"):
+        assert rel_linf(getattr(g, k).numpy(), getattr(o64, k)) < 1e-5
+    g.close()
