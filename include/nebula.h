@@ -183,6 +183,21 @@ int nb_batch_counters(nb_batch b, long long* launches);
 void nb_batch_destroy(nb_batch b);
 const char* nb_batch_last_error(nb_batch b);
 
+/* ---------------------------------------------------------------- snapshots and frames */
+/* timeline.py:19-89 k_pack / k_pack_lm: the 13 B/cell snapshot of the handle's fields into a
+ * device buffer of 13*N bytes, planes [rho fp16 | mx fp16 | my fp16 | mz fp16 | xi uint8 |
+ * dfront fp16 | g0 fp16] (values clamped to +-65000, xi = int(clamp(xi,0,1)*255 + 0.5)). */
+int nb_snapshot_pack(nb_handle h, void* out13);
+/* timeline.py k_unpack / k_unpack_lm: back into the fields (rho floored); the next step
+ * recomputes the CFL max speed. */
+int nb_snapshot_unpack(nb_handle h, const void* in13);
+/* bake.py:95-102: one frame's fields into a device buffer of 9*N bytes, planes [g0 fp16 (min
+ * 6e4) | rho fp16 | xi uint8 (round half even of clip(xi,0,1)*255) | dfront fp16 (clip +-4) |
+ * shock fp16 (min 6e4)], with the shock proxy of nebula3d.py:182-191 computed inline. */
+int nb_frame_pack(nb_handle h, void* out9);
+/* nebula3d.py:182-191 shock_field into a device buffer of N floats (Sim.shock, sim.py:827-833). */
+int nb_shock(nb_handle h, float* out);
+
 /* ---------------------------------------------------------------- diagnostics */
 /* Kernel kinds timed by nb_profile (CUDA events on the handle's stream around each launch). */
 enum {
@@ -195,6 +210,7 @@ enum {
     NB_PROF_CAST_FUV = 6,     /* nebula3d.py:320-352 */
     NB_PROF_APPLY_FUV = 7,    /* nebula3d.py:355-388, all stars */
     NB_PROF_MAX_SPEED = 8,    /* nebula3d.py:154-162 stand-alone */
+    NB_PROF_SNAPSHOT = 9,     /* snapshot / frame packing, shock proxy */
     NB_PROF_KINDS = 16
 };
 /* No reference counterpart (the reference times whole calls with perf_counter, sim.py:578-579):

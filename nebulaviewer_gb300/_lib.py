@@ -75,6 +75,10 @@ SIGNATURES = {
     "nb_profile_read": (C.c_int, [_P, C.c_double * 16, C.c_longlong * 16]),
     "nb_counters": (C.c_int, [_P, C.POINTER(C.c_longlong)]),
     "nb_set_tuning": (C.c_int, [_P, C.c_int, C.c_int]),
+    "nb_snapshot_pack": (C.c_int, [_P, _P]),
+    "nb_snapshot_unpack": (C.c_int, [_P, _P]),
+    "nb_frame_pack": (C.c_int, [_P, _P]),
+    "nb_shock": (C.c_int, [_P, _P]),
     "nb_batch_create": (C.c_int, [C.POINTER(_P), C.POINTER(C.c_int), C.c_int, C.POINTER(_P)]),
     "nb_batch_step": (C.c_int, [_P, C.c_int]),
     "nb_batch_set_option": (C.c_int, [_P, C.c_int, C.c_int]),
@@ -85,7 +89,8 @@ SIGNATURES = {
     "nb_static_last_error": (C.c_char_p, []),
 }
 TUNE = {"chunk_i": 0, "ray_group": 1, "fuv_group": 2}
-PROF_KINDS = ["ctrl", "stage1", "stage2", "cast_rays", "apply_front", "smooth", "cast_fuv", "apply_fuv", "max_speed"]
+PROF_KINDS = ["ctrl", "stage1", "stage2", "cast_rays", "apply_front", "smooth", "cast_fuv", "apply_fuv", "max_speed",
+              "snapshot"]
 
 _lib = None
 

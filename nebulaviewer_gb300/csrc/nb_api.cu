@@ -571,6 +571,42 @@ NB_EXPORT int nb_counters(nb_handle h, long long* launches) {
     return NB_OK;
 }
 
+NB_EXPORT int nb_snapshot_pack(nb_handle h, void* out13) {
+    if (!h || !out13) return fail(h, NB_ERR_ARG, "null argument");
+    const nb_fields& f = h->d.f;
+    Prof pf(h, NB_PROF_SNAPSHOT, 1);
+    CK(h, nb_launch_pack(h->c, f.rho, f.mx, f.my, f.mz, f.xi, f.dfront, f.g0, h->d.fields_fp32 ? 0 : 1, out13,
+                         h->ncell, h->stream));
+    return NB_OK;
+}
+
+NB_EXPORT int nb_snapshot_unpack(nb_handle h, const void* in13) {
+    if (!h || !in13) return fail(h, NB_ERR_ARG, "null argument");
+    const nb_fields& f = h->d.f;
+    Prof pf(h, NB_PROF_SNAPSHOT, 1);
+    CK(h, nb_launch_unpack(h->c, in13, h->ncell, f.rho, f.mx, f.my, f.mz, f.xi, f.dfront, f.g0,
+                           h->d.fields_fp32 ? 0 : 1, h->stream));
+    h->smax_valid = 0;                     // the state changed outside a step
+    return NB_OK;
+}
+
+NB_EXPORT int nb_frame_pack(nb_handle h, void* out9) {
+    if (!h || !out9) return fail(h, NB_ERR_ARG, "null argument");
+    const nb_fields& f = h->d.f;
+    Prof pf(h, NB_PROF_SNAPSHOT, 1);
+    CK(h, nb_launch_frame(h->c, f.rho, f.mx, f.my, f.mz, f.xi, f.dfront, f.g0, h->d.fields_fp32 ? 0 : 1, out9,
+                          h->ncell, h->d.nx, h->d.ny, h->stream));
+    return NB_OK;
+}
+
+NB_EXPORT int nb_shock(nb_handle h, float* out) {
+    if (!h || !out) return fail(h, NB_ERR_ARG, "null argument");
+    const nb_fields& f = h->d.f;
+    Prof pf(h, NB_PROF_SNAPSHOT, 1);
+    CK(h, nb_launch_shock(h->c, f.rho, f.mx, f.my, f.mz, out, h->d.nx, h->d.ny, h->stream));
+    return NB_OK;
+}
+
 NB_EXPORT int nb_set_tuning(nb_handle h, int key, int value) {
     if (!h) return fail(h, NB_ERR_ARG, "null handle");
     switch (key) {

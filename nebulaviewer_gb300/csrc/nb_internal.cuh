@@ -194,6 +194,16 @@ cudaError_t nb_launch_cast_fuv(const NbConst* c, const NbStarW* sw, const float4
                                int ref_layout, cudaStream_t s, int fnu, int fnphi);
 cudaError_t nb_launch_apply_fuv(const NbConst* c, const NbStarW* sw, const float* att, int nstars, void* g0,
                                 cudaStream_t s, int nx, int ny, int half);
+cudaError_t nb_launch_pack(const NbConst* c, const float* rho, const float* mx, const float* my, const float* mz,
+                           const float* xi, const void* df, const void* g0, int half, void* out, long long n,
+                           cudaStream_t s);
+cudaError_t nb_launch_unpack(const NbConst* c, const void* in, long long n, float* rho, float* mx, float* my,
+                             float* mz, float* xi, void* df, void* g0, int half, cudaStream_t s);
+cudaError_t nb_launch_shock(const NbConst* c, const float* rho, const float* mx, const float* my, const float* mz,
+                            float* out, int nx, int ny, cudaStream_t s);
+cudaError_t nb_launch_frame(const NbConst* c, const float* rho, const float* mx, const float* my, const float* mz,
+                            const float* xi, const void* df, const void* g0, int half, void* out, long long n, int nx,
+                            int ny, cudaStream_t s);
 cudaError_t nb_launch_reduce_fp64(const float* rho, const float* mx, const float* my, const float* mz, long n,
                                   double* scratch, cudaStream_t s);   // totals at scratch[4*608 .. +4)
 int nb_reduce_scratch_doubles();

@@ -484,6 +484,52 @@ class Sim:
         self.fuv_nstars = sum(1 for s in self.stars if m["t"] >= s[4])
         self.fuv_phase = self.phase
 
+    # ------------------------------------------------------------------ snapshots and frames
+    def snapshot_pack(self, buf):
+        """the 13 B/cell snapshot (timeline.py:19-89) into a device uint8 buffer of 13 * cells"""
+        if buf.numel() * buf.element_size() < 13 * self._n or not buf.is_cuda:
+            raise ValueError("snapshot buffer must be a device buffer of 13 bytes per cell")
+        self._chk(self._lib.nb_snapshot_pack(self._h, C.c_void_p(buf.data_ptr())), "nb_snapshot_pack")
+
+    def snapshot_unpack(self, buf):
+        """restore the fields from a 13 B/cell snapshot (timeline.py k_unpack)"""
+        if buf.numel() * buf.element_size() < 13 * self._n or not buf.is_cuda:
+            raise ValueError("snapshot buffer must be a device buffer of 13 bytes per cell")
+        self._chk(self._lib.nb_snapshot_unpack(self._h, C.c_void_p(buf.data_ptr())), "nb_snapshot_unpack")
+        self.version += 1
+
+    @property
+    def shock(self):
+        """compression heating proxy max(0, -div v) rho, computed now into a new fp32 grid
+        (nebula3d.py:182-191; sim.py:827-833)"""
+        out = torch.empty(self.shape, dtype=torch.float32, device=self.device)
+        self._chk(self._lib.nb_shock(self._h, C.c_void_p(out.data_ptr())), "nb_shock")
+        return Field(out)
+
+    def frame(self, pinned=None):
+        """one bake frame (bake.py:95-102): quantized on the device, read back in one copy;
+        returns dict(g0, rho, xi, df, sh) of numpy arrays in the reference's dtypes"""
+        n = self._n
+        dev = torch.empty(9 * n, dtype=torch.uint8, device=self.device)
+        self._chk(self._lib.nb_frame_pack(self._h, C.c_void_p(dev.data_ptr())), "nb_frame_pack")
+        host = pinned if pinned is not None else torch.empty(9 * n, dtype=torch.uint8).pin_memory()
+        host.copy_(dev, non_blocking=True)
+        self._sync()
+        b = host.numpy()
+        sh = self.shape
+        f16 = lambda off: b[off:off + 2 * n].view(np.float16).reshape(sh)  # noqa: E731
+        return dict(g0=f16(0), rho=f16(2 * n), xi=b[4 * n:5 * n].reshape(sh), df=f16(5 * n), sh=f16(7 * n))
+
+    def write_frame(self, root, frame):
+        """np.save the frame files f####_{g0,rho,xi,df,sh}.npy as bake.py:95-102 does"""
+        import os
+        fr = self.frame()
+        p = os.path.join(root, "frames", f"f{frame:04d}")
+        os.makedirs(os.path.dirname(p), exist_ok=True)
+        for k in ("g0", "rho", "xi", "df", "sh"):
+            np.save(f"{p}_{k}.npy", fr[k])
+        return fr
+
     def time_label(self):
         return f"t={self.t:.4f}"
 

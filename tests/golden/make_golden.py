@@ -201,6 +201,43 @@ def sim_case(S, scenario, res, overrides, nsteps, fast, rays, fuv, ion_every=Non
     return out
 
 
+def timeline_cases(ref, rng):
+    """timeline.py:19-89: the 13 B/cell snapshot pack / unpack of the reference (k_pack_lm /
+    k_unpack_lm for fp16 dfront / g0, k_pack / k_unpack for fp32)"""
+    sys.path.insert(0, ref)
+    import timeline as T
+    shape = (6, 5, 8)
+    rho = np.exp(rng.normal(0, 3.0, shape)).astype(np.float32)
+    rho.flat[:4] = [70000.0, 1e-9, 65504.0, 3.0e4]
+    mom = (rng.normal(0, 1.0, (3,) + shape) * np.exp(rng.normal(0, 4.0, (3,) + shape))).astype(np.float32)
+    mom[0].flat[:3] = [-1e6, 1e6, -0.0]
+    xi = rng.uniform(-0.2, 1.2, shape).astype(np.float32)
+    xi.flat[:6] = [0.0, 1.0, 0.5 / 255, 1.5 / 255, 254.5 / 255, 0.99999]
+    df32 = rng.normal(0, 2.0, shape).astype(np.float32) * np.float32(1e3)
+    df32.flat[:2] = [1e3, -7e4]
+    g032 = np.exp(rng.normal(0, 5.0, shape)).astype(np.float32)
+    df16, g016 = df32.astype(np.float16), g032.astype(np.float16)
+    out = {"t_rho": rho, "t_mom": mom, "t_xi": xi, "t_df16": df16, "t_g016": g016, "t_df32": df32, "t_g032": g032}
+    for tag, kp, ku, df, g0 in (("lm", T.k_pack_lm, T.k_unpack_lm, df16, g016), ("f32", T.k_pack, T.k_unpack, df32,
+                                                                             g032)):
+        o = [np.zeros(shape, np.float16) for _ in range(4)] + [np.zeros(shape, np.uint8)] + \
+            [np.zeros(shape, np.float16) for _ in range(2)]
+        kp.run(shape, [rho, mom[0], mom[1], mom[2], xi, df, g0] + o)
+        for name, a in zip(("r", "mx", "my", "mz", "xi", "df", "g0"), o):
+            out[f"t_{tag}_pack_{name}"] = a
+        fdt = np.float16 if tag == "lm" else np.float32
+        u = [np.zeros(shape, np.float32) for _ in range(5)] + [np.zeros(shape, fdt) for _ in range(2)]
+        ku.run(shape, o + [2e-3] + u)
+        for name, a in zip(("rho", "mx", "my", "mz", "xi", "df", "g0"), u):
+            out[f"t_{tag}_unpack_{name}"] = a
+    # nebula3d.py:182-191 shock_field on a positive-density state
+    rr = np.exp(rng.normal(0, 1.0, shape)).astype(np.float32) + np.float32(0.01)
+    sh = np.zeros(shape, np.float32)
+    T.N.shock_field.run(shape, [rr, mom[0], mom[1], mom[2], 0.125, sh])
+    out["t_shock_rho"], out["t_shock"] = rr, sh
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference")
@@ -211,6 +248,9 @@ def main():
     if a.only in (None, "kernels"):
         print("kernels:", flush=True)
         np.savez_compressed(os.path.join(HERE, "kernels.npz"), **kernel_cases(N, S, rng))
+    if a.only in (None, "timeline"):
+        print("timeline:", flush=True)
+        np.savez_compressed(os.path.join(HERE, "timeline.npz"), **timeline_cases(a.ref, np.random.default_rng(99)))
     cases = {
         # bubbles: 6 stars, wind, HLL + minmod, fast-mode budgets (dr = dx, ionize every 3 steps)
         "bubbles": dict(scenario="bubbles", res=8, overrides=dict(pre_t=0.0, trigger=0.0, seed=5, min_sep=0.2),
@@ -226,7 +266,7 @@ def main():
                       nsteps=3, fast=True, rays=(8, 16), fuv=(6, 8, 16), ion_every=2),
     }
     for name, c in cases.items():
-        if a.only not in (None, name):
+        if a.only not in (None, name) or a.only == "timeline":
             continue
         print(f"sim {name}:", flush=True)
         np.savez_compressed(os.path.join(HERE, f"sim_{name}.npz"), **sim_case(S, **c))
