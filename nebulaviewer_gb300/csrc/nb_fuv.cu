@@ -34,7 +34,9 @@ __global__ void __launch_bounds__(256) cast_fuv_kernel(const NbConst* __restrict
         sx = w.w.x; sy = w.w.y; sz = w.w.z;
     }
     const int iu = ray / nphi, ip = ray % nphi;
-    // bin b of this ray
+    // bin b of this ray: the reference layout [b][iu][ip], or the instance's [star][u][phi][b] (a ray's
+    // bins contiguous; a u-fastest layout makes the apply's gathers contiguous but scatters these writes,
+    // a net loss measured at 256^3)
     auto at = [&](int b) -> float& {
         return REF_LAYOUT ? att[((long long)b * nu + iu) * nphi + ip]
                           : att[((long long)s * nray + ray) * nr + b];

@@ -100,7 +100,10 @@ __global__ void __launch_bounds__(256) cast_rays_kernel(const NbConst* __restric
     }
     const NbStarW w = sw[s];
     if (!w.active) return;
-    cast_ray<G>(*c, dirs, rho, rfront + (long long)s * nray + ray, ray, w.w.x, w.w.y, w.w.z, w.q_f, lane, gmask);
+    // the instance's table is [star][phi][u] (u fastest: the cells of a warp share phi)
+    const int iu = ray / c->nphi, ip = ray - iu * c->nphi;
+    cast_ray<G>(*c, dirs, rho, rfront + (long long)s * nray + (long long)ip * c->nu + iu, ray, w.w.x, w.w.y, w.w.z,
+                w.q_f, lane, gmask);
 }
 
 // Rays of every star of every listed instance: job e owns groups [job[e].ray0, job[e+1].ray0).
@@ -124,7 +127,9 @@ __global__ void __launch_bounds__(256) cast_rays_batch_kernel(const NbRayJob* __
     if (s >= J.nstars) return;
     const NbStarW w = J.sw[s];
     if (!w.active) return;
-    cast_ray<G>(C, J.dirs, J.rho, J.rfront + (long long)s * nray + ray, ray, w.w.x, w.w.y, w.w.z, w.q_f, lane, gmask);
+    const int iu = ray / C.nphi, ip = ray - iu * C.nphi;
+    cast_ray<G>(C, J.dirs, J.rho, J.rfront + (long long)s * nray + (long long)ip * C.nu + iu, ray, w.w.x, w.w.y, w.w.z,
+                w.q_f, lane, gmask);
 }
 
 // nebula3d.py:273-307 rf_at + apply_front over one row (i, j), fused over the active stars,
@@ -139,31 +144,51 @@ __device__ __forceinline__ void apply_front_row(const NbConst& C, const float4* 
     const float dx = C.dx, width = C.width;
     const float two_pi = 2.0f * pi_f();
     const float px = ((float)i + 0.5f) * dx, py = ((float)j + 0.5f) * dx;
+    const long long rstride = (long long)nu * nphi;
+    constexpr int SG = 4;                       // stars whose gathers are in flight together
     for (int k = threadIdx.x; k < nz; k += 32) {
         const long long q = base + k;
         const float pz = ((float)k + 0.5f) * dx;
         float xi = 0.0f, df = 1e3f;
-        for (int s = 0; s < nstars; ++s) {
-            if (!act[s]) continue;
-            const float4 sp = st[s];
-            const float rx = px - sp.x, ry = py - sp.y, rz = pz - sp.z;
-            const float r = fmaxr(sqrtf((rx * rx + ry * ry) + rz * rz), 1e-6f);     // 0 + x*x == x*x
-            const float u = rz / r;
-            float phi = atan2f(ry, rx);
-            if (phi < 0.0f) phi = phi + two_pi;
-            const float fu = (u + 1.0f) * 0.5f * (float)nu - 0.5f;
-            const float fp = phi / two_pi * (float)nphi - 0.5f;
-            const int iu = (int)floorf(fu), ip = (int)floorf(fp);
-            const float tu = fu - (float)iu, tp = fp - (float)ip;
-            const float* rfs = rfront + (long long)s * nu * nphi;
-            const int u0 = iclampd(iu, 0, nu - 1), u1 = iclampd(iu + 1, 0, nu - 1);
-            const int p0 = wrap_index(ip, nphi), p1 = wrap_index(ip + 1, nphi);
-            const float ra = __ldg(rfs + u0 * nphi + p0) * (1.0f - tp) + __ldg(rfs + u0 * nphi + p1) * tp;
-            const float rb = __ldg(rfs + u1 * nphi + p0) * (1.0f - tp) + __ldg(rfs + u1 * nphi + p1) * tp;
-            const float rf = ra * (1.0f - tu) + rb * tu;
-            const float val = fminr(fmaxr(0.0f, (rf - r) / width + 0.5f), 1.0f);
-            if (val > xi) xi = val;
-            df = fminr(df, r - rf);
+        for (int s0 = 0; s0 < nstars; s0 += SG) {
+            float r[SG], tu[SG], tp[SG], g00[SG], g01[SG], g10[SG], g11[SG];
+            bool on[SG];
+#pragma unroll
+            for (int e = 0; e < SG; ++e) {
+                const int s = s0 + e;
+                on[e] = s < nstars && act[s];
+                r[e] = tu[e] = tp[e] = 0.0f;
+                g00[e] = g01[e] = g10[e] = g11[e] = 0.0f;
+                if (!on[e]) continue;
+                const float4 sp = st[s];
+                const float rx = px - sp.x, ry = py - sp.y, rz = pz - sp.z;
+                r[e] = fmaxr(sqrtf((rx * rx + ry * ry) + rz * rz), 1e-6f);     // 0 + x*x == x*x
+                const float u = rz / r[e];
+                float phi = atan2f(ry, rx);
+                if (phi < 0.0f) phi = phi + two_pi;
+                const float fu = (u + 1.0f) * 0.5f * (float)nu - 0.5f;
+                const float fp = phi / two_pi * (float)nphi - 0.5f;
+                const int iu = (int)floorf(fu), ip = (int)floorf(fp);
+                tu[e] = fu - (float)iu;
+                tp[e] = fp - (float)ip;
+                const float* rfs = rfront + (long long)s * rstride;
+                const int u0 = iclampd(iu, 0, nu - 1), u1 = iclampd(iu + 1, 0, nu - 1);
+                const int p0 = wrap_index(ip, nphi), p1 = wrap_index(ip + 1, nphi);
+                g00[e] = __ldg(rfs + p0 * nu + u0);      // table [phi][u]
+                g01[e] = __ldg(rfs + p1 * nu + u0);
+                g10[e] = __ldg(rfs + p0 * nu + u1);
+                g11[e] = __ldg(rfs + p1 * nu + u1);
+            }
+#pragma unroll
+            for (int e = 0; e < SG; ++e) {
+                if (!on[e]) continue;
+                const float ra = g00[e] * (1.0f - tp[e]) + g01[e] * tp[e];
+                const float rb = g10[e] * (1.0f - tp[e]) + g11[e] * tp[e];
+                const float rf = ra * (1.0f - tu[e]) + rb * tu[e];
+                const float val = fminr(fmaxr(0.0f, (rf - r[e]) / width + 0.5f), 1.0f);
+                if (val > xi) xi = val;              // max / min merges are exact and order-free
+                df = fminr(df, r[e] - rf);
+            }
         }
         if (C.plane_on) {                        // the -x plane-parallel source: same merge rules
             const float xf = __ldg(C.plane_xf + (long long)j * nz + k);
@@ -233,6 +258,7 @@ __device__ __forceinline__ float smooth_row(const NbConst& C, const float* __res
     const long long sj = nz, si = (long long)ny * nz;
     const long long dxm = i > 0 ? si : 0, dxp = i < nx - 1 ? si : 0;
     const long long dym = j > 0 ? sj : 0, dyp = j < ny - 1 ? sj : 0;
+#pragma unroll 4
     for (int k = threadIdx.x; k < nz; k += 32) {
         const long long q = base + k;
         const float xm = __ldg(src + q - dxm), xp = __ldg(src + q + dxp);
