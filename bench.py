@@ -71,7 +71,7 @@ def ncu_traffic():
 
 
 class ClockSampler:
-    """nvidia-smi clocks / throttle reasons sampled every 200 ms during the timed region"""
+    """nvidia-smi clocks / throttle reasons sampled every 50 ms during the timed region"""
 
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
          "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
@@ -84,7 +84,7 @@ class ClockSampler:
     def __enter__(self):
         try:
             self.p = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
-                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                       "--format=csv,noheader,nounits", "-lms", "50"],
                                       stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
         except OSError:
             self.p = None
@@ -119,6 +119,20 @@ class ClockSampler:
         if not sm:
             return None
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def replica_throughput(local_ms, cells, steps, dist=None, device="cpu"):
+    """whole-job Gcell-updates/s of N independent replicas: every rank advanced `cells` cells for
+    `steps` steps; the job time is the slowest rank's (max over ranks)"""
+    import torch
+    ws = 1
+    t_max = float(local_ms)
+    if dist is not None and dist.is_initialized():
+        ws = dist.get_world_size()
+        t = torch.tensor([float(local_ms)], dtype=torch.float64, device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_max = float(t.item())
+    return ws * cells * steps / (t_max * 1e-3) / 1e9, t_max
 
 
 def algorithmic_bytes(kind, ncell, nstars):
@@ -231,6 +245,8 @@ def run_gb300(args):
             if sim.version % sim.fuv_every == 0:          # the render-field cadence (sim.py:997-1002)
                 sim.fuv_field()
 
+    from nebulaviewer_gb300.autotune import autotune
+    tuning = {k: v[0] for k, v in autotune(sim).items()}       # untimed: launch shapes for this problem
     device_steps(args.warmup)
     torch.cuda.synchronize(dev)
     # ---------------- device-resident throughput (the metric's value)
@@ -257,12 +273,7 @@ def run_gb300(args):
     l1 = C.c_longlong()
     lib.nb_counters(sim._h, C.byref(l1))
     launches = int(l1.value - l0.value)
-    t_max = el_ms
-    if dist:
-        t = torch.tensor([el_ms], device=dev, dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_max = float(t.item())
-    value = ws * ncell * args.steps / (t_max * 1e-3) / 1e9
+    value, t_max = replica_throughput(el_ms, ncell, args.steps, dist, dev)
     # ---------------- end to end through the public API with host buffers
     # every step: sim.step(1) (returns after the step finished), the live-parameter block
     # pushed H2D as a caller that edits P each step does (bake.py), and the clock read D2H
@@ -317,7 +328,8 @@ def run_gb300(args):
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": workload(args.res), "grid": list(sim.shape), "stars": nstars, "ion_every": ion_every,
                        "fuv_every": fuv_every, "rays": list(sim.rfront.shape), "fuv_grid": list(sim.att.shape),
-                       "parallelism": f"replicas x{ws}", "l2": f"state {40 * ncell / 1e9:.2f} GB vs 129 MB L2 (no flush)"},
+                       "parallelism": f"replicas x{ws}", "l2": f"state {40 * ncell / 1e9:.2f} GB vs 129 MB L2 (no flush)",
+                       "tuning": tuning},
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_source": peak_kind,
                          "traffic": traffic, "algorithmic_bytes_per_launch": dom_bytes,

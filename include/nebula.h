@@ -218,11 +218,13 @@ enum {
  * summed milliseconds and launch counts per kind since the last read, and resets them. */
 int nb_profile(nb_handle h, int enable);
 int nb_profile_read(nb_handle h, double ms[NB_PROF_KINDS], long long count[NB_PROF_KINDS]);
-/* Launch-shape knobs picked by the package's autotuner (no reference counterpart): the i-chunk
- * of the hydro march, and the lanes per ray (4, 8, 16, 32 ionizing; 8, 16, 32 FUV) of the ray kernels.
- * Results do not depend on them except through the rounding of the ray sums. */
-enum { NB_TUNE_CHUNK_I = 0, NB_TUNE_RAY_GROUP = 1, NB_TUNE_FUV_GROUP = 2 };
+/* Launch-shape knobs picked by the package's autotuner (no reference counterpart): the tile depth
+ * along i of the hydro march (i-chunk), the tile sweep order (0: k, j, i-chunk; 1: i-chunk, k, j),
+ * and the lanes per ray (4, 8, 16, 32 ionizing; 8, 16, 32 FUV) of the ray kernels.  The hydro
+ * result does not depend on them; the ray sums only through their rounding. */
+enum { NB_TUNE_CHUNK_I = 0, NB_TUNE_RAY_GROUP = 1, NB_TUNE_FUV_GROUP = 2, NB_TUNE_TILE_ORDER = 3 };
 int nb_set_tuning(nb_handle h, int key, int value);
+int nb_get_tuning(nb_handle h, int key, int* value);
 /* Number of kernels the handle has launched (a claim the benchmark reports). */
 int nb_counters(nb_handle h, long long* launches);
 

@@ -75,6 +75,7 @@ SIGNATURES = {
     "nb_profile_read": (C.c_int, [_P, C.c_double * 16, C.c_longlong * 16]),
     "nb_counters": (C.c_int, [_P, C.POINTER(C.c_longlong)]),
     "nb_set_tuning": (C.c_int, [_P, C.c_int, C.c_int]),
+    "nb_get_tuning": (C.c_int, [_P, C.c_int, C.POINTER(C.c_int)]),
     "nb_snapshot_pack": (C.c_int, [_P, _P]),
     "nb_snapshot_unpack": (C.c_int, [_P, _P]),
     "nb_frame_pack": (C.c_int, [_P, _P]),
@@ -88,7 +89,7 @@ SIGNATURES = {
     "nb_reduce_fp64_static": (C.c_int, [_P, _P, _P, _P, C.c_longlong, _P, _P]),
     "nb_static_last_error": (C.c_char_p, []),
 }
-TUNE = {"chunk_i": 0, "ray_group": 1, "fuv_group": 2}
+TUNE = {"chunk_i": 0, "ray_group": 1, "fuv_group": 2, "tile_order": 3}
 PROF_KINDS = ["ctrl", "stage1", "stage2", "cast_rays", "apply_front", "smooth", "cast_fuv", "apply_fuv", "max_speed",
               "snapshot"]
 

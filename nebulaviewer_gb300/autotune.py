@@ -1,0 +1,100 @@
+"""A launch-shape autotuner for one simulation instance.
+
+Knobs (nb_set_tuning): the tile depth along i of the hydro march (`chunk_i`: the tile shape of
+the persistent 2.5-D sweep), the tile sweep order (`tile_order`), and the lanes per ray of the
+ionizing and FUV ray kernels (`ray_group`, `fuv_group`).  Each knob is tuned in turn
+(coordinate descent) on the instance's own state: the state and clock are saved, every
+candidate runs a few steps (or FUV passes) timed by the library's per-kernel CUDA events, the
+state is restored, and the fastest candidate is kept.  The hydro result never depends on these
+knobs; the ray sums only through rounding.  Results are cached per problem shape.
+"""
+import ctypes as C
+
+import torch
+
+from . import _lib
+
+CANDIDATES = {
+    "chunk_i": (16, 32, 64),
+    "tile_order": (0, 1),
+    "ray_group": (4, 8, 16),
+    "fuv_group": (8, 16, 32),
+}
+# which kernel kinds a knob moves (names of _lib.PROF_KINDS)
+AFFECTS = {"chunk_i": ("stage1", "stage2"), "tile_order": ("stage1", "stage2"), "ray_group": ("cast_rays",),
+           "fuv_group": ("cast_fuv",)}
+
+_CACHE = {}
+
+
+def _key(sim):
+    return (tuple(sim.shape), len(sim.stars), tuple(sim.rfront.shape), tuple(sim.att.shape), sim.P.get("solver"))
+
+
+def get(sim, knob):
+    v = C.c_int()
+    _lib.check(sim._lib.nb_get_tuning(sim._h, _lib.TUNE[knob], C.byref(v)), sim._h, "nb_get_tuning")
+    return int(v.value)
+
+
+def put(sim, knob, value):
+    _lib.check(sim._lib.nb_set_tuning(sim._h, _lib.TUNE[knob], int(value)), sim._h, "nb_set_tuning")
+
+
+def _measure(sim, knob, steps):
+    lib = sim._lib
+    ms = (C.c_double * 16)()
+    n = (C.c_longlong * 16)()
+    lib.nb_profile(sim._h, 1)
+    lib.nb_profile_read(sim._h, ms, n)
+    if knob == "fuv_group":
+        for _ in range(steps):
+            sim.fuv_field()
+    elif knob == "ray_group":
+        for _ in range(steps):
+            sim.ionize()
+    else:
+        sim.step(steps, sync=False)
+    lib.nb_profile_read(sim._h, ms, n)
+    lib.nb_profile(sim._h, 0)
+    idx = [_lib.PROF_KINDS.index(k) for k in AFFECTS[knob]]
+    return sum(ms[i] for i in idx) / max(1, max(n[i] for i in idx))
+
+
+def autotune(sim, knobs=None, steps=4, use_cache=True):
+    """pick the fastest launch shapes for `sim` (its state and clock are left unchanged);
+    returns {knob: (value, ms per launch)}"""
+    key = _key(sim)
+    if use_cache and key in _CACHE:
+        for k, (v, _) in _CACHE[key].items():
+            put(sim, k, v)
+        return dict(_CACHE[key])
+    sim._sync()
+    saved = {k: getattr(sim, "_" + k).clone() for k in ("rho", "mx", "my", "mz", "xi", "dfront", "g0")}
+    clock = sim._clock()
+    it0, ver0 = sim._it, sim.version
+
+    def restore():
+        for k, t in saved.items():
+            getattr(sim, "_" + k).copy_(t)
+        sim._set_clock(t=clock.t, dt=clock.dt, it=clock.it)
+        sim.invalidate()
+        sim._it, sim.version = it0, ver0
+
+    out = {}
+    for knob in knobs or CANDIDATES:
+        best = None
+        for v in CANDIDATES[knob]:
+            put(sim, knob, v)
+            restore()
+            _measure(sim, knob, 1)                     # warm the launch path
+            restore()
+            t = _measure(sim, knob, steps)
+            if best is None or t < best[1]:
+                best = (v, t)
+        put(sim, knob, best[0])
+        out[knob] = best
+    restore()
+    sim._sync()
+    _CACHE[key] = dict(out)
+    return out

@@ -33,6 +33,7 @@ struct nb_instance {
     long long host_it = 0;
     int smax_valid = 0;
     int chunk_i = 32, ray_group = 4, fuv_group = 16;      // measured best at 256^3 (nb_set_tuning)
+    int tile_order = 0;
     long long ncell = 0;
     long long launches = 0;             // kernels this handle launched (nb_counters)
     int profiling = 0;                  // CUDA-event timing per kernel kind (nb_profile)
@@ -164,6 +165,7 @@ int launch_stage(nb_instance* h, const float* const in[4], const float* const u0
     L.chunk_i = h->chunk_i < h->d.nx ? h->chunk_i : h->d.nx;
     L.n_chunks = (h->d.nx + L.chunk_i - 1) / L.chunk_i;
     L.nstars_host = h->nstars;
+    L.order = h->tile_order;
     Prof pf(h, smax ? NB_PROF_STAGE2 : NB_PROF_STAGE1, 1);
     CK(h, nb_launch_hydro(L, h->d.solver, h->d.limiter, h->stream));
     return NB_OK;
@@ -607,12 +609,27 @@ NB_EXPORT int nb_shock(nb_handle h, float* out) {
     return NB_OK;
 }
 
+NB_EXPORT int nb_get_tuning(nb_handle h, int key, int* value) {
+    if (!h || !value) return fail(h, NB_ERR_ARG, "null argument");
+    switch (key) {
+        case NB_TUNE_CHUNK_I: *value = h->chunk_i; return NB_OK;
+        case NB_TUNE_RAY_GROUP: *value = h->ray_group; return NB_OK;
+        case NB_TUNE_FUV_GROUP: *value = h->fuv_group; return NB_OK;
+        case NB_TUNE_TILE_ORDER: *value = h->tile_order; return NB_OK;
+        default: return fail(h, NB_ERR_ARG, "unknown tuning key");
+    }
+}
+
 NB_EXPORT int nb_set_tuning(nb_handle h, int key, int value) {
     if (!h) return fail(h, NB_ERR_ARG, "null handle");
     switch (key) {
         case NB_TUNE_CHUNK_I:
             if (value < 1) return fail(h, NB_ERR_ARG, "chunk_i must be >= 1");
             h->chunk_i = value;
+            return NB_OK;
+        case NB_TUNE_TILE_ORDER:
+            if (value != 0 && value != 1) return fail(h, NB_ERR_ARG, "tile order must be 0 or 1");
+            h->tile_order = value;
             return NB_OK;
         case NB_TUNE_RAY_GROUP:
         case NB_TUNE_FUV_GROUP:
@@ -695,6 +712,7 @@ HydroLaunch stage_desc(nb_instance* h, bool stage2) {
     L.chunk_i = h->chunk_i < h->d.nx ? h->chunk_i : h->d.nx;
     L.n_chunks = (h->d.nx + L.chunk_i - 1) / L.chunk_i;
     L.nstars_host = h->nstars;
+    L.order = h->tile_order;
     return L;
 }
 

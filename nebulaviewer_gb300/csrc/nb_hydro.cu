@@ -117,10 +117,18 @@ __device__ __forceinline__ void hydro_tile(const HydroLaunch& L, int tile, unsig
     float4* sw_j = sw_w + nstars;
 
     const int tid = threadIdx.x, tk = tid & 31, tj = tid >> 5;
-    const int kt = tile % L.tiles_k;
-    tile /= L.tiles_k;
-    const int jt = tile % L.tiles_j;
-    const int ci = tile / L.tiles_j;
+    int kt, jt, ci;
+    if (L.order == 0) {                       // sweep order 0: k tiles fastest, then j, then i-chunks
+        kt = tile % L.tiles_k;
+        tile /= L.tiles_k;
+        jt = tile % L.tiles_j;
+        ci = tile / L.tiles_j;
+    } else {                                  // sweep order 1: i-chunks fastest, then k, then j
+        ci = tile % L.n_chunks;
+        tile /= L.n_chunks;
+        kt = tile % L.tiles_k;
+        jt = tile / L.tiles_k;
+    }
     const int k0 = kt * TK, j0 = jt * TJ;
     const int i0 = ci * L.chunk_i;
     const int i_end = min(nx, i0 + L.chunk_i);

@@ -84,6 +84,7 @@ struct HydroLaunch {
     unsigned* status;
     int tiles_k, tiles_j, chunk_i, n_chunks;
     int nstars_host;             // == c->nstars (sizes the dynamic shared memory)
+    int order;                   // tile sweep order (NB_TUNE_TILE_ORDER)
 };
 
 // One instance of a batch, as the batched control kernel sees it.
