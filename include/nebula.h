@@ -33,7 +33,7 @@
 extern "C" {
 #endif
 
-#define NB_ABI_VERSION 1
+#define NB_ABI_VERSION 2
 
 enum {
     NB_OK = 0,
@@ -100,6 +100,10 @@ typedef struct nb_live {
     /* plane-parallel source on the -x face (no reference counterpart; 0 = off): ionizing flux F
      * against the column sum n^2 dx along +x, and FUV luminosity L giving G0 += L exp(-tau) */
     double plane_flux, plane_fuv;
+    /* stirring amplitude (nebula3d.py:622 pre_amp) and its main-phase factor (nebula3d.py:625
+     * drive_main): the stirring phase stirs with pre_amp, the main phase with pre_amp * drive_main
+     * while drive_main > 0 and nb_drive_enable(h, 1) */
+    double pre_amp, drive_main;
 } nb_live;
 
 /* One star: sim.py Sim.stars entry (x, y, z, qf, t_on) with its kind, and its jet axis. */
@@ -112,11 +116,14 @@ typedef struct nb_star {
     int jkind;              /* NB_JET_* */
 } nb_star;
 
-/* Simulation clock (device-resident; sim.py Sim.t / Sim.dt / Sim.it). */
+/* Simulation clock (device-resident; sim.py Sim.t / Sim.dt / Sim.it, and the stirring
+ * phase's Sim.tp / Sim.ip). */
 typedef struct nb_clock {
     double t;
     double dt;
     int64_t it;
+    double tp;
+    int64_t ip;
 } nb_clock;
 
 /* ---------------------------------------------------------------- lifetime */
@@ -149,6 +156,56 @@ int nb_fuv(nb_handle h);
 /* Marks the CFL max speed stale after the caller rewrote rho/m/xi (timeline restore). */
 int nb_invalidate(nb_handle h);
 
+/* ---------------------------------------------------------------- turbulent stirring
+ * The stirring phase before the stars switch on and the optional main-phase stirring
+ * (nebula3d.py:165-179 drive; sim.py:1030-1059 _stir / _pre_step; sim.py:1110-1111).  The
+ * forcing is a cross-fade of two solenoidal fields A and B on a coarse grid: each stirred step
+ * adds rho * amp * dt * ((1 - blend) A + blend B) to the momenta with blend = min(clock /
+ * pre_corr, 1), then clock += dt; when the clock reaches pre_corr it restarts at 0, B becomes A
+ * and the next field becomes B.  The caller generates the fields (sim.py:801-804) and pushes
+ * them into a device ring ahead of use; the clock, the blend and the swaps are evaluated on the
+ * device, so stirred steps need no host round trip.  The next step's CFL max speed is taken
+ * over the stirred state (the drive kernel computes it; stage 2 then skips its own). */
+typedef struct nb_drive_desc {
+    int sx, sy, sz;         /* forcing grid (sim.py:761-768) */
+    int slots;              /* ring capacity in fields, >= 3 */
+    double dxs;             /* forcing grid spacing; sample points (i + 1/2) dx (nebula3d.py:172) */
+    double pre_corr;        /* cross-fade time (nebula3d.py:623) */
+    double clock;           /* cross-fade clock to start from (sim.py drv['clock']) */
+} nb_drive_desc;
+
+typedef struct nb_drive_info {
+    double clock;           /* cross-fade clock */
+    int64_t swaps;          /* fields retired so far: A is field `swaps`, B field `swaps + 1` */
+    int64_t pushed;         /* fields pushed since nb_drive_config */
+    int status;             /* device status bits (as nb_device_status; 2 = a step found no field B) */
+    int pad;
+} nb_drive_info;
+
+/* (Re)configures the stirring: allocates the ring, empties it (swaps = 0), sets the clock.
+ * Synchronizes. */
+int nb_drive_config(nb_handle h, const nb_drive_desc* d);
+/* Appends n forcing fields (host memory, n x [3][sx][sy][sz] float32: x, y, z components) in
+ * the order they are to be used.  Synchronizes; NB_ERR_LIMIT when a field still to be used
+ * would be overwritten (the ring holds fields swaps .. swaps + slots - 1). */
+int nb_drive_push(nb_handle h, const float* fields, int n);
+/* 1: main-phase steps stir (the reference's drv is not None, sim.py:1110); 0: they do not. */
+int nb_drive_enable(nb_handle h, int on);
+int nb_drive_state(nb_handle h, nb_drive_info* out);    /* synchronizes */
+/* k stirring-phase steps (sim.py:1044-1050 _pre_step without its end-of-phase test): dt from
+ * the CFL max speed (no dt_cap), hydro without stars, wind or jets, the drive with amplitude
+ * pre_amp, tp += dt, ip += 1.  NB_ERR_STATE in the main phase or before two fields were pushed.
+ * Asynchronous. */
+int nb_pre_step(nb_handle h, int k);
+/* One nebula3d.py:165-179 drive launch with explicit arguments (fa, fb: device, [3][sx][sy][sz]
+ * on the grid of nb_drive_config), for parity. */
+int nb_drive_step(nb_handle h, const float* fa, const float* fb, float blend, float amp, float dt);
+/* sim.py:352-363 add_torus: rho += torus, m *= 1 - torus / (torus + rho) (torus: device,
+ * nx*ny*nz floats); sim.py:806-812 runs it when the stirring phase ends. */
+int nb_add_torus(nb_handle h, const float* torus);
+/* sim.py:501-508 mach_sums in FP64: out[0] = sum |m|^2 / rho, out[1] = sum rho.  Synchronizes. */
+int nb_mach_sums(nb_handle h, double out[2]);
+
 /* ---------------------------------------------------------------- single kernels
  * Parity and benchmarking entry points for one reference kernel launch each. */
 /* One RK2 stage: nebula3d.py:76-151 hydro_stage / sim.py:423-498 hydro_stage_hll, launched
@@ -171,7 +228,8 @@ int nb_cast_fuv(nb_handle h, const double star_xyz[3], float* att_out);
  * A batch step = one control launch for every instance, the ionization of every instance due
  * to ionize (3 launches), and one persistent launch per RK2 stage walking a tile work-list that
  * spans all instances; the step is replayed as a CUDA graph when every instance or none
- * ionizes.  The instances must share solver, limiter and stream; the batch works on its own
+ * ionizes.  The instances must share solver, limiter and stream and be in the main phase
+ * without stirring (NB_ERR_STATE otherwise: step those alone); the batch works on its own
  * stream, ordered after / before the instances' stream by events.  The instance handles stay
  * valid and usable between batch steps (nb_step, nb_fuv, nb_get_clock ...). */
 typedef struct nb_batch_s* nb_batch;
@@ -211,6 +269,7 @@ enum {
     NB_PROF_APPLY_FUV = 7,    /* nebula3d.py:355-388, all stars */
     NB_PROF_MAX_SPEED = 8,    /* nebula3d.py:154-162 stand-alone */
     NB_PROF_SNAPSHOT = 9,     /* snapshot / frame packing, shock proxy */
+    NB_PROF_DRIVE = 10,       /* nebula3d.py:165-179 stirring (+ CFL max speed), add_torus */
     NB_PROF_KINDS = 16
 };
 /* No reference counterpart (the reference times whole calls with perf_counter, sim.py:578-579):

@@ -9,7 +9,7 @@ import os
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libnebula.so")
 
-NB_ABI_VERSION = 1
+NB_ABI_VERSION = 2
 NB_OK = 0
 ERRORS = {-1: "NB_ERR_ARG", -2: "NB_ERR_CUDA", -3: "NB_ERR_STATE", -4: "NB_ERR_LIMIT", -5: "NB_ERR_TIMEOUT",
           -6: "NB_ERR_NOMEM"}
@@ -38,7 +38,7 @@ class NbLive(C.Structure):
                 ("jet_pulse", C.c_double), ("jet_period", C.c_double), ("kappa_fuv", C.c_double),
                 ("q_ramp", C.c_double), ("jet_angle_deg", C.c_double), ("jet_r", C.c_double),
                 ("dt_cap", C.c_double), ("phase_main", C.c_int), ("plane_flux", C.c_double),
-                ("plane_fuv", C.c_double)]
+                ("plane_fuv", C.c_double), ("pre_amp", C.c_double), ("drive_main", C.c_double)]
 
 
 class NbStar(C.Structure):
@@ -47,7 +47,17 @@ class NbStar(C.Structure):
 
 
 class NbClock(C.Structure):
-    _fields_ = [("t", C.c_double), ("dt", C.c_double), ("it", C.c_int64)]
+    _fields_ = [("t", C.c_double), ("dt", C.c_double), ("it", C.c_int64), ("tp", C.c_double), ("ip", C.c_int64)]
+
+
+class NbDriveDesc(C.Structure):
+    _fields_ = [("sx", C.c_int), ("sy", C.c_int), ("sz", C.c_int), ("slots", C.c_int), ("dxs", C.c_double),
+                ("pre_corr", C.c_double), ("clock", C.c_double)]
+
+
+class NbDriveInfo(C.Structure):
+    _fields_ = [("clock", C.c_double), ("swaps", C.c_int64), ("pushed", C.c_int64), ("status", C.c_int),
+                ("pad", C.c_int)]
 
 
 # name -> (restype, argtypes): every symbol include/nebula.h declares
@@ -66,6 +76,14 @@ SIGNATURES = {
     "nb_ionize": (C.c_int, [_P]),
     "nb_fuv": (C.c_int, [_P]),
     "nb_invalidate": (C.c_int, [_P]),
+    "nb_drive_config": (C.c_int, [_P, C.POINTER(NbDriveDesc)]),
+    "nb_drive_push": (C.c_int, [_P, _P, C.c_int]),
+    "nb_drive_enable": (C.c_int, [_P, C.c_int]),
+    "nb_drive_state": (C.c_int, [_P, C.POINTER(NbDriveInfo)]),
+    "nb_pre_step": (C.c_int, [_P, C.c_int]),
+    "nb_drive_step": (C.c_int, [_P, _P, _P, C.c_float, C.c_float, C.c_float]),
+    "nb_add_torus": (C.c_int, [_P, _P]),
+    "nb_mach_sums": (C.c_int, [_P, C.c_double * 2]),
     "nb_hydro_stage": (C.c_int, [_P, _F4, _F4, _F4, C.c_float, C.c_float, C.c_float, C.c_float]),
     "nb_max_speed": (C.c_int, [_P, C.POINTER(C.c_float)]),
     "nb_cast_rays": (C.c_int, [_P, C.c_double * 3, C.c_double, _P]),
@@ -91,7 +109,7 @@ SIGNATURES = {
 }
 TUNE = {"chunk_i": 0, "ray_group": 1, "fuv_group": 2, "tile_order": 3}
 PROF_KINDS = ["ctrl", "stage1", "stage2", "cast_rays", "apply_front", "smooth", "cast_fuv", "apply_fuv", "max_speed",
-              "snapshot"]
+              "snapshot", "drive"]
 
 _lib = None
 

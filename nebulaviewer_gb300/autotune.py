@@ -71,15 +71,16 @@ def autotune(sim, knobs=None, steps=4, use_cache=True):
         return dict(_CACHE[key])
     sim._sync()
     saved = {k: getattr(sim, "_" + k).clone() for k in ("rho", "mx", "my", "mz", "xi", "dfront", "g0")}
-    clock = sim._clock()
-    it0, ver0 = sim._it, sim.version
+    meta = sim.get_state_meta()                    # clocks, stirring state, forcing Generator
+    book = {k: getattr(sim, k) for k in ("_it", "version", "rf_version", "fuv_version", "fuv_nstars", "fuv_phase")
+            if hasattr(sim, k)}
 
     def restore():
         for k, t in saved.items():
             getattr(sim, "_" + k).copy_(t)
-        sim._set_clock(t=clock.t, dt=clock.dt, it=clock.it)
-        sim.invalidate()
-        sim._it, sim.version = it0, ver0
+        sim.set_state_meta(meta)
+        for k, v in book.items():
+            setattr(sim, k, v)
 
     out = {}
     for knob in knobs or CANDIDATES:

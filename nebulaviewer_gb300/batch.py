@@ -21,6 +21,10 @@ class BatchSim:
         if not sims:
             raise ValueError("a batch needs at least one Sim")
         self.sims = list(sims)
+        for s in self.sims:
+            if s.phase != "main" or s._stirring():
+                raise NotImplementedError("batched steps are main-phase steps without stirring: step stirred "
+                                          "instances alone (Sim.step)")
         self._lib = _lib.load()
         n = len(self.sims)
         for s in self.sims:

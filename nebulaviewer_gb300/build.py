@@ -10,7 +10,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libnebula.so")
-SOURCES = ["nb_hydro.cu", "nb_step.cu", "nb_rays.cu", "nb_fuv.cu", "nb_snap.cu", "nb_api.cu"]
+SOURCES = ["nb_hydro.cu", "nb_step.cu", "nb_rays.cu", "nb_fuv.cu", "nb_snap.cu", "nb_stir.cu", "nb_api.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # -fmad=false: no contraction of a*b+c, so every float operation is the reference's own
 NVCC_FLAGS = ARCH + ["-O3", "-std=c++17", "-lineinfo", "-fmad=false", "-Xcompiler", "-fPIC,-fvisibility=hidden",

@@ -29,6 +29,8 @@ struct nb_instance {
     float* scratch3 = nullptr;          // 3 floats: a single star position for the one-star kernels
     float* plane_xf = nullptr;          // [ny][nz] front of the -x plane source
     double* red = nullptr;              // FP64 reduction partials
+    float* drive_ring = nullptr;        // stirring fields [slots][3][sx][sy][sz]
+    long long drive_field = 0;          // floats per forcing field (3 components)
     int nstars = 0, star_alloc = 0;
     long long host_it = 0;
     int smax_valid = 0;
@@ -139,7 +141,8 @@ int upload_const(nb_instance* h) {
 float* plane(nb_instance* h, int p) { return h->d.f.stage + (long long)p * h->ncell; }
 
 int launch_stage(nb_instance* h, const float* const in[4], const float* const u0[4], float* const out[4], int map_in,
-                 const CUtensorMap* maps, float a, float b, bool override_, float dt, float pulse, bool smax) {
+                 const CUtensorMap* maps, float a, float b, bool override_, float dt, float pulse, bool smax,
+                 bool stage2 = false, bool no_sources = false) {
     HydroLaunch L{};
     L.c = h->c;
     L.st = h->st;
@@ -166,7 +169,8 @@ int launch_stage(nb_instance* h, const float* const in[4], const float* const u0
     L.n_chunks = (h->d.nx + L.chunk_i - 1) / L.chunk_i;
     L.nstars_host = h->nstars;
     L.order = h->tile_order;
-    Prof pf(h, smax ? NB_PROF_STAGE2 : NB_PROF_STAGE1, 1);
+    L.no_sources = no_sources ? 1 : 0;
+    Prof pf(h, (smax || stage2) ? NB_PROF_STAGE2 : NB_PROF_STAGE1, 1);
     CK(h, nb_launch_hydro(L, h->d.solver, h->d.limiter, h->stream));
     return NB_OK;
 }
@@ -200,30 +204,68 @@ int do_ionize(nb_instance* h) {
     return NB_OK;
 }
 
-int do_step(nb_instance* h, int ion_every) {
+bool stirring_main(const nb_instance* h) { return h->hc.drive_on && h->hc.drive_main > 0.0; }
+
+// The two RK2 stages of sim.py:1014-1028 and, when the step stirs, the drive of sim.py:1030-1042;
+// the step's last kernel leaves the next step's CFL max speed in st->smax_bits.
+int hydro_and_stir(nb_instance* h, bool stir, bool no_sources) {
     const nb_fields& f = h->d.f;
     int rc;
-    if (ion_every > 0 && h->host_it % ion_every == 0) {           // sim.py:1102-1103
-        if ((rc = do_ionize(h)) != NB_OK) return rc;
-    } else if (!h->smax_valid) {
-        Prof pf(h, NB_PROF_MAX_SPEED, 2);
-        CK(h, nb_launch_max_speed(h->c, f.rho, f.mx, f.my, f.mz, f.xi, &h->st->smax_bits, h->ncell, h->stream));
-    }
-    // sim.py:1104-1108: star weights at t, dt from the max speed (dt_cap), pulse; t += dt
-    {
-        Prof pf(h, NB_PROF_CTRL, 1);
-        CK(h, nb_launch_ctrl(h->c, h->st, h->stars, h->sw, h->nstars, 1, h->stream));
-    }
     const float* U[4] = {f.rho, f.mx, f.my, f.mz};
     float* Uw[4] = {f.rho, f.mx, f.my, f.mz};
     float* S[4] = {plane(h, 0), plane(h, 1), plane(h, 2), plane(h, 3)};
     const float* Sc[4] = {S[0], S[1], S[2], S[3]};
     // sim.py:1025: U -> U1 (a = 0, b = 1);  sim.py:1028: U1 -> U in place (a = b = 1/2) + max speed
-    if ((rc = launch_stage(h, U, U, S, NB_MAP_RHO, h->maps, 0.0f, 1.0f, false, 0.f, 0.f, false)) != NB_OK) return rc;
-    if ((rc = launch_stage(h, Sc, U, Uw, NB_MAP_S0, h->maps, 0.5f, 0.5f, false, 0.f, 0.f, true)) != NB_OK) return rc;
-    h->host_it += 1;
+    if ((rc = launch_stage(h, U, U, S, NB_MAP_RHO, h->maps, 0.0f, 1.0f, false, 0.f, 0.f, false, false, no_sources)) !=
+        NB_OK)
+        return rc;
+    if ((rc = launch_stage(h, Sc, U, Uw, NB_MAP_S0, h->maps, 0.5f, 0.5f, false, 0.f, 0.f, !stir, true, no_sources)) !=
+        NB_OK)
+        return rc;
+    if (stir) {
+        Prof pf(h, NB_PROF_DRIVE, 2);
+        CK(h, nb_launch_drive(h->c, h->st, f.rho, f.mx, f.my, f.mz, f.xi, &h->st->smax_bits, h->d.nx, h->d.ny,
+                              h->stream));
+    }
     h->smax_valid = 1;
     return NB_OK;
+}
+
+int ensure_smax(nb_instance* h) {
+    if (h->smax_valid) return NB_OK;
+    const nb_fields& f = h->d.f;
+    Prof pf(h, NB_PROF_MAX_SPEED, 2);
+    CK(h, nb_launch_max_speed(h->c, f.rho, f.mx, f.my, f.mz, f.xi, &h->st->smax_bits, h->ncell, h->stream));
+    h->smax_valid = 1;
+    return NB_OK;
+}
+
+int do_step(nb_instance* h, int ion_every) {
+    int rc;
+    if (ion_every > 0 && h->host_it % ion_every == 0) {           // sim.py:1102-1103
+        if ((rc = do_ionize(h)) != NB_OK) return rc;
+    } else if ((rc = ensure_smax(h)) != NB_OK) {
+        return rc;
+    }
+    // sim.py:1104-1108: star weights at t, dt from the max speed (dt_cap), pulse; t += dt
+    {
+        Prof pf(h, NB_PROF_CTRL, 1);
+        CK(h, nb_launch_ctrl(h->c, h->st, h->stars, h->sw, h->nstars, NB_ADV_MAIN, h->stream));
+    }
+    if ((rc = hydro_and_stir(h, stirring_main(h), false)) != NB_OK) return rc;
+    h->host_it += 1;
+    return NB_OK;
+}
+
+// sim.py:1044-1050 _pre_step (the end-of-phase test is the caller's)
+int do_pre_step(nb_instance* h) {
+    int rc;
+    if ((rc = ensure_smax(h)) != NB_OK) return rc;
+    {
+        Prof pf(h, NB_PROF_CTRL, 1);
+        CK(h, nb_launch_ctrl(h->c, h->st, h->stars, h->sw, h->nstars, NB_ADV_PRE, h->stream));
+    }
+    return hydro_and_stir(h, true, true);
 }
 
 }  // namespace
@@ -326,7 +368,7 @@ NB_EXPORT void nb_destroy(nb_handle h) {
     if (h->stream) cudaStreamSynchronize(h->stream);
     else cudaDeviceSynchronize();
     void* ps[] = {h->c, h->st, h->stars, h->sw, h->maps, h->tmp_maps, h->dirs, h->dirs_fuv,
-                  h->rfront, h->att, h->scratch3, h->red, h->plane_xf};
+                  h->rfront, h->att, h->scratch3, h->red, h->plane_xf, h->drive_ring};
     for (void* p : ps)
         if (p) cudaFree(p);
     for (auto& r : h->recs) {
@@ -361,6 +403,8 @@ NB_EXPORT int nb_set_live(nb_handle h, const nb_live* L) {
     c.plane_on = L->plane_flux > 0.0 ? 1 : 0;
     c.plane_F_f = (float)L->plane_flux;
     c.plane_lum_f = (float)L->plane_fuv;
+    c.pre_amp = L->pre_amp;
+    c.drive_main = L->drive_main;
     return upload_const(h);
 }
 
@@ -403,6 +447,8 @@ NB_EXPORT int nb_set_clock(nb_handle h, const nb_clock* c) {
     s.t = c->t;
     s.dt = c->dt;
     s.it = c->it;
+    s.tp = c->tp;
+    s.ip = c->ip;
     CK(h, cudaMemcpyAsync(h->st, &s, sizeof(NbState), cudaMemcpyHostToDevice, h->stream));
     CK(h, cudaStreamSynchronize(h->stream));
     h->host_it = c->it;
@@ -418,6 +464,8 @@ NB_EXPORT int nb_get_clock(nb_handle h, nb_clock* c) {
     c->t = s.t;
     c->dt = s.dt;
     c->it = s.it;
+    c->tp = s.tp;
+    c->ip = s.ip;
     return NB_OK;
 }
 
@@ -444,6 +492,131 @@ NB_EXPORT int nb_step(nb_handle h, int k, int ion_every) {
         int rc = do_step(h, ion_every);
         if (rc != NB_OK) return rc;
     }
+    return NB_OK;
+}
+
+NB_EXPORT int nb_pre_step(nb_handle h, int k) {
+    if (!h) return fail(h, NB_ERR_ARG, "null handle");
+    if (k < 0) return fail(h, NB_ERR_ARG, "k >= 0 required");
+    if (h->hc.phase_main) return fail(h, NB_ERR_STATE, "the stirring phase is over");
+    if (!h->drive_ring || h->hc.drive_pushed < 2)
+        return fail(h, NB_ERR_STATE, "stirring needs nb_drive_config and two pushed forcing fields");
+    for (int s = 0; s < k; ++s) {
+        int rc = do_pre_step(h);
+        if (rc != NB_OK) return rc;
+    }
+    return NB_OK;
+}
+
+// ============================================================================ stirring
+NB_EXPORT int nb_drive_config(nb_handle h, const nb_drive_desc* d) {
+    if (!h || !d) return fail(h, NB_ERR_ARG, "null argument");
+    if (d->sx < 1 || d->sy < 1 || d->sz < 1 || d->slots < 3 || !(d->dxs > 0.0) || !(d->pre_corr > 0.0) ||
+        !(d->clock >= 0.0))
+        return fail(h, NB_ERR_ARG, "forcing grid >= 1 cell per axis, slots >= 3, dxs > 0, pre_corr > 0, clock >= 0");
+    const long long field = 3LL * d->sx * d->sy * d->sz;
+    if (field * d->slots > (1LL << 31)) return fail(h, NB_ERR_LIMIT, "forcing ring above 2^31 floats");
+    CK(h, cudaStreamSynchronize(h->stream));
+    if (h->drive_ring) cudaFree(h->drive_ring);
+    h->drive_ring = nullptr;
+    if (cudaMalloc(&h->drive_ring, sizeof(float) * field * d->slots) != cudaSuccess) {
+        cudaGetLastError();
+        h->hc.drive_ring = nullptr;
+        h->hc.drive_slots = 0;
+        h->hc.drive_pushed = 0;
+        upload_const(h);
+        return fail(h, NB_ERR_NOMEM, "forcing ring allocation refused");
+    }
+    h->drive_field = field;
+    NbConst& c = h->hc;
+    c.drive_ring = h->drive_ring;
+    c.drive_sx = d->sx; c.drive_sy = d->sy; c.drive_sz = d->sz;
+    c.drive_slots = d->slots;
+    c.drive_pushed = 0;
+    c.drive_dxs_f = (float)d->dxs;
+    c.drive_pre_corr = d->pre_corr;
+    NbState s{};
+    CK(h, cudaMemcpyAsync(&s, h->st, sizeof(NbState), cudaMemcpyDeviceToHost, h->stream));
+    CK(h, cudaStreamSynchronize(h->stream));
+    s.dclock = d->clock;
+    s.dswaps = 0;
+    s.drive_go = 0;
+    CK(h, cudaMemcpyAsync(h->st, &s, sizeof(NbState), cudaMemcpyHostToDevice, h->stream));
+    int rc = upload_const(h);
+    if (rc != NB_OK) return rc;
+    CK(h, cudaStreamSynchronize(h->stream));
+    return NB_OK;
+}
+
+NB_EXPORT int nb_drive_push(nb_handle h, const float* fields, int n) {
+    if (!h || (n > 0 && !fields)) return fail(h, NB_ERR_ARG, "null argument");
+    if (n < 0) return fail(h, NB_ERR_ARG, "n >= 0 required");
+    if (!h->drive_ring) return fail(h, NB_ERR_STATE, "nb_drive_config first");
+    if (n == 0) return NB_OK;
+    NbState s{};
+    CK(h, cudaMemcpyAsync(&s, h->st, sizeof(NbState), cudaMemcpyDeviceToHost, h->stream));
+    CK(h, cudaStreamSynchronize(h->stream));
+    NbConst& c = h->hc;
+    // the ring holds fields dswaps .. dswaps + slots - 1; A and B (fields dswaps, dswaps + 1) stay
+    if (c.drive_pushed + n > s.dswaps + c.drive_slots)
+        return fail(h, NB_ERR_LIMIT, "forcing ring full: the fields in it are still to be used");
+    for (int m = 0; m < n; ++m) {
+        const long long slot = (c.drive_pushed + m) % c.drive_slots;
+        CK(h, cudaMemcpyAsync(h->drive_ring + slot * h->drive_field, fields + (long long)m * h->drive_field,
+                              sizeof(float) * h->drive_field, cudaMemcpyHostToDevice, h->stream));
+    }
+    c.drive_pushed += n;
+    int rc = upload_const(h);
+    if (rc != NB_OK) return rc;
+    CK(h, cudaStreamSynchronize(h->stream));
+    return NB_OK;
+}
+
+NB_EXPORT int nb_drive_enable(nb_handle h, int on) {
+    if (!h) return fail(h, NB_ERR_ARG, "null handle");
+    h->hc.drive_on = on ? 1 : 0;
+    return upload_const(h);
+}
+
+NB_EXPORT int nb_drive_state(nb_handle h, nb_drive_info* out) {
+    if (!h || !out) return fail(h, NB_ERR_ARG, "null argument");
+    NbState s{};
+    CK(h, cudaMemcpyAsync(&s, h->st, sizeof(NbState), cudaMemcpyDeviceToHost, h->stream));
+    CK(h, cudaStreamSynchronize(h->stream));
+    out->clock = s.dclock;
+    out->swaps = s.dswaps;
+    out->pushed = h->hc.drive_pushed;
+    out->status = (int)s.status;
+    return NB_OK;
+}
+
+NB_EXPORT int nb_drive_step(nb_handle h, const float* fa, const float* fb, float blend, float amp, float dt) {
+    if (!h || !fa || !fb) return fail(h, NB_ERR_ARG, "null argument");
+    if (!h->drive_ring) return fail(h, NB_ERR_STATE, "nb_drive_config first (it sets the forcing grid)");
+    const nb_fields& f = h->d.f;
+    Prof pf(h, NB_PROF_DRIVE, 1);
+    CK(h, nb_launch_drive_explicit(h->c, f.rho, f.mx, f.my, f.mz, fa, fb, blend, amp, dt, h->d.nx, h->d.ny,
+                                   h->stream));
+    return NB_OK;
+}
+
+NB_EXPORT int nb_add_torus(nb_handle h, const float* torus) {
+    if (!h || !torus) return fail(h, NB_ERR_ARG, "null argument");
+    const nb_fields& f = h->d.f;
+    Prof pf(h, NB_PROF_DRIVE, 1);
+    CK(h, nb_launch_add_torus(torus, f.rho, f.mx, f.my, f.mz, h->ncell, h->stream));
+    h->smax_valid = 0;
+    return NB_OK;
+}
+
+NB_EXPORT int nb_mach_sums(nb_handle h, double out[2]) {
+    if (!h || !out) return fail(h, NB_ERR_ARG, "null argument");
+    if (nb_mach_scratch_doubles() > nb_reduce_scratch_doubles()) return fail(h, NB_ERR_LIMIT, "reduction scratch");
+    const nb_fields& f = h->d.f;
+    CK(h, nb_launch_mach_sums(f.rho, f.mx, f.my, f.mz, h->ncell, h->red, h->stream));
+    CK(h, cudaMemcpyAsync(out, h->red + nb_mach_scratch_doubles() - 2, 2 * sizeof(double), cudaMemcpyDeviceToHost,
+                          h->stream));
+    CK(h, cudaStreamSynchronize(h->stream));
     return NB_OK;
 }
 
@@ -930,6 +1103,9 @@ NB_EXPORT int nb_batch_step(nb_batch b, int k) {
     for (int i = 0; i < n; ++i)
         if (b->inst[i]->rfront != b->rfront0[i] || b->inst[i]->nstars != b->nstars0[i])
             return bfail(b, NB_ERR_STATE, "an instance's star table changed size since nb_batch_create: rebuild the batch");
+    for (int i = 0; i < n; ++i)
+        if (!b->inst[i]->hc.phase_main || stirring_main(b->inst[i]))
+            return bfail(b, NB_ERR_STATE, "batched steps are main-phase steps without stirring: step stirred instances alone");
     BCK(b, cudaEventRecord(b->ev_in, b->user));
     BCK(b, cudaStreamWaitEvent(b->bs, b->ev_in, 0));
     // an instance whose CFL max speed is stale and that does not ionize first needs a fresh one

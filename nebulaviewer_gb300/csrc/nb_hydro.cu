@@ -113,7 +113,7 @@ __device__ __forceinline__ void hydro_tile(const HydroLaunch& L, int tile, unsig
     uint64_t* bar = reinterpret_cast<uint64_t*>(smem + SM::FIXED - SM::BAR_BYTES);
     float4* sw_w = reinterpret_cast<float4*>(smem + SM::FIXED);
     const NbConst& C = *L.c;
-    const int nx = C.nx, ny = C.ny, nz = C.nz, nstars = C.nstars;
+    const int nx = C.nx, ny = C.ny, nz = C.nz, nstars = L.no_sources ? 0 : C.nstars;
     float4* sw_j = sw_w + nstars;
 
     const int tid = threadIdx.x, tk = tid & 31, tj = tid >> 5;
@@ -137,7 +137,7 @@ __device__ __forceinline__ void hydro_tile(const HydroLaunch& L, int tile, unsig
     const float floor_ = C.floor_, cn2 = C.cn2, ci2 = C.ci2, vmax = C.vmax, dx = C.dx;
     const float dt = L.use_override ? L.dt_override : L.st->dt_f;
     const float pulse = L.use_override ? L.pulse_override : L.st->pulse_f;
-    const float wind = C.wind_f, jet_cos = C.jet_cos_f, jet_r = C.jet_r_f;
+    const float wind = L.no_sources ? 0.0f : C.wind_f, jet_cos = C.jet_cos_f, jet_r = C.jet_r_f;
     const float a = L.a, b = L.b;
 
     for (int s = tid; s < nstars; s += blockDim.x) {

@@ -12,6 +12,9 @@
 
 // Device-status bits (NbState::status), reported by nb_device_status.
 #define NB_DEV_TMA_TIMEOUT 1u
+#define NB_ADV_MAIN 1             // control-kernel modes (weights only = 0)
+#define NB_ADV_PRE 2
+#define NB_DEV_DRIVE_EMPTY 2u    // a stirred step found no pushed field B (the step did not stir)
 
 // ------------------------------------------------------------------ device-resident data
 // Scalars written by the host (geometry, physics, live parameters).  float copies are the
@@ -36,6 +39,13 @@ struct NbConst {
     double plane_F, plane_lum;
     const float* plane_xf;      // [ny][nz] front position along +x per column
     const float* plane_g0;      // [nx][ny][nz] plane FUV term (stage plane 2, written by the FUV pass)
+    // turbulent stirring (nebula3d.py:165-179, sim.py:1030-1059)
+    int drive_on;                // main-phase stirring allowed (the reference's drv is not None)
+    int drive_sx, drive_sy, drive_sz, drive_slots;
+    long long drive_pushed;      // forcing fields pushed into the ring so far
+    float drive_dxs_f;
+    double drive_pre_corr, pre_amp, drive_main;
+    const float* drive_ring;     // [slots][3][sx][sy][sz]
 };
 
 // Written by device kernels every step.
@@ -45,6 +55,14 @@ struct NbState {
     float dt_f, pulse_f;         // float32 arguments of the step's hydro stages
     unsigned smax_bits;          // CFL max speed (non-negative float bits; atomicMax on uint)
     unsigned status;             // NB_DEV_* failure bits
+    double tp;                   // stirring-phase time and steps (sim.py Sim.tp / Sim.ip)
+    long long ip;
+    double dclock;               // stirring cross-fade clock (sim.py drv['clock'])
+    long long dswaps;            // forcing fields retired: A = field dswaps, B = field dswaps + 1
+    float blend_f, amp_f;        // this step's drive arguments (sim.py:1032, 1047 / 1111)
+    int drive_a, drive_b;        // ring slots of A and B for this step
+    int drive_go;                // this step stirs
+    int pad_;
 };
 
 struct NbStarDev {
@@ -84,6 +102,7 @@ struct HydroLaunch {
     unsigned* status;
     int tiles_k, tiles_j, chunk_i, n_chunks;
     int nstars_host;             // == c->nstars (sizes the dynamic shared memory)
+    int no_sources;              // stirring-phase hydro: no stars, wind or jets (sim.py:1046)
     int order;                   // tile sweep order (NB_TUNE_TILE_ORDER)
 };
 
@@ -176,6 +195,16 @@ cudaError_t nb_launch_weights(const NbConst* c, const NbState* st, const NbStarD
                               int nstars, cudaStream_t s);
 cudaError_t nb_launch_max_speed(const NbConst* c, const float* rho, const float* mx, const float* my,
                                 const float* mz, const float* xi, unsigned* smax_bits, long n, cudaStream_t s);
+cudaError_t nb_launch_drive(const NbConst* c, const NbState* st, const float* rho, float* mx, float* my, float* mz,
+                            const float* xi, unsigned* smax_bits, int nx, int ny, cudaStream_t s);
+cudaError_t nb_launch_drive_explicit(const NbConst* c, const float* rho, float* mx, float* my, float* mz,
+                                     const float* fa, const float* fb, float blend, float amp, float dt, int nx,
+                                     int ny, cudaStream_t s);
+cudaError_t nb_launch_add_torus(const float* torus, float* rho, float* mx, float* my, float* mz, long long n,
+                                cudaStream_t s);
+int nb_mach_scratch_doubles();
+cudaError_t nb_launch_mach_sums(const float* rho, const float* mx, const float* my, const float* mz, long long n,
+                                double* scratch, cudaStream_t s);
 cudaError_t nb_launch_ray_dirs(int nu, int nphi, float4* dirs, cudaStream_t s);
 cudaError_t nb_launch_cast_rays(const NbConst* c, const NbStarW* sw, const float4* dirs, const float* rho,
                                 float* rfront, int nstars, int group, const float* star_override, float q_override,

@@ -38,6 +38,8 @@ __device__ void star_weight(const NbConst& c, const NbStarDev& s, double t, NbSt
     w.pad = 0;
 }
 
+// advance: 0 = star weights only; NB_ADV_MAIN = a main-phase step (sim.py:1104-1113);
+// NB_ADV_PRE = a stirring-phase step (sim.py:1044-1050: dt without dt_cap, tp += dt)
 __device__ __forceinline__ void ctrl_body(const NbConst* __restrict__ c, NbState* __restrict__ st,
                                           const NbStarDev* __restrict__ stars, NbStarW* __restrict__ sw, int nstars,
                                           int advance) {
@@ -45,20 +47,51 @@ __device__ __forceinline__ void ctrl_body(const NbConst* __restrict__ c, NbState
     for (int s = threadIdx.x; s < nstars; s += blockDim.x) star_weight(*c, stars[s], t, sw[s]);
     __syncthreads();                                      // every thread has read t before it moves
     if (!advance || threadIdx.x != 0) return;
+    const bool pre = advance == NB_ADV_PRE;
     // sim.py:1012: P['cfl'] * dx / float(smax)
     const double smax = (double)__uint_as_float(st->smax_bits);
     double dt = __ddiv_rn(__dmul_rn(c->cfl, c->dx_d), smax);
-    if (c->dt_cap > 0.0 && c->dt_cap < dt) dt = c->dt_cap;                               // sim.py:1106-1107
-    // sim.py:1108: max(0, 1 + jet_pulse * sin(2 pi t / jet_period))
-    const double arg = __ddiv_rn(__dmul_rn(6.283185307179586, t), c->jet_period);
-    double pulse = __dadd_rn(1.0, __dmul_rn(c->jet_pulse, sin(arg)));
-    if (!(pulse > 0.0)) pulse = 0.0;
+    double pulse = 0.0;
+    if (!pre) {
+        if (c->dt_cap > 0.0 && c->dt_cap < dt) dt = c->dt_cap;                           // sim.py:1106-1107
+        // sim.py:1108: max(0, 1 + jet_pulse * sin(2 pi t / jet_period))
+        const double arg = __ddiv_rn(__dmul_rn(6.283185307179586, t), c->jet_period);
+        pulse = __dadd_rn(1.0, __dmul_rn(c->jet_pulse, sin(arg)));
+        if (!(pulse > 0.0)) pulse = 0.0;
+    }
     st->dt = dt;
     st->dt_f = (float)dt;
     st->pulse_f = (float)pulse;
-    st->smax_bits = 0u;                                   // the stage-2 epilogue accumulates the next max
-    st->t = __dadd_rn(t, dt);                             // sim.py:1112-1113
-    st->it = st->it + 1;
+    st->smax_bits = 0u;                                   // the step's last kernel accumulates the next max
+    // sim.py:1030-1042 _stir: blend from the clock before this step, then clock += dt and, at
+    // pre_corr, B becomes A and the next pushed field becomes B
+    st->drive_go = 0;
+    if (pre || (c->drive_on && c->drive_main > 0.0)) {
+        const double q = __ddiv_rn(st->dclock, c->drive_pre_corr);
+        st->blend_f = (float)(1.0 < q ? 1.0 : q);                                      // min(clock / pre_corr, 1)
+        st->amp_f = (float)(pre ? c->pre_amp : __dmul_rn(c->pre_amp, c->drive_main));   // sim.py:1047, 1111
+        if (st->dswaps + 1 < c->drive_pushed && c->drive_slots > 0) {
+            st->drive_a = (int)(st->dswaps % c->drive_slots);
+            st->drive_b = (int)((st->dswaps + 1) % c->drive_slots);
+            st->drive_go = 1;
+            const double clk = __dadd_rn(st->dclock, dt);
+            if (clk >= c->drive_pre_corr) {
+                st->dswaps = st->dswaps + 1;
+                st->dclock = 0.0;
+            } else {
+                st->dclock = clk;
+            }
+        } else {
+            st->status |= NB_DEV_DRIVE_EMPTY;
+        }
+    }
+    if (pre) {
+        st->tp = __dadd_rn(st->tp, dt);                   // sim.py:1048-1049
+        st->ip = st->ip + 1;
+    } else {
+        st->t = __dadd_rn(t, dt);                         // sim.py:1112-1113
+        st->it = st->it + 1;
+    }
 }
 
 __global__ void ctrl_kernel(const NbConst* __restrict__ c, NbState* __restrict__ st,

@@ -12,6 +12,10 @@ generators make the workloads this package is measured on, with fixed seeds:
              stars seeded inside the sheet with rates log-uniform over one decade.
   cliffwall  box [0,1]^3: a density step n = 1 -> 200 at mid-x with seeded Gaussian clumps
              (n = 500-2000, radius 0.01-0.05) on its face; 3 stars in the low-density side.
+  torus_stirred  the torus scene with a stirring phase first (as the reference's bipolar
+             scenario, sim.py:51, 667-672): the log-normal background is stirred to
+             supersonic turbulence for pre_t, then the torus joins and the star switches on;
+             stirring continues at drive_main x pre_amp in the main phase.
 
 Random fields are sums of seeded random plane waves (resolution independent, so a small
 and a large grid of the same scenario share their large scales) evaluated with torch on
@@ -73,9 +77,10 @@ def solenoidal_velocity(shape, dx, seed, slope, rms, n=96, kmin=1.0, kmax=None, 
     return [s * _eval(shape, dx, kv, ph, amp, device, comp=e[:, c]) for c in range(3)]
 
 
-def torus(res=32, seed=1, device="cpu", shape=None, nstars=1):
+def torus(res=32, seed=1, device="cpu", shape=None, nstars=1, stir=False):
     """the torus scene; `shape` gives a non-cubic box (dx = 2 / min(shape), torus at the centre),
-    `nstars` > 1 adds seeded weaker stars near the centre"""
+    `nstars` > 1 adds seeded weaker stars near the centre; `stir` returns the torus apart
+    (it joins when the stirring phase ends) with the stirring parameters in P"""
     if shape is None:
         shape = (2 * res, 2 * res, 2 * res)
         dx = 1.0 / res
@@ -89,7 +94,12 @@ def torus(res=32, seed=1, device="cpu", shape=None, nstars=1):
     inside = 0.5 * (1.0 - torch.tanh((d - 0.15) / dx))
     sig = 0.3
     g = grf(shape, dx, seed, 3.8, device=device).to(torch.float64)
-    rho = ((1.0 + 99.0 * inside) * torch.exp(sig * g - 0.5 * sig * sig)).to(torch.float32)
+    ln = torch.exp(sig * g - 0.5 * sig * sig)
+    rho = ((1.0 + 99.0 * inside) * ln).to(torch.float32)
+    torus_part = None
+    if stir:
+        torus_part = (99.0 * inside * ln).to(torch.float32)
+        rho = ln.to(torch.float32)
     Q = 0.25 ** 3 / 3.0                       # n^2 R^3 / 3 with n = 1, R = 0.25 (no 4 pi in cast_rays)
     P = dict(q_main=Q, wind=0.0, jet=0.0, q_ramp=0.0, kappa_fuv=10.0, cn2=1.0, ci2=144.0, vmax=72.0,
              solver="hll", limiter="minmod", cfl=0.3, floor=2e-3, seed=seed, ion_every=2)
@@ -98,8 +108,15 @@ def torus(res=32, seed=1, device="cpu", shape=None, nstars=1):
     for _ in range(nstars - 1):
         off = rng.uniform(-0.3, 0.3, 3)
         stars.append((c[0] + off[0], c[1] + off[1], c[2] + off[2], float(rng.uniform(0.1, 0.5)), 0.0))
+    if stir:
+        # sound speed 1: stirring to supersonic turbulence in pre_t = 0.05, forcing renewed every 0.02
+        P.update(pre_t=0.05, pre_amp=60.0, pre_corr=0.02, pre_kmax=4.0, drive_main=0.25)
     return dict(shape=shape, dx=dx, rho=rho, mom=None, stars=stars, kinds=["main"] * nstars,
-                jets=[(0.0, 0.0, 1.0)] * nstars, jkinds=["none"] * nstars, P=P)
+                jets=[(0.0, 0.0, 1.0)] * nstars, jkinds=["none"] * nstars, P=P, torus=torus_part)
+
+
+def torus_stirred(res=32, seed=1, device="cpu", shape=None, nstars=1):
+    return torus(res=res, seed=seed, device=device, shape=shape, nstars=nstars, stir=True)
 
 
 def sheet(res=256, seed=2, nstars=6, device="cpu", shape=None):
@@ -167,7 +184,7 @@ def cliffwall(res=1024, seed=5, nclumps=40, device="cpu", shape=None):
                 jets=[(0.0, 0.0, 1.0)] * 3, jkinds=["none"] * 3, P=P)
 
 
-SCENARIOS = {"torus": torus, "sheet": sheet, "cliffwall": cliffwall}
+SCENARIOS = {"torus": torus, "torus_stirred": torus_stirred, "sheet": sheet, "cliffwall": cliffwall}
 
 
 def batch_scenes(n=32, seed=7, device="cpu", lo=64, hi=192):

@@ -9,12 +9,18 @@ t, it, dt, phase, P, prof, profile, dt_cap, version, rf_version, stars, kinds, j
 events, ion_every, fuv_every.  Fields are device buffers with the wp.array surface the
 callers use (.numpy(), .shape, .dtype, .ptr, .fill_, .zero_, .assign, __cuda_array_interface__).
 
-What differs by design: the clock (t, dt, it) lives on the device, so step(k) enqueues k
-steps without a host round trip per step (the reference blocks on a max-speed read every
-step, sim.py:1012); reading `t` synchronizes.  The pre-turbulence (stirring) phase, the
-triggered star formation and cropped domains are outside this package's scope: a
-parameter set that asks for them is rejected.
+What differs by design: the clock (t, dt, it, tp, ip) lives on the device, so step(k)
+enqueues k steps without a host round trip per step (the reference blocks on a max-speed
+read every step, sim.py:1012); reading `t` synchronizes.  The stirring (pre-turbulence)
+phase and main-phase stirring (sim.py:1030-1059, 1110-1111) run on the device too: the
+cross-fade clock and the field swaps are evaluated there, and the host pushes forcing
+fields into a device ring ahead of use, synchronizing once per chunk of steps that the CFL
+bound dt <= cfl dx / c_n proves cannot end the phase or exhaust the ring.  Triggered star
+formation and cropped domains are outside this package's scope: a parameter set that asks
+for them is rejected.
 """
+import collections
+import copy
 import ctypes as C
 import math
 import time
@@ -24,7 +30,10 @@ import torch
 
 from . import _lib
 from . import ics as _ics
+from . import stir as _stir
 from .params import LIVE, make_params, sound_speeds
+
+DRIVE_SLOTS = 16          # forcing fields the device ring holds
 
 
 class Field:
@@ -108,9 +117,13 @@ class Sim:
     # ------------------------------------------------------------------ construction
     @classmethod
     def from_state(cls, shape, dx, rho, stars, kinds, jets, jkinds, P, mom=None, rays=None, fuv_grid=None,
-                   ion_every=None, fast=True, device="cuda:0", verbose=False, start_main=True):
+                   ion_every=None, fast=True, device="cuda:0", verbose=False, start_main=True, torus=None,
+                   stir_fields=None, stir_grid=None):
         """An instance from explicit fields and star lists (what the reference's reset() leaves
-        behind, sim.py:710-795), e.g. initial conditions built by the reference's own IC code."""
+        behind, sim.py:710-795), e.g. initial conditions built by the reference's own IC code.
+        `torus` joins rho when the main phase starts (at once without a stirring phase);
+        `stir_fields` ([3][sx][sy][sz] arrays) replaces the forcing generator, in order of use;
+        `stir_grid` = ((sx, sy, sz), dxs) overrides the forcing grid."""
         self = cls.__new__(cls)
         self.device = torch.device(device)
         self.fast = fast
@@ -124,7 +137,7 @@ class Sim:
         self.scenario = "state"
         self.res = None
         ic = dict(shape=tuple(shape), dx=float(dx), rho=rho, mom=mom, stars=stars, kinds=kinds, jets=jets,
-                  jkinds=jkinds, P={})
+                  jkinds=jkinds, P={}, torus=torus, stir_fields=stir_fields, stir_grid=stir_grid)
         self._setup(ic, dict(P), start_main=start_main)
         return self
 
@@ -147,10 +160,8 @@ class Sim:
         t_setup = time.perf_counter()
         self.close()
         P = make_params(overrides, base=ic["P"])
-        for key, what in (("pre_t", "the pre-turbulence (stirring) phase"), ("trigger", "triggered star formation"),
-                          ("drive_main", "main-phase stirring")):
-            if float(P.get(key, 0.0) or 0.0) > 0.0:
-                raise NotImplementedError(f"{what} ({key} > 0) is outside this package's simulation step")
+        if float(P.get("trigger", 0.0) or 0.0) > 0.0:
+            raise NotImplementedError("triggered star formation (trigger > 0) is outside this package's simulation step")
         if P.get("crop"):
             raise NotImplementedError("cropped domains are outside this package's simulation step")
         self.P = P
@@ -163,6 +174,16 @@ class Sim:
         dev = self.device
         f32 = dict(device=dev, dtype=torch.float32)
         self._rho = torch.as_tensor(ic["rho"]).to(**f32).contiguous().clone()
+        pre = float(P.get("pre_t", 0.0) or 0.0) > 0.0
+        torus = ic.get("torus")
+        self.torus = None
+        if torus is not None:                                                       # sim.py:669-671, 737
+            torus = torch.as_tensor(np.asarray(torus, np.float32)).to(**f32).contiguous()
+            if pre:
+                self.torus = torus
+            else:
+                self._rho += torus
+        self.torus0 = self.torus
         if ic.get("mom") is None:
             m = [torch.zeros(self.shape, **f32) for _ in range(3)]
         else:
@@ -230,13 +251,24 @@ class Sim:
         self.last_birth = -1e9
         self.mach = None
         self.sm0 = None
-        self.tp, self.ip = 0.0, 0
         self.P_reset = dict(P)
         self.q_main0 = P["q_main"]
-        self.phase = "main"
+        # stirring (sim.py:760-768, 786-790): the forcing grid, the Generator, the ring
+        self.rng = np.random.default_rng(P["seed"])
+        src = ic.get("stir_fields")
+        self._stir_src = None if src is None else collections.deque(np.asarray(f, np.float32) for f in src)
+        grid = ic.get("stir_grid")
+        if grid is None:
+            grid = _stir.forcing_grid(self.L, self.dx, self.shape, physical=self.ic_mode != "nebula3d")
+        self.sshape, self.dxs = tuple(int(v) for v in grid[0]), float(grid[1])
+        self._drv_on = False
+        self._forcing = []              # (field, Generator state before it) per field pushed since the ring reset
+        self.phase = "pre" if pre else "main"
         self._push(force=True)
-        if start_main:
-            self.ionize()                                                           # sim.py:806-818
+        if pre:
+            self._drive_new(0.0)
+        elif start_main:
+            self._start_main()
         self._sync()
         self.setup_s = time.perf_counter() - t_setup
         self.log(f"{self.scenario} grid {nx}x{ny}x{nz} ({n / 1e6:.1f}M cells) rays {rays[0]}x{rays[1]} "
@@ -277,7 +309,8 @@ class Sim:
         live = (float(P["q_main"]), float(P["wind"]), float(P["jet"]), float(P["jet_proto"]), float(P["jet_pulse"]),
                 float(P["jet_period"]), float(P["kappa_fuv"]), float(P.get("q_ramp", 0.0)), float(P["jet_angle"]),
                 float(P["jet_r"]), float(cap), 1 if self.phase == "main" else 0,
-                float(P.get("plane_flux", 0.0) or 0.0), float(P.get("plane_fuv", 0.0) or 0.0))
+                float(P.get("plane_flux", 0.0) or 0.0), float(P.get("plane_fuv", 0.0) or 0.0),
+                float(P.get("pre_amp", 0.0) or 0.0), float(P.get("drive_main", 0.0) or 0.0))
         if force or live != self._live_key:
             L = _lib.NbLive(*live)
             self._chk(self._lib.nb_set_live(self._h, C.byref(L)), "nb_set_live")
@@ -321,17 +354,21 @@ class Sim:
         self._chk(self._lib.nb_get_clock(self._h, C.byref(c)), "nb_get_clock")
         return c
 
-    def _set_clock(self, t=None, dt=None, it=None):
+    def _set_clock(self, t=None, dt=None, it=None, tp=None, ip=None):
         c = self._clock()
         c.t = c.t if t is None else float(t)
         c.dt = c.dt if dt is None else float(dt)
         c.it = c.it if it is None else int(it)
+        c.tp = c.tp if tp is None else float(tp)
+        c.ip = c.ip if ip is None else int(ip)
         self._chk(self._lib.nb_set_clock(self._h, C.byref(c)), "nb_set_clock")
         self._it = int(c.it)
 
     t = property(lambda self: self._clock().t, lambda self, v: self._set_clock(t=v))
     dt = property(lambda self: self._clock().dt, lambda self, v: self._set_clock(dt=v))
     it = property(lambda self: self._it, lambda self, v: self._set_clock(it=v))
+    tp = property(lambda self: self._clock().tp, lambda self, v: self._set_clock(tp=v))
+    ip = property(lambda self: int(self._clock().ip), lambda self, v: self._set_clock(ip=v))
 
     @property
     def dt_cap(self):
@@ -411,18 +448,169 @@ class Sim:
         return True
 
     def step(self, k=1, sync=True):
-        """advance k main-phase steps (sim.py:1141-1152).  Returns wall seconds.  With sync=False
-        the steps are only enqueued on the stream."""
+        """advance k hydro steps, stirring-phase or main-phase (sim.py:1141-1152).  Returns wall
+        seconds.  With sync=False the steps are only enqueued on the stream (the stirring phase
+        and stirred main-phase steps still synchronize once per chunk)."""
         t0 = time.perf_counter()
         self._push()
-        self._chk(self._lib.nb_step(self._h, int(k), int(self.ion_every)), "nb_step")
-        self._it += int(k)
-        self.version += int(k)
+        left = int(k)
+        while left > 0:
+            n = self._pre_chunk(left) if self.phase == "pre" else self._main_chunk(left)
+            left -= n
+            self.version += n
         if sync:
             self._sync()
+            if self._drv_on:
+                self._drive_info()                 # raises if a stirred step found no forcing field
         self._tick("step", t0)
         self.prof["n_steps"] = self.prof.get("n_steps", 0) + k
         return time.perf_counter() - t0
+
+    def _stirring(self):
+        return self._drv_on and float(self.P.get("drive_main", 0.0) or 0.0) > 0.0
+
+    def _main_chunk(self, left):
+        """main-phase steps (sim.py:1099-1114); stirred steps in ring-sized chunks"""
+        n = left
+        if self._stirring():
+            info = self._drive_info()
+            n = min(left, self._ring_steps())
+            self._drive_fill(info.swaps + 2 + self._max_swaps(n))
+        self._chk(self._lib.nb_step(self._h, int(n), int(self.ion_every)), "nb_step")
+        self._it += n
+        return n
+
+    def _pre_chunk(self, left):
+        """stirring-phase steps (sim.py:1044-1059): as many as provably cannot reach pre_t but
+        the last, then the end-of-phase test"""
+        c = self._clock()
+        gap = float(self.P["pre_t"]) - c.tp
+        n_end = max(1, math.ceil(gap / self._dt_bound())) if gap > 0.0 else 1
+        info = self._drive_info()
+        n = min(left, n_end, self._ring_steps())
+        self._drive_fill(info.swaps + 2 + self._max_swaps(n))
+        self._chk(self._lib.nb_pre_step(self._h, int(n)), "nb_pre_step")
+        if n == n_end and self._clock().tp >= float(self.P["pre_t"]):
+            self._end_pre()
+        return n
+
+    # ---- stirring helpers
+    def _dt_bound(self):
+        """an upper bound of the CFL dt (sim.py:1012): the max speed is at least the smallest
+        sound speed sqrt(cn2 + xi (ci2 - cn2)), xi in [0, 1], as the kernels round it"""
+        c = min(float(np.sqrt(np.float32(self.cn2))), float(np.sqrt(np.float32(self.ci2))))
+        return float(self.P["cfl"]) * self.dx / c * (1.0 + 1e-6)
+
+    def _max_swaps(self, n):
+        """most field swaps n steps can make: the first may come at once, each next one needs
+        at least ceil(pre_corr / dt_max) steps"""
+        m = max(1, math.ceil(float(self.P["pre_corr"]) / self._dt_bound()))
+        return 1 + (n - 1) // m if n > 0 else 0
+
+    def _ring_steps(self):
+        """steps whose swaps fit the ring: A and B stay, DRIVE_SLOTS - 2 fields ahead"""
+        m = max(1, math.ceil(float(self.P["pre_corr"]) / self._dt_bound()))
+        return (DRIVE_SLOTS - 3) * m + 1
+
+    def _drive_info(self):
+        info = _lib.NbDriveInfo()
+        self._chk(self._lib.nb_drive_state(self._h, C.byref(info)), "nb_drive_state")
+        if info.status & 2:
+            raise _lib.NebulaError("a stirred step found no forcing field B in the ring")
+        return info
+
+    def _mkF(self):
+        """sim.py:801-804: the next forcing field, [3][sx][sy][sz] float32"""
+        if self._stir_src is not None:
+            if not self._stir_src:
+                raise _lib.NebulaError("the given forcing fields are used up")
+            return np.ascontiguousarray(self._stir_src.popleft(), np.float32)
+        return np.ascontiguousarray(np.stack(_stir.solenoidal(self.sshape, self.rng, 1.0,
+                                                              float(self.P["pre_kmax"]))), np.float32)
+
+    def _drive_fill(self, upto):
+        """push forcing fields until `upto` fields were pushed since the ring reset (a given, finite
+        list of fields is pushed as far as it goes: a step that finds no field B raises)"""
+        new = []
+        while len(self._forcing) < upto:
+            if self._stir_src is not None and not self._stir_src:
+                break
+            st = copy.deepcopy(self.rng.bit_generator.state)
+            f = self._mkF()
+            self._forcing.append((f, st))
+            new.append(f)
+        if new:
+            buf = np.ascontiguousarray(np.stack(new))
+            self._chk(self._lib.nb_drive_push(self._h, C.c_void_p(buf.ctypes.data), len(new)), "nb_drive_push")
+
+    def _drive_new(self, clock, fields=None):
+        """a fresh cross-fade (sim.py:788, 1160-1161): reset the ring, push A and B"""
+        self._drive_rewind()
+        d = _lib.NbDriveDesc(self.sshape[0], self.sshape[1], self.sshape[2], DRIVE_SLOTS, self.dxs,
+                             float(self.P["pre_corr"]), float(clock))
+        self._chk(self._lib.nb_drive_config(self._h, C.byref(d)), "nb_drive_config")
+        self._forcing = []
+        if fields is not None:
+            buf = np.ascontiguousarray(np.stack([np.asarray(f, np.float32) for f in fields]))
+            self._forcing = [(f, None) for f in buf]
+            self._chk(self._lib.nb_drive_push(self._h, C.c_void_p(buf.ctypes.data), len(buf)), "nb_drive_push")
+        else:
+            self._drive_fill(2)
+        self._drv_on = True
+        self._chk(self._lib.nb_drive_enable(self._h, 1), "nb_drive_enable")
+
+    def _drive_rewind(self):
+        """return the fields pushed ahead of use to the source: the Generator goes back to the
+        state after the last field the reference would have drawn (A and B of now)"""
+        if not self._forcing:
+            return
+        info = self._drive_info() if self._drv_on else None
+        used = len(self._forcing) if info is None else min(len(self._forcing), int(info.swaps) + 2)
+        extra = self._forcing[used:]
+        if extra:
+            if self._stir_src is not None:
+                self._stir_src.extendleft(f for f, _ in reversed(extra))
+            elif extra[0][1] is not None:
+                self.rng.bit_generator.state = extra[0][1]
+        self._forcing = self._forcing[:used]
+
+    def _drive_drop(self):
+        """drv = None (sim.py:1057-1058)"""
+        self._drive_rewind()
+        self._drv_on = False
+        self._forcing = []
+        self._chk(self._lib.nb_drive_enable(self._h, 0), "nb_drive_enable")
+
+    @property
+    def drv(self):
+        """the reference's drv dict {'A', 'B', 'clock'} (host copies), or None"""
+        if not self._drv_on:
+            return None
+        info = self._drive_info()
+        a = self._forcing[int(info.swaps)][0]
+        b = self._forcing[int(info.swaps) + 1][0]
+        return {"A": list(a), "B": list(b), "clock": float(info.clock)}
+
+    def _end_pre(self):
+        """sim.py:1051-1059: Mach number of the turbulence, end of the stirring phase"""
+        s = (C.c_double * 2)()
+        self._chk(self._lib.nb_mach_sums(self._h, s), "nb_mach_sums")
+        a, b = float(s[0]), float(s[1])
+        self.mach = math.sqrt(a / b) * float(self.P["ci_over_cn"])
+        self.log(f"pre-turbulence done: {self.ip} steps t={self.tp:.3f} mass-weighted Mach ~{self.mach:.1f}")
+        if float(self.P.get("drive_main", 0.0) or 0.0) <= 0:
+            self._drive_drop()
+        self._start_main()
+
+    def _start_main(self):
+        """sim.py:806-818: the torus joins (through the scratch block), the main phase starts, first ionization"""
+        if self.torus is not None:
+            self._stage[0].copy_(self.torus)
+            self._chk(self._lib.nb_add_torus(self._h, C.c_void_p(self._stage[0].data_ptr())), "nb_add_torus")
+            self.torus = None
+        self.phase = "main"
+        self._push()
+        self.ionize()
 
     def set_param(self, name, value):
         """sim.py:1154-1166: live parameters take effect on the next step and are logged"""
@@ -430,6 +618,8 @@ class Sim:
         if isinstance(old, int) and not isinstance(old, bool):
             value = int(round(value))
         self.P[name] = value
+        if name == "drive_main" and value > 0 and not self._drv_on and self.phase == "main":
+            self._drive_new(0.0)
         if name in LIVE:
             self.events.append((float(self.t if self.phase == "main" else 0.0), name, value))
         return value
@@ -459,23 +649,40 @@ class Sim:
         return self.t if self.phase == "main" else self.tp - self.P["pre_t"]
 
     def get_state_meta(self):
-        """sim.py:1173-1183: everything but the big fields needed to resume from this moment"""
+        """sim.py:1173-1183: everything but the big fields needed to resume from this moment.
+        The Generator state is the one after the fields in use (A and B), as the reference's."""
         c = self._clock()
-        return dict(t=c.t, it=int(c.it), tp=self.tp, ip=self.ip, dt=c.dt, phase=self.phase, mach=self.mach,
+        drv, rng = None, copy.deepcopy(self.rng.bit_generator.state)
+        if self._drv_on:
+            info = self._drive_info()
+            sw = int(info.swaps)
+            drv = {"A": list(self._forcing[sw][0]), "B": list(self._forcing[sw + 1][0]), "clock": float(info.clock)}
+            if sw + 2 < len(self._forcing) and self._forcing[sw + 2][1] is not None:
+                rng = copy.deepcopy(self._forcing[sw + 2][1])
+        return dict(t=c.t, it=int(c.it), tp=c.tp, ip=int(c.ip), dt=c.dt, phase=self.phase, mach=self.mach,
                     stars=list(self.stars), kinds=list(self.kinds), jets=list(self.jets), jkinds=list(self.jkinds),
                     births=list(self.births), n_born=self.n_born, last_birth=self.last_birth, P=dict(self.P),
-                    n_events=len(self.events), sm0=self.sm0, drv=None, rng=None, noise_calls=0)
+                    n_events=len(self.events), sm0=self.sm0, drv=drv, rng=rng, noise_calls=0)
 
     def set_state_meta(self, m):
         """sim.py:1185-1211: after the fields were restored"""
-        for k in ("tp", "ip", "phase", "mach", "n_born", "last_birth", "sm0"):
+        for k in ("phase", "mach", "n_born", "last_birth", "sm0"):
             setattr(self, k, m[k])
         self.stars, self.kinds = list(m["stars"]), list(m["kinds"])
         self.jets, self.jkinds = list(m["jets"]), list(m["jkinds"])
         self.births = list(m["births"])
         self.P = dict(m["P"])
         self.events = self.events[:m["n_events"]]
-        self._set_clock(t=m["t"], dt=m["dt"], it=m["it"])
+        self._set_clock(t=m["t"], dt=m["dt"], it=m["it"], tp=m.get("tp", 0.0), ip=m.get("ip", 0))
+        d = m.get("drv")
+        if d is None:
+            if self._drv_on:
+                self._drive_drop()
+        else:
+            self._drive_new(d["clock"], fields=[np.stack(d["A"]), np.stack(d["B"])])
+        if m.get("rng") is not None:
+            self.rng.bit_generator.state = copy.deepcopy(m["rng"])
+        self.torus = self.torus0 if self.phase == "pre" else None
         self._chk(self._lib.nb_invalidate(self._h), "nb_invalidate")
         self._push(force=True)
         self.version += 1
@@ -531,6 +738,8 @@ class Sim:
         return fr
 
     def time_label(self):
+        if self.phase == "pre":
+            return f"pre-turb {self.tp:.3f}/{self.P['pre_t']:.2f}"
         return f"t={self.t:.4f}"
 
     def stats(self):

@@ -50,6 +50,8 @@ def lib():
             getattr(L, f"oracle_plane_front_{sfx}").argtypes = [C.c_int] * 3 + [P, T, T, T, P]
             getattr(L, f"oracle_apply_plane_{sfx}").argtypes = [C.c_int] * 3 + [P, T, T, P, P]
             getattr(L, f"oracle_plane_fuv_{sfx}").argtypes = [C.c_int] * 3 + [P, P, T, T, T, P]
+            getattr(L, f"oracle_drive_{sfx}").argtypes = [C.c_int] * 3 + [P] * 4 + [C.c_int] * 3 + [P, P] + [T] * 5
+            getattr(L, f"oracle_add_torus_{sfx}").argtypes = [C.c_long] + [P] * 5
         L.oracle_to_half.argtypes = [P, P, C.c_long]
         L.oracle_threads.restype = C.c_int
         _LIB = L
@@ -165,6 +167,24 @@ class Kernels:
         return out
 
 
+    # nebula3d.py:165-179 drive (momenta updated in place); fa / fb: [3][sx][sy][sz]
+    def drive(self, rho, mx, my, mz, fa, fb, blend, amp, dt, dx, dxs):
+        nx, ny, nz = rho.shape
+        for m in (mx, my, mz):
+            assert m.dtype == self.dt and m.flags.c_contiguous
+        r, a, b = self._a(rho), self._a(fa), self._a(fb)
+        sx, sy, sz = a.shape[1:]
+        self._fn("drive")(nx, ny, nz, _p(r), _p(mx), _p(my), _p(mz), sx, sy, sz, _p(a), _p(b), blend, amp, dt, dx,
+                          dxs)
+
+    # sim.py:352-363 add_torus (fields updated in place)
+    def add_torus(self, torus, rho, mx, my, mz):
+        for m in (rho, mx, my, mz):
+            assert m.dtype == self.dt and m.flags.c_contiguous
+        t = self._a(torus)
+        self._fn("add_torus")(rho.size, _p(t), _p(rho), _p(mx), _p(my), _p(mz))
+
+
 def to_half(x):
     """sim.py:511-514 to_half (round to nearest even) restated in C."""
     x = np.ascontiguousarray(x, np.float32)
@@ -175,13 +195,17 @@ def to_half(x):
 
 # ----------------------------------------------------------------------------- the Sim driver
 class OracleSim:
-    """sim.py Sim's main-phase driver restated over the oracle kernels (host numpy state).
+    """sim.py Sim's driver restated over the oracle kernels (host numpy state): the stirring
+    phase (sim.py:1030-1059), its end (sim.py:806-818) and the main phase (sim.py:1099-1114).
 
     Inputs mirror what reset() leaves behind (sim.py:591-795): the grid, the fields, the
-    star / jet lists with their kinds, the parameter dict P and the ray budgets."""
+    star / jet lists with their kinds, the parameter dict P and the ray budgets; with
+    P['pre_t'] > 0 also the torus that joins at the end of the stirring phase, the forcing
+    fields in order of use ([3][sx][sy][sz] arrays) and the forcing grid ((sx, sy, sz), dxs)."""
 
     def __init__(self, shape, dx, rho, stars, kinds, jets, jkinds, P, rays=None, fuv_grid=None, ion_every=None,
-                 fast=True, mom=None, dtype=np.float32, start_main=True, cn2=None, ci2=None, vmax=None):
+                 fast=True, mom=None, dtype=np.float32, start_main=True, cn2=None, ci2=None, vmax=None,
+                 torus=None, stir_fields=None, stir_grid=None):
         self.K = Kernels(dtype)
         self.T = np.dtype(dtype)
         self.shape = tuple(int(v) for v in shape)
@@ -223,14 +247,27 @@ class OracleSim:
         self.fuv_every = (8 if nz <= 160 else 16) if fast else 8
         self.bmax = (Lx, Ly, Lz)
         self.t, self.it, self.dt = 0.0, 0, 0.0
+        self.tp, self.ip, self.mach = 0.0, 0, None
         self.version, self.rf_version, self.fuv_version = 0, -1, -10 ** 9
-        self.phase = "main"
         self.dt_cap = None
         self.star_arr = np.zeros((self.cap, 4), np.float32)
         self.jet_arr = np.zeros((self.cap, 4), np.float32)
-        if start_main:
-            self._set_star_weights()
-            self.ionize()
+        pre = float(self.P.get("pre_t", 0.0) or 0.0) > 0.0
+        self.torus = None
+        if torus is not None:
+            if pre:
+                self.torus = np.array(torus, dtype=self.T)
+            else:
+                self.rho += np.asarray(torus, dtype=self.T)
+        self._src = None if stir_fields is None else [np.asarray(f, dtype=self.T) for f in stir_fields]
+        if stir_grid is not None:
+            self.sshape, self.dxs = tuple(stir_grid[0]), float(stir_grid[1])
+        self.drv = None
+        self.phase = "pre" if pre else "main"
+        if pre:
+            self.drv = {"A": self._mkF(), "B": self._mkF(), "clock": 0.0}          # sim.py:786-788
+        elif start_main:
+            self._start_main()
 
     # sim.py:880-902
     def q_of(self, i):
@@ -349,11 +386,53 @@ class OracleSim:
             dt = min(dt, self.dt_cap)
         pulse = max(0.0, 1.0 + P["jet_pulse"] * math.sin(2 * math.pi * self.t / P["jet_period"]))
         self._hydro(dt, len(self.stars), P["wind"], pulse)
+        if P.get("drive_main", 0.0) > 0 and self.drv is not None:
+            self._stir(dt, P["pre_amp"] * P["drive_main"])
         self.t += dt
         self.it += 1
         self.dt = dt
 
     def step(self, k=1):                                           # sim.py:1141-1152
         for _ in range(k):
-            self._main_step()
+            if self.phase == "pre":
+                self._pre_step()
+            else:
+                self._main_step()
             self.version += 1
+
+    # ---- stirring
+    def _mkF(self):                                                # sim.py:801-804 (fields given in order)
+        if not self._src:
+            raise RuntimeError("the oracle ran out of forcing fields")
+        return self._src.pop(0)
+
+    def _stir(self, dt, amp):                                      # sim.py:1030-1042
+        d = self.drv
+        blend = min(d["clock"] / self.P["pre_corr"], 1.0)
+        self.K.drive(self.rho, self.mx, self.my, self.mz, d["A"], d["B"], blend, amp, dt, self.dx, self.dxs)
+        d["clock"] += dt
+        if d["clock"] >= self.P["pre_corr"]:
+            d["A"], d["B"], d["clock"] = d["B"], self._mkF(), 0.0
+
+    def _pre_step(self):                                           # sim.py:1044-1059
+        dt = self._compute_dt()
+        self._hydro(dt, 0, 0.0, 0.0)
+        self._stir(dt, self.P["pre_amp"])
+        self.tp += dt
+        self.ip += 1
+        self.dt = dt
+        if self.tp >= self.P["pre_t"]:
+            r = self.rho.astype(np.float64)
+            m2 = (self.mx * self.mx + self.my * self.my + self.mz * self.mz) / self.rho
+            self.mach = math.sqrt(float(m2.astype(np.float64).sum()) / float(r.sum())) * self.P["ci_over_cn"]
+            if self.P["drive_main"] <= 0:
+                self.drv = None
+            self._start_main()
+
+    def _start_main(self):                                         # sim.py:806-818
+        if self.torus is not None:
+            self.K.add_torus(self.torus, self.rho, self.mx, self.my, self.mz)
+            self.torus = None
+        self.phase = "main"
+        self._set_star_weights()
+        self.ionize()

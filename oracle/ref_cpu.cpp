@@ -532,6 +532,46 @@ static inline uint16_t f32_to_f16_rne(float f) {
     return (uint16_t)(sign | q);
 }
 
+// nebula3d.py:165-179 drive: m += rho * amp * dt * ((1 - blend) F_A + blend F_B), the forcing
+// sampled (sample_n) on the coarse grid gs of spacing dxs at the cell centre (i + 1/2) dx
+template <class T>
+static void drive_t(int nx, int ny, int nz, const T* rho, T* mx, T* my, T* mz, int sx, int sy, int sz, const T* fa,
+                    const T* fb, T blend, T amp, T dt, T dx, T dxs) {
+    const Grid gs{sx, sy, sz};
+    const long S = (long)sx * sy * sz;
+#pragma omp parallel for collapse(2) schedule(static)
+    for (int i = 0; i < nx; ++i)
+        for (int j = 0; j < ny; ++j)
+            for (int k = 0; k < nz; ++k) {
+                const V3<T> p{{(T(i) + T(0.5)) * dx, (T(j) + T(0.5)) * dx, (T(k) + T(0.5)) * dx}};
+                T f[3];
+                for (int c = 0; c < 3; ++c) {
+                    const T a = sample_n(gs, fa + c * S, p, dxs);
+                    const T b = sample_n(gs, fb + c * S, p, dxs);
+                    f[c] = (T(1) - blend) * a + blend * b;
+                }
+                const long q = ((long)i * ny + j) * nz + k;
+                const T r = rho[q] * amp * dt;
+                mx[q] = mx[q] + r * f[0];
+                my[q] = my[q] + r * f[1];
+                mz[q] = mz[q] + r * f[2];
+            }
+}
+
+// sim.py:352-363 add_torus
+template <class T>
+static void add_torus_t(long n, const T* torus, T* rho, T* mx, T* my, T* mz) {
+#pragma omp parallel for schedule(static)
+    for (long q = 0; q < n; ++q) {
+        const T r = rho[q], tq = torus[q];
+        const T f = T(1) - tq / (tq + r);
+        rho[q] = r + tq;
+        mx[q] = mx[q] * f;
+        my[q] = my[q] * f;
+        mz[q] = mz[q] * f;
+    }
+}
+
 // ==================================================================================== C ABI
 #define NB_ORACLE_EXPORT extern "C" __attribute__((visibility("default")))
 
@@ -582,6 +622,18 @@ static inline uint16_t f32_to_f16_rne(float f) {
                                                  T dx, T* g) {                                                \
         plane_fuv_t<T>(nx, ny, nz, rho, xi, kappa, lum, dx, g);                                               \
     }
+#define INSTANTIATE_STIR(T, SFX)                                                                              \
+    NB_ORACLE_EXPORT void oracle_drive_##SFX(int nx, int ny, int nz, const T* rho, T* mx, T* my, T* mz, int sx,      \
+                                             int sy, int sz, const T* fa, const T* fb, T blend, T amp, T dt, T dx,   \
+                                             T dxs) {                                                               \
+        drive_t<T>(nx, ny, nz, rho, mx, my, mz, sx, sy, sz, fa, fb, blend, amp, dt, dx, dxs);                       \
+    }                                                                                                               \
+    NB_ORACLE_EXPORT void oracle_add_torus_##SFX(long n, const T* torus, T* rho, T* mx, T* my, T* mz) {             \
+        add_torus_t<T>(n, torus, rho, mx, my, mz);                                                                  \
+    }
+INSTANTIATE_STIR(float, f32)
+INSTANTIATE_STIR(double, f64)
+
 INSTANTIATE_PLANE(float, f32)
 INSTANTIATE_PLANE(double, f64)
 

@@ -16,6 +16,11 @@ Fixtures (all small, committed):
                    apply_front, smooth_xi, cast_fuv, apply_fuv, to_half.
   sim_<name>.npz   end-to-end reference `Sim` runs: the state after reset (first
                    ionization included) and after every step, clocks, the FUV field.
+  stir.npz         the stirring kernels (drive, add_torus) and the solenoidal forcing
+                   generator on a seeded Generator.
+  sim_bipolar_pre.npz  a reference `Sim` run through the pre-turbulence (stirring) phase,
+                   its end (torus added, first ionization) and main-phase stirring, with
+                   every forcing field the run drew.
 Test infrastructure only: nothing in the product reads these files.
 """
 import argparse
@@ -238,6 +243,83 @@ def timeline_cases(ref, rng):
     return out
 
 
+# ----------------------------------------------------------------------------- stirring
+def stir_cases(N, S, rng):
+    """nebula3d.py:165-179 drive, sim.py:352-363 add_torus, nebula3d.py:514-525 solenoidal"""
+    out = {}
+    shape = (10, 9, 8)
+    dx = 1.0 / 8.0
+    rho = np.exp(rng.normal(0.0, 1.0, shape)).astype(np.float32)
+    mom = (rng.normal(0.0, 1.0, (3,) + shape) * rho).astype(np.float32)
+    # coarse grids: one covering the domain, one too short along y (samples outside read 0)
+    for tag, sshape, dxs in (("in", (7, 6, 5), 0.23), ("out", (6, 3, 5), 0.3)):
+        A = [rng.normal(0.0, 1.0, sshape).astype(np.float32) for _ in range(3)]
+        B = [rng.normal(0.0, 1.0, sshape).astype(np.float32) for _ in range(3)]
+        m = [a.copy() for a in mom]
+        blend, amp, dt = 0.37, 7.0, 1.3e-3
+        N.drive.run(shape, [rho, m[0], m[1], m[2]] + A + B + [blend, amp, dt, dx, dxs])
+        out[f"d_{tag}_A"], out[f"d_{tag}_B"] = np.stack(A), np.stack(B)
+        out[f"d_{tag}_out"] = np.stack(m)
+        out[f"d_{tag}_scalars"] = np.array([blend, amp, dt, dx, dxs], np.float64)
+    out["d_rho"], out["d_mom"] = rho, mom
+    # add_torus
+    tq = (np.exp(rng.normal(0.0, 2.0, shape)) * (rng.random(shape) < 0.5)).astype(np.float32)
+    r2, m2 = rho.copy(), [a.copy() for a in mom]
+    S.add_torus.run(shape, [r2, m2[0], m2[1], m2[2], tq])
+    out["a_torus"], out["a_rho"], out["a_mom"] = tq, r2, np.stack(m2)
+    # the forcing generator on a seeded Generator, odd and even grid sizes
+    for tag, sshape, kmax in (("odd", (7, 6, 5), 4.0), ("even", (8, 6, 10), 6.0)):
+        g = np.random.default_rng(4242)
+        v = N.solenoidal(sshape, g, 1.0, kmax)
+        out[f"sol_{tag}"] = np.stack(v)
+        out[f"sol_{tag}_next"] = g.standard_normal(4)          # the Generator state it leaves behind
+    return out
+
+
+def sim_pre_case(S, scenario, res, overrides, nsteps, rays, fuv, ic_mode):
+    """a reference Sim through the stirring phase and into the main phase (sim.py:1044-1059, 1099-1114)"""
+    P = S.make_params(scenario, overrides)
+    sim = S.Sim(scenario, res=res, params=P, ic_mode=ic_mode, rays=rays, fuv_grid=fuv, device="cpu",
+                verbose=False, fast=True)
+    print(f"  {scenario} {sim.shape} phase {sim.phase}, {len(sim.stars)} stars", flush=True)
+    fields = []                                    # every forcing field the run drew, in order
+
+    def note():
+        for F in (sim.drv["A"], sim.drv["B"]) if sim.drv else ():
+            a = np.stack([c.numpy() for c in F])
+            if not any(a.shape == f.shape and np.array_equal(a, f) for f in fields):
+                fields.append(a)
+
+    def snap():
+        return dict(rho=sim.rho.numpy(), mx=sim.mx.numpy(), my=sim.my.numpy(), mz=sim.mz.numpy(),
+                    xi=sim.xi.numpy(), dfront=sim.dfront.numpy())
+
+    note()
+    s0 = snap()
+    meta = dict(scenario=scenario, res=res, shape=list(sim.shape), dx=sim.dx, L=list(sim.L), rays=list(rays),
+                fuv=list(fuv), ion_every=sim.ion_every, fuv_every=sim.fuv_every,
+                stars=[list(map(float, s)) for s in sim.stars], kinds=list(sim.kinds),
+                jets=[list(map(float, j)) for j in sim.jets], jkinds=list(sim.jkinds),
+                P={k: v for k, v in sim.P.items() if isinstance(v, (int, float, str, bool, type(None), list))},
+                sshape=list(sim.sshape), dxs=sim.dxs, cn2=sim.cn2, ci2=sim.ci2, steps=[])
+    out = {"rho_ic": s0["rho"], "torus": sim.torus0}
+    for k, v in s0.items():
+        out[f"s0_{k}"] = v
+    for n in range(nsteps):
+        sim.step(1)
+        note()
+        for k, v in snap().items():
+            out[f"s{n + 1}_{k}"] = v
+        d = sim.drv
+        meta["steps"].append(dict(t=sim.t, it=sim.it, tp=sim.tp, ip=sim.ip, dt=sim.dt, phase=sim.phase,
+                                  clock=None if d is None else d["clock"], mach=sim.mach))
+        print(f"    step {n}: phase {sim.phase} tp={sim.tp:.5g} t={sim.t:.5g} dt={sim.dt:.5g} "
+              f"clock={None if d is None else round(d['clock'], 5)} fields={len(fields)}", flush=True)
+    out["fields"] = np.stack(fields)
+    out["meta"] = np.array(json.dumps(meta))
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference")
@@ -248,6 +330,15 @@ def main():
     if a.only in (None, "kernels"):
         print("kernels:", flush=True)
         np.savez_compressed(os.path.join(HERE, "kernels.npz"), **kernel_cases(N, S, rng))
+    if a.only in (None, "stir"):
+        print("stir:", flush=True)
+        np.savez_compressed(os.path.join(HERE, "stir.npz"), **stir_cases(N, S, np.random.default_rng(515)))
+    if a.only in (None, "bipolar_pre"):
+        print("sim bipolar_pre:", flush=True)
+        c = dict(scenario="bipolar", res=8, overrides=dict(pre_t=0.49, pre_corr=0.02, pre_amp=7.0, drive_main=0.5,
+                                                            seed=13, jet_r=0.35, jet_angle=35.0, clumps=0),
+                 nsteps=14, rays=(8, 16), fuv=(6, 8, 16), ic_mode="nebula3d")   # 6-cell forcing grid
+        np.savez_compressed(os.path.join(HERE, "sim_bipolar_pre.npz"), **sim_pre_case(S, **c))
     if a.only in (None, "timeline"):
         print("timeline:", flush=True)
         np.savez_compressed(os.path.join(HERE, "timeline.npz"), **timeline_cases(a.ref, np.random.default_rng(99)))
@@ -266,7 +357,7 @@ def main():
                       nsteps=3, fast=True, rays=(8, 16), fuv=(6, 8, 16), ion_every=2),
     }
     for name, c in cases.items():
-        if a.only not in (None, name) or a.only == "timeline":
+        if a.only not in (None, name):
             continue
         print(f"sim {name}:", flush=True)
         np.savez_compressed(os.path.join(HERE, f"sim_{name}.npz"), **sim_case(S, **c))

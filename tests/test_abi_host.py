@@ -24,13 +24,33 @@ def test_library_exports_every_declared_symbol(lib_built):
     assert set(names) == set(_lib.SIGNATURES), "ctypes signatures must cover the header exactly"
 
 
-def test_struct_layouts_match_header():
-    """field order / sizes of the ctypes mirrors (x86-64 and aarch64 share this ABI)"""
+def test_struct_layouts_match_header(tmp_path):
+    """every ctypes mirror has the size and field offsets the C compiler gives the header's struct"""
+    import shutil
+    import subprocess
     from nebulaviewer_gb300 import _lib
-    assert C.sizeof(_lib.NbStar) == 8 * 8 + 2 * 4
-    assert C.sizeof(_lib.NbClock) == 24
-    assert _lib.NbDesc.f.offset % 8 == 0
-    assert C.sizeof(_lib.NbLive) == 11 * 8 + 8 + 2 * 8
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    mirrors = {"nb_desc": _lib.NbDesc, "nb_fields": _lib.NbFields, "nb_live": _lib.NbLive, "nb_star": _lib.NbStar,
+               "nb_clock": _lib.NbClock, "nb_drive_desc": _lib.NbDriveDesc, "nb_drive_info": _lib.NbDriveInfo}
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "nebula.h"', "int main(void) {"]
+    for cname, py in mirrors.items():
+        lines.append(f'printf("{cname} size %zu\\n", sizeof({cname}));')
+        for fname, _ in py._fields_:
+            lines.append(f'printf("{cname} {fname} %zu\\n", offsetof({cname}, {fname}));')
+    lines.append("return 0; }")
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    inc = os.path.join(ROOT, "include")
+    subprocess.run([cc, "-std=c11", "-I", inc, str(src), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split("\n")
+    got = {tuple(l.split()[:2]): int(l.split()[2]) for l in out if l.strip()}
+    for cname, py in mirrors.items():
+        assert got[(cname, "size")] == C.sizeof(py), cname
+        for fname, _ in py._fields_:
+            assert got[(cname, fname)] == getattr(py, fname).offset, (cname, fname)
 
 
 def test_null_handle_errors_without_gpu(lib_built):

@@ -126,3 +126,64 @@ def test_fp64_twin_runs_and_is_close(kernels_npz):
                       1.0, floor, cn2, ci2, vmax, 1, 0)
         out[T] = o
     assert rel_linf(out[np.float32], out[np.float64]) < 1e-5
+
+
+# ---------------------------------------------------------------------------- stirring
+@pytest.mark.parametrize("tag", ("in", "out"))
+def test_drive_bit_exact(tag):
+    """nebula3d.py:165-179 drive; 'out': part of the domain lies outside the forcing grid (samples 0)"""
+    from conftest import golden
+    z = golden("stir.npz")
+    m = [a.copy() for a in z["d_mom"]]
+    blend, amp, dt, dx, dxs = z[f"d_{tag}_scalars"]
+    O.Kernels().drive(z["d_rho"], *m, z[f"d_{tag}_A"], z[f"d_{tag}_B"], blend, amp, dt, dx, dxs)
+    for a, b in zip(m, z[f"d_{tag}_out"]):
+        assert bits_equal(a, b)
+
+
+def test_add_torus_bit_exact():
+    from conftest import golden
+    z = golden("stir.npz")
+    r, m = z["d_rho"].copy(), [a.copy() for a in z["d_mom"]]
+    O.Kernels().add_torus(z["a_torus"], r, *m)
+    assert bits_equal(r, z["a_rho"])
+    for a, b in zip(m, z["a_mom"]):
+        assert bits_equal(a, b)
+
+
+@pytest.mark.parametrize("tag,shape,kmax", (("odd", (7, 6, 5), 4.0), ("even", (8, 6, 10), 6.0)))
+def test_forcing_generator_reproduces_reference_draws(tag, shape, kmax):
+    """the package's forcing generator: the reference's field bit for bit from an equal Generator
+    state, and the Generator left in the same state"""
+    from conftest import golden
+    from nebulaviewer_gb300 import stir
+    z = golden("stir.npz")
+    g = np.random.default_rng(4242)
+    assert bits_equal(np.stack(stir.solenoidal(shape, g, 1.0, kmax)), z[f"sol_{tag}"])
+    assert np.array_equal(g.standard_normal(4), z[f"sol_{tag}_next"])
+
+
+def test_forcing_grid_rules():
+    """sim.py:761-768: 24 cells per unit + 2 (resolution independent), or one per 6 cells + 2"""
+    from nebulaviewer_gb300 import stir
+    assert stir.forcing_grid((1.6, 1.6, 1.6), 1 / 128, (205, 205, 205)) == ((41, 41, 41), 1 / 24)
+    assert stir.forcing_grid((2.0, 2.0, 2.0), 0.125, (16, 16, 16), physical=False) == ((4, 4, 4), 0.75)
+
+
+def test_oracle_sim_through_stirring_phase_matches_reference_sim():
+    """the oracle's Sim driver against the reference Sim: stirring phase with a field swap, its end
+    (torus, first ionization), main-phase stirring with another swap -- every field bit for bit"""
+    d, m = golden_sim("bipolar_pre")
+    o = O.OracleSim(m["shape"], m["dx"], d["rho_ic"], m["stars"], m["kinds"], m["jets"], m["jkinds"], m["P"],
+                    rays=m["rays"], fuv_grid=m["fuv"], ion_every=m["ion_every"], fast=True, torus=d["torus"],
+                    stir_fields=list(d["fields"]), stir_grid=(m["sshape"], m["dxs"]), cn2=m["cn2"], ci2=m["ci2"])
+    for n, st in enumerate(m["steps"]):
+        o.step(1)
+        assert o.phase == st["phase"] and o.tp == st["tp"] and o.t == st["t"] and o.dt == st["dt"]
+        assert (o.drv is None) == (st["clock"] is None)
+        if o.drv is not None:
+            assert o.drv["clock"] == st["clock"]
+        for f in ("rho", "mx", "my", "mz", "xi"):
+            assert bits_equal(getattr(o, f), d[f"s{n + 1}_{f}"]), (n, f)
+        if st["mach"] is not None:
+            assert abs(o.mach - st["mach"]) <= 1e-5 * st["mach"]        # FP64 sum vs the reference's FP32 atomics
