@@ -231,8 +231,9 @@ def run_gb300(args):
     dev = torch.device("cuda", local)
     from nebulaviewer_gb300 import _lib
     from nebulaviewer_gb300.sim import Sim
-    lib = _lib.load()
-    sim = Sim("sheet", res=args.res, device=dev, verbose=False)
+    arith = _lib.arith_of(args.arith)
+    lib = _lib.load(arith)
+    sim = Sim("sheet", res=args.res, device=dev, verbose=False, arith=arith)
     ncell = sim._n
     nstars = len(sim.stars)
     ic_host = host_ic(sim) if (rank == 0 and ws == 1 and not args.no_cpu_baseline) else None
@@ -345,6 +346,29 @@ def run_gb300(args):
             "clocks": clocks,
         }
     sim.close()
+    if rank == 0:
+        # the other library build on the same workload, device-resident, for comparison
+        other = "exact" if arith == "fast" else "fast"
+        s2 = Sim("sheet", res=args.res, device=dev, verbose=False, arith=other)
+        autotune(s2)
+        for _ in range(args.warmup):
+            s2.step(1, sync=False)
+            if s2.version % s2.fuv_every == 0:
+                s2.fuv_field()
+        torch.cuda.synchronize(dev)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            s2.step(1, sync=False)
+            if s2.version % s2.fuv_every == 0:
+                s2.fuv_field()
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        ms2 = e0.elapsed_time(e1)
+        res["arith"] = arith
+        res[f"arith_{other}"] = {"value": ncell * args.steps / (ms2 * 1e-3) / 1e9, "unit": UNIT,
+                                 "ms_per_step": ms2 / args.steps}
+        s2.close()
     if rank == 0 and ic_host is not None:
         cv, cores, per_step, _ = cpu_sample(ic_host, steps=3)
         res["cpu_baseline"] = {"value": cv, "unit": UNIT, "cores": cores, "kind": "port",
@@ -368,7 +392,7 @@ def run_batch(args):
     nb_build.build(verbose=False)
     from nebulaviewer_gb300.batch import BatchSim, batch_workload
     dev = torch.device("cuda", 0)
-    sims = batch_workload(n=args.instances, device=dev, verbose=False)
+    sims = batch_workload(n=args.instances, device=dev, verbose=False, arith=args.arith)
     cells = sum(s._n for s in sims)
     # plain: each instance alone, blocking steps (the reference's calling pattern)
     plain_steps = max(3, args.steps // 5)
@@ -403,7 +427,7 @@ def run_batch(args):
            "step_roofline": {"bytes_per_cell_step": 108.0, "achieved": 108.0 * val, "peak": peak, "unit": "GB/s",
                              "frac": 108.0 * val / peak, "peak_source": peak_kind,
                              "note": "hydro bytes only (the ionization share varies per instance)"},
-           "gpu_launches": B.launches() - l0, "clocks": clk.summary()}
+           "gpu_launches": B.launches() - l0, "clocks": clk.summary(), "arith": sims[0].arith}
     B.close()
     print(json.dumps(res), flush=True)
     return 0
@@ -424,7 +448,7 @@ def run_served(args):
         ic = (ics.sheet(res=e, seed=40 + m, nstars=4, device=dev) if m % 2 == 0 else
               ics.torus(seed=50 + m, device=dev, shape=(e, e, e), nstars=3))
         s = Sim.from_state(ic["shape"], ic["dx"], ic["rho"], ic["stars"], ic["kinds"], ic["jets"], ic["jkinds"],
-                           ic["P"], mom=ic["mom"], device=dev)
+                           ic["P"], mom=ic["mom"], device=dev, arith=args.arith)
         s.step(8)
         snaps.append(serve.Snapshot(s))
         s.close()
@@ -438,7 +462,7 @@ def run_served(args):
            "p50_ms": stats["p50_ms"], "p99_ms": stats["p99_ms"],
            "config": {"workload": f"{args.requests} requests, Poisson {args.rate:g}/s, snapshots 96^3/160^3/256^3/320^3, "
                                   "+-50% on a star's Q or the wind, 10-100 steps, 150 GB budget at 48 B/cell"},
-           "stats": stats}
+           "stats": stats, "arith": snaps[0].arith}
     print(json.dumps(res), flush=True)
     return 0
 
@@ -452,7 +476,7 @@ def run_cliff(args):
     from nebulaviewer_gb300.sim import Sim
     dev = torch.device("cuda", 0)
     res = args.res if args.res != RES else 1024
-    sim = Sim("cliffwall", res=res, device=dev, verbose=False)
+    sim = Sim("cliffwall", res=res, device=dev, verbose=False, arith=args.arith)
     m0 = sim.conservation()
     sim.step(args.warmup)
     torch.cuda.synchronize(dev)
@@ -484,7 +508,7 @@ def run_cliff(args):
                              "t_end": sim.t},
              "step_roofline": {"bytes_per_cell_step": b_step, "achieved": b_step * val, "peak": peak, "unit": "GB/s",
                                "frac": b_step * val / peak, "peak_source": peak_kind},
-             "clocks": clk.summary()}
+             "clocks": clk.summary(), "arith": sim.arith}
     sim.close()
     print(json.dumps(res_d), flush=True)
     return 0
@@ -502,6 +526,9 @@ def main():
     ap.add_argument("--requests", type=int, default=100)
     ap.add_argument("--rate", type=float, default=200.0)
     ap.add_argument("--instances", type=int, default=32)
+    ap.add_argument("--arith", default=None, choices=["exact", "fast"],
+                    help="library build: exact (bit-identical to the reference kernels) or fast (FMA, approximate "
+                         "division / square root); default: the package default")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

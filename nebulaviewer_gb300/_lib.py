@@ -1,13 +1,19 @@
-"""ctypes binding of libnebula.so (include/nebula.h).
+"""ctypes binding of libnebula.so / libnebula_fast.so (include/nebula.h).
 
-The library is built in-tree by `nebulaviewer_gb300.build.build()`; importing this module
-without it raises immediately: there is no CPU or PyTorch fallback for the simulation step.
+The libraries are built in-tree by `nebulaviewer_gb300.build.build()`; loading one that is
+missing raises immediately: there is no CPU or PyTorch fallback for the simulation step.
+Two builds of the same ABI: "exact" (every float operation the reference's: bit-identical
+results) and "fast" (FMA contraction, approximate division / square root, flush-to-zero:
+within the path's tolerance of the exact build).  DEFAULT_ARITH is what a Sim uses unless
+told otherwise (environment variable NEBULA_ARITH overrides it).
 """
 import ctypes as C
 import os
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(HERE, "libnebula.so")
+LIB_PATHS = {"exact": os.path.join(HERE, "libnebula.so"), "fast": os.path.join(HERE, "libnebula_fast.so")}
+LIB_PATH = LIB_PATHS["exact"]
+DEFAULT_ARITH = os.environ.get("NEBULA_ARITH", "fast")
 
 NB_ABI_VERSION = 2
 NB_OK = 0
@@ -111,32 +117,43 @@ TUNE = {"chunk_i": 0, "ray_group": 1, "fuv_group": 2, "tile_order": 3}
 PROF_KINDS = ["ctrl", "stage1", "stage2", "cast_rays", "apply_front", "smooth", "cast_fuv", "apply_fuv", "max_speed",
               "snapshot", "drive"]
 
-_lib = None
+_libs = {}
 
 
 class NebulaError(RuntimeError):
     pass
 
 
-def load(path=LIB_PATH):
-    """Load libnebula.so (once).  Raises if it is missing: build it first."""
-    global _lib
-    if _lib is not None:
-        return _lib
-    if not os.path.exists(path):
-        raise NebulaError(f"{path} is missing: run nebulaviewer_gb300.build.build() (nvcc, sm_103a) first")
-    lib = C.CDLL(path)
+def arith_of(arith):
+    a = DEFAULT_ARITH if arith is None else arith
+    if a not in LIB_PATHS:
+        raise ValueError(f"arith must be one of {sorted(LIB_PATHS)}, not {a!r}")
+    return a
+
+
+def load(arith=None, path=None):
+    """Load libnebula.so ("exact") or libnebula_fast.so ("fast") once; `path` loads another build
+    of the same ABI.  Raises if the file is missing: build it first."""
+    key = path or arith_of(arith)
+    if key in _libs:
+        return _libs[key]
+    p = path or LIB_PATHS[key]
+    if not os.path.exists(p):
+        raise NebulaError(f"{p} is missing: run nebulaviewer_gb300.build.build() (nvcc, sm_103a) first")
+    lib = C.CDLL(p)
     for name, (res, args) in SIGNATURES.items():
         fn = getattr(lib, name)
         fn.restype = res
         fn.argtypes = args
-    _lib = lib
+    _libs[key] = lib
     return lib
 
 
-def check(rc, handle=None, what=""):
+def check(rc, handle=None, what="", lib=None):
+    """raise NebulaError with the library's message for a non-zero status (`lib`: the library
+    that returned it; for a handle, either build reads the handle's own message)"""
     if rc != NB_OK:
-        lib = load()
+        lib = lib or load()
         msg = lib.nb_last_error(handle).decode(errors="replace")
         raise NebulaError(f"{what}: {ERRORS.get(rc, rc)}: {msg}")
     return rc

@@ -28,7 +28,8 @@ _CACHE = {}
 
 
 def _key(sim):
-    return (tuple(sim.shape), len(sim.stars), tuple(sim.rfront.shape), tuple(sim.att.shape), sim.P.get("solver"))
+    return (tuple(sim.shape), len(sim.stars), tuple(sim.rfront.shape), tuple(sim.att.shape), sim.P.get("solver"),
+            sim.arith)
 
 
 def get(sim, knob):

@@ -25,7 +25,9 @@ class BatchSim:
             if s.phase != "main" or s._stirring():
                 raise NotImplementedError("batched steps are main-phase steps without stirring: step stirred "
                                           "instances alone (Sim.step)")
-        self._lib = _lib.load()
+        if len({s.arith for s in self.sims}) != 1:
+            raise ValueError("the instances of a batch must come from one library build (same arith)")
+        self._lib = self.sims[0]._lib
         n = len(self.sims)
         for s in self.sims:
             s._push()

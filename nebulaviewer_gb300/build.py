@@ -1,5 +1,16 @@
-"""In-tree build of libnebula.so for sm_103a (nvcc, one -gencode, translation units compiled
-in parallel).  `python -m nebulaviewer_gb300.build` or `build()`."""
+"""In-tree build of the two libraries for sm_103a (nvcc, one -gencode, translation units
+compiled in parallel).  `python -m nebulaviewer_gb300.build` or `build()`.
+
+Both export the same C ABI (include/nebula.h) and differ only in floating-point code
+generation:
+  libnebula.so       exact: no contraction of a*b+c, IEEE division and square root, no
+                     flush-to-zero -- every float operation is the reference's, so results are
+                     bit-identical to the reference's kernels;
+  libnebula_fast.so  fast: a*b+c contracted to FMA, approximate division and square root,
+                     denormals flushed to zero in the compute kernels (the snapshot / frame
+                     formats keep the exact flags, their bytes are part of the format); stays
+                     within the path's stated tolerance of the exact build.
+"""
 import concurrent.futures as cf
 import os
 import shutil
@@ -9,12 +20,17 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
-LIB = os.path.join(HERE, "libnebula.so")
+LIBS = {"exact": os.path.join(HERE, "libnebula.so"), "fast": os.path.join(HERE, "libnebula_fast.so")}
+LIB = LIBS["exact"]
 SOURCES = ["nb_hydro.cu", "nb_step.cu", "nb_rays.cu", "nb_fuv.cu", "nb_snap.cu", "nb_stir.cu", "nb_api.cu"]
+EXACT_ONLY = {"nb_snap.cu"}          # byte formats: same code generation in both libraries
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-# -fmad=false: no contraction of a*b+c, so every float operation is the reference's own
-NVCC_FLAGS = ARCH + ["-O3", "-std=c++17", "-lineinfo", "-fmad=false", "-Xcompiler", "-fPIC,-fvisibility=hidden",
-                     "-Xptxas", "-v"]
+COMMON = ARCH + ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-fvisibility=hidden", "-Xptxas", "-v"]
+ARITH_FLAGS = {
+    "exact": ["-fmad=false", "-prec-div=true", "-prec-sqrt=true", "-ftz=false"],
+    "fast": ["-fmad=true", "-prec-div=false", "-prec-sqrt=false", "-ftz=true"],
+}
+NVCC_FLAGS = COMMON + ARITH_FLAGS["exact"]
 
 
 def nvcc():
@@ -24,23 +40,26 @@ def nvcc():
     return exe
 
 
-def _compile(src, verbose):
-    obj = os.path.join(BUILD, os.path.splitext(src)[0] + ".o")
-    cmd = [nvcc()] + NVCC_FLAGS + ["-c", os.path.join(CSRC, src), "-o", obj]
+def _compile(job, verbose):
+    arith, src = job
+    flavour = "exact" if src in EXACT_ONLY else arith
+    out = os.path.join(BUILD, arith)
+    obj = os.path.join(out, os.path.splitext(src)[0] + ".o")
+    cmd = [nvcc()] + COMMON + ARITH_FLAGS[flavour] + ["-c", os.path.join(CSRC, src), "-o", obj]
     p = subprocess.run(cmd, capture_output=True, text=True)
     if p.returncode != 0:
-        raise RuntimeError(f"nvcc failed on {src}:\n{p.stdout}\n{p.stderr}")
-    with open(os.path.join(BUILD, os.path.splitext(src)[0] + ".ptxas.txt"), "w") as f:
+        raise RuntimeError(f"nvcc failed on {src} ({arith}):\n{p.stdout}\n{p.stderr}")
+    with open(os.path.join(out, os.path.splitext(src)[0] + ".ptxas.txt"), "w") as f:
         f.write(p.stderr)
     if verbose:
-        print(f"  built {src}", flush=True)
+        print(f"  built {src} ({arith})", flush=True)
     return obj
 
 
 def _stale():
-    if not os.path.exists(LIB):
+    if not all(os.path.exists(p) for p in LIBS.values()):
         return True
-    t = os.path.getmtime(LIB)
+    t = min(os.path.getmtime(p) for p in LIBS.values())
     for d in (CSRC, os.path.join(HERE, "..", "include")):
         for n in os.listdir(d):
             if os.path.getmtime(os.path.join(d, n)) > t:
@@ -49,20 +68,24 @@ def _stale():
 
 
 def build(force=False, verbose=True):
-    """Compile every translation unit for sm_103a and link libnebula.so in the package dir."""
+    """Compile every translation unit for sm_103a, twice (exact and fast code generation), and
+    link libnebula.so and libnebula_fast.so in the package dir."""
     if not force and not _stale():
         return LIB
-    os.makedirs(BUILD, exist_ok=True)
-    with cf.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
-        objs = list(ex.map(lambda s: _compile(s, verbose), SOURCES))
-    tmp = LIB + ".tmp"
-    cmd = [nvcc()] + ARCH + ["-shared", "-o", tmp] + objs
-    p = subprocess.run(cmd, capture_output=True, text=True)
-    if p.returncode != 0:
-        raise RuntimeError(f"link failed:\n{p.stdout}\n{p.stderr}")
-    os.replace(tmp, LIB)
-    if verbose:
-        print(f"  linked {LIB}", flush=True)
+    for arith in LIBS:
+        os.makedirs(os.path.join(BUILD, arith), exist_ok=True)
+    jobs = [(a, s) for a in LIBS for s in SOURCES]
+    with cf.ThreadPoolExecutor(max_workers=min(len(jobs), os.cpu_count() or 4)) as ex:
+        objs = list(ex.map(lambda j: _compile(j, verbose), jobs))
+    for arith, path in LIBS.items():
+        mine = [o for (a, _), o in zip(jobs, objs) if a == arith]
+        tmp = path + ".tmp"
+        p = subprocess.run([nvcc()] + ARCH + ["-shared", "-o", tmp] + mine, capture_output=True, text=True)
+        if p.returncode != 0:
+            raise RuntimeError(f"link failed:\n{p.stdout}\n{p.stderr}")
+        os.replace(tmp, path)
+        if verbose:
+            print(f"  linked {path}", flush=True)
     return LIB
 
 

@@ -30,7 +30,9 @@ class Snapshot:
         self.fields = {k: getattr(sim, "_" + k).clone() for k in ("rho", "mx", "my", "mz", "xi", "dfront", "g0")}
         self.meta = sim.get_state_meta()
         self.rays, self.fuv = sim.rfront.shape, sim.att.shape
-        self.ion_every, self.fast = sim.ion_every, sim.fast
+        self.ion_every, self.fast, self.arith = sim.ion_every, sim.fast, sim.arith
+        self.torus = sim.torus0 if sim.phase == "pre" else None          # joins when the stirring phase ends
+        self.stir_grid = (sim.sshape, sim.dxs)
 
     @property
     def cells(self):
@@ -42,7 +44,8 @@ class Snapshot:
         f = self.fields
         s = Sim.from_state(self.shape, self.dx, f["rho"], m["stars"], m["kinds"], m["jets"], m["jkinds"], m["P"],
                            mom=[f["mx"], f["my"], f["mz"]], rays=self.rays, fuv_grid=self.fuv,
-                           ion_every=self.ion_every, fast=self.fast, device=self.device, start_main=False)
+                           ion_every=self.ion_every, fast=self.fast, device=self.device, start_main=False,
+                           torus=self.torus, stir_grid=self.stir_grid, arith=self.arith)
         s._xi.copy_(f["xi"])
         s._dfront.copy_(f["dfront"])
         s._g0.copy_(f["g0"])

@@ -102,7 +102,8 @@ class Sim:
     profile = False
 
     def __init__(self, scenario="torus", res=None, params=None, ic_mode="synthetic", rays=None, fuv_grid=None,
-                 ion_every=None, device="cuda:0", verbose=True, fast=True, seed=None):
+                 ion_every=None, device="cuda:0", verbose=True, fast=True, seed=None, arith=None):
+        self.arith = _lib.arith_of(arith)
         self.device = torch.device(device)
         self.fast = fast
         self.verbose = verbose
@@ -118,13 +119,15 @@ class Sim:
     @classmethod
     def from_state(cls, shape, dx, rho, stars, kinds, jets, jkinds, P, mom=None, rays=None, fuv_grid=None,
                    ion_every=None, fast=True, device="cuda:0", verbose=False, start_main=True, torus=None,
-                   stir_fields=None, stir_grid=None):
+                   stir_fields=None, stir_grid=None, arith=None):
         """An instance from explicit fields and star lists (what the reference's reset() leaves
         behind, sim.py:710-795), e.g. initial conditions built by the reference's own IC code.
         `torus` joins rho when the main phase starts (at once without a stirring phase);
         `stir_fields` ([3][sx][sy][sz] arrays) replaces the forcing generator, in order of use;
-        `stir_grid` = ((sx, sy, sz), dxs) overrides the forcing grid."""
+        `stir_grid` = ((sx, sy, sz), dxs) overrides the forcing grid.  `arith`: "exact" (bit-identical
+        to the reference's kernels) or "fast" (FMA, approximate division / square root)."""
         self = cls.__new__(cls)
+        self.arith = _lib.arith_of(arith)
         self.device = torch.device(device)
         self.fast = fast
         self.verbose = verbose
@@ -210,7 +213,7 @@ class Sim:
         self.ion_every = self.ion_every_override or (max(P["ion_every"], 3) if self.fast else P["ion_every"])
         self.fuv_every = (8 if nz <= 160 else 16) if self.fast else 8               # sim.py:759
         self._stream = torch.cuda.current_stream(dev) if dev.type == "cuda" else None
-        lib = _lib.load()
+        lib = _lib.load(self.arith)
         d = _lib.NbDesc()
         d.abi_version = _lib.NB_ABI_VERSION
         d.nx, d.ny, d.nz = nx, ny, nz
@@ -233,7 +236,7 @@ class Sim:
                             self._xi.data_ptr(), st.data_ptr(), self._dfront.data_ptr(), self._g0.data_ptr())
         d.stream = self._stream.cuda_stream if self._stream is not None else None
         h = C.c_void_p()
-        _lib.check(lib.nb_create(C.byref(d), C.byref(h)), None, "nb_create")
+        _lib.check(lib.nb_create(C.byref(d), C.byref(h)), None, "nb_create", lib)
         self._h = h
         self._lib = lib
         self._n = n
@@ -299,7 +302,7 @@ class Sim:
         self.prof[key] = self.prof.get(key, 0.0) + (time.perf_counter() - t0)
 
     def _chk(self, rc, what):
-        _lib.check(rc, self._h, what)
+        _lib.check(rc, self._h, what, self._lib)
 
     def _push(self, force=False):
         """upload live parameters / the star table when they changed (P may be edited directly,

@@ -15,12 +15,15 @@ def header_symbols():
     return sorted(set(re.findall(r"^\s*(?:int|void|const char\*)\s+(nb_\w+)\s*\(", src, re.M)))
 
 
-def test_library_exports_every_declared_symbol(lib_built):
+@pytest.mark.parametrize("arith", ("exact", "fast"))
+def test_library_exports_every_declared_symbol(lib_built, arith):
+    """both builds (exact and fast code generation) export every symbol the header declares"""
     from nebulaviewer_gb300 import _lib
+    lib = _lib.load(arith)
     names = header_symbols()
     assert len(names) >= 17
     for n in names:
-        assert hasattr(lib_built, n), n
+        assert hasattr(lib, n), n
     assert set(names) == set(_lib.SIGNATURES), "ctypes signatures must cover the header exactly"
 
 

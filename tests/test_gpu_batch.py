@@ -30,9 +30,10 @@ def scenes(ics):
     return out
 
 
-def make(S, ic, ion_every=None):
+def make(S, ic, ion_every=None, arith=None):
     return S.Sim.from_state(ic["shape"], ic["dx"], ic["rho"], ic["stars"], ic["kinds"], ic["jets"], ic["jkinds"],
-                            ic["P"], mom=ic["mom"], rays=(64, 128), fuv_grid=(16, 16, 32), ion_every=ion_every)
+                            ic["P"], mom=ic["mom"], rays=(64, 128), fuv_grid=(16, 16, 32), ion_every=ion_every,
+                            arith=arith)
 
 
 def state(s):
@@ -47,19 +48,20 @@ def same(a, b):
     assert a[6:] == b[6:]
 
 
+@pytest.mark.parametrize("arith", ("exact", "fast"))
 @pytest.mark.parametrize("cadence,graphs", (("lockstep", True), ("lockstep", False), ("mixed", True)))
-def test_batch_bit_identical_to_alone(nb, cadence, graphs):
+def test_batch_bit_identical_to_alone(nb, cadence, graphs, arith):
     batch, ics, S = nb
     ics_list = scenes(ics)
     ie = [None] * 4 if cadence == "lockstep" else [2, 3, 5, 1]
     steps = 7
     alone = []
     for ic, e in zip(ics_list, ie):
-        s = make(S, ic, e)
+        s = make(S, ic, e, arith)
         s.step(steps)
         alone.append(state(s))
         s.close()
-    sims = [make(S, ic, e) for ic, e in zip(ics_list, ie)]
+    sims = [make(S, ic, e, arith) for ic, e in zip(ics_list, ie)]
     B = batch.BatchSim(sims, graphs=graphs)
     B.step(3)
     B.step(steps - 3)

@@ -3,6 +3,10 @@
   * the CPU oracle on seeded inputs,
   * size-independent properties at the benchmark size (256^3).
 
+Both library builds are tested: "exact" (libnebula.so) where the assertions are bit for bit,
+"exact" and "fast" (libnebula_fast.so: FMA, approximate division / square root) wherever the
+path's tolerances apply.
+
 Tolerances (stated by the specification of this path):
   hydro stage        bit-identical to the reference kernels (no fused multiply-add, IEEE
                      division / sqrt, the reference's operation order);
@@ -21,6 +25,7 @@ from conftest import bits_equal, golden_sim, rel_linf
 
 torch = pytest.importorskip("torch")
 pytestmark = pytest.mark.gpu
+ARITH = ("exact", "fast")
 
 
 @pytest.fixture(scope="module")
@@ -37,7 +42,7 @@ def t32(a):
 
 
 def kernel_sim(nb, d, P_extra=None, rays=(6, 12), fuv=(5, 4, 8), fast=True, rho=None, stars=None, kinds=None,
-               jets=None, jkinds=None):
+               jets=None, jkinds=None, arith="exact"):
     _lib, S = nb
     dx = float(d["k_scalars"][0])
     rho = d["k_rho"] if rho is None else rho
@@ -51,7 +56,7 @@ def kernel_sim(nb, d, P_extra=None, rays=(6, 12), fuv=(5, 4, 8), fast=True, rho=
         jets = [tuple(float(v) for v in j[:3]) for j in kj]
         jkinds = ["jet", "none", "proto"]
     return S.Sim.from_state(rho.shape, dx, rho, stars, kinds, jets, jkinds, P, mom=None, rays=rays, fuv_grid=fuv,
-                            fast=fast, start_main=False)
+                            fast=fast, start_main=False, arith=arith)
 
 
 HYDRO = (("rus", "rusanov", "minmod"), ("hll0", "hll", "minmod"), ("hll1", "hll", "vanleer"), ("hll2", "hll", "mc"))
@@ -94,13 +99,14 @@ def test_max_speed_matches_reference(nb, kernels_npz):
     sim.close()
 
 
+@pytest.mark.parametrize("arith", ARITH)
 @pytest.mark.parametrize("tag,fast", (("full", True), ("half", False)))
-def test_ionize_matches_reference_kernels(nb, kernels_npz, tag, fast):
+def test_ionize_matches_reference_kernels(nb, kernels_npz, tag, fast, arith):
     d = kernels_npz
     rs = d["r_stars"]
     stars = [(float(s[0]), float(s[1]), float(s[2]), float(s[3]), 0.0) for s in rs]
     sim = kernel_sim(nb, d, dict(q_main=0.1, wind=0.0), rho=d["r_rho"], fast=fast, stars=stars, kinds=["abs"] * 3,
-                     jets=[(0.0, 0.0, 1.0)] * 3, jkinds=["none"] * 3)
+                     jets=[(0.0, 0.0, 1.0)] * 3, jkinds=["none"] * 3, arith=arith)
     _lib = nb[0]
     # the ray kernel alone, one star at a time
     rf = torch.zeros((6, 12), device="cuda")
@@ -115,7 +121,11 @@ def test_ionize_matches_reference_kernels(nb, kernels_npz, tag, fast):
     assert np.mean((xi > 0.5) != (d[f"r_{tag}_xi"] > 0.5)) <= 1e-3
     df = sim.dfront.numpy().astype(np.float32)
     ref = d[f"r_{tag}_df"].astype(np.float16).astype(np.float32)
-    assert np.all(np.abs(df - ref) <= 2 * np.abs(ref) * 2.0 ** -10 + 1e-6)
+    # exact: 2 fp16 ulps; fast: plus rel-L_inf 1e-5 of the finite dfront values (the approximate
+    # square root moves r - rf by a few 1e-6 at cells on the front, where dfront is near 0)
+    fin = np.abs(ref[ref < 500.0]).max()
+    slack = 1e-6 if arith == "exact" else 1e-5 * fin
+    assert np.all(np.abs(df - ref) <= 2 * np.abs(ref) * 2.0 ** -10 + slack)
     if tag == "full":
         sim.fuv_field()
         torch.cuda.synchronize()
@@ -131,13 +141,14 @@ def test_ionize_matches_reference_kernels(nb, kernels_npz, tag, fast):
     sim.close()
 
 
+@pytest.mark.parametrize("arith", ARITH)
 @pytest.mark.parametrize("name", ("bubbles", "bipolar", "cliff"))
-def test_sim_matches_reference_sim_end_to_end(nb, name):
+def test_sim_matches_reference_sim_end_to_end(nb, name, arith):
     """the drop-in Sim against the reference Sim run by its own driver code"""
     d, m = golden_sim(name)
     _, S = nb
     sim = S.Sim.from_state(m["shape"], m["dx"], d["s0_rho"], m["stars"], m["kinds"], m["jets"], m["jkinds"], m["P"],
-                           rays=m["rays"], fuv_grid=m["fuv"], ion_every=m["ion_every"], fast=m["fast"])
+                           rays=m["rays"], fuv_grid=m["fuv"], ion_every=m["ion_every"], fast=m["fast"], arith=arith)
     torch.cuda.synchronize()
     assert np.abs(sim.xi.numpy() - d["s0_xi"]).max() < 1e-4
     n = 1
@@ -156,13 +167,13 @@ def test_sim_matches_reference_sim_end_to_end(nb, name):
     sim.close()
 
 
-def _oracle_pair(nb, scenario, res, rays=(128, 256), fuv=(32, 32, 64), **kw):
+def _oracle_pair(nb, scenario, res, rays=(128, 256), fuv=(32, 32, 64), arith="exact", **kw):
     import oracle as O
     from nebulaviewer_gb300 import ics
     _, S = nb
     ic = ics.SCENARIOS[scenario](res=res, **kw)
     g = S.Sim.from_state(ic["shape"], ic["dx"], ic["rho"], ic["stars"], ic["kinds"], ic["jets"], ic["jkinds"],
-                         ic["P"], mom=ic["mom"], rays=rays, fuv_grid=fuv)
+                         ic["P"], mom=ic["mom"], rays=rays, fuv_grid=fuv, arith=arith)
     from nebulaviewer_gb300.params import make_params, sound_speeds
     P = make_params(base=ic["P"])
     cn2, ci2, vmax = sound_speeds(P)
@@ -180,9 +191,10 @@ def _compare(g, o, tol_state, tol_xi=1e-4):
     assert np.mean((x > 0.5) != (o.xi > 0.5)) <= 1e-3
 
 
-def test_torus_against_oracle_100_steps(nb):
+@pytest.mark.parametrize("arith", ARITH)
+def test_torus_against_oracle_100_steps(nb, arith):
     """the plain-step workload (torus, one central star, HLL + minmod, RK2, CFL 0.3) at 32^3"""
-    g, o = _oracle_pair(nb, "torus", 16)
+    g, o = _oracle_pair(nb, "torus", 16, arith=arith)
     _compare(g, o, 1e-6)
     for n in range(100):
         g.step(1)
@@ -194,9 +206,10 @@ def test_torus_against_oracle_100_steps(nb):
     g.close()
 
 
-def test_sheet_against_oracle(nb):
+@pytest.mark.parametrize("arith", ARITH)
+def test_sheet_against_oracle(nb, arith):
     """the turbulent-sheet workload (6 stars, wind, Mach 5) at 48^3 for 12 steps, FUV at the end"""
-    g, o = _oracle_pair(nb, "sheet", 48, shape=(48, 48, 48))
+    g, o = _oracle_pair(nb, "sheet", 48, shape=(48, 48, 48), arith=arith)
     for n in range(12):
         g.step(1)
         o.step(1)
@@ -207,12 +220,13 @@ def test_sheet_against_oracle(nb):
     g.close()
 
 
-def test_uniform_rest_state_stays_exactly_at_rest_256(nb):
+@pytest.mark.parametrize("arith", ARITH)
+def test_uniform_rest_state_stays_exactly_at_rest_256(nb, arith):
     """size-independent property at the benchmark size: a uniform gas at rest, no stars"""
     _, S = nb
     n = 256
     rho = torch.full((n, n, n), 3.0, device="cuda")
-    sim = S.Sim.from_state((n, n, n), 1.0 / n, rho, [], [], [], [], dict(cn2=1.0, ci2=144.0, vmax=72.0))
+    sim = S.Sim.from_state((n, n, n), 1.0 / n, rho, [], [], [], [], dict(cn2=1.0, ci2=144.0, vmax=72.0), arith=arith)
     sim.step(4)
     assert torch.all(sim._rho == 3.0) and torch.all(sim._mx == 0) and torch.all(sim._my == 0)
     assert torch.all(sim._mz == 0) and torch.all(sim._xi == 0)
@@ -220,7 +234,8 @@ def test_uniform_rest_state_stays_exactly_at_rest_256(nb):
     sim.close()
 
 
-def test_stromgren_radius_uniform_gas(nb):
+@pytest.mark.parametrize("arith", ARITH)
+def test_stromgren_radius_uniform_gas(nb, arith):
     """known answer: the front radius in uniform density n is (3Q/n^2)^(1/3) within a ray step"""
     _, S = nb
     n = 128
@@ -229,7 +244,7 @@ def test_stromgren_radius_uniform_gas(nb):
     Q = 4.0 * 0.2 ** 3 / 3.0                             # R = 0.2 at n = 2
     star = (0.5, 0.5, 0.5, 1.0, 0.0)
     sim = S.Sim.from_state((n, n, n), 1.0 / n, rho, [star], ["main"], [(0, 0, 1.0)], ["none"],
-                           dict(q_main=Q, q_ramp=0.0), rays=(64, 128), start_main=False)
+                           dict(q_main=Q, q_ramp=0.0), rays=(64, 128), start_main=False, arith=arith)
     rf = torch.zeros((64, 128), device="cuda")
     xyz = (C.c_double * 3)(0.5, 0.5, 0.5)
     nb[0].check(sim._lib.nb_cast_rays(sim._h, xyz, Q, C.c_void_p(rf.data_ptr())), sim._h, "rays")
@@ -240,12 +255,13 @@ def test_stromgren_radius_uniform_gas(nb):
     sim.close()
 
 
-def test_sheet_256_deterministic_and_conserving(nb):
+@pytest.mark.parametrize("arith", ARITH)
+def test_sheet_256_deterministic_and_conserving(nb, arith):
     """benchmark size: two runs give identical bits; FP64 totals move only by boundary flux"""
     _, S = nb
     runs = []
     for _ in range(2):
-        sim = S.Sim("sheet", res=256, verbose=False)
+        sim = S.Sim("sheet", res=256, verbose=False, arith=arith)
         m0 = sim.conservation()
         sim.step(6)
         m1 = sim.conservation()
@@ -257,11 +273,12 @@ def test_sheet_256_deterministic_and_conserving(nb):
     assert abs(a[4][0] - a[3][0]) / a[3][0] < 5e-3
 
 
-def test_cliffwall_plane_source_against_oracle(nb):
+@pytest.mark.parametrize("arith", ARITH)
+def test_cliffwall_plane_source_against_oracle(nb, arith):
     """the ionized cloud wall: a density step with clumps, 3 stars and the -x plane-parallel
     source (no reference counterpart: checked against the oracle's FP32 and FP64 restatement)"""
     import oracle as O
-    g, o = _oracle_pair(nb, "cliffwall", 64, rays=(128, 256), fuv=(32, 32, 64), nclumps=8)
+    g, o = _oracle_pair(nb, "cliffwall", 64, rays=(128, 256), fuv=(32, 32, 64), nclumps=8, arith=arith)
     from nebulaviewer_gb300 import ics
     from nebulaviewer_gb300.params import make_params, sound_speeds
     ic = ics.cliffwall(res=64, nclumps=8)

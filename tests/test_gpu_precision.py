@@ -17,7 +17,8 @@ def rel_l2(a, b):
     return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
 
 
-def test_fp32_error_against_fp64_rerun_torus64():
+@pytest.mark.parametrize("arith", ("exact", "fast"))
+def test_fp32_error_against_fp64_rerun_torus64(arith):
     import oracle as O
     from nebulaviewer_gb300 import build, ics
     from nebulaviewer_gb300.params import make_params, sound_speeds
@@ -32,7 +33,7 @@ def test_fp32_error_against_fp64_rerun_torus64():
     o64 = O.OracleSim(*args, dtype=np.float64, **kw)
     o32 = O.OracleSim(*args, dtype=np.float32, **kw)
     g = Sim.from_state(ic["shape"], ic["dx"], ic["rho"], ic["stars"], ic["kinds"], ic["jets"], ic["jkinds"], ic["P"],
-                       rays=rays, fuv_grid=fuv)
+                       rays=rays, fuv_grid=fuv, arith=arith)
     steps = 100
     o64.step(steps)
     o32.step(steps)
@@ -43,7 +44,7 @@ def test_fp32_error_against_fp64_rerun_torus64():
         gv = getattr(g, k).numpy()
         cv = getattr(o32, k)
         rows.append((k, rel_linf(gv, ref), rel_l2(gv, ref), rel_linf(cv, ref), rel_l2(cv, ref)))
-    print("\nfield  gpu32-vs-fp64 Linf  L2   | cpu32-vs-fp64 Linf  L2   (torus 64^3, 100 steps)")
+    print(f"\nfield  gpu32-vs-fp64 Linf  L2   | cpu32-vs-fp64 Linf  L2   (torus 64^3, 100 steps, {arith})")
     for r in rows:
         print(f"{r[0]:5s}  {r[1]:.3e}  {r[2]:.3e}  |  {r[3]:.3e}  {r[4]:.3e}")
     print(f"t: gpu {g.t!r} fp64 {o64.t!r} cpu32 {o32.t!r}")
