@@ -467,6 +467,60 @@ def run_served(args):
     return 0
 
 
+def run_stirred(args):
+    """The stirring phase at 256^3 (torus_stirred: log-normal background, solenoidal forcing on the
+    1/24-unit grid cross-faded every pre_corr): hydro without sources + the drive kernel with the
+    fused CFL max speed, forcing fields pushed ahead into the device ring (host syncs once per
+    ring-sized chunk).  pre_t is raised so the timed steps all stay in the stirring phase."""
+    import ctypes as C
+    import torch
+    from nebulaviewer_gb300 import _lib, build as nb_build
+    nb_build.build(verbose=False)
+    from nebulaviewer_gb300.sim import Sim
+    dev = torch.device("cuda", 0)
+    res = (args.res if args.res != RES else 256) // 2
+    sim = Sim("torus_stirred", res=res, device=dev, verbose=False, arith=args.arith, params=dict(pre_t=1e9))
+    lib = sim._lib
+    sim.step(args.warmup)
+    torch.cuda.synchronize(dev)
+    lib.nb_profile(sim._h, 1)
+    prof_ms, prof_n = (C.c_double * 16)(), (C.c_longlong * 16)()
+    lib.nb_profile_read(sim._h, prof_ms, prof_n)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(0) as clk:
+        ev0.record()
+        sim.step(args.steps, sync=False)
+        ev1.record()
+        torch.cuda.synchronize(dev)
+    el = ev0.elapsed_time(ev1)
+    lib.nb_profile_read(sim._h, prof_ms, prof_n)
+    lib.nb_profile(sim._h, 0)
+    cells = sim._n
+    val = cells * args.steps / (el * 1e-3) / 1e9
+    peak, peak_kind = measured_peaks()
+    kinds = {name: (prof_ms[i], int(prof_n[i])) for i, name in enumerate(_lib.PROF_KINDS) if prof_n[i]}
+    d_ms, d_n = kinds.get("drive", (0.0, 0))
+    drive_gbs = 32.0 * cells / (d_ms / max(d_n, 1) * 1e-3) / 1e9 if d_n else None
+    b_step = 36.0 + 52.0 + 32.0                     # stage 1, stage 2, drive (+ max speed)
+    res_d = {"metric": METRIC + " stirring phase", "value": val, "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+             "warmup": args.warmup, "ms_per_step": el / args.steps, "higher_is_better": True, "dtype": "f32",
+             "data": "synthetic",
+             "config": {"workload": f"torus_stirred {list(sim.shape)} stirring phase: forcing grid "
+                                    f"{list(sim.sshape)} (dxs {sim.dxs:.4g}), pre_corr {sim.P['pre_corr']}, "
+                                    f"pre_amp {sim.P['pre_amp']}", "grid": list(sim.shape)},
+             "roofline": {"bound": "hbm", "kernel": "drive", "achieved": drive_gbs, "peak": peak, "unit": "GB/s",
+                          "frac": drive_gbs / peak if drive_gbs else None, "peak_source": peak_kind,
+                          "algorithmic_bytes_per_launch": 32 * cells,
+                          "avg_launch_ms": d_ms / max(d_n, 1)},
+             "step_roofline": {"bytes_per_cell_step": b_step, "achieved": b_step * val, "peak": peak, "unit": "GB/s",
+                               "frac": b_step * val / peak, "peak_source": peak_kind},
+             "kernels_ms": {k: {"ms_total": v[0], "launches": v[1]} for k, v in kinds.items()},
+             "clocks": clk.summary(), "arith": sim.arith}
+    sim.close()
+    print(json.dumps(res_d), flush=True)
+    return 0
+
+
 def run_cliff(args):
     """The large single instance: the 1024^3 ionized cloud wall (density step n = 1 -> 200, 40
     clumps, the -x plane-parallel source + 3 stars, FUV on), FP64 conservation totals."""
@@ -522,7 +576,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--res", type=int, default=RES, help="grid size (the workload is defined at 256)")
-    ap.add_argument("--workload", default="sheet256", choices=["sheet256", "batch32", "served", "cliff1024"])
+    ap.add_argument("--workload", default="sheet256",
+                    choices=["sheet256", "batch32", "served", "cliff1024", "stirred256"])
     ap.add_argument("--requests", type=int, default=100)
     ap.add_argument("--rate", type=float, default=200.0)
     ap.add_argument("--instances", type=int, default=32)
@@ -538,6 +593,8 @@ def main():
         return run_batch(args)
     if args.workload == "served":
         return run_served(args)
+    if args.workload == "stirred256":
+        return run_stirred(args)
     if args.workload == "cliff1024":
         return run_cliff(args)
     return run_gb300(args)

@@ -225,7 +225,7 @@ int hydro_and_stir(nb_instance* h, bool stir, bool no_sources) {
     if (stir) {
         Prof pf(h, NB_PROF_DRIVE, 2);
         CK(h, nb_launch_drive(h->c, h->st, f.rho, f.mx, f.my, f.mz, f.xi, &h->st->smax_bits, h->d.nx, h->d.ny,
-                              h->stream));
+                              h->hc.drive_sz, h->stream));
     }
     h->smax_valid = 1;
     return NB_OK;
@@ -596,7 +596,7 @@ NB_EXPORT int nb_drive_step(nb_handle h, const float* fa, const float* fb, float
     const nb_fields& f = h->d.f;
     Prof pf(h, NB_PROF_DRIVE, 1);
     CK(h, nb_launch_drive_explicit(h->c, f.rho, f.mx, f.my, f.mz, fa, fb, blend, amp, dt, h->d.nx, h->d.ny,
-                                   h->stream));
+                                   h->hc.drive_sz, h->stream));
     return NB_OK;
 }
 

@@ -196,10 +196,10 @@ cudaError_t nb_launch_weights(const NbConst* c, const NbState* st, const NbStarD
 cudaError_t nb_launch_max_speed(const NbConst* c, const float* rho, const float* mx, const float* my,
                                 const float* mz, const float* xi, unsigned* smax_bits, long n, cudaStream_t s);
 cudaError_t nb_launch_drive(const NbConst* c, const NbState* st, const float* rho, float* mx, float* my, float* mz,
-                            const float* xi, unsigned* smax_bits, int nx, int ny, cudaStream_t s);
+                            const float* xi, unsigned* smax_bits, int nx, int ny, int sz, cudaStream_t s);
 cudaError_t nb_launch_drive_explicit(const NbConst* c, const float* rho, float* mx, float* my, float* mz,
                                      const float* fa, const float* fb, float blend, float amp, float dt, int nx,
-                                     int ny, cudaStream_t s);
+                                     int ny, int sz, cudaStream_t s);
 cudaError_t nb_launch_add_torus(const float* torus, float* rho, float* mx, float* my, float* mz, long long n,
                                 cudaStream_t s);
 int nb_mach_scratch_doubles();

@@ -7,6 +7,13 @@
 //    the step's control kernel wrote, so a stirred step needs no host round trip.  The CFL max
 //    speed of the stirred state (nebula3d.py:154-162, what the next step's _compute_dt reads) is
 //    folded into the same pass: stage 2 then skips its own.
+//    The trilinear sample interpolates along x, then y, then z (sample_n's order).  Along one
+//    (i, j) row of cells the x and y weights and corner indices are the same for every cell, so
+//    the x-then-y interpolated value at each coarse z level is a property of the row: a warp
+//    (one row) evaluates it once per level and field into shared memory, and each cell then
+//    does only the z interpolation between its two levels -- the same float operations on the
+//    same operands as the direct form, so the same bits, with 12 shared loads per cell instead
+//    of 48 gathers.
 //  * add_torus (sim.py:352-363): the dense torus joins the turbulent envelope at the start of
 //    the main phase (sim.py:806-812).
 //  * mach_sums (sim.py:501-508): sum |m|^2 / rho and sum rho, here in FP64 with a fixed
@@ -50,6 +57,18 @@ __device__ __forceinline__ float trilerp(const float* __restrict__ g, int sy, in
     return c0 + (c1 - c0) * Z.f;
 }
 
+// x-then-y interpolated value of one coarse z level of one field (the c0 / c1 of sample_n)
+__device__ __forceinline__ float xy_level(const float* __restrict__ g, int sy, int sz, const Axis& X, const Axis& Y,
+                                          int kz) {
+    const float* pa = g + (long long)X.a * sy * sz;
+    const float* pb = g + (long long)X.b * sy * sz;
+    const float c_a = __ldg(pa + Y.a * sz + kz), c_b = __ldg(pb + Y.a * sz + kz);
+    const float d_a = __ldg(pa + Y.b * sz + kz), d_b = __ldg(pb + Y.b * sz + kz);
+    const float cx = c_a + (c_b - c_a) * X.f;
+    const float dxv = d_a + (d_b - d_a) * X.f;
+    return cx + (dxv - cx) * Y.f;
+}
+
 __device__ __forceinline__ void block_max_to(float m, unsigned* dst) {
     for (int o = 16; o > 0; o >>= 1) m = fmaxr(m, __shfl_xor_sync(0xffffffffu, m, o));
     __shared__ float red[32];
@@ -64,8 +83,11 @@ __device__ __forceinline__ void block_max_to(float m, unsigned* dst) {
     }
 }
 
-// One thread per row (i, j), cells k = lane + 32 m (RowWalk).  With `explicit_args` the
+// One warp per row (i, j), cells k = lane + 32 m (RowWalk).  With `explicit_args` the
 // blend / amp / dt / fields come from the arguments (the single-kernel parity entry point).
+// STAGED: the per-row x-y levels in shared memory (6 fields x sz floats per warp); otherwise
+// every cell gathers its 48 corners (forcing grids too tall for shared memory).
+template <bool STAGED>
 __global__ void __launch_bounds__(256) drive_kernel(const NbConst* __restrict__ c, const NbState* __restrict__ st,
                                                     const float* __restrict__ rho, float* __restrict__ mx,
                                                     float* __restrict__ my, float* __restrict__ mz,
@@ -73,6 +95,7 @@ __global__ void __launch_bounds__(256) drive_kernel(const NbConst* __restrict__ 
                                                     const float* __restrict__ fa_arg,
                                                     const float* __restrict__ fb_arg, float blend_arg,
                                                     float amp_arg, float dt_arg, int explicit_args) {
+    extern __shared__ float levels[];                       // [warp][6][sz] when STAGED
     const NbConst& C = *c;
     const RowWalk w(C.nx, C.ny, C.nz);
     float vm = 0.0f;
@@ -96,6 +119,15 @@ __global__ void __launch_bounds__(256) drive_kernel(const NbConst* __restrict__ 
         const float wa = 1.0f - blend;
         const Axis X(((float)w.i + 0.5f) * dx, dxs, sx);
         const Axis Y(((float)w.j + 0.5f) * dx, dxs, sy);
+        float* lv = levels + threadIdx.y * 6 * sz;
+        if (STAGED && go && !(X.out || Y.out)) {
+            for (int t = threadIdx.x; t < 6 * sz; t += 32) {
+                const int f = t / sz, kz = t - f * sz;
+                const float* g = (f < 3 ? fa : fb) + (long long)(f < 3 ? f : f - 3) * S;
+                lv[t] = xy_level(g, sy, sz, X, Y, kz);
+            }
+        }
+        if (STAGED) __syncwarp();
         for (int k = w.k0; k < C.nz; k += 32) {
             const long long q = w.base + k;
             const float r = rho[q];
@@ -104,12 +136,21 @@ __global__ void __launch_bounds__(256) drive_kernel(const NbConst* __restrict__ 
                 const Axis Z(((float)k + 0.5f) * dx, dxs, sz);
                 float a0 = 0.0f, a1 = 0.0f, a2 = 0.0f, b0 = 0.0f, b1 = 0.0f, b2 = 0.0f;
                 if (!(X.out || Y.out || Z.out)) {
-                    a0 = trilerp(fa, sy, sz, X, Y, Z);
-                    a1 = trilerp(fa + S, sy, sz, X, Y, Z);
-                    a2 = trilerp(fa + 2 * S, sy, sz, X, Y, Z);
-                    b0 = trilerp(fb, sy, sz, X, Y, Z);
-                    b1 = trilerp(fb + S, sy, sz, X, Y, Z);
-                    b2 = trilerp(fb + 2 * S, sy, sz, X, Y, Z);
+                    if (STAGED) {
+                        auto zl = [&](int f) {
+                            const float c0 = lv[f * sz + Z.a], c1 = lv[f * sz + Z.b];
+                            return c0 + (c1 - c0) * Z.f;
+                        };
+                        a0 = zl(0); a1 = zl(1); a2 = zl(2);
+                        b0 = zl(3); b1 = zl(4); b2 = zl(5);
+                    } else {
+                        a0 = trilerp(fa, sy, sz, X, Y, Z);
+                        a1 = trilerp(fa + S, sy, sz, X, Y, Z);
+                        a2 = trilerp(fa + 2 * S, sy, sz, X, Y, Z);
+                        b0 = trilerp(fb, sy, sz, X, Y, Z);
+                        b1 = trilerp(fb + S, sy, sz, X, Y, Z);
+                        b2 = trilerp(fb + 2 * S, sy, sz, X, Y, Z);
+                    }
                 }
                 const float f0 = wa * a0 + blend * b0, f1 = wa * a1 + blend * b1, f2 = wa * a2 + blend * b2;
                 const float s = r * amp * dt;
@@ -190,20 +231,39 @@ int grid_n(long long n) {
 
 }  // namespace
 
-cudaError_t nb_launch_drive(const NbConst* c, const NbState* st, const float* rho, float* mx, float* my, float* mz,
-                            const float* xi, unsigned* smax_bits, int nx, int ny, cudaStream_t s) {
-    if (smax_bits) cudaMemsetAsync(smax_bits, 0, sizeof(unsigned), s);
-    drive_kernel<<<rowwalk_blocks(nx, ny), dim3(32, 8), 0, s>>>(c, st, rho, mx, my, mz, xi, smax_bits, nullptr,
-                                                                nullptr, 0.f, 0.f, 0.f, 0);
+namespace {
+constexpr int DRIVE_STAGED_MAX_SZ = 1024;           // 8 warps x 6 x 1024 floats = 192 KiB of shared memory
+
+cudaError_t launch_drive(const NbConst* c, const NbState* st, const float* rho, float* mx, float* my, float* mz,
+                         const float* xi, unsigned* smax_bits, const float* fa, const float* fb, float blend, float amp,
+                         float dt, int explicit_args, int nx, int ny, int sz, cudaStream_t s) {
+    const dim3 grid(rowwalk_blocks(nx, ny)), block(32, 8);
+    if (sz <= DRIVE_STAGED_MAX_SZ) {
+        const int smem = 8 * 6 * sz * (int)sizeof(float);
+        if (smem > 48 * 1024) {
+            cudaError_t e = cudaFuncSetAttribute(drive_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+            if (e != cudaSuccess) return e;
+        }
+        drive_kernel<true><<<grid, block, smem, s>>>(c, st, rho, mx, my, mz, xi, smax_bits, fa, fb, blend, amp, dt,
+                                                     explicit_args);
+    } else {
+        drive_kernel<false><<<grid, block, 0, s>>>(c, st, rho, mx, my, mz, xi, smax_bits, fa, fb, blend, amp, dt,
+                                                   explicit_args);
+    }
     return cudaGetLastError();
+}
+}  // namespace
+
+cudaError_t nb_launch_drive(const NbConst* c, const NbState* st, const float* rho, float* mx, float* my, float* mz,
+                            const float* xi, unsigned* smax_bits, int nx, int ny, int sz, cudaStream_t s) {
+    if (smax_bits) cudaMemsetAsync(smax_bits, 0, sizeof(unsigned), s);
+    return launch_drive(c, st, rho, mx, my, mz, xi, smax_bits, nullptr, nullptr, 0.f, 0.f, 0.f, 0, nx, ny, sz, s);
 }
 
 cudaError_t nb_launch_drive_explicit(const NbConst* c, const float* rho, float* mx, float* my, float* mz,
                                      const float* fa, const float* fb, float blend, float amp, float dt, int nx,
-                                     int ny, cudaStream_t s) {
-    drive_kernel<<<rowwalk_blocks(nx, ny), dim3(32, 8), 0, s>>>(c, nullptr, rho, mx, my, mz, nullptr, nullptr, fa, fb,
-                                                                blend, amp, dt, 1);
-    return cudaGetLastError();
+                                     int ny, int sz, cudaStream_t s) {
+    return launch_drive(c, nullptr, rho, mx, my, mz, nullptr, nullptr, fa, fb, blend, amp, dt, 1, nx, ny, sz, s);
 }
 
 cudaError_t nb_launch_add_torus(const float* torus, float* rho, float* mx, float* my, float* mz, long long n,

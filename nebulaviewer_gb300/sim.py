@@ -34,6 +34,7 @@ from . import stir as _stir
 from .params import LIVE, make_params, sound_speeds
 
 DRIVE_SLOTS = 16          # forcing fields the device ring holds
+DRIVE_LOOKAHEAD = 2       # fields pushed beyond B before a chunk of stirred steps
 
 
 class Field:
@@ -181,7 +182,8 @@ class Sim:
         torus = ic.get("torus")
         self.torus = None
         if torus is not None:                                                       # sim.py:669-671, 737
-            torus = torch.as_tensor(np.asarray(torus, np.float32)).to(**f32).contiguous()
+            torus = (torus if torch.is_tensor(torus) else torch.as_tensor(np.asarray(torus, np.float32)))
+            torus = torus.to(**f32).contiguous()
             if pre:
                 self.torus = torus
             else:
@@ -265,7 +267,8 @@ class Sim:
             grid = _stir.forcing_grid(self.L, self.dx, self.shape, physical=self.ic_mode != "nebula3d")
         self.sshape, self.dxs = tuple(int(v) for v in grid[0]), float(grid[1])
         self._drv_on = False
-        self._forcing = []              # (field, Generator state before it) per field pushed since the ring reset
+        self._forcing = []              # (field, Generator state before it) per field drawn since the ring reset
+        self._pushed = 0                # of which pushed into the device ring
         self.phase = "pre" if pre else "main"
         self._push(force=True)
         if pre:
@@ -473,26 +476,28 @@ class Sim:
         return self._drv_on and float(self.P.get("drive_main", 0.0) or 0.0) > 0.0
 
     def _main_chunk(self, left):
-        """main-phase steps (sim.py:1099-1114); stirred steps in ring-sized chunks"""
-        n = left
-        if self._stirring():
-            info = self._drive_info()
-            n = min(left, self._ring_steps())
-            self._drive_fill(info.swaps + 2 + self._max_swaps(n))
+        """main-phase steps (sim.py:1099-1114); stirred steps in chunks the pushed fields cover"""
+        if not self._stirring():
+            self._chk(self._lib.nb_step(self._h, int(left), int(self.ion_every)), "nb_step")
+            self._it += left
+            return left
+        info = self._drive_ready()
+        n = min(left, self._drive_steps())
         self._chk(self._lib.nb_step(self._h, int(n), int(self.ion_every)), "nb_step")
         self._it += n
+        self._drive_ahead(info)
         return n
 
     def _pre_chunk(self, left):
         """stirring-phase steps (sim.py:1044-1059): as many as provably cannot reach pre_t but
-        the last, then the end-of-phase test"""
+        the last (and whose field swaps the pushed fields cover), then the end-of-phase test"""
         c = self._clock()
         gap = float(self.P["pre_t"]) - c.tp
         n_end = max(1, math.ceil(gap / self._dt_bound())) if gap > 0.0 else 1
-        info = self._drive_info()
-        n = min(left, n_end, self._ring_steps())
-        self._drive_fill(info.swaps + 2 + self._max_swaps(n))
+        info = self._drive_ready()
+        n = min(left, n_end, self._drive_steps())
         self._chk(self._lib.nb_pre_step(self._h, int(n)), "nb_pre_step")
+        self._drive_ahead(info)
         if n == n_end and self._clock().tp >= float(self.P["pre_t"]):
             self._end_pre()
         return n
@@ -504,16 +509,22 @@ class Sim:
         c = min(float(np.sqrt(np.float32(self.cn2))), float(np.sqrt(np.float32(self.ci2))))
         return float(self.P["cfl"]) * self.dx / c * (1.0 + 1e-6)
 
-    def _max_swaps(self, n):
-        """most field swaps n steps can make: the first may come at once, each next one needs
-        at least ceil(pre_corr / dt_max) steps"""
+    def _drive_steps(self):
+        """steps a chunk may take with DRIVE_LOOKAHEAD fields pushed beyond B: n steps make at
+        most 1 + (n - 1) // m field swaps (the first may come at once, each next one needs at
+        least m = ceil(pre_corr / dt_max) steps)"""
         m = max(1, math.ceil(float(self.P["pre_corr"]) / self._dt_bound()))
-        return 1 + (n - 1) // m if n > 0 else 0
+        return (DRIVE_LOOKAHEAD - 1) * m + 1
 
-    def _ring_steps(self):
-        """steps whose swaps fit the ring: A and B stay, DRIVE_SLOTS - 2 fields ahead"""
-        m = max(1, math.ceil(float(self.P["pre_corr"]) / self._dt_bound()))
-        return (DRIVE_SLOTS - 3) * m + 1
+    def _drive_ready(self):
+        """the device's swap count (synchronizes) and the fields a chunk may need pushed"""
+        info = self._drive_info()
+        self._drive_fill(int(info.swaps) + 2 + DRIVE_LOOKAHEAD)
+        return info
+
+    def _drive_ahead(self, info):
+        """draw the next fields on the host while the GPU runs the chunk just launched"""
+        self._drive_make(int(info.swaps) + 2 + 2 * DRIVE_LOOKAHEAD)
 
     def _drive_info(self):
         info = _lib.NbDriveInfo()
@@ -531,20 +542,23 @@ class Sim:
         return np.ascontiguousarray(np.stack(_stir.solenoidal(self.sshape, self.rng, 1.0,
                                                               float(self.P["pre_kmax"]))), np.float32)
 
-    def _drive_fill(self, upto):
-        """push forcing fields until `upto` fields were pushed since the ring reset (a given, finite
-        list of fields is pushed as far as it goes: a step that finds no field B raises)"""
-        new = []
+    def _drive_make(self, upto):
+        """draw forcing fields on the host until `upto` exist since the ring reset (a given, finite
+        list of fields goes as far as it goes: a step that then finds no field B raises)"""
         while len(self._forcing) < upto:
             if self._stir_src is not None and not self._stir_src:
                 break
             st = copy.deepcopy(self.rng.bit_generator.state)
-            f = self._mkF()
-            self._forcing.append((f, st))
-            new.append(f)
+            self._forcing.append((self._mkF(), st))
+
+    def _drive_fill(self, upto):
+        """push forcing fields until `upto` fields were pushed since the ring reset"""
+        self._drive_make(upto)
+        new = [f for f, _ in self._forcing[self._pushed:upto]]
         if new:
             buf = np.ascontiguousarray(np.stack(new))
             self._chk(self._lib.nb_drive_push(self._h, C.c_void_p(buf.ctypes.data), len(new)), "nb_drive_push")
+            self._pushed += len(new)
 
     def _drive_new(self, clock, fields=None):
         """a fresh cross-fade (sim.py:788, 1160-1161): reset the ring, push A and B"""
@@ -553,10 +567,12 @@ class Sim:
                              float(self.P["pre_corr"]), float(clock))
         self._chk(self._lib.nb_drive_config(self._h, C.byref(d)), "nb_drive_config")
         self._forcing = []
+        self._pushed = 0
         if fields is not None:
             buf = np.ascontiguousarray(np.stack([np.asarray(f, np.float32) for f in fields]))
             self._forcing = [(f, None) for f in buf]
             self._chk(self._lib.nb_drive_push(self._h, C.c_void_p(buf.ctypes.data), len(buf)), "nb_drive_push")
+            self._pushed = len(buf)
         else:
             self._drive_fill(2)
         self._drv_on = True
@@ -576,12 +592,14 @@ class Sim:
             elif extra[0][1] is not None:
                 self.rng.bit_generator.state = extra[0][1]
         self._forcing = self._forcing[:used]
+        self._pushed = min(self._pushed, used)
 
     def _drive_drop(self):
         """drv = None (sim.py:1057-1058)"""
         self._drive_rewind()
         self._drv_on = False
         self._forcing = []
+        self._pushed = 0
         self._chk(self._lib.nb_drive_enable(self._h, 0), "nb_drive_enable")
 
     @property
