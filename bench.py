@@ -10,10 +10,20 @@ photon rates, winds on, ionization every 3 steps with 512 x 1024 rays (dr = dx),
 16 steps on a 160 x 160 x 320 grid -- the reference Sim's fast-mode budgets for this grid
 (sim.py:753-759).  HLL + minmod, RK2, CFL 0.3, cs_n = 1, cs_i = 12.  Synthetic seeded data.
 
+The step runs on the package's default library build (libnebula_fast.so: FMA contraction,
+approximate division / square root, within the path's tolerance of the exact build); the same
+line reports the exact build (libnebula.so, bit-identical to the reference kernels) on the same
+workload under "arith_exact".  --arith picks the build of the headline.
+
 --impl reference times the reference scheme's CPU implementation (the CPU restatement of its
 kernels in oracle/, all host threads) on the same workload and metric.
 Under torchrun (N > 1) every rank advances its own independent instance (replicas; the path
 does not shard) and the job throughput is N x cells x steps / max-over-ranks time.
+
+Other workloads (--workload): batch32 (32 uneven instances, persistent kernels + CUDA graphs,
+beside the same instances stepped one at a time), served (Poisson branch requests from device
+snapshots under an HBM budget, p50/p99), cliff1024 (the 1024^3 cloud wall with the -x plane
+source, FP64 totals), stirred256 (the stirring phase at 256^3: hydro without sources + drive).
 """
 import argparse
 import json
@@ -71,7 +81,8 @@ def ncu_traffic():
 
 
 class ClockSampler:
-    """nvidia-smi clocks / throttle reasons sampled every 50 ms during the timed region"""
+    """nvidia-smi clocks / throttle reasons sampled every 50 ms during the timed region, which
+    is also marked as the NVTX range "timed" (ncu --nvtx --nvtx-include timed/ captures only it)"""
 
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
          "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
@@ -88,9 +99,13 @@ class ClockSampler:
                                       stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
         except OSError:
             self.p = None
+        import torch
+        torch.cuda.nvtx.range_push("timed")
         return self
 
     def __exit__(self, *a):
+        import torch
+        torch.cuda.nvtx.range_pop()
         self.lines = []
         if self.p is not None:
             self.p.terminate()
@@ -510,6 +525,7 @@ def run_stirred(args):
                                     f"pre_amp {sim.P['pre_amp']}", "grid": list(sim.shape)},
              "roofline": {"bound": "hbm", "kernel": "drive", "achieved": drive_gbs, "peak": peak, "unit": "GB/s",
                           "frac": drive_gbs / peak if drive_gbs else None, "peak_source": peak_kind,
+                          "traffic": ncu_traffic().get("drive") if tuple(sim.shape) == (256, 256, 256) else None,
                           "algorithmic_bytes_per_launch": 32 * cells,
                           "avg_launch_ms": d_ms / max(d_n, 1)},
              "step_roofline": {"bytes_per_cell_step": b_step, "achieved": b_step * val, "peak": peak, "unit": "GB/s",
