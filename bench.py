@@ -23,7 +23,8 @@ does not shard) and the job throughput is N x cells x steps / max-over-ranks tim
 Other workloads (--workload): batch32 (32 uneven instances, persistent kernels + CUDA graphs,
 beside the same instances stepped one at a time), served (Poisson branch requests from device
 snapshots under an HBM budget, p50/p99), cliff1024 (the 1024^3 cloud wall with the -x plane
-source, FP64 totals), stirred256 (the stirring phase at 256^3: hydro without sources + drive).
+source, FP64 totals), stirred256 (the stirring phase at 256^3: hydro without sources + drive),
+render256 (the renderer's voxel pack + prefilter of the 256^3 sheet).
 """
 import argparse
 import json
@@ -537,6 +538,57 @@ def run_stirred(args):
     return 0
 
 
+def run_render(args):
+    """The renderer's voxel pack (render.py:176-205 pack_volume_lm with the shock proxy inline +
+    the three [1 4 1] prefilter passes of render.py:281-298) on the 256^3 sheet after a few steps:
+    the per-frame cost of handing the fields to the display side."""
+    import ctypes as C
+    import torch
+    from nebulaviewer_gb300 import _lib, build as nb_build
+    nb_build.build(verbose=False)
+    from nebulaviewer_gb300.sim import Sim
+    dev = torch.device("cuda", 0)
+    sim = Sim("sheet", res=args.res, device=dev, verbose=False, arith=args.arith)
+    sim.step(3)
+    sim.update_render_fields(force=True)
+    L = sim.L
+    pp = {"c_ha": (0.33, 0.675, 1.5), "c_o3": (0.45, 1.125, 1.5), "c_s2": (1.2, 0.66, 0.3), "c_dg": (0.07, 0.035, 0.01),
+          "c_sh": (0.02, 0.007, 0.009), "gs": 12.0, "ambient": 0.1, "edge": 0.08, "inv_L": [1.0 / v for v in L],
+          "dx": sim.dx}
+    for _ in range(args.warmup):
+        sim.render_pack(pp)
+    torch.cuda.synchronize(dev)
+    lib = sim._lib
+    lib.nb_profile(sim._h, 1)
+    prof_ms, prof_n = (C.c_double * 16)(), (C.c_longlong * 16)()
+    lib.nb_profile_read(sim._h, prof_ms, prof_n)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(0) as clk:
+        ev0.record()
+        for _ in range(args.steps):
+            sim.render_pack(pp)
+        ev1.record()
+        torch.cuda.synchronize(dev)
+    el = ev0.elapsed_time(ev1) / args.steps
+    lib.nb_profile_read(sim._h, prof_ms, prof_n)
+    lib.nb_profile(sim._h, 0)
+    cells = sim._n
+    peak, peak_kind = measured_peaks()
+    b_cell = 32.0 + 3 * 16.0            # pack: rho, xi, dfront, g0, m (shock) in, 8 B out; 3 passes of 8 B in + out
+    res_d = {"metric": "render pack Gcell/s", "value": cells / (el * 1e-3) / 1e9, "unit": "Gcell/s", "n_gpus": 1,
+             "steps": args.steps, "warmup": args.warmup, "ms_per_pack": el, "higher_is_better": True,
+             "dtype": "f32->f16", "data": "synthetic",
+             "config": {"workload": f"voxel pack + [1 4 1] prefilter of the sheet {list(sim.shape)} (shock proxy on)",
+                        "grid": list(sim.shape)},
+             "roofline": {"bound": "hbm", "kernel": "render pack + 3 prefilter passes", "achieved": b_cell * cells / (el * 1e-3) / 1e9,
+                          "peak": peak, "unit": "GB/s", "frac": b_cell * cells / (el * 1e-3) / 1e9 / peak,
+                          "peak_source": peak_kind, "algorithmic_bytes_per_cell": b_cell},
+             "gpu_launches": 4 * args.steps, "clocks": clk.summary(), "arith": sim.arith}
+    sim.close()
+    print(json.dumps(res_d), flush=True)
+    return 0
+
+
 def run_cliff(args):
     """The large single instance: the 1024^3 ionized cloud wall (density step n = 1 -> 200, 40
     clumps, the -x plane-parallel source + 3 stars, FUV on), FP64 conservation totals."""
@@ -593,7 +645,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--res", type=int, default=RES, help="grid size (the workload is defined at 256)")
     ap.add_argument("--workload", default="sheet256",
-                    choices=["sheet256", "batch32", "served", "cliff1024", "stirred256"])
+                    choices=["sheet256", "batch32", "served", "cliff1024", "stirred256", "render256"])
     ap.add_argument("--requests", type=int, default=100)
     ap.add_argument("--rate", type=float, default=200.0)
     ap.add_argument("--instances", type=int, default=32)
@@ -609,6 +661,8 @@ def main():
         return run_batch(args)
     if args.workload == "served":
         return run_served(args)
+    if args.workload == "render256":
+        return run_render(args)
     if args.workload == "stirred256":
         return run_stirred(args)
     if args.workload == "cliff1024":

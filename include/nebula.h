@@ -256,6 +256,22 @@ int nb_frame_pack(nb_handle h, void* out9);
 /* nebula3d.py:182-191 shock_field into a device buffer of N floats (Sim.shock, sim.py:827-833). */
 int nb_shock(nb_handle h, float* out);
 
+/* ---------------------------------------------------------------- renderer pack
+ * render.py:77-88 PackParams: palette colours times the line weights (c_dg multiplies
+ * dust * g0eff), the FUV saturation Gs and ambient term, the box-edge fade width, 1 / L and dx. */
+typedef struct nb_pack_params {
+    float c_ha[3], c_o3[3], c_s2[3], c_dg[3], c_sh[3];
+    float gs, ambient, edge;
+    float inv_L[3];
+    float dx;
+} nb_pack_params;
+/* render.py:176-205 pack_volume_lm: the RGBA16F voxel grid (emission r, g, b; dust) of the
+ * handle's fields, the shock proxy computed inline when shock_on != 0, into `out8` (device,
+ * 8 B/cell, C order [i][j][k][4] float16).  With smooth != 0 also render.py:281-298 smooth_axis
+ * along x, y, z, with `tmp8` (device, 8 B/cell) as the second grid; the result is in out8
+ * either way.  Renderer.pack packs into Sim.render_scratch (sim.py:821-825): the stage block. */
+int nb_render_pack(nb_handle h, const nb_pack_params* pp, int shock_on, int smooth, void* out8, void* tmp8);
+
 /* ---------------------------------------------------------------- diagnostics */
 /* Kernel kinds timed by nb_profile (CUDA events on the handle's stream around each launch). */
 enum {
@@ -270,6 +286,7 @@ enum {
     NB_PROF_MAX_SPEED = 8,    /* nebula3d.py:154-162 stand-alone */
     NB_PROF_SNAPSHOT = 9,     /* snapshot / frame packing, shock proxy */
     NB_PROF_DRIVE = 10,       /* nebula3d.py:165-179 stirring (+ CFL max speed), add_torus */
+    NB_PROF_RENDER = 11,      /* render.py:176-205, 281-298 voxel pack + prefilter */
     NB_PROF_KINDS = 16
 };
 /* No reference counterpart (the reference times whole calls with perf_counter, sim.py:578-579):

@@ -66,6 +66,12 @@ class NbDriveInfo(C.Structure):
                 ("pad", C.c_int)]
 
 
+class NbPackParams(C.Structure):
+    _fields_ = [("c_ha", C.c_float * 3), ("c_o3", C.c_float * 3), ("c_s2", C.c_float * 3), ("c_dg", C.c_float * 3),
+                ("c_sh", C.c_float * 3), ("gs", C.c_float), ("ambient", C.c_float), ("edge", C.c_float),
+                ("inv_L", C.c_float * 3), ("dx", C.c_float)]
+
+
 # name -> (restype, argtypes): every symbol include/nebula.h declares
 _P = C.c_void_p
 _F4 = C.c_void_p * 4
@@ -104,6 +110,7 @@ SIGNATURES = {
     "nb_snapshot_unpack": (C.c_int, [_P, _P]),
     "nb_frame_pack": (C.c_int, [_P, _P]),
     "nb_shock": (C.c_int, [_P, _P]),
+    "nb_render_pack": (C.c_int, [_P, C.POINTER(NbPackParams), C.c_int, C.c_int, _P, _P]),
     "nb_batch_create": (C.c_int, [C.POINTER(_P), C.POINTER(C.c_int), C.c_int, C.POINTER(_P)]),
     "nb_batch_step": (C.c_int, [_P, C.c_int]),
     "nb_batch_set_option": (C.c_int, [_P, C.c_int, C.c_int]),
@@ -115,7 +122,7 @@ SIGNATURES = {
 }
 TUNE = {"chunk_i": 0, "ray_group": 1, "fuv_group": 2, "tile_order": 3}
 PROF_KINDS = ["ctrl", "stage1", "stage2", "cast_rays", "apply_front", "smooth", "cast_fuv", "apply_fuv", "max_speed",
-              "snapshot", "drive"]
+              "snapshot", "drive", "render"]
 
 _libs = {}
 

@@ -8,7 +8,8 @@ generation:
                      bit-identical to the reference's kernels;
   libnebula_fast.so  fast: a*b+c contracted to FMA, approximate division and square root,
                      denormals flushed to zero in the compute kernels (the snapshot / frame
-                     formats keep the exact flags, their bytes are part of the format); stays
+                     formats and the renderer's voxel pack keep the exact flags, their bytes
+                     are part of a format); stays
                      within the path's stated tolerance of the exact build.
 """
 import concurrent.futures as cf
@@ -22,8 +23,9 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIBS = {"exact": os.path.join(HERE, "libnebula.so"), "fast": os.path.join(HERE, "libnebula_fast.so")}
 LIB = LIBS["exact"]
-SOURCES = ["nb_hydro.cu", "nb_step.cu", "nb_rays.cu", "nb_fuv.cu", "nb_snap.cu", "nb_stir.cu", "nb_api.cu"]
-EXACT_ONLY = {"nb_snap.cu"}          # byte formats: same code generation in both libraries
+SOURCES = ["nb_hydro.cu", "nb_step.cu", "nb_rays.cu", "nb_fuv.cu", "nb_snap.cu", "nb_stir.cu", "nb_render.cu",
+           "nb_api.cu"]
+EXACT_ONLY = {"nb_snap.cu", "nb_render.cu"}   # byte formats: same code generation in both libraries
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ARCH + ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-fvisibility=hidden", "-Xptxas", "-v"]
 ARITH_FLAGS = {

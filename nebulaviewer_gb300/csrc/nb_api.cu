@@ -620,6 +620,17 @@ NB_EXPORT int nb_mach_sums(nb_handle h, double out[2]) {
     return NB_OK;
 }
 
+NB_EXPORT int nb_render_pack(nb_handle h, const nb_pack_params* pp, int shock_on, int smooth, void* out8,
+                             void* tmp8) {
+    if (!h || !pp || !out8 || (smooth && !tmp8)) return fail(h, NB_ERR_ARG, "null argument");
+    if (!aligned16(out8) || (smooth && !aligned16(tmp8))) return fail(h, NB_ERR_ARG, "voxel grids must be 16-byte aligned");
+    const nb_fields& f = h->d.f;
+    Prof pf(h, NB_PROF_RENDER, smooth ? 4 : 1);
+    CK(h, nb_launch_render_pack(h->c, f.rho, f.mx, f.my, f.mz, f.xi, f.dfront, f.g0, h->d.fields_fp32 ? 0 : 1, *pp,
+                                shock_on, smooth, out8, tmp8, h->d.nx, h->d.ny, h->stream));
+    return NB_OK;
+}
+
 NB_EXPORT int nb_ionize(nb_handle h) {
     if (!h) return fail(h, NB_ERR_ARG, "null handle");
     return do_ionize(h);

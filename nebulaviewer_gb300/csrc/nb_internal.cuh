@@ -205,6 +205,10 @@ cudaError_t nb_launch_add_torus(const float* torus, float* rho, float* mx, float
 int nb_mach_scratch_doubles();
 cudaError_t nb_launch_mach_sums(const float* rho, const float* mx, const float* my, const float* mz, long long n,
                                 double* scratch, cudaStream_t s);
+cudaError_t nb_launch_render_pack(const NbConst* c, const float* rho, const float* mx, const float* my, const float* mz,
+                                  const float* xi, const void* dfront, const void* g0, int half,
+                                  const nb_pack_params& pp, int shock_on, int smooth, void* out8, void* tmp8, int nx,
+                                  int ny, cudaStream_t s);
 cudaError_t nb_launch_ray_dirs(int nu, int nphi, float4* dirs, cudaStream_t s);
 cudaError_t nb_launch_cast_rays(const NbConst* c, const NbStarW* sw, const float4* dirs, const float* rho,
                                 float* rfront, int nstars, int group, const float* star_override, float q_override,

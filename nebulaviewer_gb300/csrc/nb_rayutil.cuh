@@ -82,3 +82,19 @@ __device__ __forceinline__ int wrap_index(int ip, int n) {
     if (ip == n) return 0;
     return ((ip % n) + n) % n;
 }
+
+// nebula3d.py:182-191 shock_field at (i, j, k) (also render.py:165-174 shock_at): max(0, -div v) * rho,
+// central differences on clamped neighbours
+__device__ __forceinline__ float nb_shock_at(const NbConst& C, const float* __restrict__ rho,
+                                             const float* __restrict__ mx, const float* __restrict__ my,
+                                             const float* __restrict__ mz, int i, int j, int k) {
+    const int nx = C.nx, ny = C.ny, nz = C.nz;
+    auto at = [&](const float* a, int ii, int jj, int kk) {
+        return __ldg(a + ((long long)iclampd(ii, 0, nx - 1) * ny + iclampd(jj, 0, ny - 1)) * nz + iclampd(kk, 0, nz - 1));
+    };
+    const float du = at(mx, i + 1, j, k) / at(rho, i + 1, j, k) - at(mx, i - 1, j, k) / at(rho, i - 1, j, k);
+    const float dv = at(my, i, j + 1, k) / at(rho, i, j + 1, k) - at(my, i, j - 1, k) / at(rho, i, j - 1, k);
+    const float dw = at(mz, i, j, k + 1) / at(rho, i, j, k + 1) - at(mz, i, j, k - 1) / at(rho, i, j, k - 1);
+    const float div = (du + dv + dw) / (2.0f * C.dx);
+    return fmaxr(-div, 0.0f) * at(rho, i, j, k);
+}

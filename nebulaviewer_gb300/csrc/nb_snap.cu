@@ -70,29 +70,13 @@ __global__ void __launch_bounds__(256) unpack_kernel(const NbConst* __restrict__
     }
 }
 
-// nebula3d.py:182-191 shock_field at (i, j, k): max(0, -div v) * rho, central differences on
-// clamped neighbours
-__device__ __forceinline__ float shock_at(const NbConst& C, const float* __restrict__ rho,
-                                          const float* __restrict__ mx, const float* __restrict__ my,
-                                          const float* __restrict__ mz, int i, int j, int k) {
-    const int nx = C.nx, ny = C.ny, nz = C.nz;
-    auto at = [&](const float* a, int ii, int jj, int kk) {
-        return __ldg(a + ((long long)iclampd(ii, 0, nx - 1) * ny + iclampd(jj, 0, ny - 1)) * nz + iclampd(kk, 0, nz - 1));
-    };
-    const float du = at(mx, i + 1, j, k) / at(rho, i + 1, j, k) - at(mx, i - 1, j, k) / at(rho, i - 1, j, k);
-    const float dv = at(my, i, j + 1, k) / at(rho, i, j + 1, k) - at(my, i, j - 1, k) / at(rho, i, j - 1, k);
-    const float dw = at(mz, i, j, k + 1) / at(rho, i, j, k + 1) - at(mz, i, j, k - 1) / at(rho, i, j, k - 1);
-    const float div = (du + dv + dw) / (2.0f * C.dx);
-    return fmaxr(-div, 0.0f) * at(rho, i, j, k);
-}
-
 __global__ void __launch_bounds__(256) shock_kernel(const NbConst* __restrict__ c, const float* __restrict__ rho,
                                                     const float* __restrict__ mx, const float* __restrict__ my,
                                                     const float* __restrict__ mz, float* __restrict__ out) {
     const NbConst& C = *c;
     const RowWalk w(C.nx, C.ny, C.nz);
     if (!w.valid) return;
-    for (int k = w.k0; k < C.nz; k += 32) out[w.base + k] = shock_at(C, rho, mx, my, mz, w.i, w.j, k);
+    for (int k = w.k0; k < C.nz; k += 32) out[w.base + k] = nb_shock_at(C, rho, mx, my, mz, w.i, w.j, k);
 }
 
 __global__ void __launch_bounds__(256) frame_kernel(const NbConst* __restrict__ c, const float* __restrict__ rho,
@@ -117,7 +101,7 @@ __global__ void __launch_bounds__(256) frame_kernel(const NbConst* __restrict__ 
         o_xi[q] = (unsigned char)rintf(fminr(fmaxr(0.0f, xi[q]), 1.0f) * 255.0f);
         const float d = ld_field(df, q, half);
         o_df[q] = __float2half_rn(fminr(fmaxr(d, -4.0f), 4.0f));
-        const float sh = shock_at(C, rho, mx, my, mz, w.i, w.j, k);
+        const float sh = nb_shock_at(C, rho, mx, my, mz, w.i, w.j, k);
         o_sh[q] = __float2half_rn(sh < 60000.0f ? sh : 60000.0f);
     }
 }

@@ -748,6 +748,29 @@ class Sim:
         f16 = lambda off: b[off:off + 2 * n].view(np.float16).reshape(sh)  # noqa: E731
         return dict(g0=f16(0), rho=f16(2 * n), xi=b[4 * n:5 * n].reshape(sh), df=f16(5 * n), sh=f16(7 * n))
 
+    PACK_FIELDS = ("c_ha", "c_o3", "c_s2", "c_dg", "c_sh", "gs", "ambient", "edge", "inv_L", "dx")
+
+    def render_pack(self, pp, shock_on=None, smooth=True):
+        """render.py:176-205 pack_volume_lm (+ render.py:281-298 smooth_axis x, y, z): the RGBA16F
+        voxel grid (emission r, g, b; dust) of the current fields, packed into the render scratch
+        (the stage block, free between steps) as Renderer.pack does; returns it as a
+        (nx, ny, nz, 4) float16 Field.  `pp`: the reference's PackParams (render.py:77-88,
+        Renderer.pack_params) or a mapping with the same keys; shock_on defaults to any(c_sh)."""
+        get = (lambda k: pp[k]) if isinstance(pp, dict) else (lambda k: getattr(pp, k))
+        vals = {k: get(k) for k in self.PACK_FIELDS}
+        P = _lib.NbPackParams()
+        for k in ("c_ha", "c_o3", "c_s2", "c_dg", "c_sh", "inv_L"):
+            getattr(P, k)[:] = [float(v) for v in vals[k]]
+        for k in ("gs", "ambient", "edge", "dx"):
+            setattr(P, k, float(vals[k]))
+        if shock_on is None:
+            shock_on = any(float(v) != 0.0 for v in vals["c_sh"])                # render.py:734
+        packed, packed2 = self.render_scratch()
+        out, tmp = (packed2, packed) if smooth else (packed, packed2)          # render.py:725-730
+        self._chk(self._lib.nb_render_pack(self._h, C.byref(P), 1 if shock_on else 0, 1 if smooth else 0,
+                                           C.c_void_p(out.ptr), C.c_void_p(tmp.ptr)), "nb_render_pack")
+        return out
+
     def write_frame(self, root, frame):
         """np.save the frame files f####_{g0,rho,xi,df,sh}.npy as bake.py:95-102 does"""
         import os

@@ -53,6 +53,8 @@ def lib():
             getattr(L, f"oracle_drive_{sfx}").argtypes = [C.c_int] * 3 + [P] * 4 + [C.c_int] * 3 + [P, P] + [T] * 5
             getattr(L, f"oracle_add_torus_{sfx}").argtypes = [C.c_long] + [P] * 5
         L.oracle_to_half.argtypes = [P, P, C.c_long]
+        L.oracle_render_pack.argtypes = [C.c_int] * 3 + [P] * 8 + [C.c_int, P]
+        L.oracle_render_smooth.argtypes = [C.c_int] * 3 + [P, P, C.c_int]
         L.oracle_threads.restype = C.c_int
         _LIB = L
     return _LIB
@@ -183,6 +185,28 @@ class Kernels:
             assert m.dtype == self.dt and m.flags.c_contiguous
         t = self._a(torus)
         self._fn("add_torus")(rho.size, _p(t), _p(rho), _p(mx), _p(my), _p(mz))
+
+
+def render_pack(rho, mom, xi, df16, g016, params, shock_on, smooth=True):
+    """render.py:176-205 pack_volume_lm (+ render.py:281-298 smooth_axis x, y, z when `smooth`):
+    float16 (nx, ny, nz, 4) voxels.  params: the 22 PackParams floats (c_ha, c_o3, c_s2, c_dg,
+    c_sh, gs, ambient, edge, inv_L, dx)."""
+    L = lib()
+    f = lambda a: np.ascontiguousarray(a, np.float32)  # noqa: E731
+    h = lambda a: np.ascontiguousarray(np.asarray(a, np.float16)).view(np.uint16)  # noqa: E731
+    r, x, m = f(rho), f(xi), [f(v) for v in mom]
+    d, g, pp = h(df16), h(g016), f(np.asarray(params, np.float32)[:22])
+    nx, ny, nz = r.shape
+    out = np.zeros((nx, ny, nz, 4), np.uint16)
+    L.oracle_render_pack(nx, ny, nz, _p(r), _p(m[0]), _p(m[1]), _p(m[2]), _p(x), _p(d), _p(g), _p(pp), int(shock_on),
+                         _p(out))
+    if smooth:
+        tmp = np.zeros_like(out)
+        for ax in range(3):                                         # render.py:725-728
+            src, dst = (out, tmp) if ax != 1 else (tmp, out)
+            L.oracle_render_smooth(nx, ny, nz, _p(src), _p(dst), ax)
+        out = tmp
+    return out.view(np.float16)
 
 
 def to_half(x):

@@ -21,6 +21,7 @@
 #include <cstdint>
 #include <cstring>
 #include <algorithm>
+#include <limits>
 #ifdef _OPENMP
 #include <omp.h>
 #endif
@@ -572,6 +573,101 @@ static void add_torus_t(long n, const T* torus, T* rho, T* mx, T* my, T* mz) {
     }
 }
 
+// float16 bits -> float (exact)
+static inline float f16_to_f32(uint16_t h) {
+    const uint32_t sign = (uint32_t)(h & 0x8000u) << 16;
+    const uint32_t e = (h >> 10) & 0x1fu, m = h & 0x3ffu;
+    float v;
+    if (e == 0) {
+        v = std::ldexp((float)m, -24);                                   // zero / subnormal
+    } else if (e == 31) {
+        v = m ? std::numeric_limits<float>::quiet_NaN() : std::numeric_limits<float>::infinity();
+    } else {
+        v = std::ldexp((float)(m | 0x400u), (int)e - 25);
+    }
+    uint32_t b;
+    std::memcpy(&b, &v, 4);
+    b |= sign;
+    std::memcpy(&v, &b, 4);
+    return v;
+}
+
+// nebula3d.py:182-191 shock_field at one cell (render.py:165-174 shock_at): max(0, -div v) rho,
+// central differences on clamped neighbours
+static inline float shock_at_f(const Grid& g, const float* rho, const float* mx, const float* my, const float* mz,
+                               int i, int j, int k, float dx) {
+    const float du = mx[g.idxc(i + 1, j, k)] / rho[g.idxc(i + 1, j, k)] - mx[g.idxc(i - 1, j, k)] / rho[g.idxc(i - 1, j, k)];
+    const float dv = my[g.idxc(i, j + 1, k)] / rho[g.idxc(i, j + 1, k)] - my[g.idxc(i, j - 1, k)] / rho[g.idxc(i, j - 1, k)];
+    const float dw = mz[g.idxc(i, j, k + 1)] / rho[g.idxc(i, j, k + 1)] - mz[g.idxc(i, j, k - 1)] / rho[g.idxc(i, j, k - 1)];
+    const float div = (du + dv + dw) / (2.0f * dx);
+    return tmax(-div, 0.0f) * rho[g.idx(i, j, k)];
+}
+
+// render.py:127-131 sstep, 135-139 fade_axis
+static inline float sstep_f(float e0, float e1, float x) {
+    const float t = tclamp((x - e0) / (e1 - e0), 0.0f, 1.0f);
+    return t * t * (3.0f - 2.0f * t);
+}
+static inline float fade_f(float u, float e) { return e <= 0.0f ? 1.0f : sstep_f(0.0f, e, u) * sstep_f(0.0f, e, 1.0f - u); }
+
+// render.py:176-205 pack_volume_lm: one RGBA16F voxel (emission rgb, dust) per cell.
+// pp: c_ha[3] c_o3[3] c_s2[3] c_dg[3] c_sh[3] gs ambient edge inv_L[3] dx (render.py:77-88 PackParams)
+static void render_pack_f(int nx, int ny, int nz, const float* rho, const float* mx, const float* my, const float* mz,
+                          const float* xi, const uint16_t* df16, const uint16_t* g016, const float* pp, int shock_on,
+                          uint16_t* out) {
+    const Grid g{nx, ny, nz};
+    const float *c_ha = pp, *c_o3 = pp + 3, *c_s2 = pp + 6, *c_dg = pp + 9, *c_sh = pp + 12;
+    const float gs = pp[15], ambient = pp[16], edge = pp[17], *inv_L = pp + 18, dx = pp[21];
+#pragma omp parallel for collapse(2) schedule(static)
+    for (int i = 0; i < nx; ++i)
+        for (int j = 0; j < ny; ++j)
+            for (int k = 0; k < nz; ++k) {
+                const long q = g.idx(i, j, k);
+                const float r = rho[q];
+                const float x = tclamp(xi[q], 0.0f, 1.0f);
+                const float df = f16_to_f32(df16[q]);
+                const float ni = r * x;
+                const float ha = ni * ni;
+                const float oiii = ha * sstep_f(-0.03f, -0.12f, df);
+                const float sii = ha * sstep_f(-0.05f, -0.005f, df);
+                float dust = r * (1.0f - x) + 0.08f * ni;
+                const float gv = f16_to_f32(g016[q]);
+                const float geff = gv / (1.0f + gv / gs) + ambient;
+                const float sh = shock_on ? shock_at_f(g, rho, mx, my, mz, i, j, k, dx) : 0.0f;
+                float em[3];
+                for (int c = 0; c < 3; ++c)
+                    em[c] = ha * c_ha[c] + oiii * c_o3[c] + sii * c_s2[c] + (dust * geff) * c_dg[c] + sh * c_sh[c];
+                const float p0 = ((float)i + 0.5f) * dx * inv_L[0];
+                const float p1 = ((float)j + 0.5f) * dx * inv_L[1];
+                const float p2 = ((float)k + 0.5f) * dx * inv_L[2];
+                const float f = fade_f(p0, edge) * fade_f(p1, edge) * fade_f(p2, edge);
+                for (int c = 0; c < 3; ++c) em[c] = em[c] * f;
+                dust = dust * f;
+                const float m = 60000.0f;
+                for (int c = 0; c < 3; ++c) out[q * 4 + c] = f32_to_f16_rne(tmin(em[c], m));
+                out[q * 4 + 3] = f32_to_f16_rne(tmin(dust, m));
+            }
+}
+
+// render.py:281-298 smooth_axis: [1 4 1]/6 along one axis, clamped at the faces
+static void render_smooth_f(int nx, int ny, int nz, const uint16_t* src, uint16_t* dst, int axis) {
+    const Grid g{nx, ny, nz};
+    const int oi = axis == 0, oj = axis == 1, ok = axis == 2;
+#pragma omp parallel for collapse(2) schedule(static)
+    for (int i = 0; i < nx; ++i)
+        for (int j = 0; j < ny; ++j)
+            for (int k = 0; k < nz; ++k) {
+                const long a = g.idx(imax(i - oi, 0), imax(j - oj, 0), imax(k - ok, 0));
+                const long b = g.idx(i, j, k);
+                const long c = g.idx(imin(i + oi, nx - 1), imin(j + oj, ny - 1), imin(k + ok, nz - 1));
+                for (int ch = 0; ch < 4; ++ch) {
+                    const float v = (f16_to_f32(src[a * 4 + ch]) + 4.0f * f16_to_f32(src[b * 4 + ch]) +
+                                     f16_to_f32(src[c * 4 + ch])) / 6.0f;
+                    dst[b * 4 + ch] = f32_to_f16_rne(v);
+                }
+            }
+}
+
 // ==================================================================================== C ABI
 #define NB_ORACLE_EXPORT extern "C" __attribute__((visibility("default")))
 
@@ -643,6 +739,16 @@ INSTANTIATE(double, f64)
 NB_ORACLE_EXPORT void oracle_to_half(const float* src, uint16_t* dst, long n) {
 #pragma omp parallel for schedule(static)
     for (long q = 0; q < n; ++q) dst[q] = f32_to_f16_rne(src[q]);
+}
+
+NB_ORACLE_EXPORT void oracle_render_pack(int nx, int ny, int nz, const float* rho, const float* mx, const float* my,
+                                          const float* mz, const float* xi, const uint16_t* df16,
+                                          const uint16_t* g016, const float* pp, int shock_on, uint16_t* out) {
+    render_pack_f(nx, ny, nz, rho, mx, my, mz, xi, df16, g016, pp, shock_on, out);
+}
+
+NB_ORACLE_EXPORT void oracle_render_smooth(int nx, int ny, int nz, const uint16_t* src, uint16_t* dst, int axis) {
+    render_smooth_f(nx, ny, nz, src, dst, axis);
 }
 
 NB_ORACLE_EXPORT int oracle_threads(void) {

@@ -18,6 +18,7 @@ Fixtures (all small, committed):
                    ionization included) and after every step, clocks, the FUV field.
   stir.npz         the stirring kernels (drive, add_torus) and the solenoidal forcing
                    generator on a seeded Generator.
+  render.npz       the renderer's voxel pack (pack_volume_lm) and [1 4 1] prefilter.
   sim_bipolar_pre.npz  a reference `Sim` run through the pre-turbulence (stirring) phase,
                    its end (torus added, first ionization) and main-phase stirring, with
                    every forcing field the run drew.
@@ -320,6 +321,46 @@ def sim_pre_case(S, scenario, res, overrides, nsteps, rays, fuv, ic_mode):
     return out
 
 
+# ----------------------------------------------------------------------------- renderer pack
+def render_cases(ref, rng):
+    """render.py:176-205 pack_volume_lm (RGBA16F voxel: emission rgb + dust, shock proxy inline,
+    box-edge fade) and render.py:281-298 smooth_axis ([1 4 1]/6 along each axis, three passes)"""
+    sys.path.insert(0, ref)
+    import types
+    import render as R
+    shape = (10, 9, 8)
+    dx = 0.125
+    L = tuple(n * dx for n in shape)
+    rho = np.exp(rng.normal(0.0, 1.5, shape)).astype(np.float32) + np.float32(0.01)
+    rho.flat[:2] = [3e3, 0.05]
+    mom = (rng.normal(0.0, 2.0, (3,) + shape) * rho).astype(np.float32)
+    xi = rng.uniform(-0.2, 1.2, shape).astype(np.float32)
+    df = rng.uniform(-0.2, 0.1, shape).astype(np.float16)
+    df[rng.random(shape) < 0.15] = np.float16(1e3)
+    g0 = np.exp(rng.normal(0.0, 3.0, shape)).astype(np.float16)
+    g0.flat[:2] = [np.float16(65504.0), np.float16(0.0)]
+    out = {"p_rho": rho, "p_mom": mom, "p_xi": xi, "p_df": df, "p_g0": g0, "p_dx": np.float64(dx)}
+    fake = types.SimpleNamespace(L=L, dx=dx)
+    cases = (("jwst", dict(R.make_look("bipolar"), shock=0.002, edge_fade=0.3), 1),
+             ("sho", dict(R.make_look("bubbles"), palette="sho", edge_fade=0.0), 0),
+             ("nat", dict(R.make_look("cliff"), palette="natural", gs=12.0, edge_fade=0.08), 1))
+    for tag, look, shock_on in cases:
+        pp = R.Renderer.pack_params(look, fake)
+        o = np.zeros(shape + (4,), np.float16)
+        R.pack_volume_lm.run(shape, [rho, mom[0], mom[1], mom[2], xi, df, g0, pp, shock_on, o])
+        a, b = o.copy(), np.zeros_like(o)
+        for ax in range(3):                                   # render.py:725-728
+            src, dst = (a, b) if ax != 1 else (b, a)
+            R.smooth_axis.run(shape, [src, dst, ax])
+        out[f"p_{tag}_params"] = np.array(
+            list(pp.c_ha) + list(pp.c_o3) + list(pp.c_s2) + list(pp.c_dg) + list(pp.c_sh) +
+            [pp.gs, pp.ambient, pp.edge] + list(pp.inv_L) + [pp.dx, shock_on], np.float32)
+        out[f"p_{tag}_packed"] = o
+        out[f"p_{tag}_smooth"] = b
+        print(f"  pack {tag}: max {float(np.abs(o.astype(np.float32)).max()):.4g}", flush=True)
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference")
@@ -330,6 +371,9 @@ def main():
     if a.only in (None, "kernels"):
         print("kernels:", flush=True)
         np.savez_compressed(os.path.join(HERE, "kernels.npz"), **kernel_cases(N, S, rng))
+    if a.only in (None, "render"):
+        print("render:", flush=True)
+        np.savez_compressed(os.path.join(HERE, "render.npz"), **render_cases(a.ref, np.random.default_rng(77)))
     if a.only in (None, "stir"):
         print("stir:", flush=True)
         np.savez_compressed(os.path.join(HERE, "stir.npz"), **stir_cases(N, S, np.random.default_rng(515)))

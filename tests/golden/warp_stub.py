@@ -103,14 +103,68 @@ class vec4(_Vec):
     N = 4
 
 
-class vec4h:                         # only referenced by Sim.render_scratch (never called here)
+class vec4h:
+    """four float16 components (render.py's packed voxel), mutable as Warp's vectors are"""
+    __array_ufunc__ = None
+
+    def __init__(self, *args):
+        vals = args if args else (0.0, 0.0, 0.0, 0.0)
+        self.v = [np.float16(x) for x in vals]
+
+    def __getitem__(self, i):
+        return self.v[i]
+
+    def __setitem__(self, i, x):
+        self.v[i] = np.float16(x)
+
+    def __iter__(self):
+        return iter(self.v)
+
+    def __len__(self):
+        return 4
+
+
+def cw_mul(a, b):
+    return a._of(x * y for x, y in zip(a.v, b.v))
+
+
+def struct(cls):
+    """@wp.struct: instances convert assigned values to the annotated Warp types (float -> float32)"""
+    ann = dict(getattr(cls, "__annotations__", {}))
+
+    def __setattr__(self, name, value):
+        t = ann.get(name)
+        if t is float:
+            value = f32(value)
+        elif t is int:
+            value = int(value)
+        elif isinstance(t, type) and issubclass(t, _Vec) and not isinstance(value, _Vec):
+            value = t(*value)
+        object.__setattr__(self, name, value)
+
+    cls.__setattr__ = __setattr__
+    return cls
+
+
+class Texture3D:                     # annotation only (render.py's ray marcher is not run here)
     pass
+
+
+class TextureFilterMode:
+    LINEAR = 1
+    CLOSEST = 0
+
+
+class TextureAddressMode:
+    CLAMP = 0
+    WRAP = 1
 
 
 float32 = np.float32
 float16 = np.float16
 uint8 = np.uint8
 int32 = np.int32
+uint32 = np.uint32
 pi = f32(math.pi)
 LOG_WARNING = 2
 config = types.SimpleNamespace(log_level=None, quiet=False, mode="release")
@@ -217,6 +271,8 @@ class array:
         self.is_vec = self.dtype in (vec4, vec3, vec2)
         if _np is not None:
             self.np = _np
+        elif data is None:                       # wp.array(dtype=...) as an annotation
+            self.np = np.zeros(0, np.float32 if self.is_vec else self.dtype)
         else:
             base = np.float32 if self.is_vec else self.dtype
             self.np = np.array(data, dtype=base, copy=True)

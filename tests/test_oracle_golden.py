@@ -187,3 +187,16 @@ def test_oracle_sim_through_stirring_phase_matches_reference_sim():
             assert bits_equal(getattr(o, f), d[f"s{n + 1}_{f}"]), (n, f)
         if st["mach"] is not None:
             assert abs(o.mach - st["mach"]) <= 1e-5 * st["mach"]        # FP64 sum vs the reference's FP32 atomics
+
+
+# ---------------------------------------------------------------------------- renderer pack
+@pytest.mark.parametrize("tag", ("jwst", "sho", "nat"))
+def test_render_pack_bit_exact(tag):
+    """render.py:176-205 pack_volume_lm and the [1 4 1] prefilter of render.py:281-298"""
+    from conftest import golden
+    z = golden("render.npz")
+    pp = z[f"p_{tag}_params"]
+    a = O.render_pack(z["p_rho"], z["p_mom"], z["p_xi"], z["p_df"], z["p_g0"], pp, int(pp[22]), smooth=False)
+    b = O.render_pack(z["p_rho"], z["p_mom"], z["p_xi"], z["p_df"], z["p_g0"], pp, int(pp[22]), smooth=True)
+    assert np.array_equal(a.view(np.uint16), z[f"p_{tag}_packed"].view(np.uint16))
+    assert np.array_equal(b.view(np.uint16), z[f"p_{tag}_smooth"].view(np.uint16))
