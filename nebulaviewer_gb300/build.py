@@ -30,7 +30,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ARCH + ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-fvisibility=hidden", "-Xptxas", "-v"]
 ARITH_FLAGS = {
     "exact": ["-fmad=false", "-prec-div=true", "-prec-sqrt=true", "-ftz=false"],
-    "fast": ["-fmad=true", "-prec-div=false", "-prec-sqrt=false", "-ftz=true"],
+    "fast": ["-fmad=true", "-prec-div=false", "-prec-sqrt=false", "-ftz=true", "-DNB_ARITH_FAST=1"],
 }
 NVCC_FLAGS = COMMON + ARITH_FLAGS["exact"]
 

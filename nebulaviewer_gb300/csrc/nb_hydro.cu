@@ -38,12 +38,86 @@ __device__ __forceinline__ float comp(const float4& v, int c) {
     return c == 0 ? v.x : (c == 1 ? v.y : (c == 2 ? v.z : v.w));
 }
 
+// ---- paired FP32 arithmetic (sm_100+ add/sub/mul/fma.rn.f32x2): a state's four components are
+// handled as the pairs (0,1) and (2,3), one instruction issue for two float operations.  Used in
+// the fast build only: each paired operation alone rounds as the scalar one, but the assembler
+// fuses a dependent mul.rn.f32x2 -> add.rn.f32x2 into one fused multiply-add even with explicit
+// round-to-nearest modifiers and -fmad=false (measured on random operands: 13% differ by an ulp),
+// which the exact build cannot allow.  The fast build contracts a*b+c anyway.
+#ifndef NB_PAIRED
+#if defined(NB_ARITH_FAST) && NB_ARITH_FAST
+#define NB_PAIRED 1
+#else
+#define NB_PAIRED 0
+#endif
+#endif
+struct F2 {
+    unsigned long long v;
+};
+__device__ __forceinline__ F2 mk2(float a, float b) {
+    F2 r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r.v) : "f"(a), "f"(b));
+    return r;
+}
+__device__ __forceinline__ float lo(F2 a) {
+    float x, y;
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(x), "=f"(y) : "l"(a.v));
+    return x;
+}
+__device__ __forceinline__ float hi(F2 a) {
+    float x, y;
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(x), "=f"(y) : "l"(a.v));
+    return y;
+}
+__device__ __forceinline__ F2 add2(F2 a, F2 b) {
+    F2 r;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r.v) : "l"(a.v), "l"(b.v));
+    return r;
+}
+__device__ __forceinline__ F2 sub2(F2 a, F2 b) {
+    F2 r;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r.v) : "l"(a.v), "l"(b.v));
+    return r;
+}
+__device__ __forceinline__ F2 mul2(F2 a, F2 b) {
+    F2 r;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r.v) : "l"(a.v), "l"(b.v));
+    return r;
+}
+// a*b + c: one fused operation in the fast build, a rounded product then a rounded sum in the exact one
+__device__ __forceinline__ F2 madd2(F2 a, F2 b, F2 c) {
+#if NB_ARITH_FAST
+    F2 r;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r.v) : "l"(a.v), "l"(b.v), "l"(c.v));
+    return r;
+#else
+    return add2(mul2(a, b), c);
+#endif
+}
+// c - a*b with the same rounding rules
+__device__ __forceinline__ F2 nmsub2(F2 c, F2 a, F2 b) {
+#if NB_ARITH_FAST
+    F2 r, na = mk2(-lo(a), -hi(a));
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r.v) : "l"(na.v), "l"(b.v), "l"(c.v));
+    return r;
+#else
+    return sub2(c, mul2(a, b));
+#endif
+}
+__device__ __forceinline__ F2 splat2(float a) { return mk2(a, a); }
+
+// minmod given the product a*b (nebula3d.py:40-46)
+__device__ __forceinline__ float minmod_p(float a, float b, float ab) {
+    if (ab <= 0.0f) return 0.0f;
+    return fabsf(a) < fabsf(b) ? a : b;
+}
+
 // Face flux between cells b and c along axis AX (1 = x, 2 = y, 3 = z: the velocity
 // component normal to the face).  cs = (c^2, c) of a cell.
 //   dot((0, L1, L2, L3), e_AX) == 0 + L_AX exactly (the other products are +-0 and the
 //   velocities are finite), and e_c * (rho c^2) == +0 for c != AX.
 template <int SOLVER, int LIM, int AX>
-__device__ __forceinline__ float4 face_flux(const float4 qa, const float4 qb, const float4 qc, const float4 qd,
+__device__ __forceinline__ float4 face_flux_scalar(const float4 qa, const float4 qb, const float4 qc, const float4 qd,
                                             const float2 csb, const float2 csc, const float floor_) {
     constexpr int LM = SOLVER == NB_SOLVER_HLL ? LIM : 0;
     float L[4], R[4];
@@ -80,6 +154,81 @@ __device__ __forceinline__ float4 face_flux(const float4 qa, const float4 qb, co
 #pragma unroll
     for (int c = 0; c < 4; ++c) F[c] = (SR * FL[c] - SL * FR[c] + slsr * (UR[c] - UL[c])) / den;
     return make_float4(F[0], F[1], F[2], F[3]);
+}
+
+// The same face flux on component pairs: the float operations and operands of face_flux_scalar
+// (the minmod sign test multiplies the same two differences), with a*b+c fused.
+template <int SOLVER, int LIM, int AX>
+__device__ __forceinline__ float4 face_flux_paired(const float4 qa, const float4 qb, const float4 qc, const float4 qd,
+                                                   const float2 csb, const float2 csc, const float floor_) {
+    constexpr int LM = SOLVER == NB_SOLVER_HLL ? LIM : 0;
+    const F2 a0 = mk2(qa.x, qa.y), a1 = mk2(qa.z, qa.w), b0 = mk2(qb.x, qb.y), b1 = mk2(qb.z, qb.w);
+    const F2 c0 = mk2(qc.x, qc.y), c1 = mk2(qc.z, qc.w), e0 = mk2(qd.x, qd.y), e1 = mk2(qd.z, qd.w);
+    const F2 d1_0 = sub2(b0, a0), d1_1 = sub2(b1, a1);
+    const F2 d2_0 = sub2(c0, b0), d2_1 = sub2(c1, b1);
+    const F2 d3_0 = sub2(e0, c0), d3_1 = sub2(e1, c1);
+    F2 sl0, sl1, sr0, sr1;
+    if (LM == 0) {
+        const F2 p12_0 = mul2(d1_0, d2_0), p12_1 = mul2(d1_1, d2_1);
+        const F2 p23_0 = mul2(d2_0, d3_0), p23_1 = mul2(d2_1, d3_1);
+        sl0 = mk2(minmod_p(lo(d1_0), lo(d2_0), lo(p12_0)), minmod_p(hi(d1_0), hi(d2_0), hi(p12_0)));
+        sl1 = mk2(minmod_p(lo(d1_1), lo(d2_1), lo(p12_1)), minmod_p(hi(d1_1), hi(d2_1), hi(p12_1)));
+        sr0 = mk2(minmod_p(lo(d2_0), lo(d3_0), lo(p23_0)), minmod_p(hi(d2_0), hi(d3_0), hi(p23_0)));
+        sr1 = mk2(minmod_p(lo(d2_1), lo(d3_1), lo(p23_1)), minmod_p(hi(d2_1), hi(d3_1), hi(p23_1)));
+    } else {
+        sl0 = mk2(slope_lim<LM>(lo(d1_0), lo(d2_0)), slope_lim<LM>(hi(d1_0), hi(d2_0)));
+        sl1 = mk2(slope_lim<LM>(lo(d1_1), lo(d2_1)), slope_lim<LM>(hi(d1_1), hi(d2_1)));
+        sr0 = mk2(slope_lim<LM>(lo(d2_0), lo(d3_0)), slope_lim<LM>(hi(d2_0), hi(d3_0)));
+        sr1 = mk2(slope_lim<LM>(lo(d2_1), lo(d3_1)), slope_lim<LM>(hi(d2_1), hi(d3_1)));
+    }
+    const F2 half = splat2(0.5f);
+    const F2 L0 = madd2(half, sl0, b0), L1 = madd2(half, sl1, b1);      // b + 0.5 * slope
+    const F2 R0 = nmsub2(c0, half, sr0), R1 = nmsub2(c1, half, sr1);    // c - 0.5 * slope
+    const float rL = fmaxr(lo(L0), floor_), rR = fmaxr(lo(R0), floor_);
+    const float unL = 0.0f + (AX == 1 ? hi(L0) : (AX == 2 ? lo(L1) : hi(L1)));
+    const float unR = 0.0f + (AX == 1 ? hi(R0) : (AX == 2 ? lo(R1) : hi(R1)));
+    // U = (r, r u, r v, r w): r * 1 == r exactly
+    const F2 UL0 = mul2(splat2(rL), mk2(1.0f, hi(L0))), UL1 = mul2(splat2(rL), L1);
+    const F2 UR0 = mul2(splat2(rR), mk2(1.0f, hi(R0))), UR1 = mul2(splat2(rR), R1);
+    const float pL = rL * csb.x, pR = rR * csc.x;
+    // F = U * un + p e_AX (the other components add +0, as the reference's e_c * p does)
+    const F2 pL0 = mk2(0.0f, AX == 1 ? pL : 0.0f), pL1 = mk2(AX == 2 ? pL : 0.0f, AX == 3 ? pL : 0.0f);
+    const F2 pR0 = mk2(0.0f, AX == 1 ? pR : 0.0f), pR1 = mk2(AX == 2 ? pR : 0.0f, AX == 3 ? pR : 0.0f);
+    const F2 FL0 = madd2(UL0, splat2(unL), pL0), FL1 = madd2(UL1, splat2(unL), pL1);
+    const F2 FR0 = madd2(UR0, splat2(unR), pR0), FR1 = madd2(UR1, splat2(unR), pR1);
+    if (SOLVER == NB_SOLVER_RUSANOV) {
+        const float amax = fmaxr(fabsf(unL) + csb.y, fabsf(unR) + csc.y);
+        const F2 ha = splat2(0.5f * amax);
+        const F2 F0 = nmsub2(mul2(half, add2(FL0, FR0)), ha, sub2(UR0, UL0));
+        const F2 F1 = nmsub2(mul2(half, add2(FL1, FR1)), ha, sub2(UR1, UL1));
+        return make_float4(lo(F0), hi(F0), lo(F1), hi(F1));
+    }
+    const float SL = fminr(unL - csb.y, unR - csc.y);
+    const float SR = fmaxr(unL + csb.y, unR + csc.y);
+    if (SL >= 0.0f) return make_float4(lo(FL0), hi(FL0), lo(FL1), hi(FL1));
+    if (SR <= 0.0f) return make_float4(lo(FR0), hi(FR0), lo(FR1), hi(FR1));
+    const F2 slsr = splat2(SL * SR);
+    const float den = SR - SL;
+    // (SR FL - SL FR + SL SR (UR - UL)) / den
+    const F2 T0 = madd2(slsr, sub2(UR0, UL0), sub2(mul2(splat2(SR), FL0), mul2(splat2(SL), FR0)));
+    const F2 T1 = madd2(slsr, sub2(UR1, UL1), sub2(mul2(splat2(SR), FL1), mul2(splat2(SL), FR1)));
+#if NB_ARITH_FAST
+    const F2 inv = splat2(1.0f / den);
+    const F2 F0 = mul2(T0, inv), F1 = mul2(T1, inv);
+    return make_float4(lo(F0), hi(F0), lo(F1), hi(F1));
+#else
+    return make_float4(lo(T0) / den, hi(T0) / den, lo(T1) / den, hi(T1) / den);
+#endif
+}
+
+template <int SOLVER, int LIM, int AX>
+__device__ __forceinline__ float4 face_flux(const float4 qa, const float4 qb, const float4 qc, const float4 qd,
+                                            const float2 csb, const float2 csc, const float floor_) {
+#if NB_PAIRED
+    return face_flux_paired<SOLVER, LIM, AX>(qa, qb, qc, qd, csb, csc, floor_);
+#else
+    return face_flux_scalar<SOLVER, LIM, AX>(qa, qb, qc, qd, csb, csc, floor_);
+#endif
 }
 
 template <int TJ>
