@@ -109,6 +109,7 @@ __global__ void __launch_bounds__(256) apply_fuv_kernel(const NbConst* __restric
     __shared__ float4 st[NB_MAX_STARS];
     __shared__ float lum[NB_MAX_STARS];
     __shared__ int act[NB_MAX_STARS];
+    __shared__ float4 rowtab[8][NB_ROW_STARS];
     for (int s = threadIdx.y * blockDim.x + threadIdx.x; s < nstars; s += blockDim.x * blockDim.y) {
         st[s] = sw[s].w;
         lum[s] = sw[s].lum_f;
@@ -123,6 +124,9 @@ __global__ void __launch_bounds__(256) apply_fuv_kernel(const NbConst* __restric
     const RowWalk w(nx, ny, nz);
     if (!w.valid) return;
     const float px = ((float)w.i + 0.5f) * dx, py = ((float)w.j + 0.5f) * dx;
+    // per-row azimuth constants (star_row_table): the same values the per-cell form computes
+    float4* tab = nstars <= NB_ROW_STARS ? rowtab[threadIdx.y] : nullptr;
+    if (tab) star_row_table(st, act, nstars, px, py, nphi, 1, tab);
     for (int k = w.k0; k < nz; k += 32) {
         const long long q = w.base + k;
         const float pz = ((float)k + 0.5f) * dx;
@@ -130,18 +134,32 @@ __global__ void __launch_bounds__(256) apply_fuv_kernel(const NbConst* __restric
         for (int s = 0; s < nstars; ++s) {
             if (!act[s]) continue;
             const float4 sp = st[s];
-            const float rx = px - sp.x, ry = py - sp.y, rz = pz - sp.z;
-            const float r = fmaxr(sqrtf((rx * rx + ry * ry) + rz * rz), 1e-6f);     // 0 + x*x == x*x
+            const float rz = pz - sp.z;
+            float r, tp;
+            int pw[2];
+            if (tab) {
+                const float4 tb = tab[s];
+                r = fmaxr(sqrtf(tb.x + rz * rz), 1e-6f);                          // (rx^2 + ry^2) + rz^2
+                tp = tb.y;
+                pw[0] = __float_as_int(tb.z);
+                pw[1] = __float_as_int(tb.w);
+            } else {
+                const float rx = px - sp.x, ry = py - sp.y;
+                r = fmaxr(sqrtf((rx * rx + ry * ry) + rz * rz), 1e-6f);             // 0 + x*x == x*x
+                float phi = atan2f(ry, rx);
+                if (phi < 0.0f) phi = phi + two_pi;
+                const float fp = phi / two_pi * (float)nphi - 0.5f;
+                const int ip = (int)floorf(fp);
+                tp = fp - (float)ip;
+                pw[0] = wrap_index(ip, nphi);
+                pw[1] = wrap_index(ip + 1, nphi);
+            }
             const float u = rz / r;
-            float phi = atan2f(ry, rx);
-            if (phi < 0.0f) phi = phi + two_pi;
             const float fr = r / binr - 0.5f;
             const float fu = (u + 1.0f) * 0.5f * (float)nu - 0.5f;
-            const float fp = phi / two_pi * (float)nphi - 0.5f;
-            const int ir = (int)floorf(fr), iu = (int)floorf(fu), ip = (int)floorf(fp);
-            const float tr = fr - (float)ir, tu = fu - (float)iu, tp = fp - (float)ip;
+            const int ir = (int)floorf(fr), iu = (int)floorf(fu);
+            const float tr = fr - (float)ir, tu = fu - (float)iu;
             const float* as = att + (long long)s * nu * nphi * nr;
-            const int pw[2] = {wrap_index(ip, nphi), wrap_index(ip + 1, nphi)};
             float acc = 0.0f;
 #pragma unroll
             for (int aa = 0; aa < 2; ++aa)

@@ -133,10 +133,11 @@ __global__ void __launch_bounds__(256) cast_rays_batch_kernel(const NbRayJob* __
 }
 
 // nebula3d.py:273-307 rf_at + apply_front over one row (i, j), fused over the active stars,
-// with the fp16 store of the front distance (sim.py:942, 980-985).
+// with the fp16 store of the front distance (sim.py:942, 980-985).  `tab`: this warp's row
+// table (NB_ROW_STARS entries) or null for the per-cell form.
 __device__ __forceinline__ void apply_front_row(const NbConst& C, const float4* st, const int* act, int nstars,
                                                 const float* __restrict__ rfront, float* __restrict__ xi_raw,
-                                                void* __restrict__ dfront, bool half, int row) {
+                                                void* __restrict__ dfront, bool half, int row, float4* tab) {
     const int nx = C.nx, ny = C.ny, nz = C.nz, nu = C.nu, nphi = C.nphi;
     if (row >= nx * ny) return;
     const int i = row / ny, j = row - (row / ny) * ny;
@@ -145,6 +146,8 @@ __device__ __forceinline__ void apply_front_row(const NbConst& C, const float4* 
     const float two_pi = 2.0f * pi_f();
     const float px = ((float)i + 0.5f) * dx, py = ((float)j + 0.5f) * dx;
     const long long rstride = (long long)nu * nphi;
+    if (tab && nstars > NB_ROW_STARS) tab = nullptr;
+    if (tab) star_row_table(st, act, nstars, px, py, nphi, nu, tab);
     constexpr int SG = 4;                       // stars whose gathers are in flight together
     for (int k = threadIdx.x; k < nz; k += 32) {
         const long long q = base + k;
@@ -161,23 +164,35 @@ __device__ __forceinline__ void apply_front_row(const NbConst& C, const float4* 
                 g00[e] = g01[e] = g10[e] = g11[e] = 0.0f;
                 if (!on[e]) continue;
                 const float4 sp = st[s];
-                const float rx = px - sp.x, ry = py - sp.y, rz = pz - sp.z;
-                r[e] = fmaxr(sqrtf((rx * rx + ry * ry) + rz * rz), 1e-6f);     // 0 + x*x == x*x
-                const float u = rz / r[e];
-                float phi = atan2f(ry, rx);
-                if (phi < 0.0f) phi = phi + two_pi;
-                const float fu = (u + 1.0f) * 0.5f * (float)nu - 0.5f;
-                const float fp = phi / two_pi * (float)nphi - 0.5f;
-                const int iu = (int)floorf(fu), ip = (int)floorf(fp);
-                tu[e] = fu - (float)iu;
-                tp[e] = fp - (float)ip;
                 const float* rfs = rfront + (long long)s * rstride;
+                const float rz = pz - sp.z;
+                int c0, c1;                      // phi columns times nu (table [phi][u])
+                if (tab) {
+                    const float4 tb = tab[s];
+                    r[e] = fmaxr(sqrtf(tb.x + rz * rz), 1e-6f);                  // (rx^2 + ry^2) + rz^2
+                    tp[e] = tb.y;
+                    c0 = __float_as_int(tb.z);
+                    c1 = __float_as_int(tb.w);
+                } else {
+                    const float rx = px - sp.x, ry = py - sp.y;
+                    r[e] = fmaxr(sqrtf((rx * rx + ry * ry) + rz * rz), 1e-6f);     // 0 + x*x == x*x
+                    float phi = atan2f(ry, rx);
+                    if (phi < 0.0f) phi = phi + two_pi;
+                    const float fp = phi / two_pi * (float)nphi - 0.5f;
+                    const int ip = (int)floorf(fp);
+                    tp[e] = fp - (float)ip;
+                    c0 = wrap_index(ip, nphi) * nu;
+                    c1 = wrap_index(ip + 1, nphi) * nu;
+                }
+                const float u = rz / r[e];
+                const float fu = (u + 1.0f) * 0.5f * (float)nu - 0.5f;
+                const int iu = (int)floorf(fu);
+                tu[e] = fu - (float)iu;
                 const int u0 = iclampd(iu, 0, nu - 1), u1 = iclampd(iu + 1, 0, nu - 1);
-                const int p0 = wrap_index(ip, nphi), p1 = wrap_index(ip + 1, nphi);
-                g00[e] = __ldg(rfs + p0 * nu + u0);      // table [phi][u]
-                g01[e] = __ldg(rfs + p1 * nu + u0);
-                g10[e] = __ldg(rfs + p0 * nu + u1);
-                g11[e] = __ldg(rfs + p1 * nu + u1);
+                g00[e] = __ldg(rfs + c0 + u0);
+                g01[e] = __ldg(rfs + c1 + u0);
+                g10[e] = __ldg(rfs + c0 + u1);
+                g11[e] = __ldg(rfs + c1 + u1);
             }
 #pragma unroll
             for (int e = 0; e < SG; ++e) {
@@ -215,22 +230,25 @@ __device__ __forceinline__ int load_stars(const NbStarW* sw, int nstars, float4*
 }
 
 template <bool HALF>
-__global__ void __launch_bounds__(256) apply_front_kernel(const NbConst* __restrict__ c,
+__global__ void __launch_bounds__(256, 3) apply_front_kernel(const NbConst* __restrict__ c,
                                                           const NbStarW* __restrict__ sw,
                                                           const float* __restrict__ rfront, int nstars,
                                                           float* __restrict__ xi_raw, void* __restrict__ dfront,
                                                           unsigned* smax_reset) {
     __shared__ float4 st[NB_MAX_STARS];
     __shared__ int act[NB_MAX_STARS];
+    __shared__ float4 tab[8][NB_ROW_STARS];
     const int tlin = load_stars(sw, nstars, st, act);
     if (smax_reset && blockIdx.x == 0 && tlin == 0) *smax_reset = 0u;
-    apply_front_row(*c, st, act, nstars, rfront, xi_raw, dfront, HALF, blockIdx.x * blockDim.y + threadIdx.y);
+    apply_front_row(*c, st, act, nstars, rfront, xi_raw, dfront, HALF, blockIdx.x * blockDim.y + threadIdx.y,
+                    tab[threadIdx.y]);
 }
 
 // Rows of every listed instance; job e owns blocks [job[e].blk0, job[e+1].blk0) (8 rows each).
 __global__ void __launch_bounds__(256) apply_front_batch_kernel(const NbRayJob* __restrict__ jobs, int n_jobs) {
     __shared__ float4 st[NB_MAX_STARS];
     __shared__ int act[NB_MAX_STARS];
+    __shared__ float4 tab[8][NB_ROW_STARS];
     int lo = 0, hi = n_jobs - 1;
     while (lo < hi) {
         const int mid = (lo + hi + 1) >> 1;
@@ -240,7 +258,8 @@ __global__ void __launch_bounds__(256) apply_front_batch_kernel(const NbRayJob* 
     const int lb = (int)(blockIdx.x - J.blk0);
     const int tlin = load_stars(J.sw, J.nstars, st, act);
     if (lb == 0 && tlin == 0) *J.smax = 0u;
-    apply_front_row(*J.c, st, act, J.nstars, J.rfront, J.xi_raw, J.dfront, J.half != 0, lb * blockDim.y + threadIdx.y);
+    apply_front_row(*J.c, st, act, J.nstars, J.rfront, J.xi_raw, J.dfront, J.half != 0, lb * blockDim.y + threadIdx.y,
+                    tab[threadIdx.y]);
 }
 
 // nebula3d.py:310-315 smooth_xi (+ sim.py:941 copy back) of one row, then the CFL max speed

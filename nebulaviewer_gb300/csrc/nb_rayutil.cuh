@@ -98,3 +98,27 @@ __device__ __forceinline__ float nb_shock_at(const NbConst& C, const float* __re
     const float div = (du + dv + dw) / (2.0f * C.dx);
     return fmaxr(-div, 0.0f) * at(rho, i, j, k);
 }
+
+// Per-row star constants.  Seen from a star, the cells of one (i, j) row differ only in z: the
+// azimuth atan2(ry, rx) of rf_at (nebula3d.py:273-278) / apply_fuv (nebula3d.py:365-368), its
+// table column and interpolation weight, and rx^2 + ry^2 are the same for the whole row.  A warp
+// (one row) evaluates them once per star, with the same float operations as the per-cell form,
+// so every cell sees the same values.  Entry: (rx^2 + ry^2, phi weight, column p0, column p1).
+constexpr int NB_ROW_STARS = 32;                 // stars a row table holds (more: per-cell form)
+
+__device__ __forceinline__ void star_row_table(const float4* st, const int* act, int nstars, float px, float py,
+                                               int nphi, int colmul, float4* tab) {
+    const float two_pi = 2.0f * pi_f();
+    for (int s = threadIdx.x; s < nstars; s += 32) {
+        if (!act[s]) continue;
+        const float4 sp = st[s];
+        const float rx = px - sp.x, ry = py - sp.y;
+        float phi = atan2f(ry, rx);
+        if (phi < 0.0f) phi = phi + two_pi;
+        const float fp = phi / two_pi * (float)nphi - 0.5f;
+        const int ip = (int)floorf(fp);
+        tab[s] = make_float4(rx * rx + ry * ry, fp - (float)ip, __int_as_float(wrap_index(ip, nphi) * colmul),
+                             __int_as_float(wrap_index(ip + 1, nphi) * colmul));
+    }
+    __syncwarp();
+}
