@@ -648,9 +648,9 @@ NB_EXPORT int nb_fuv(nb_handle h) {
         CK(h, nb_launch_weights(h->c, h->st, h->stars, h->sw, h->nstars, h->stream));
     }
     if (h->nstars > 0) {
-        Prof pf(h, NB_PROF_CAST_FUV, 1);
+        Prof pf(h, NB_PROF_CAST_FUV, 2);                // the (rho, xi) pack into stage planes 0-1 + the rays
         CK(h, nb_launch_cast_fuv(h->c, h->sw, h->dirs_fuv, h->d.f.rho, h->d.f.xi, h->att, h->nstars, h->fuv_group,
-                                 nullptr, 0, h->stream, h->d.fnu, h->d.fnphi));
+                                 nullptr, 0, h->stream, h->d.fnu, h->d.fnphi, plane(h, 0), h->ncell));
     }
     if (h->hc.plane_on) {
         Prof pf(h, NB_PROF_CAST_FUV, 1);
@@ -709,7 +709,7 @@ NB_EXPORT int nb_cast_fuv(nb_handle h, const double xyz[3], float* att_out) {
     float s3[4] = {(float)xyz[0], (float)xyz[1], (float)xyz[2], 0.f};
     CK(h, cudaMemcpyAsync(h->scratch3, s3, sizeof(s3), cudaMemcpyHostToDevice, h->stream));
     CK(h, nb_launch_cast_fuv(h->c, h->sw, h->dirs_fuv, h->d.f.rho, h->d.f.xi, att_out, 1, 32, h->scratch3, 1,
-                             h->stream, h->d.fnu, h->d.fnphi));
+                             h->stream, h->d.fnu, h->d.fnphi, plane(h, 0), h->ncell));
     CK(h, cudaStreamSynchronize(h->stream));
     return NB_OK;
 }

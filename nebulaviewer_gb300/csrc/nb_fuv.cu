@@ -5,7 +5,8 @@
 //
 // GB300 design: cast_fuv marches a ray with a group of G lanes, the optical depth being an
 // inclusive group scan over a Kahan-compensated carry; a lane that crosses into new radial
-// bins writes them.  All rays of all active stars are one launch, into one attenuation grid
+// bins writes them.  Density and ionized fraction are sampled at the same corners, so they
+// are first packed as (rho, xi) pairs into free scratch: one 8-byte gather per corner.  All rays of all active stars are one launch, into one attenuation grid
 // per star laid out [star][u][phi][r] (r fastest: a ray's bins are contiguous).  apply_fuv
 // then accumulates every active star for a cell in one register, in the reference's star
 // order (so the float32 sum is the reference's), and stores G0 once as fp16.
@@ -13,10 +14,16 @@
 
 namespace {
 
+__global__ void __launch_bounds__(256) pack_rx_kernel(const float* __restrict__ rho, const float* __restrict__ xi,
+                                                      float2* __restrict__ rx, long long n) {
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x)
+        rx[q] = make_float2(rho[q], xi[q]);
+}
+
 template <int G, bool REF_LAYOUT>
 __global__ void __launch_bounds__(256) cast_fuv_kernel(const NbConst* __restrict__ c, const NbStarW* __restrict__ sw,
                                                        const float4* __restrict__ dirs,
-                                                       const float* __restrict__ rho, const float* __restrict__ xi,
+                                                       const float2* __restrict__ rx,
                                                        float* __restrict__ att, int nstars,
                                                        const float* star_override) {
     const int nr = c->fnr, nu = c->fnu, nphi = c->fnphi, nray = nu * nphi;
@@ -60,9 +67,8 @@ __global__ void __launch_bounds__(256) cast_fuv_kernel(const NbConst* __restrict
         int nb = ib;
         if (valid) {
             const float qx = sx + d.x * r, qy = sy + d.y * r, qz = sz + d.z * r;
-            const float n_tot = sample_n(rho, nx, ny, nz, qx, qy, qz, dx, inv_dx, pow2);
-            const float x_i = sample_n(xi, nx, ny, nz, qx, qy, qz, dx, inv_dx, pow2);
-            dtau = kappa * n_tot * (1.0f - 0.92f * x_i) * dr;
+            const float2 nx_i = sample_n2(rx, nx, ny, nz, qx, qy, qz, dx, inv_dx, pow2);   // (n_tot, x_i)
+            dtau = kappa * nx_i.x * (1.0f - 0.92f * nx_i.y) * dr;
             nb = trunc_i(r / binr);
         }
         float incl = dtau;
@@ -131,8 +137,16 @@ __global__ void __launch_bounds__(256) apply_fuv_kernel(const NbConst* __restric
         const long long q = w.base + k;
         const float pz = ((float)k + 0.5f) * dx;
         float g = 0.0f;
-        for (int s = 0; s < nstars; ++s) {
-            if (!act[s]) continue;
+        constexpr int SG = 2;                    // stars whose gathers are in flight together
+        for (int s0 = 0; s0 < nstars; s0 += SG) {
+          float term[SG];
+          bool on[SG];
+#pragma unroll
+          for (int e = 0; e < SG; ++e) {
+            const int s = s0 + e;
+            on[e] = s < nstars && act[s];
+            term[e] = 0.0f;
+            if (!on[e]) continue;
             const float4 sp = st[s];
             const float rz = pz - sp.z;
             float r, tp;
@@ -173,7 +187,11 @@ __global__ void __launch_bounds__(256) apply_fuv_kernel(const NbConst* __restric
                         acc = acc + wgt * __ldg(as + ((long long)uu * nphi + pw[cc]) * nr + rr);
                     }
             const float r2 = fmaxr(r * r, 0.0004f);
-            g = g + lum[s] * acc / r2;
+            term[e] = lum[s] * acc / r2;
+          }
+#pragma unroll
+          for (int e = 0; e < SG; ++e)
+            if (on[e]) g = g + term[e];                 // the reference's star order
         }
         if (C_plane_on) g = g + __ldg(C_plane_g0 + q);      // the -x plane source, after the stars
         if (HALF)
@@ -212,10 +230,15 @@ cudaError_t nb_launch_plane_fuv(const NbConst* c, const float* rho, const float*
 
 cudaError_t nb_launch_cast_fuv(const NbConst* c, const NbStarW* sw, const float4* dirs, const float* rho,
                                const float* xi, float* att, int nstars, int group, const float* star_override,
-                               int ref_layout, cudaStream_t s, int fnu, int fnphi) {
+                               int ref_layout, cudaStream_t s, int fnu, int fnphi, void* rx_scratch, long long ncell) {
+    float2* rx = static_cast<float2*>(rx_scratch);
+    {
+        const long long b = (ncell + 255) / 256;
+        pack_rx_kernel<<<(int)(b < 152LL * 16 ? (b < 1 ? 1 : b) : 152LL * 16), 256, 0, s>>>(rho, xi, rx, ncell);
+    }
     const long long threads = (long long)fnu * fnphi * nstars * group;
     const int blocks = (int)((threads + 255) / 256);
-#define NB_FUV_LAUNCH(G, R) cast_fuv_kernel<G, R><<<blocks, 256, 0, s>>>(c, sw, dirs, rho, xi, att, nstars, star_override)
+#define NB_FUV_LAUNCH(G, R) cast_fuv_kernel<G, R><<<blocks, 256, 0, s>>>(c, sw, dirs, rx, att, nstars, star_override)
     if (ref_layout) {
         NB_FUV_LAUNCH(32, true);
     } else {

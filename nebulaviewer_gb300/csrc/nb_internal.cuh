@@ -223,9 +223,10 @@ cudaError_t nb_launch_ionize_batch(const NbRayJob* jobs, int n_jobs, long long n
 cudaError_t nb_launch_plane_front(const NbConst* c, const float* rho, float* xf, int ny, int nz, cudaStream_t s);
 cudaError_t nb_launch_plane_fuv(const NbConst* c, const float* rho, const float* xi, float* g, int ny, int nz,
                                 cudaStream_t s);
+// packs (rho, xi) pairs into rx_scratch (ncell float2, 8-byte aligned) first
 cudaError_t nb_launch_cast_fuv(const NbConst* c, const NbStarW* sw, const float4* dirs, const float* rho,
                                const float* xi, float* att, int nstars, int group, const float* star_override,
-                               int ref_layout, cudaStream_t s, int fnu, int fnphi);
+                               int ref_layout, cudaStream_t s, int fnu, int fnphi, void* rx_scratch, long long ncell);
 cudaError_t nb_launch_apply_fuv(const NbConst* c, const NbStarW* sw, const float* att, int nstars, void* g0,
                                 cudaStream_t s, int nx, int ny, int half);
 cudaError_t nb_launch_pack(const NbConst* c, const float* rho, const float* mx, const float* my, const float* mz,

@@ -32,6 +32,42 @@ __device__ __forceinline__ float sample_n(const float* __restrict__ a, int nx, i
     return c0 + (c1 - c0) * fz;
 }
 
+// sample_n of two fields stored interleaved ((rho, xi) pairs): the same corners, weights and
+// float operations per field as two sample_n calls, with one 8-byte load per corner.
+__device__ __forceinline__ float2 sample_n2(const float2* __restrict__ a, int nx, int ny, int nz, float px, float py,
+                                           float pz, float dx, float inv_dx, bool pow2) {
+    const float gx = (pow2 ? px * inv_dx : px / dx) - 0.5f;
+    const float gy = (pow2 ? py * inv_dx : py / dx) - 0.5f;
+    const float gz = (pow2 ? pz * inv_dx : pz / dx) - 0.5f;
+    if (gx < -0.5f || gy < -0.5f || gz < -0.5f) return make_float2(0.0f, 0.0f);
+    if (gx > (float)nx - 0.5f || gy > (float)ny - 0.5f || gz > (float)nz - 0.5f) return make_float2(0.0f, 0.0f);
+    const int i0 = (int)floorf(gx), j0 = (int)floorf(gy), k0 = (int)floorf(gz);
+    const float fx = gx - (float)i0, fy = gy - (float)j0, fz = gz - (float)k0;
+    const int ia = iclampd(i0, 0, nx - 1), ib = iclampd(i0 + 1, 0, nx - 1);
+    const int ja = iclampd(j0, 0, ny - 1), jb = iclampd(j0 + 1, 0, ny - 1);
+    const int ka = iclampd(k0, 0, nz - 1), kb = iclampd(k0 + 1, 0, nz - 1);
+    const long long sa = (long long)ia * ny, sb = (long long)ib * ny;
+    const float2 c000 = __ldg(a + (sa + ja) * nz + ka), c100 = __ldg(a + (sb + ja) * nz + ka);
+    const float2 c010 = __ldg(a + (sa + jb) * nz + ka), c110 = __ldg(a + (sb + jb) * nz + ka);
+    const float2 c001 = __ldg(a + (sa + ja) * nz + kb), c101 = __ldg(a + (sb + ja) * nz + kb);
+    const float2 c011 = __ldg(a + (sa + jb) * nz + kb), c111 = __ldg(a + (sb + jb) * nz + kb);
+    float out[2];
+#pragma unroll
+    for (int f = 0; f < 2; ++f) {
+        const float v000 = f ? c000.y : c000.x, v100 = f ? c100.y : c100.x, v010 = f ? c010.y : c010.x;
+        const float v110 = f ? c110.y : c110.x, v001 = f ? c001.y : c001.x, v101 = f ? c101.y : c101.x;
+        const float v011 = f ? c011.y : c011.x, v111 = f ? c111.y : c111.x;
+        const float c00 = v000 + (v100 - v000) * fx;
+        const float c10 = v010 + (v110 - v010) * fx;
+        const float c01 = v001 + (v101 - v001) * fx;
+        const float c11 = v011 + (v111 - v011) * fx;
+        const float c0 = c00 + (c10 - c00) * fy;
+        const float c1 = c01 + (c11 - c01) * fy;
+        out[f] = c0 + (c1 - c0) * fz;
+    }
+    return make_float2(out[0], out[1]);
+}
+
 // nebula3d.py:229-244 box_range
 __device__ __forceinline__ void nb_box_range(float ox, float oy, float oz, float dxr, float dyr, float dzr, const float* bmax,
                              float& t0, float& t1) {
