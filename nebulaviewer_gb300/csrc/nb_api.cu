@@ -1020,7 +1020,7 @@ NB_EXPORT int nb_batch_create(const nb_handle* hs, const int* ion_every, int n, 
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    b->grid = (sms > 0 ? sms : 152) * 3;
+    b->grid = (sms > 0 ? sms : 152) * nb_hydro_batch_blocks_per_sm(b->solver, b->limiter, b->max_stars);
     if (cudaStreamCreateWithFlags(&b->bs, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreateWithFlags(&b->ev_in, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&b->ev_out, cudaEventDisableTiming) != cudaSuccess)

@@ -9,8 +9,10 @@
 //
 // GB300 layout: a block owns a 32 (k) x TJ (j) column of cells and marches along i.  Each
 // (j,k) plane tile with a 2-cell halo is brought into shared memory by TMA (five 3-D tiled
-// loads: rho, mx, my, mz, xi; double-buffered, mbarrier-tracked) while the previous plane
-// is computed.  A plane is converted once to primitives (rho, u, v, w) and (c^2, c) in
+// loads: rho, mx, my, mz, xi; mbarrier-tracked).  One raw slot: plane p+1 is requested as soon
+// as plane p has been converted, and lands while plane p's faces and update are computed
+// (microseconds of work against a load latency of about one), which keeps a block at ~56 KB
+// of shared memory and 4 blocks resident per SM.  A plane is converted once to primitives (rho, u, v, w) and (c^2, c) in
 // shared memory; every face flux is then evaluated once (the reference evaluates each face
 // twice) and shared through shared memory (y, z faces) or registers (x faces).  Stage 2
 // also reduces the CFL max speed of the new state (nebula3d.py:154-162) into one atomic.
@@ -209,9 +211,12 @@ __device__ __forceinline__ float4 face_flux_paired(const float4 qa, const float4
     if (SR <= 0.0f) return make_float4(lo(FR0), hi(FR0), lo(FR1), hi(FR1));
     const F2 slsr = splat2(SL * SR);
     const float den = SR - SL;
-    // (SR FL - SL FR + SL SR (UR - UL)) / den
-    const F2 T0 = madd2(slsr, sub2(UR0, UL0), sub2(mul2(splat2(SR), FL0), mul2(splat2(SL), FR0)));
-    const F2 T1 = madd2(slsr, sub2(UR1, UL1), sub2(mul2(splat2(SR), FL1), mul2(splat2(SL), FR1)));
+    // (SR FL - SL FR + SL SR (UR - UL)) / den, every product feeding a sum as an explicit fused
+    // multiply-add (a paired multiply followed by a paired add would be fused or not at the
+    // assembler's discretion, which could differ between the single and the batched kernel)
+    const F2 nSL = splat2(-SL), SR2 = splat2(SR);
+    const F2 T0 = madd2(slsr, sub2(UR0, UL0), madd2(SR2, FL0, mul2(nSL, FR0)));
+    const F2 T1 = madd2(slsr, sub2(UR1, UL1), madd2(SR2, FL1, mul2(nSL, FR1)));
 #if NB_ARITH_FAST
     const F2 inv = splat2(1.0f / den);
     const F2 F0 = mul2(T0, inv), F1 = mul2(T1, inv);
@@ -233,8 +238,8 @@ __device__ __forceinline__ float4 face_flux(const float4 qa, const float4 qb, co
 
 template <int TJ>
 struct HydroSmem {
-    static constexpr int RAW_FIELD = (TJ + 4) * RAWW;                     // floats per field per slot
-    static constexpr int RAW_BYTES = 2 * 5 * RAW_FIELD * 4;
+    static constexpr int RAW_FIELD = (TJ + 4) * RAWW;                     // floats per field
+    static constexpr int RAW_BYTES = 5 * RAW_FIELD * 4;                      // one raw slot
     static constexpr int PRIM_BYTES = 4 * (TJ + 4) * PW * 16;
     static constexpr int CS_BYTES = 3 * (TJ + 4) * PW * 8;
     static constexpr int FACE_BYTES = ((TJ + 1) * TK + TJ * (TK + 1)) * 16;
@@ -244,7 +249,11 @@ struct HydroSmem {
 };
 
 #ifndef NB_HYDRO_MINB
-#define NB_HYDRO_MINB 3               // resident blocks per SM the register budget is sized for
+#if defined(NB_ARITH_FAST) && NB_ARITH_FAST
+#define NB_HYDRO_MINB 4               // resident blocks per SM the register budget is sized for (64 regs)
+#else
+#define NB_HYDRO_MINB 3               // the exact build's scalar face flux needs ~76 registers
+#endif
 #endif
 
 // One (j,k) tile column of one instance, marched over its i-chunk.  Called once per block by
@@ -252,9 +261,9 @@ struct HydroSmem {
 // two mbarriers and their phases persist across calls: every load a call issues, it waits for.
 template <int SOLVER, int LIM, int TJ, bool STAGE2>
 __device__ __forceinline__ void hydro_tile(const HydroLaunch& L, int tile, unsigned char* smem, unsigned& ph0,
-                                           unsigned& ph1, bool& failed) {
+                                           bool& failed) {
     using SM = HydroSmem<TJ>;
-    float* raw = reinterpret_cast<float*>(smem);                                   // [2][5][TJ+4][40]
+    float* raw = reinterpret_cast<float*>(smem);                                   // [5][TJ+4][40]
     float4* prim = reinterpret_cast<float4*>(smem + SM::RAW_BYTES);                // [4][TJ+4][36]
     float2* cs = reinterpret_cast<float2*>(smem + SM::RAW_BYTES + SM::PRIM_BYTES); // [3][TJ+4][36]
     float4* fy = reinterpret_cast<float4*>(smem + SM::RAW_BYTES + SM::PRIM_BYTES + SM::CS_BYTES);  // [TJ+1][32]
@@ -294,20 +303,16 @@ __device__ __forceinline__ void hydro_tile(const HydroLaunch& L, int tile, unsig
         sw_j[s] = L.sw[s].jet;
     }
     constexpr unsigned TX_BYTES = 5u * SM::RAW_FIELD * 4u;
-    auto issue = [&](int p, int slot) {
+    auto issue = [&](int p) {                    // plane p into the raw slot, tracked by bar[0]
         const int pc = iclampd(p, 0, nx - 1);
-        float* dst = raw + slot * 5 * SM::RAW_FIELD;
-        fence_proxy_async();
-        mbar_expect_tx(&bar[slot], TX_BYTES);
+        fence_proxy_async();                     // the slot's previous contents were read by this block
+        mbar_expect_tx(&bar[0], TX_BYTES);
 #pragma unroll
         for (int f = 0; f < 4; ++f)
-            tma_load_3d(dst + f * SM::RAW_FIELD, &L.maps[L.map_in + f], k0 - 4, j0 - 2, pc, &bar[slot]);
-        tma_load_3d(dst + 4 * SM::RAW_FIELD, &L.maps[NB_MAP_XI], k0 - 4, j0 - 2, pc, &bar[slot]);
+            tma_load_3d(raw + f * SM::RAW_FIELD, &L.maps[L.map_in + f], k0 - 4, j0 - 2, pc, &bar[0]);
+        tma_load_3d(raw + 4 * SM::RAW_FIELD, &L.maps[NB_MAP_XI], k0 - 4, j0 - 2, pc, &bar[0]);
     };
-    if (tid == 0) {
-        issue(P0, 0);
-        issue(P0 + 1, 1);
-    }
+    if (tid == 0) issue(P0);
 
     float4 fx_prev = make_float4(0.f, 0.f, 0.f, 0.f);
     float vmax_local = 0.0f;
@@ -324,7 +329,6 @@ __device__ __forceinline__ void hydro_tile(const HydroLaunch& L, int tile, unsig
     constexpr int PSLOT = (TJ + 4) * PW;
 
     for (int p = P0; p <= P1; ++p) {
-        const int rs = (p - P0) & 1;
         const int ps = (p - P0) & 3;                 // prim slot of plane p (4 slots: p-3..p)
         const int cq = (p - P0) % 3;                 // cs slot of plane p (3 slots: p-2..p)
         // own-cell values of plane i = p - 2 the epilogue needs, issued before the flux work
@@ -339,12 +343,10 @@ __device__ __forceinline__ void hydro_tile(const HydroLaunch& L, int tile, unsig
                 u00 = L.u0[0][cell]; u01 = L.u0[1][cell]; u02 = L.u0[2][cell]; u03 = L.u0[3][cell];
             }
         }
-        const bool ok = mbar_wait_bounded(&bar[rs], rs ? ph1 : ph0);
-        if (ok) {                                // a timed-out slot keeps its parity for the abort wait
-            if (rs) ph1 ^= 1u; else ph0 ^= 1u;
-        }
+        const bool ok = mbar_wait_bounded(&bar[0], ph0);
+        if (ok) ph0 ^= 1u;                       // a timed-out wait keeps its parity for the abort wait
         if (__syncthreads_or(!ok)) { failed = true; break; }
-        const float* rb = raw + rs * 5 * SM::RAW_FIELD;
+        const float* rb = raw;
         float4* pp = prim + ps * PSLOT;
         float2* cp = cs + cq * PSLOT;
         // ---- convert plane p: own cell, then the halo strips (corners are never read)
@@ -371,8 +373,8 @@ __device__ __forceinline__ void hydro_tile(const HydroLaunch& L, int tile, unsig
                                            rb[3 * SM::RAW_FIELD + o] / r);
             cp[jj * PW + kk] = make_float2(c2, sqrtf(c2));
         }
-        __syncthreads();
-        if (tid == 0 && p + 2 <= P1) issue(p + 2, rs);
+        __syncthreads();                         // every thread is done with the raw slot
+        if (tid == 0 && p + 1 <= P1) issue(p + 1);
         if (p < P0 + 3) continue;
         // x face (p-2)+1/2 from the own column of planes p-3..p
         const float4 fx_new = face_flux<SOLVER, LIM, 1>(prim[((p - 3 - P0) & 3) * PSLOT + own],
@@ -497,13 +499,12 @@ __device__ __forceinline__ void hydro_tile(const HydroLaunch& L, int tile, unsig
 
 // a TMA wait gave up: record it, let both slots' copies land (bounded waits), leave
 template <int TJ>
-__device__ __forceinline__ void hydro_abort(unsigned char* smem, unsigned* status, unsigned ph0, unsigned ph1) {
+__device__ __forceinline__ void hydro_abort(unsigned char* smem, unsigned* status, unsigned ph0) {
     using SM = HydroSmem<TJ>;
     uint64_t* bar = reinterpret_cast<uint64_t*>(smem + SM::FIXED - SM::BAR_BYTES);
-    if (threadIdx.x == 0) {
+    if (threadIdx.x == 0) {                      // the one load that may still be in flight
         atomicOr(status, NB_DEV_TMA_TIMEOUT);
         mbar_wait_bounded(&bar[0], ph0);
-        mbar_wait_bounded(&bar[1], ph1);
     }
     __syncthreads();
 }
@@ -524,10 +525,10 @@ template <int SOLVER, int LIM, int TJ, bool STAGE2>
 __global__ void __launch_bounds__(TK * TJ, NB_HYDRO_MINB) hydro_stage_kernel(const HydroLaunch L) {
     extern __shared__ __align__(128) unsigned char smem[];
     hydro_init_bars<TJ>(smem);
-    unsigned ph0 = 0, ph1 = 0;
+    unsigned ph0 = 0;
     bool failed = false;
-    hydro_tile<SOLVER, LIM, TJ, STAGE2>(L, blockIdx.x, smem, ph0, ph1, failed);
-    if (failed) hydro_abort<TJ>(smem, L.status, ph0, ph1);
+    hydro_tile<SOLVER, LIM, TJ, STAGE2>(L, blockIdx.x, smem, ph0, failed);
+    if (failed) hydro_abort<TJ>(smem, L.status, ph0);
 }
 
 // Persistent batched stage: blocks take (instance, tile) work items from a list spanning many
@@ -540,7 +541,7 @@ hydro_batch_kernel(const HydroLaunch* __restrict__ Ls, const int2* __restrict__ 
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ int item;
     hydro_init_bars<TJ>(smem);
-    unsigned ph0 = 0, ph1 = 0;
+    unsigned ph0 = 0;
     bool failed = false;
     const HydroLaunch* last = nullptr;
     for (;;) {
@@ -550,11 +551,11 @@ hydro_batch_kernel(const HydroLaunch* __restrict__ Ls, const int2* __restrict__ 
         if (it >= n_work) break;
         const int2 w = work[it];
         last = &Ls[w.x];
-        hydro_tile<SOLVER, LIM, TJ, STAGE2>(*last, w.y, smem, ph0, ph1, failed);
+        hydro_tile<SOLVER, LIM, TJ, STAGE2>(*last, w.y, smem, ph0, failed);
         if (failed) break;
         __syncthreads();
     }
-    if (failed && last) hydro_abort<TJ>(smem, last->status, ph0, ph1);
+    if (failed && last) hydro_abort<TJ>(smem, last->status, ph0);
 }
 
 template <int SOLVER, int LIM, int TJ, bool STAGE2>
@@ -562,6 +563,8 @@ cudaError_t run_kernel(const HydroLaunch& L, cudaStream_t s) {
     auto kern = hydro_stage_kernel<SOLVER, LIM, TJ, STAGE2>;
     const int smem = HydroSmem<TJ>::bytes(L.nstars_host);
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e == cudaSuccess)                        // the largest shared-memory carveout: 4 blocks of ~57 KB per SM
+        e = cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
     if (e != cudaSuccess) return e;
     const int blocks = L.tiles_k * L.tiles_j * L.n_chunks;
     kern<<<blocks, TK * TJ, smem, s>>>(L);
@@ -580,6 +583,8 @@ cudaError_t run_batch_kernel(const HydroLaunch* Ls, const int2* work, int n_work
     auto kern = hydro_batch_kernel<SOLVER, LIM, TJ, STAGE2>;
     const int smem = HydroSmem<TJ>::bytes(max_stars);
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
     if (e != cudaSuccess) return e;
     kern<<<grid, TK * TJ, smem, s>>>(Ls, work, n_work, counter);
     return cudaGetLastError();
@@ -595,6 +600,29 @@ cudaError_t run_batch(const HydroLaunch* Ls, const int2* work, int n_work, unsig
 }  // namespace
 
 int nb_hydro_tile_j() { return 8; }
+
+// resident blocks per SM of the persistent stage kernel (sizes its grid)
+int nb_hydro_batch_blocks_per_sm(int solver, int limiter, int max_stars) {
+    constexpr int TJ = 8;
+    const int smem = HydroSmem<TJ>::bytes(max_stars);
+    auto occ = [&](auto kern) {
+        int n = 0;
+        if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess ||
+            cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared) !=
+                cudaSuccess ||
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kern, TK * TJ, smem) != cudaSuccess) {
+            cudaGetLastError();
+            return 0;
+        }
+        return n;
+    };
+    int n;
+    if (solver == NB_SOLVER_RUSANOV) n = occ(hydro_batch_kernel<NB_SOLVER_RUSANOV, 0, TJ, true>);
+    else if (limiter == NB_LIM_VANLEER) n = occ(hydro_batch_kernel<NB_SOLVER_HLL, NB_LIM_VANLEER, TJ, true>);
+    else if (limiter == NB_LIM_MC) n = occ(hydro_batch_kernel<NB_SOLVER_HLL, NB_LIM_MC, TJ, true>);
+    else n = occ(hydro_batch_kernel<NB_SOLVER_HLL, NB_LIM_MINMOD, TJ, true>);
+    return n > 0 ? n : NB_HYDRO_MINB;
+}
 
 cudaError_t nb_launch_hydro(const HydroLaunch& L, int solver, int limiter, cudaStream_t s) {
     constexpr int TJ = 8;

@@ -1,6 +1,8 @@
 """Serving with continuous batching: requests branch from device snapshots, are admitted as
-slots / HBM budget free up, overlap on the device in one batch, and each result is the same
-(bit-identical) as running the request alone."""
+slots / HBM budget free up, overlap on the device in one batch, and each result is the same as
+running the request alone: bit-identical with the exact build; within the path's tolerance
+(rel-L_inf 1e-5) with the fast build, whose batched and single-instance kernels may contract
+multiply-adds differently."""
 import numpy as np
 import pytest
 
@@ -8,8 +10,8 @@ torch = pytest.importorskip("torch")
 pytestmark = pytest.mark.gpu
 
 
-@pytest.fixture(scope="module")
-def env():
+@pytest.fixture(scope="module", params=("exact", "fast"))
+def env(request):
     from nebulaviewer_gb300 import build
     build.build(verbose=False)
     from nebulaviewer_gb300 import ics, serve, sim
@@ -18,16 +20,24 @@ def env():
     snaps = []
     for ic in bases:
         s = sim.Sim.from_state(ic["shape"], ic["dx"], ic["rho"], ic["stars"], ic["kinds"], ic["jets"], ic["jkinds"],
-                               ic["P"], mom=ic["mom"], rays=(64, 128), fuv_grid=(16, 16, 32))
+                               ic["P"], mom=ic["mom"], rays=(64, 128), fuv_grid=(16, 16, 32), arith=request.param)
         s.step(4)
         snaps.append(serve.Snapshot(s))
         s.close()
     return serve, snaps
 
 
+def _close(a, b, exact):
+    if exact:
+        return torch.equal(a, b)
+    a, b = a.double(), b.double()
+    return float((a - b).abs().max()) <= 1e-5 * max(float(b.abs().max()), 1e-30)
+
+
 @pytest.mark.parametrize("slots,budget_cells", ((3, None), (8, 2 * 32 * 40 * 24)))
 def test_served_results_equal_alone(env, slots, budget_cells):
     serve, snaps = env
+    exact = snaps[0].arith == "exact"
     reqs = serve.poisson_requests(snaps, 8, rate=1000.0, seed=slots, steps=(3, 9))
     budget = 1e12 if budget_cells is None else 48.0 * budget_cells
     srv = serve.Server(snaps, budget_bytes=budget, max_slots=slots, keep_state=True)
@@ -36,10 +46,14 @@ def test_served_results_equal_alone(env, slots, budget_cells):
     assert stats["batch_rebuilds"] > 1                    # admissions happened while others ran
     for r in done:
         ref = serve.run_alone(snaps[r.snap], r)
-        assert r.result["t"] == ref["t"] and r.result["it"] == ref["it"]
+        assert r.result["it"] == ref["it"]
+        assert r.result["t"] == ref["t"] if exact else abs(r.result["t"] - ref["t"]) <= 1e-6 * ref["t"]
         for a, b in zip(r.result["state"], ref["state"]):
-            assert torch.equal(a, b)
-        assert r.result["totals"] == ref["totals"]
+            assert _close(a, b, exact)
+        if exact:
+            assert r.result["totals"] == ref["totals"]
+        else:
+            assert all(abs(x - y) <= 1e-6 * max(abs(y), 1e-30) + 1e-9 for x, y in zip(r.result["totals"], ref["totals"]))
 
 
 def test_snapshot_branch_resumes_the_state(env):
