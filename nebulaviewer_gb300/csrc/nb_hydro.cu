@@ -249,11 +249,7 @@ struct HydroSmem {
 };
 
 #ifndef NB_HYDRO_MINB
-#if defined(NB_ARITH_FAST) && NB_ARITH_FAST
 #define NB_HYDRO_MINB 4               // resident blocks per SM the register budget is sized for (64 regs)
-#else
-#define NB_HYDRO_MINB 3               // the exact build's scalar face flux needs ~76 registers
-#endif
 #endif
 
 // One (j,k) tile column of one instance, marched over its i-chunk.  Called once per block by
