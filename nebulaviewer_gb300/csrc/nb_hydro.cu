@@ -406,18 +406,30 @@ __device__ __forceinline__ void hydro_tile(const HydroLaunch& L, int tile, unsig
         const float4 fxp = fx_new, fxm = fx_prev;
         fx_prev = fx_new;
         // div = 0 + (fR-fL)_x, then += (fR-fL)_y, then += (fR-fL)_z  (nebula3d.py:87-109)
+        float du0, du1, du2, du3;
+#if NB_PAIRED
+        {
+            const F2 dA = add2(add2(sub2(mk2(fxp.x, fxp.y), mk2(fxm.x, fxm.y)), sub2(mk2(fyp.x, fyp.y), mk2(fym.x, fym.y))),
+                               sub2(mk2(fzp.x, fzp.y), mk2(fzm.x, fzm.y)));
+            const F2 dB = add2(add2(sub2(mk2(fxp.z, fxp.w), mk2(fxm.z, fxm.w)), sub2(mk2(fyp.z, fyp.w), mk2(fym.z, fym.w))),
+                               sub2(mk2(fzp.z, fzp.w), mk2(fzm.z, fzm.w)));
+            const F2 sc = splat2(C.dx_pow2 ? -C.inv_dx : -1.0f / dx);
+            const F2 uA = mul2(dA, sc), uB = mul2(dB, sc);
+            du0 = lo(uA); du1 = hi(uA); du2 = lo(uB); du3 = hi(uB);
+        }
+#else
         float d0 = 0.0f + (fxp.x - fxm.x), d1 = 0.0f + (fxp.y - fxm.y);
         float d2 = 0.0f + (fxp.z - fxm.z), d3 = 0.0f + (fxp.w - fxm.w);
         d0 = d0 + (fyp.x - fym.x); d1 = d1 + (fyp.y - fym.y); d2 = d2 + (fyp.z - fym.z); d3 = d3 + (fyp.w - fym.w);
         d0 = d0 + (fzp.x - fzm.x); d1 = d1 + (fzp.y - fzm.y); d2 = d2 + (fzp.z - fzm.z); d3 = d3 + (fzp.w - fzm.w);
         // ---- sources and RK combination (nebula3d.py:111-151)
-        float du0, du1, du2, du3;
         if (C.dx_pow2) {
             const float sc = C.inv_dx;
             du0 = -d0 * sc; du1 = -d1 * sc; du2 = -d2 * sc; du3 = -d3 * sc;
         } else {
             du0 = -d0 / dx; du1 = -d1 / dx; du2 = -d2 / dx; du3 = -d3 / dx;
         }
+#endif
         const float px = ((float)i + 0.5f) * dx, py = ((float)j + 0.5f) * dx, pz = ((float)k + 0.5f) * dx;
         const float x_ion = uxi;
         if (wind > 0.0f && x_ion > 0.01f) {
@@ -454,11 +466,23 @@ __device__ __forceinline__ void hydro_tile(const HydroLaunch& L, int tile, unsig
         }
         du0 = du0 + 0.0f;
         du1 = du1 + ur * jx; du2 = du2 + ur * jy; du3 = du3 + ur * jz;
-        const float un0 = ur + dt * du0, un1 = umx + dt * du1, un2 = umy + dt * du2, un3 = umz + dt * du3;
         if (!STAGE2) {
             u00 = ur; u01 = umx; u02 = umy; u03 = umz;
         }
+#if NB_PAIRED
+        float o0, o1, o2, o3;
+        {
+            const F2 dt2 = splat2(dt);
+            const F2 nA = madd2(dt2, mk2(du0, du1), mk2(ur, umx)), nB = madd2(dt2, mk2(du2, du3), mk2(umy, umz));
+            const F2 a2 = splat2(a);
+            const F2 oA = madd2(a2, mk2(u00, u01), mul2(splat2(b), nA));
+            const F2 oB = madd2(a2, mk2(u02, u03), mul2(splat2(b), nB));
+            o0 = lo(oA); o1 = hi(oA); o2 = lo(oB); o3 = hi(oB);
+        }
+#else
+        const float un0 = ur + dt * du0, un1 = umx + dt * du1, un2 = umy + dt * du2, un3 = umz + dt * du3;
         const float o0 = a * u00 + b * un0, o1 = a * u01 + b * un1, o2 = a * u02 + b * un2, o3 = a * u03 + b * un3;
+#endif
         const float r = fmaxr(o0, floor_);
         float vx = o1 / r, vy = o2 / r, vz = o3 / r;
         const float sp = sqrtf((vx * vx + vy * vy) + vz * vz);
