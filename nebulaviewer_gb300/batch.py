@@ -59,6 +59,7 @@ class BatchSim:
         t0 = time.perf_counter()
         for s in self.sims:
             s._push()
+            s._clock_fresh = False               # the batch advances the clocks: read them from the device
         self._chk(self._lib.nb_batch_step(self._b, int(k)), "nb_batch_step")
         for s in self.sims:
             s._it += int(k)

@@ -30,6 +30,7 @@ struct nb_instance {
     float* plane_xf = nullptr;          // [ny][nz] front of the -x plane source
     double* red = nullptr;              // FP64 reduction partials
     float* drive_ring = nullptr;        // stirring fields [slots][3][sx][sy][sz]
+    NbState* state_mirror = nullptr;    // pinned host copy of the control block, refreshed by every step call
     long long drive_field = 0;          // floats per forcing field (3 components)
     int nstars = 0, star_alloc = 0;
     long long host_it = 0;
@@ -206,6 +207,12 @@ int do_ionize(nb_instance* h) {
 
 bool stirring_main(const nb_instance* h) { return h->hc.drive_on && h->hc.drive_main > 0.0; }
 
+// the control block into pinned host memory at the end of a step call (read by nb_peek_clock)
+int mirror_state(nb_instance* h) {
+    CK(h, cudaMemcpyAsync(h->state_mirror, h->st, sizeof(NbState), cudaMemcpyDeviceToHost, h->stream));
+    return NB_OK;
+}
+
 // The two RK2 stages of sim.py:1014-1028 and, when the step stirs, the drive of sim.py:1030-1042;
 // the step's last kernel leaves the next step's CFL max speed in st->smax_bits.
 int hydro_and_stir(nb_instance* h, bool stir, bool no_sources) {
@@ -343,6 +350,8 @@ NB_EXPORT int nb_create(const nb_desc* d, nb_handle* out) {
     c.plane_xf = h->plane_xf;
     c.plane_g0 = f.stage + 2 * h->ncell;
     CKC(cudaMalloc(&h->red, sizeof(double) * nb_reduce_scratch_doubles()));
+    CKC(cudaMallocHost(&h->state_mirror, sizeof(NbState)));
+    std::memset(h->state_mirror, 0, sizeof(NbState));
     CKC(cudaMemsetAsync(h->st, 0, sizeof(NbState), h->stream));
     CKC(cudaMemsetAsync(h->sw, 0, sizeof(NbStarW) * d->max_stars, h->stream));
     CUtensorMap hm[NB_NMAPS];
@@ -371,6 +380,7 @@ NB_EXPORT void nb_destroy(nb_handle h) {
                   h->rfront, h->att, h->scratch3, h->red, h->plane_xf, h->drive_ring};
     for (void* p : ps)
         if (p) cudaFree(p);
+    if (h->state_mirror) cudaFreeHost(h->state_mirror);
     for (auto& r : h->recs) {
         cudaEventDestroy(r.a);
         cudaEventDestroy(r.b);
@@ -451,8 +461,20 @@ NB_EXPORT int nb_set_clock(nb_handle h, const nb_clock* c) {
     s.ip = c->ip;
     CK(h, cudaMemcpyAsync(h->st, &s, sizeof(NbState), cudaMemcpyHostToDevice, h->stream));
     CK(h, cudaStreamSynchronize(h->stream));
+    *h->state_mirror = s;
     h->host_it = c->it;
     h->smax_valid = 0;
+    return NB_OK;
+}
+
+NB_EXPORT int nb_peek_clock(nb_handle h, nb_clock* c) {
+    if (!h || !c) return fail(h, NB_ERR_ARG, "null argument");
+    const NbState& s = *h->state_mirror;
+    c->t = s.t;
+    c->dt = s.dt;
+    c->it = s.it;
+    c->tp = s.tp;
+    c->ip = s.ip;
     return NB_OK;
 }
 
@@ -492,7 +514,7 @@ NB_EXPORT int nb_step(nb_handle h, int k, int ion_every) {
         int rc = do_step(h, ion_every);
         if (rc != NB_OK) return rc;
     }
-    return NB_OK;
+    return mirror_state(h);
 }
 
 NB_EXPORT int nb_pre_step(nb_handle h, int k) {
@@ -505,7 +527,7 @@ NB_EXPORT int nb_pre_step(nb_handle h, int k) {
         int rc = do_pre_step(h);
         if (rc != NB_OK) return rc;
     }
-    return NB_OK;
+    return mirror_state(h);
 }
 
 // ============================================================================ stirring

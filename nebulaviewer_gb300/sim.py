@@ -163,6 +163,7 @@ class Sim:
     def _setup(self, ic, overrides, start_main=True):
         t_setup = time.perf_counter()
         self.close()
+        self._clock_fresh = False
         P = make_params(overrides, base=ic["P"])
         if float(P.get("trigger", 0.0) or 0.0) > 0.0:
             raise NotImplementedError("triggered star formation (trigger > 0) is outside this package's simulation step")
@@ -356,8 +357,13 @@ class Sim:
 
     # ------------------------------------------------------------------ clock (device resident)
     def _clock(self):
+        """the device clock; right after a synchronized step(k) it is read from the pinned copy the
+        step refreshed (no round trip), otherwise from the device (synchronizes)"""
         c = _lib.NbClock()
-        self._chk(self._lib.nb_get_clock(self._h, C.byref(c)), "nb_get_clock")
+        if getattr(self, "_clock_fresh", False):
+            self._chk(self._lib.nb_peek_clock(self._h, C.byref(c)), "nb_peek_clock")
+        else:
+            self._chk(self._lib.nb_get_clock(self._h, C.byref(c)), "nb_get_clock")
         return c
 
     def _set_clock(self, t=None, dt=None, it=None, tp=None, ip=None):
@@ -369,6 +375,7 @@ class Sim:
         c.ip = c.ip if ip is None else int(ip)
         self._chk(self._lib.nb_set_clock(self._h, C.byref(c)), "nb_set_clock")
         self._it = int(c.it)
+        self._clock_fresh = True                     # nb_set_clock synchronized and refreshed the copy
 
     t = property(lambda self: self._clock().t, lambda self, v: self._set_clock(t=v))
     dt = property(lambda self: self._clock().dt, lambda self, v: self._set_clock(dt=v))
@@ -458,6 +465,7 @@ class Sim:
         seconds.  With sync=False the steps are only enqueued on the stream (the stirring phase
         and stirred main-phase steps still synchronize once per chunk)."""
         t0 = time.perf_counter()
+        self._clock_fresh = False
         self._push()
         left = int(k)
         while left > 0:
@@ -466,6 +474,7 @@ class Sim:
             self.version += n
         if sync:
             self._sync()
+            self._clock_fresh = True                 # the stream passed the step's clock copy
             if self._drv_on:
                 self._drive_info()                 # raises if a stirred step found no forcing field
         self._tick("step", t0)
