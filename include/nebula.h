@@ -143,9 +143,11 @@ int nb_set_stars(nb_handle h, const nb_star* stars, int n);
 /* Sim.t / dt / it, as written by set_state_meta (sim.py:1185-1211). */
 int nb_set_clock(nb_handle h, const nb_clock* c);
 int nb_get_clock(nb_handle h, nb_clock* c);          /* synchronizes the stream */
-/* The clock as the last nb_step / nb_pre_step / nb_set_clock call left it, read from a pinned host
- * copy each of those calls refreshes at its end: no synchronization and no copy here, so it is
- * valid once the caller has synchronized with the stream after that call (Sim.step(k) does). */
+/* Enqueues a copy of the clock into pinned host memory, in stream order (asynchronous). */
+int nb_mirror_clock(nb_handle h);
+/* The clock as of the last nb_mirror_clock (once the stream has passed it: the caller
+ * synchronizes, as Sim.step(k) does after the steps and the mirror) or nb_set_clock: no
+ * synchronization and no device access here. */
 int nb_peek_clock(nb_handle h, nb_clock* c);
 
 /* ---------------------------------------------------------------- the step */

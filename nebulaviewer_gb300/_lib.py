@@ -85,6 +85,7 @@ SIGNATURES = {
     "nb_set_clock": (C.c_int, [_P, C.POINTER(NbClock)]),
     "nb_get_clock": (C.c_int, [_P, C.POINTER(NbClock)]),
     "nb_peek_clock": (C.c_int, [_P, C.POINTER(NbClock)]),
+    "nb_mirror_clock": (C.c_int, [_P]),
     "nb_step": (C.c_int, [_P, C.c_int, C.c_int]),
     "nb_ionize": (C.c_int, [_P]),
     "nb_fuv": (C.c_int, [_P]),

@@ -30,7 +30,7 @@ struct nb_instance {
     float* plane_xf = nullptr;          // [ny][nz] front of the -x plane source
     double* red = nullptr;              // FP64 reduction partials
     float* drive_ring = nullptr;        // stirring fields [slots][3][sx][sy][sz]
-    NbState* state_mirror = nullptr;    // pinned host copy of the control block, refreshed by every step call
+    NbState* state_mirror = nullptr;    // pinned host copy of the control block (nb_mirror_clock, nb_set_clock)
     long long drive_field = 0;          // floats per forcing field (3 components)
     int nstars = 0, star_alloc = 0;
     long long host_it = 0;
@@ -207,7 +207,7 @@ int do_ionize(nb_instance* h) {
 
 bool stirring_main(const nb_instance* h) { return h->hc.drive_on && h->hc.drive_main > 0.0; }
 
-// the control block into pinned host memory at the end of a step call (read by nb_peek_clock)
+// the control block into pinned host memory, in stream order (read by nb_peek_clock)
 int mirror_state(nb_instance* h) {
     CK(h, cudaMemcpyAsync(h->state_mirror, h->st, sizeof(NbState), cudaMemcpyDeviceToHost, h->stream));
     return NB_OK;
@@ -467,6 +467,11 @@ NB_EXPORT int nb_set_clock(nb_handle h, const nb_clock* c) {
     return NB_OK;
 }
 
+NB_EXPORT int nb_mirror_clock(nb_handle h) {
+    if (!h) return fail(h, NB_ERR_ARG, "null handle");
+    return mirror_state(h);
+}
+
 NB_EXPORT int nb_peek_clock(nb_handle h, nb_clock* c) {
     if (!h || !c) return fail(h, NB_ERR_ARG, "null argument");
     const NbState& s = *h->state_mirror;
@@ -514,7 +519,7 @@ NB_EXPORT int nb_step(nb_handle h, int k, int ion_every) {
         int rc = do_step(h, ion_every);
         if (rc != NB_OK) return rc;
     }
-    return mirror_state(h);
+    return NB_OK;
 }
 
 NB_EXPORT int nb_pre_step(nb_handle h, int k) {
@@ -527,7 +532,7 @@ NB_EXPORT int nb_pre_step(nb_handle h, int k) {
         int rc = do_pre_step(h);
         if (rc != NB_OK) return rc;
     }
-    return mirror_state(h);
+    return NB_OK;
 }
 
 // ============================================================================ stirring

@@ -188,7 +188,7 @@ __device__ __forceinline__ void apply_front_row(const NbConst& C, const float4* 
                 const float fu = (u + 1.0f) * 0.5f * (float)nu - 0.5f;
                 const int iu = (int)floorf(fu);
                 tu[e] = fu - (float)iu;
-                const int u0 = iclampd(iu, 0, nu - 1), u1 = iclampd(iu + 1, 0, nu - 1);
+                const int u0 = max(iu, 0), u1 = min(iu + 1, nu - 1);    // u in [-1, 1]: iu in [-1, nu - 1]
                 g00[e] = __ldg(rfs + c0 + u0);
                 g01[e] = __ldg(rfs + c1 + u0);
                 g10[e] = __ldg(rfs + c0 + u1);

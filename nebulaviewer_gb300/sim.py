@@ -357,8 +357,8 @@ class Sim:
 
     # ------------------------------------------------------------------ clock (device resident)
     def _clock(self):
-        """the device clock; right after a synchronized step(k) it is read from the pinned copy the
-        step refreshed (no round trip), otherwise from the device (synchronizes)"""
+        """the device clock; right after a synchronized step(k) it is read from the pinned copy made
+        at its end (no round trip), otherwise from the device (synchronizes)"""
         c = _lib.NbClock()
         if getattr(self, "_clock_fresh", False):
             self._chk(self._lib.nb_peek_clock(self._h, C.byref(c)), "nb_peek_clock")
@@ -473,8 +473,9 @@ class Sim:
             left -= n
             self.version += n
         if sync:
+            self._chk(self._lib.nb_mirror_clock(self._h), "nb_mirror_clock")
             self._sync()
-            self._clock_fresh = True                 # the stream passed the step's clock copy
+            self._clock_fresh = True                 # the stream passed the clock's copy to host memory
             if self._drv_on:
                 self._drive_info()                 # raises if a stirred step found no forcing field
         self._tick("step", t0)
