@@ -245,7 +245,10 @@ struct HydroSmem {
     static constexpr int FACE_BYTES = ((TJ + 1) * TK + TJ * (TK + 1)) * 16;
     static constexpr int BAR_BYTES = 64;
     static constexpr int FIXED = RAW_BYTES + PRIM_BYTES + CS_BYTES + FACE_BYTES + BAR_BYTES;
-    static int bytes(int nstars) { return FIXED + nstars * 32; }
+    // star tables: positions / wind weights and jets (2 x float4 per star), then the tile's jet
+    // list: a count and the indices (one byte each) of the stars whose jet can reach the tile
+    __host__ __device__ static int jet_list_offset(int nstars) { return FIXED + nstars * 32; }
+    static int bytes(int nstars) { return jet_list_offset(nstars) + 16 + ((nstars + 15) & ~15); }
 };
 
 #ifndef NB_HYDRO_MINB
@@ -284,8 +287,9 @@ __device__ __forceinline__ void hydro_tile(const HydroLaunch& L, int tile, unsig
         jt = tile / L.tiles_k;
     }
     const int k0 = kt * TK, j0 = jt * TJ;
-    const int i0 = ci * L.chunk_i;
-    const int i_end = min(nx, i0 + L.chunk_i);
+    // n_chunks = ceil(nx / chunk_i) chunks of equal depth (within one plane): no short last chunk
+    const int i0 = (int)((long long)ci * nx / L.n_chunks);
+    const int i_end = (int)((long long)(ci + 1) * nx / L.n_chunks);
     const int P0 = i0 - 2, P1 = i_end + 1;
 
     const float floor_ = C.floor_, cn2 = C.cn2, ci2 = C.ci2, vmax = C.vmax, dx = C.dx;
@@ -294,6 +298,8 @@ __device__ __forceinline__ void hydro_tile(const HydroLaunch& L, int tile, unsig
     const float wind = L.no_sources ? 0.0f : C.wind_f, jet_cos = C.jet_cos_f, jet_r = C.jet_r_f;
     const float a = L.a, b = L.b;
 
+    int* n_jet_p = reinterpret_cast<int*>(smem + SM::jet_list_offset(nstars));
+    unsigned char* jet_ix = smem + SM::jet_list_offset(nstars) + 16;
     for (int s = tid; s < nstars; s += blockDim.x) {
         sw_w[s] = L.sw[s].w;
         sw_j[s] = L.sw[s].jet;
@@ -309,6 +315,34 @@ __device__ __forceinline__ void hydro_tile(const HydroLaunch& L, int tile, unsig
         tma_load_3d(raw + 4 * SM::RAW_FIELD, &L.maps[NB_MAP_XI], k0 - 4, j0 - 2, pc, &bar[0]);
     };
     if (tid == 0) issue(P0);
+    if (tj == 0) {
+        // The stars whose jet (nebula3d.py:131-149: strength > 0, an active star, r < jet_r) can reach
+        // a cell centre of this tile, in star order: the distance from the star to the box of the
+        // tile's cell centres, less a margin of two cells for the float rounding of the per-cell
+        // distance, must be below jet_r.  Stars left out add exactly nothing to any cell here.
+        const float bx0 = ((float)i0 + 0.5f) * dx, bx1 = ((float)(i_end - 1) + 0.5f) * dx;
+        const float by0 = ((float)j0 + 0.5f) * dx, by1 = ((float)(min(j0 + TJ, ny) - 1) + 0.5f) * dx;
+        const float bz0 = ((float)k0 + 0.5f) * dx, bz1 = ((float)(min(k0 + TK, nz) - 1) + 0.5f) * dx;
+        const float reach = jet_r + 2.0f * dx;
+        int n = 0;
+        for (int s0 = 0; s0 < nstars; s0 += 32) {
+            const int s = s0 + tk;
+            bool keep = false;
+            if (s < nstars) {
+                const float4 st = L.sw[s].w, jt = L.sw[s].jet;
+                if (jt.w > 0.0f && st.w > 0.0f) {
+                    const float ex = fmaxf(0.0f, fmaxf(bx0 - st.x, st.x - bx1));
+                    const float ey = fmaxf(0.0f, fmaxf(by0 - st.y, st.y - by1));
+                    const float ez = fmaxf(0.0f, fmaxf(bz0 - st.z, st.z - bz1));
+                    keep = !(ex * ex + ey * ey + ez * ez >= reach * reach);    // NaN keeps the star
+                }
+            }
+            const unsigned m = __ballot_sync(0xffffffffu, keep);
+            if (keep) jet_ix[n + __popc(m & ((1u << tk) - 1u))] = (unsigned char)s;
+            n += __popc(m);
+        }
+        if (tk == 0) *n_jet_p = n;
+    }
 
     float4 fx_prev = make_float4(0.f, 0.f, 0.f, 0.f);
     float vmax_local = 0.0f;
@@ -449,10 +483,12 @@ __device__ __forceinline__ void hydro_tile(const HydroLaunch& L, int tile, unsig
             du1 = du1 + ur * ax; du2 = du2 + ur * ay; du3 = du3 + ur * az;
         }
         float jx = 0.0f, jy = 0.0f, jz = 0.0f;
-        for (int s = 0; s < nstars; ++s) {
+        const int n_jet = *n_jet_p;
+        for (int m = 0; m < n_jet; ++m) {
+            const int s = jet_ix[m];
             const float4 jt = sw_j[s];
             const float4 st = sw_w[s];
-            if (jt.w > 0.0f && st.w > 0.0f) {
+            {
                 const float rx = px - st.x, ry = py - st.y, rz = pz - st.z;
                 const float r = sqrtf((rx * rx + ry * ry) + rz * rz);
                 if (r < jet_r && r > 1e-6f) {
