@@ -29,6 +29,7 @@ struct nb_instance {
     float* scratch3 = nullptr;          // 3 floats: a single star position for the one-star kernels
     float* plane_xf = nullptr;          // [ny][nz] front of the -x plane source
     double* red = nullptr;              // FP64 reduction partials
+    float2* front_parts = nullptr;      // per-star front-radius ranges (apply_front)
     float* drive_ring = nullptr;        // stirring fields [slots][3][sx][sy][sz]
     NbState* state_mirror = nullptr;    // pinned host copy of the control block (nb_mirror_clock, nb_set_clock)
     long long drive_field = 0;          // floats per forcing field (3 components)
@@ -37,6 +38,7 @@ struct nb_instance {
     int smax_valid = 0;
     int chunk_i = 32, ray_group = 4, fuv_group = 16;      // measured best at 256^3 (nb_set_tuning)
     int tile_order = 0;
+    int front_cull = 1;                 // apply_front skips the stars that cannot change a segment
     long long ncell = 0;
     long long launches = 0;             // kernels this handle launched (nb_counters)
     int profiling = 0;                  // CUDA-event timing per kernel kind (nb_profile)
@@ -193,9 +195,12 @@ int do_ionize(nb_instance* h) {
     }
     float* xi_raw = plane(h, 0);            // sim.py:928-941: xi_tmp lives in the stage block
     {
-        Prof pf(h, NB_PROF_APPLY_FRONT, 1);
+        const bool cull = h->front_cull && h->nstars >= 1 && h->nstars <= NB_ROW_STARS;
+        Prof pf(h, NB_PROF_APPLY_FRONT, cull ? 2 : 1);
         CK(h, nb_launch_apply_front(h->c, h->sw, h->rfront, h->nstars, xi_raw, f.dfront, &h->st->smax_bits,
-                                    h->stream, h->d.nx, h->d.ny, h->d.fields_fp32 ? 0 : 1));
+                                    h->stream, h->d.nx, h->d.ny, h->d.fields_fp32 ? 0 : 1,
+                                    cull ? h->front_parts : nullptr,
+                                    (long long)h->d.nu * h->d.nphi));
     }
     {
         Prof pf(h, NB_PROF_SMOOTH, 1);
@@ -350,6 +355,7 @@ NB_EXPORT int nb_create(const nb_desc* d, nb_handle* out) {
     c.plane_xf = h->plane_xf;
     c.plane_g0 = f.stage + 2 * h->ncell;
     CKC(cudaMalloc(&h->red, sizeof(double) * nb_reduce_scratch_doubles()));
+    CKC(cudaMalloc(&h->front_parts, sizeof(float2) * NB_ROW_STARS * NB_FRONT_PARTS));
     CKC(cudaMallocHost(&h->state_mirror, sizeof(NbState)));
     std::memset(h->state_mirror, 0, sizeof(NbState));
     CKC(cudaMemsetAsync(h->st, 0, sizeof(NbState), h->stream));
@@ -377,7 +383,7 @@ NB_EXPORT void nb_destroy(nb_handle h) {
     if (h->stream) cudaStreamSynchronize(h->stream);
     else cudaDeviceSynchronize();
     void* ps[] = {h->c, h->st, h->stars, h->sw, h->maps, h->tmp_maps, h->dirs, h->dirs_fuv,
-                  h->rfront, h->att, h->scratch3, h->red, h->plane_xf, h->drive_ring};
+                  h->rfront, h->att, h->scratch3, h->red, h->plane_xf, h->drive_ring, h->front_parts};
     for (void* p : ps)
         if (p) cudaFree(p);
     if (h->state_mirror) cudaFreeHost(h->state_mirror);
@@ -827,6 +833,7 @@ NB_EXPORT int nb_get_tuning(nb_handle h, int key, int* value) {
         case NB_TUNE_RAY_GROUP: *value = h->ray_group; return NB_OK;
         case NB_TUNE_FUV_GROUP: *value = h->fuv_group; return NB_OK;
         case NB_TUNE_TILE_ORDER: *value = h->tile_order; return NB_OK;
+        case NB_TUNE_FRONT_CULL: *value = h->front_cull; return NB_OK;
         default: return fail(h, NB_ERR_ARG, "unknown tuning key");
     }
 }
@@ -841,6 +848,10 @@ NB_EXPORT int nb_set_tuning(nb_handle h, int key, int value) {
         case NB_TUNE_TILE_ORDER:
             if (value != 0 && value != 1) return fail(h, NB_ERR_ARG, "tile order must be 0 or 1");
             h->tile_order = value;
+            return NB_OK;
+        case NB_TUNE_FRONT_CULL:
+            if (value != 0 && value != 1) return fail(h, NB_ERR_ARG, "front culling must be 0 or 1");
+            h->front_cull = value;
             return NB_OK;
         case NB_TUNE_RAY_GROUP:
         case NB_TUNE_FUV_GROUP:

@@ -7,6 +7,8 @@
 
 #include "../../include/nebula.h"
 
+#define NB_FRONT_PARTS 32         // partial front-radius ranges per star (apply_front culling)
+#define NB_ROW_STARS 32           // stars a per-row table holds (more: per-cell form)
 #define NB_MAX_STARS 256          // star-table capacity limit (smem-resident in the kernels)
 #define NB_WAIT_LIMIT (1u << 22)  // iteration cap of every device-side spin wait
 
@@ -214,9 +216,12 @@ cudaError_t nb_launch_ray_dirs(int nu, int nphi, float4* dirs, cudaStream_t s);
 cudaError_t nb_launch_cast_rays(const NbConst* c, const NbStarW* sw, const float4* dirs, const float* rho,
                                 float* rfront, int nstars, int group, const float* star_override, float q_override,
                                 cudaStream_t s, int nu, int nphi);
+// with front_parts (NB_ROW_STARS * NB_FRONT_PARTS float2 scratch) and 1 <= nstars <= NB_ROW_STARS:
+// first each star's front-radius range (one more launch), then segments skip the stars that
+// cannot change them
 cudaError_t nb_launch_apply_front(const NbConst* c, const NbStarW* sw, const float* rfront, int nstars,
                                   float* xi_raw, void* dfront, unsigned* smax_reset, cudaStream_t s, int nx, int ny,
-                                  int half);
+                                  int half, float2* front_parts = nullptr, long long nray = 0);
 cudaError_t nb_launch_smooth(const NbConst* c, const float* xi_raw, float* xi, const float* rho, const float* mx,
                              const float* my, const float* mz, unsigned* smax_bits, cudaStream_t s, int nx, int ny);
 cudaError_t nb_launch_ionize_batch(const NbRayJob* jobs, int n_jobs, long long n_groups, long long n_blocks, int group,

@@ -132,12 +132,46 @@ __global__ void __launch_bounds__(256) cast_rays_batch_kernel(const NbRayJob* __
                 w.q_f, lane, gmask);
 }
 
+// The stars that can change xi or the front distance of the 32-cell segment [kb, kb + 32) of a
+// row, as a mask (nstars <= NB_ROW_STARS; lane s bounds star s).  Over the segment a star's
+// r - rf lies in [LB, UB]: LB = (least distance to the segment) - (largest front radius of the
+// star), UB = (largest distance) - (smallest front radius).  A star with LB at or above both
+// min(1e3, least UB over the stars) and width / 2, plus a margin of one cell for float rounding,
+// gives every cell of the segment val = 0 (no xi) and an r - rf above another star's (no front
+// distance): leaving it out changes no bit.  A NaN bound (NaN radii or positions, whose min /
+// max merges depend on order) keeps every active star.
+__device__ __forceinline__ unsigned segment_stars(const float4* st, const int* act, const float4* tab,
+                                                  const float2* bnd, int nstars, int kb, int nz, float dx,
+                                                  float width) {
+    const int lane = threadIdx.x;
+    const bool on = lane < nstars && act[lane];
+    float lb = __int_as_float(0x7f800000), ub = lb;       // +inf: the lane has no star
+    if (on) {
+        const float sz = st[lane].z, d2 = tab[lane].x;
+        const float2 b = bnd[lane];                       // (least, largest) front radius
+        const float z0 = ((float)kb + 0.5f) * dx, z1 = ((float)(min(kb + 31, nz - 1)) + 0.5f) * dx;
+        const float en = fmaxf(0.0f, fmaxf(z0 - sz, sz - z1));
+        const float ex = fmaxf(fabsf(sz - z0), fabsf(sz - z1));
+        lb = sqrtf(d2 + en * en) - b.y;
+        ub = sqrtf(d2 + ex * ex) - b.x;
+    }
+    const unsigned all = __ballot_sync(0xffffffffu, on);
+    if (__any_sync(0xffffffffu, isnan(lb) || isnan(ub))) return all;
+    float m = ub;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) m = fminf(m, __shfl_xor_sync(0xffffffffu, m, o));
+    const float thr = fmaxf(fminf(1e3f, m), 0.5f * width) + dx;
+    return __ballot_sync(0xffffffffu, on && lb < thr);
+}
+
 // nebula3d.py:273-307 rf_at + apply_front over one row (i, j), fused over the active stars,
 // with the fp16 store of the front distance (sim.py:942, 980-985).  `tab`: this warp's row
-// table (NB_ROW_STARS entries) or null for the per-cell form.
+// table (NB_ROW_STARS entries) or null for the per-cell form; `bnd`: each star's (least, largest)
+// front radius, or null to merge every active star in every segment.
 __device__ __forceinline__ void apply_front_row(const NbConst& C, const float4* st, const int* act, int nstars,
                                                 const float* __restrict__ rfront, float* __restrict__ xi_raw,
-                                                void* __restrict__ dfront, bool half, int row, float4* tab) {
+                                                void* __restrict__ dfront, bool half, int row, float4* tab,
+                                                const float2* bnd) {
     const int nx = C.nx, ny = C.ny, nz = C.nz, nu = C.nu, nphi = C.nphi;
     if (row >= nx * ny) return;
     const int i = row / ny, j = row - (row / ny) * ny;
@@ -147,19 +181,32 @@ __device__ __forceinline__ void apply_front_row(const NbConst& C, const float4* 
     const float px = ((float)i + 0.5f) * dx, py = ((float)j + 0.5f) * dx;
     const long long rstride = (long long)nu * nphi;
     if (tab && nstars > NB_ROW_STARS) tab = nullptr;
+    if (!tab) bnd = nullptr;
     if (tab) star_row_table(st, act, nstars, px, py, nphi, nu, tab);
+    const unsigned row_stars = tab ? __ballot_sync(0xffffffffu, (int)threadIdx.x < nstars && act[threadIdx.x]) : 0u;
     constexpr int SG = 4;                       // stars whose gathers are in flight together
-    for (int k = threadIdx.x; k < nz; k += 32) {
+    for (int kb = 0; kb < nz; kb += 32) {
+        const unsigned seg = bnd ? segment_stars(st, act, tab, bnd, nstars, kb, nz, dx, width) : row_stars;
+        const int k = kb + (int)threadIdx.x;
+        if (k >= nz) continue;
         const long long q = base + k;
         const float pz = ((float)k + 0.5f) * dx;
         float xi = 0.0f, df = 1e3f;
-        for (int s0 = 0; s0 < nstars; s0 += SG) {
+        unsigned left = seg;                     // mask form: the segment's stars in star order
+        for (int s0 = 0; tab ? left != 0u : s0 < nstars; s0 += SG) {
             float r[SG], tu[SG], tp[SG], g00[SG], g01[SG], g10[SG], g11[SG];
             bool on[SG];
 #pragma unroll
             for (int e = 0; e < SG; ++e) {
-                const int s = s0 + e;
-                on[e] = s < nstars && act[s];
+                int s;
+                if (tab) {
+                    on[e] = left != 0u;
+                    s = on[e] ? __ffs(left) - 1 : 0;
+                    left &= left - 1u;
+                } else {
+                    s = s0 + e;
+                    on[e] = s < nstars && act[s];
+                }
                 r[e] = tu[e] = tp[e] = 0.0f;
                 g00[e] = g01[e] = g10[e] = g11[e] = 0.0f;
                 if (!on[e]) continue;
@@ -201,7 +248,7 @@ __device__ __forceinline__ void apply_front_row(const NbConst& C, const float4* 
                 const float rb = g10[e] * (1.0f - tp[e]) + g11[e] * tp[e];
                 const float rf = ra * (1.0f - tu[e]) + rb * tu[e];
                 const float val = fminr(fmaxr(0.0f, (rf - r[e]) / width + 0.5f), 1.0f);
-                if (val > xi) xi = val;              // max / min merges are exact and order-free
+                if (val > xi) xi = val;              // in star order, as the reference merges
                 df = fminr(df, r[e] - rf);
             }
         }
@@ -219,6 +266,59 @@ __device__ __forceinline__ void apply_front_row(const NbConst& C, const float4* 
     }
 }
 
+// Each active star's least and largest front radius over its rays, as NB_FRONT_PARTS partial
+// (least, largest) pairs per star: block (b, s) reduces the b-th slice of star s.  The largest is
+// NaN when a NaN radius was seen (the least skips NaNs).
+__global__ void __launch_bounds__(256) front_bounds_kernel(const NbStarW* __restrict__ sw,
+                                                           const float* __restrict__ rfront, long long nray,
+                                                           float2* __restrict__ parts) {
+    const int s = blockIdx.y, b = blockIdx.x;
+    if (!sw[s].active) return;                  // uniform over the block
+    const float* r = rfront + (long long)s * nray;
+    const long long per = (nray + NB_FRONT_PARTS - 1) / NB_FRONT_PARTS;
+    const long long lo = (long long)b * per, hi = min(nray, lo + per);
+    float mn = __int_as_float(0x7f800000), mx = -mn;
+    bool nan = false;
+    for (long long q = lo + threadIdx.x; q < hi; q += blockDim.x) {
+        const float v = __ldg(r + q);
+        nan |= isnan(v);
+        mn = fminf(mn, v);
+        mx = fmaxf(mx, v);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        mn = fminf(mn, __shfl_xor_sync(0xffffffffu, mn, o));
+        mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    }
+    __shared__ float2 wpart[8];
+    const bool any_nan = __syncthreads_or(nan);
+    if ((threadIdx.x & 31) == 0) wpart[threadIdx.x >> 5] = make_float2(mn, mx);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int w = 1; w < (int)(blockDim.x >> 5); ++w) {
+            mn = fminf(mn, wpart[w].x);
+            mx = fmaxf(mx, wpart[w].y);
+        }
+        parts[s * NB_FRONT_PARTS + b] = make_float2(mn, any_nan ? __int_as_float(0x7fc00000) : mx);
+    }
+}
+
+// the partials into (least, largest) per star in shared memory (after load_stars' barrier)
+__device__ __forceinline__ void load_front_bounds(const float2* parts, int nstars, float2* bnd, int tlin) {
+    for (int s = tlin; s < nstars; s += blockDim.x * blockDim.y) {
+        float mn = __int_as_float(0x7f800000), mx = -mn;
+        bool nan = false;
+        for (int b = 0; b < NB_FRONT_PARTS; ++b) {
+            const float2 p = parts[s * NB_FRONT_PARTS + b];
+            mn = fminf(mn, p.x);
+            nan |= isnan(p.y);
+            mx = fmaxf(mx, p.y);
+        }
+        bnd[s] = make_float2(mn, nan ? __int_as_float(0x7fc00000) : mx);
+    }
+    __syncthreads();
+}
+
 __device__ __forceinline__ int load_stars(const NbStarW* sw, int nstars, float4* st, int* act) {
     const int tlin = threadIdx.y * blockDim.x + threadIdx.x;
     for (int s = tlin; s < nstars; s += blockDim.x * blockDim.y) {
@@ -234,14 +334,16 @@ __global__ void __launch_bounds__(256, 3) apply_front_kernel(const NbConst* __re
                                                           const NbStarW* __restrict__ sw,
                                                           const float* __restrict__ rfront, int nstars,
                                                           float* __restrict__ xi_raw, void* __restrict__ dfront,
-                                                          unsigned* smax_reset) {
+                                                          unsigned* smax_reset, const float2* __restrict__ parts) {
     __shared__ float4 st[NB_MAX_STARS];
     __shared__ int act[NB_MAX_STARS];
     __shared__ float4 tab[8][NB_ROW_STARS];
+    __shared__ float2 bnd[NB_ROW_STARS];
     const int tlin = load_stars(sw, nstars, st, act);
     if (smax_reset && blockIdx.x == 0 && tlin == 0) *smax_reset = 0u;
+    if (parts) load_front_bounds(parts, nstars, bnd, tlin);      // parts only with nstars <= NB_ROW_STARS
     apply_front_row(*c, st, act, nstars, rfront, xi_raw, dfront, HALF, blockIdx.x * blockDim.y + threadIdx.y,
-                    tab[threadIdx.y]);
+                    tab[threadIdx.y], parts ? bnd : nullptr);
 }
 
 // Rows of every listed instance; job e owns blocks [job[e].blk0, job[e+1].blk0) (8 rows each).
@@ -259,7 +361,7 @@ __global__ void __launch_bounds__(256) apply_front_batch_kernel(const NbRayJob* 
     const int tlin = load_stars(J.sw, J.nstars, st, act);
     if (lb == 0 && tlin == 0) *J.smax = 0u;
     apply_front_row(*J.c, st, act, J.nstars, J.rfront, J.xi_raw, J.dfront, J.half != 0, lb * blockDim.y + threadIdx.y,
-                    tab[threadIdx.y]);
+                    tab[threadIdx.y], nullptr);
 }
 
 // nebula3d.py:310-315 smooth_xi (+ sim.py:941 copy back) of one row, then the CFL max speed
@@ -381,13 +483,18 @@ cudaError_t nb_launch_cast_rays(const NbConst* c, const NbStarW* sw, const float
 
 cudaError_t nb_launch_apply_front(const NbConst* c, const NbStarW* sw, const float* rfront, int nstars,
                                   float* xi_raw, void* dfront, unsigned* smax_reset, cudaStream_t s, int nx, int ny,
-                                  int half) {
+                                  int half, float2* front_parts, long long nray) {
     const dim3 blk(32, 8);
     const int blocks = rowwalk_blocks(nx, ny);
+    const float2* parts = nullptr;
+    if (front_parts && nstars >= 1 && nstars <= NB_ROW_STARS) {
+        front_bounds_kernel<<<dim3(NB_FRONT_PARTS, nstars), 256, 0, s>>>(sw, rfront, nray, front_parts);
+        parts = front_parts;
+    }
     if (half)
-        apply_front_kernel<true><<<blocks, blk, 0, s>>>(c, sw, rfront, nstars, xi_raw, dfront, smax_reset);
+        apply_front_kernel<true><<<blocks, blk, 0, s>>>(c, sw, rfront, nstars, xi_raw, dfront, smax_reset, parts);
     else
-        apply_front_kernel<false><<<blocks, blk, 0, s>>>(c, sw, rfront, nstars, xi_raw, dfront, smax_reset);
+        apply_front_kernel<false><<<blocks, blk, 0, s>>>(c, sw, rfront, nstars, xi_raw, dfront, smax_reset, parts);
     return cudaGetLastError();
 }
 

@@ -140,8 +140,6 @@ __device__ __forceinline__ float nb_shock_at(const NbConst& C, const float* __re
 // table column and interpolation weight, and rx^2 + ry^2 are the same for the whole row.  A warp
 // (one row) evaluates them once per star, with the same float operations as the per-cell form,
 // so every cell sees the same values.  Entry: (rx^2 + ry^2, phi weight, column p0, column p1).
-constexpr int NB_ROW_STARS = 32;                 // stars a row table holds (more: per-cell form)
-
 __device__ __forceinline__ void star_row_table(const float4* st, const int* act, int nstars, float px, float py,
                                                int nphi, int colmul, float4* tab) {
     const float two_pi = 2.0f * pi_f();

@@ -299,3 +299,42 @@ def test_cliffwall_plane_source_against_oracle(nb, arith):
     for k in ("rho", "mx"):
         assert rel_linf(getattr(g, k).numpy(), getattr(o64, k)) < 1e-5
     g.close()
+
+
+def _front_fields(sim):
+    sim.ionize()
+    torch.cuda.synchronize()
+    df = sim._dfront
+    return (sim._xi.clone().view(torch.int32), df.clone().view(torch.int16 if df.dtype == torch.float16 else torch.int32))
+
+
+@pytest.mark.parametrize("arith", ARITH)
+@pytest.mark.parametrize("case", ("sheet12", "overlapping8"))
+def test_front_culling_changes_no_bit(nb, arith, case):
+    """apply_front's per-segment star culling (bounds from each star's front-radius range) gives
+    the same xi and front distance, bit for bit, as merging every star in every cell: a 12-star
+    sheet with small fronts (most stars culled) and 8 stars in thin gas whose fronts overlap"""
+    from nebulaviewer_gb300 import autotune as at, ics
+    _, S = nb
+    if case == "sheet12":
+        ic = ics.sheet(res=128, nstars=12)
+        sim = S.Sim.from_state(ic["shape"], ic["dx"], ic["rho"], ic["stars"], ic["kinds"], ic["jets"], ic["jkinds"],
+                               ic["P"], mom=ic["mom"], rays=(128, 256), fuv_grid=(32, 32, 64), arith=arith)
+        sim.step(9)
+    else:
+        n = 96
+        g = torch.Generator().manual_seed(5)
+        rho = (0.05 + 0.02 * torch.rand((n, n, n), generator=g)).to("cuda")
+        pos = torch.rand((8, 3), generator=g).double() * 0.8 + 0.1
+        stars = [(float(p[0]), float(p[1]), float(p[2]), 1.0, 0.0) for p in pos]
+        sim = S.Sim.from_state((n, n, n), 1.0 / n, rho, stars, ["main"] * 8, [(0, 0, 1.0)] * 8, ["none"] * 8,
+                               dict(q_main=1e-5, q_ramp=0.0), rays=(96, 192), fuv_grid=(16, 16, 32), arith=arith)
+    at.put(sim, "front_cull", 0)
+    xi0, df0 = _front_fields(sim)
+    at.put(sim, "front_cull", 1)
+    xi1, df1 = _front_fields(sim)
+    assert at.get(sim, "front_cull") == 1
+    assert torch.equal(xi0, xi1) and torch.equal(df0, df1)
+    ion = (xi1.view(torch.float32) > 0.5).float().mean().item()
+    assert (0.0 < ion < 0.2) if case == "sheet12" else (0.05 < ion < 0.95)
+    sim.close()
