@@ -308,7 +308,11 @@ NB_EXPORT int nb_create(const nb_desc* d, nb_handle* out) {
     h->d = *d;
     h->stream = static_cast<cudaStream_t>(d->stream);
     h->ncell = (long long)d->nx * d->ny * d->nz;
-    if (h->ncell * 4 > (1LL << 62)) { delete h; return fail(nullptr, NB_ERR_LIMIT, "grid too large"); }
+    if (h->ncell * 4 > (1LL << 62) || (long long)d->ny * d->nz >= (1LL << 31) ||
+        (long long)d->fnu * d->fnphi * d->fnr >= (1LL << 31)) {
+        delete h;
+        return fail(nullptr, NB_ERR_LIMIT, "grid too large (ny * nz and fnu * fnphi * fnr must stay below 2^31)");
+    }
     NbConst& c = h->hc;
     c.nx = d->nx; c.ny = d->ny; c.nz = d->nz; c.nstars = 0;
     c.dx_pow2 = is_pow2(d->dx) ? 1 : 0;

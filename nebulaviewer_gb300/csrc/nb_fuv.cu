@@ -184,7 +184,7 @@ __global__ void __launch_bounds__(256) apply_fuv_kernel(const NbConst* __restric
                         const float wgt = (aa == 0 ? 1.0f - tr : tr) * (bb == 0 ? 1.0f - tu : tu) * (cc == 0 ? 1.0f - tp : tp);
                         const int rr = iclampd(ir + aa, 0, nr - 1);
                         const int uu = iclampd(iu + bb, 0, nu - 1);
-                        acc = acc + wgt * __ldg(as + ((long long)uu * nphi + pw[cc]) * nr + rr);
+                        acc = acc + wgt * __ldg(as + ((uu * nphi + pw[cc]) * nr + rr));   // < 2^31 per star
                     }
             const float r2 = fmaxr(r * r, 0.0004f);
             term[e] = lum[s] * acc / r2;

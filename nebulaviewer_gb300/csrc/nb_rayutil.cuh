@@ -18,11 +18,14 @@ __device__ __forceinline__ float sample_n(const float* __restrict__ a, int nx, i
     const int ia = iclampd(i0, 0, nx - 1), ib = iclampd(i0 + 1, 0, nx - 1);
     const int ja = iclampd(j0, 0, ny - 1), jb = iclampd(j0 + 1, 0, ny - 1);
     const int ka = iclampd(k0, 0, nz - 1), kb = iclampd(k0 + 1, 0, nz - 1);
-    const long long sa = (long long)ia * ny, sb = (long long)ib * ny;
-    const float c000 = __ldg(a + (sa + ja) * nz + ka), c100 = __ldg(a + (sb + ja) * nz + ka);
-    const float c010 = __ldg(a + (sa + jb) * nz + ka), c110 = __ldg(a + (sb + jb) * nz + ka);
-    const float c001 = __ldg(a + (sa + ja) * nz + kb), c101 = __ldg(a + (sb + ja) * nz + kb);
-    const float c011 = __ldg(a + (sa + jb) * nz + kb), c111 = __ldg(a + (sb + jb) * nz + kb);
+    // corner (ia, ja, ka) once in 64 bits, the other seven as 32-bit steps from it (a plane
+    // ny * nz below 2^31 cells, which nb_create requires)
+    const float* p = a + (((long long)ia * ny + ja) * nz + ka);
+    const int dk = kb - ka, dj = (jb - ja) * nz, di = (ib - ia) * (ny * nz);
+    const float c000 = __ldg(p), c100 = __ldg(p + di);
+    const float c010 = __ldg(p + dj), c110 = __ldg(p + (di + dj));
+    const float c001 = __ldg(p + dk), c101 = __ldg(p + (di + dk));
+    const float c011 = __ldg(p + (dj + dk)), c111 = __ldg(p + (di + dj + dk));
     const float c00 = c000 + (c100 - c000) * fx;
     const float c10 = c010 + (c110 - c010) * fx;
     const float c01 = c001 + (c101 - c001) * fx;
@@ -46,11 +49,12 @@ __device__ __forceinline__ float2 sample_n2(const float2* __restrict__ a, int nx
     const int ia = iclampd(i0, 0, nx - 1), ib = iclampd(i0 + 1, 0, nx - 1);
     const int ja = iclampd(j0, 0, ny - 1), jb = iclampd(j0 + 1, 0, ny - 1);
     const int ka = iclampd(k0, 0, nz - 1), kb = iclampd(k0 + 1, 0, nz - 1);
-    const long long sa = (long long)ia * ny, sb = (long long)ib * ny;
-    const float2 c000 = __ldg(a + (sa + ja) * nz + ka), c100 = __ldg(a + (sb + ja) * nz + ka);
-    const float2 c010 = __ldg(a + (sa + jb) * nz + ka), c110 = __ldg(a + (sb + jb) * nz + ka);
-    const float2 c001 = __ldg(a + (sa + ja) * nz + kb), c101 = __ldg(a + (sb + ja) * nz + kb);
-    const float2 c011 = __ldg(a + (sa + jb) * nz + kb), c111 = __ldg(a + (sb + jb) * nz + kb);
+    const float2* p = a + (((long long)ia * ny + ja) * nz + ka);      // as sample_n
+    const int dk = kb - ka, dj = (jb - ja) * nz, di = (ib - ia) * (ny * nz);
+    const float2 c000 = __ldg(p), c100 = __ldg(p + di);
+    const float2 c010 = __ldg(p + dj), c110 = __ldg(p + (di + dj));
+    const float2 c001 = __ldg(p + dk), c101 = __ldg(p + (di + dk));
+    const float2 c011 = __ldg(p + (dj + dk)), c111 = __ldg(p + (di + dj + dk));
     float out[2];
 #pragma unroll
     for (int f = 0; f < 2; ++f) {
