@@ -306,9 +306,11 @@ int nb_profile_read(nb_handle h, double ms[NB_PROF_KINDS], long long count[NB_PR
  * result does not depend on them; the ray sums only through their rounding.  NB_TUNE_FRONT_CULL
  * (default 1; up to 32 stars): the front pass first bounds each star's front radius and then
  * leaves out, per 32-cell segment of a row, the stars that cannot change its ionized fraction or
- * front distance; the result is the same either way, bit for bit. */
+ * front distance; NB_TUNE_FUV_CUT (default 1): a FUV ray stops once its optical depth passes 120,
+ * where exp(-tau) is 0.0f for good, and writes 0 to its remaining bins.  The result is the same
+ * either way, bit for bit. */
 enum { NB_TUNE_CHUNK_I = 0, NB_TUNE_RAY_GROUP = 1, NB_TUNE_FUV_GROUP = 2, NB_TUNE_TILE_ORDER = 3,
-       NB_TUNE_FRONT_CULL = 4 };
+       NB_TUNE_FRONT_CULL = 4, NB_TUNE_FUV_CUT = 5 };
 int nb_set_tuning(nb_handle h, int key, int value);
 int nb_get_tuning(nb_handle h, int key, int* value);
 /* Number of kernels the handle has launched (a claim the benchmark reports). */

@@ -122,7 +122,7 @@ SIGNATURES = {
     "nb_reduce_fp64_static": (C.c_int, [_P, _P, _P, _P, C.c_longlong, _P, _P]),
     "nb_static_last_error": (C.c_char_p, []),
 }
-TUNE = {"chunk_i": 0, "ray_group": 1, "fuv_group": 2, "tile_order": 3, "front_cull": 4}
+TUNE = {"chunk_i": 0, "ray_group": 1, "fuv_group": 2, "tile_order": 3, "front_cull": 4, "fuv_cut": 5}
 PROF_KINDS = ["ctrl", "stage1", "stage2", "cast_rays", "apply_front", "smooth", "cast_fuv", "apply_fuv", "max_speed",
               "snapshot", "drive", "render"]
 

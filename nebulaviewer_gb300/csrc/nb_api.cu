@@ -39,6 +39,7 @@ struct nb_instance {
     int chunk_i = 32, ray_group = 4, fuv_group = 16;      // measured best at 256^3 (nb_set_tuning)
     int tile_order = 0;
     int front_cull = 1;                 // apply_front skips the stars that cannot change a segment
+    int fuv_cut = 1;                    // FUV rays stop where exp(-tau) has reached 0.0f
     long long ncell = 0;
     long long launches = 0;             // kernels this handle launched (nb_counters)
     int profiling = 0;                  // CUDA-event timing per kernel kind (nb_profile)
@@ -687,7 +688,8 @@ NB_EXPORT int nb_fuv(nb_handle h) {
     if (h->nstars > 0) {
         Prof pf(h, NB_PROF_CAST_FUV, 2);                // the (rho, xi) pack into stage planes 0-1 + the rays
         CK(h, nb_launch_cast_fuv(h->c, h->sw, h->dirs_fuv, h->d.f.rho, h->d.f.xi, h->att, h->nstars, h->fuv_group,
-                                 nullptr, 0, h->stream, h->d.fnu, h->d.fnphi, plane(h, 0), h->ncell));
+                                 nullptr, 0, h->stream, h->d.fnu, h->d.fnphi, plane(h, 0), h->ncell,
+                                 h->fuv_cut ? NB_FUV_TAU_CUT : 0.0f));
     }
     if (h->hc.plane_on) {
         Prof pf(h, NB_PROF_CAST_FUV, 1);
@@ -746,7 +748,7 @@ NB_EXPORT int nb_cast_fuv(nb_handle h, const double xyz[3], float* att_out) {
     float s3[4] = {(float)xyz[0], (float)xyz[1], (float)xyz[2], 0.f};
     CK(h, cudaMemcpyAsync(h->scratch3, s3, sizeof(s3), cudaMemcpyHostToDevice, h->stream));
     CK(h, nb_launch_cast_fuv(h->c, h->sw, h->dirs_fuv, h->d.f.rho, h->d.f.xi, att_out, 1, 32, h->scratch3, 1,
-                             h->stream, h->d.fnu, h->d.fnphi, plane(h, 0), h->ncell));
+                             h->stream, h->d.fnu, h->d.fnphi, plane(h, 0), h->ncell, h->fuv_cut ? NB_FUV_TAU_CUT : 0.0f));
     CK(h, cudaStreamSynchronize(h->stream));
     return NB_OK;
 }
@@ -838,6 +840,7 @@ NB_EXPORT int nb_get_tuning(nb_handle h, int key, int* value) {
         case NB_TUNE_FUV_GROUP: *value = h->fuv_group; return NB_OK;
         case NB_TUNE_TILE_ORDER: *value = h->tile_order; return NB_OK;
         case NB_TUNE_FRONT_CULL: *value = h->front_cull; return NB_OK;
+        case NB_TUNE_FUV_CUT: *value = h->fuv_cut; return NB_OK;
         default: return fail(h, NB_ERR_ARG, "unknown tuning key");
     }
 }
@@ -856,6 +859,10 @@ NB_EXPORT int nb_set_tuning(nb_handle h, int key, int value) {
         case NB_TUNE_FRONT_CULL:
             if (value != 0 && value != 1) return fail(h, NB_ERR_ARG, "front culling must be 0 or 1");
             h->front_cull = value;
+            return NB_OK;
+        case NB_TUNE_FUV_CUT:
+            if (value != 0 && value != 1) return fail(h, NB_ERR_ARG, "FUV cut must be 0 or 1");
+            h->fuv_cut = value;
             return NB_OK;
         case NB_TUNE_RAY_GROUP:
         case NB_TUNE_FUV_GROUP:

@@ -25,7 +25,7 @@ __global__ void __launch_bounds__(256) cast_fuv_kernel(const NbConst* __restrict
                                                        const float4* __restrict__ dirs,
                                                        const float2* __restrict__ rx,
                                                        float* __restrict__ att, int nstars,
-                                                       const float* star_override) {
+                                                       const float* star_override, float tau_cut) {
     const int nr = c->fnr, nu = c->fnu, nphi = c->fnphi, nray = nu * nphi;
     const long long gid = (blockIdx.x * (long long)blockDim.x + threadIdx.x) / G;
     const int lane = threadIdx.x % G;
@@ -82,7 +82,10 @@ __global__ void __launch_bounds__(256) cast_fuv_kernel(const NbConst* __restrict
         int prev = __shfl_up_sync(gmask, nb, 1, G);
         if (lane == 0) prev = ib;
         const bool stop = valid && nb >= nr;
-        const unsigned bal = __ballot_sync(gmask, stop);
+        // Past tau_cut (> 0) exp(-tau) is 0.0f (exp(-120) ~ 8e-53 lies far below the least float
+        // denormal) and stays 0 along the ray (dtau >= 0): the bins from here on are all 0.
+        const bool dark = tau_cut > 0.0f && valid && tau > tau_cut;
+        const unsigned bal = __ballot_sync(gmask, stop || dark);
         const unsigned mine = G == 32 ? bal : (bal >> ((threadIdx.x & 31) / G * G)) & ((1u << G) - 1u);
         const int first_stop = mine ? __ffs(mine) - 1 : G;
         if (valid && lane <= first_stop && nb > prev) {
@@ -90,7 +93,9 @@ __global__ void __launch_bounds__(256) cast_fuv_kernel(const NbConst* __restrict
             const int e = min(nb, nr);
             for (int b = prev; b < e; ++b) at(b) = v;
         }
-        if (mine) {
+        if (mine) {                              // a lane ran out of bins or into the dark
+            const int e_first = __shfl_sync(gmask, min(nb, nr), first_stop, G);
+            for (int b = e_first + lane; b < nr; b += G) at(b) = 0.0f;
             stopped = true;
             break;
         }
@@ -230,7 +235,8 @@ cudaError_t nb_launch_plane_fuv(const NbConst* c, const float* rho, const float*
 
 cudaError_t nb_launch_cast_fuv(const NbConst* c, const NbStarW* sw, const float4* dirs, const float* rho,
                                const float* xi, float* att, int nstars, int group, const float* star_override,
-                               int ref_layout, cudaStream_t s, int fnu, int fnphi, void* rx_scratch, long long ncell) {
+                               int ref_layout, cudaStream_t s, int fnu, int fnphi, void* rx_scratch, long long ncell,
+                               float tau_cut) {
     float2* rx = static_cast<float2*>(rx_scratch);
     {
         const long long b = (ncell + 255) / 256;
@@ -238,7 +244,8 @@ cudaError_t nb_launch_cast_fuv(const NbConst* c, const NbStarW* sw, const float4
     }
     const long long threads = (long long)fnu * fnphi * nstars * group;
     const int blocks = (int)((threads + 255) / 256);
-#define NB_FUV_LAUNCH(G, R) cast_fuv_kernel<G, R><<<blocks, 256, 0, s>>>(c, sw, dirs, rx, att, nstars, star_override)
+#define NB_FUV_LAUNCH(G, R) \
+    cast_fuv_kernel<G, R><<<blocks, 256, 0, s>>>(c, sw, dirs, rx, att, nstars, star_override, tau_cut)
     if (ref_layout) {
         NB_FUV_LAUNCH(32, true);
     } else {

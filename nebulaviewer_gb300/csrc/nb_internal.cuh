@@ -232,7 +232,9 @@ cudaError_t nb_launch_plane_fuv(const NbConst* c, const float* rho, const float*
 // packs (rho, xi) pairs into rx_scratch (ncell float2, 8-byte aligned) first
 cudaError_t nb_launch_cast_fuv(const NbConst* c, const NbStarW* sw, const float4* dirs, const float* rho,
                                const float* xi, float* att, int nstars, int group, const float* star_override,
-                               int ref_layout, cudaStream_t s, int fnu, int fnphi, void* rx_scratch, long long ncell);
+                               int ref_layout, cudaStream_t s, int fnu, int fnphi, void* rx_scratch, long long ncell,
+                               float tau_cut);
+#define NB_FUV_TAU_CUT 120.0f            // optical depth past which a FUV ray's remaining bins are 0
 cudaError_t nb_launch_apply_fuv(const NbConst* c, const NbStarW* sw, const float* att, int nstars, void* g0,
                                 cudaStream_t s, int nx, int ny, int half);
 cudaError_t nb_launch_pack(const NbConst* c, const float* rho, const float* mx, const float* my, const float* mz,

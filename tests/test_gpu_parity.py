@@ -338,3 +338,33 @@ def test_front_culling_changes_no_bit(nb, arith, case):
     ion = (xi1.view(torch.float32) > 0.5).float().mean().item()
     assert (0.0 < ion < 0.2) if case == "sheet12" else (0.05 < ion < 0.95)
     sim.close()
+
+
+@pytest.mark.parametrize("arith", ARITH)
+def test_fuv_cut_changes_no_bit(nb, arith):
+    """a FUV ray that stops once its optical depth passes the cut (exp(-tau) is 0.0f from there
+    on) leaves the same attenuation bins and the same G0, bit for bit, as marching to the edge;
+    the dense 12-star sheet has rays well past the cut"""
+    from nebulaviewer_gb300 import autotune as at, ics
+    _lib, S = nb
+    ic = ics.sheet(res=128, nstars=12)
+    fg = (32, 32, 64)
+    sim = S.Sim.from_state(ic["shape"], ic["dx"], ic["rho"], ic["stars"], ic["kinds"], ic["jets"], ic["jkinds"],
+                           ic["P"], mom=ic["mom"], rays=(128, 256), fuv_grid=fg, arith=arith)
+    sim.step(3)
+    out = {}
+    for cut in (0, 1):
+        at.put(sim, "fuv_cut", cut)
+        tabs = []
+        for st in sim.stars_absolute()[0]:
+            a = torch.empty(fg[2], fg[0], fg[1], device="cuda")
+            xyz = (C.c_double * 3)(*[float(v) for v in st[:3]])
+            _lib.check(sim._lib.nb_cast_fuv(sim._h, xyz, C.c_void_p(a.data_ptr())), sim._h, "nb_cast_fuv")
+            tabs.append(a.clone())
+        sim.update_render_fields(force=True)
+        torch.cuda.synchronize()
+        out[cut] = (torch.stack(tabs).view(torch.int32), sim._g0.clone().view(torch.int16))
+    assert torch.equal(out[0][0], out[1][0]) and torch.equal(out[0][1], out[1][1])
+    dark = (out[1][0].view(torch.float32) == 0.0).float().mean().item()
+    assert dark > 0.05                          # a good share of the bins lies past the cut
+    sim.close()
