@@ -17,7 +17,7 @@ from . import _lib
 CANDIDATES = {
     "chunk_i": (16, 32, 64),
     "tile_order": (0, 1),
-    "ray_group": (4, 8, 16),
+    "ray_group": (2, 4, 8, 16),
     "fuv_group": (8, 16, 32),
 }
 # which kernel kinds a knob moves (names of _lib.PROF_KINDS)

@@ -866,8 +866,9 @@ NB_EXPORT int nb_set_tuning(nb_handle h, int key, int value) {
             return NB_OK;
         case NB_TUNE_RAY_GROUP:
         case NB_TUNE_FUV_GROUP:
-            if (value != 8 && value != 16 && value != 32 && !(value == 4 && key == NB_TUNE_RAY_GROUP))
-                return fail(h, NB_ERR_ARG, "lanes per ray must be 4 (ionizing rays only), 8, 16 or 32");
+            if (value != 8 && value != 16 && value != 32 &&
+                !((value == 1 || value == 2 || value == 4) && key == NB_TUNE_RAY_GROUP))
+                return fail(h, NB_ERR_ARG, "lanes per ray must be 1, 2, 4 (ionizing rays only), 8, 16 or 32");
             (key == NB_TUNE_RAY_GROUP ? h->ray_group : h->fuv_group) = value;
             return NB_OK;
         default:
@@ -1142,7 +1143,8 @@ NB_EXPORT int nb_batch_set_option(nb_batch b, int key, int value) {
             b->grid = value;
             break;
         case NB_BATCH_RAY_GROUP:
-            if (value != 4 && value != 8 && value != 16 && value != 32) return bfail(b, NB_ERR_ARG, "bad ray group");
+            if (value != 1 && value != 2 && value != 4 && value != 8 && value != 16 && value != 32)
+                return bfail(b, NB_ERR_ARG, "bad ray group");
             b->ray_group = value;
             break;
         default: return bfail(b, NB_ERR_ARG, "unknown batch option");

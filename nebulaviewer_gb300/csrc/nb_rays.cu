@@ -473,6 +473,8 @@ cudaError_t nb_launch_cast_rays(const NbConst* c, const NbStarW* sw, const float
     const long long threads = (long long)nu * nphi * nstars * group;
     const int blocks = (int)((threads + 255) / 256);
     switch (group) {
+        case 1: cast_rays_kernel<1><<<blocks, 256, 0, s>>>(c, sw, dirs, rho, rfront, nstars, star_override, q_override); break;
+        case 2: cast_rays_kernel<2><<<blocks, 256, 0, s>>>(c, sw, dirs, rho, rfront, nstars, star_override, q_override); break;
         case 4: cast_rays_kernel<4><<<blocks, 256, 0, s>>>(c, sw, dirs, rho, rfront, nstars, star_override, q_override); break;
         case 8: cast_rays_kernel<8><<<blocks, 256, 0, s>>>(c, sw, dirs, rho, rfront, nstars, star_override, q_override); break;
         case 16: cast_rays_kernel<16><<<blocks, 256, 0, s>>>(c, sw, dirs, rho, rfront, nstars, star_override, q_override); break;
@@ -511,6 +513,8 @@ cudaError_t nb_launch_ionize_batch(const NbRayJob* jobs, int n_jobs, long long n
     const long long blocks = (threads + 255) / 256;
     if (blocks > 0) {
         switch (group) {
+            case 1: cast_rays_batch_kernel<1><<<(unsigned)blocks, 256, 0, s>>>(jobs, n_jobs, n_groups); break;
+            case 2: cast_rays_batch_kernel<2><<<(unsigned)blocks, 256, 0, s>>>(jobs, n_jobs, n_groups); break;
             case 4: cast_rays_batch_kernel<4><<<(unsigned)blocks, 256, 0, s>>>(jobs, n_jobs, n_groups); break;
             case 8: cast_rays_batch_kernel<8><<<(unsigned)blocks, 256, 0, s>>>(jobs, n_jobs, n_groups); break;
             case 16: cast_rays_batch_kernel<16><<<(unsigned)blocks, 256, 0, s>>>(jobs, n_jobs, n_groups); break;

@@ -54,10 +54,16 @@ __device__ __forceinline__ void ctrl_body(const NbConst* __restrict__ c, NbState
     double pulse = 0.0;
     if (!pre) {
         if (c->dt_cap > 0.0 && c->dt_cap < dt) dt = c->dt_cap;                           // sim.py:1106-1107
-        // sim.py:1108: max(0, 1 + jet_pulse * sin(2 pi t / jet_period))
-        const double arg = __ddiv_rn(__dmul_rn(6.283185307179586, t), c->jet_period);
-        pulse = __dadd_rn(1.0, __dmul_rn(c->jet_pulse, sin(arg)));
-        if (!(pulse > 0.0)) pulse = 0.0;
+        // sim.py:1108: max(0, 1 + jet_pulse * sin(2 pi t / jet_period)).  Only the jet source reads
+        // it; with jet == jet_proto == 0 every star's jet strength is 0 (sim.py:900-902) and the
+        // FP64 sine is skipped
+        if (c->jet != 0.0 || c->jet_proto != 0.0) {
+            const double arg = __ddiv_rn(__dmul_rn(6.283185307179586, t), c->jet_period);
+            pulse = __dadd_rn(1.0, __dmul_rn(c->jet_pulse, sin(arg)));
+            if (!(pulse > 0.0)) pulse = 0.0;
+        } else {
+            pulse = 1.0;
+        }
     }
     st->dt = dt;
     st->dt_f = (float)dt;

@@ -368,3 +368,38 @@ def test_fuv_cut_changes_no_bit(nb, arith):
     dark = (out[1][0].view(torch.float32) == 0.0).float().mean().item()
     assert dark > 0.05                          # a good share of the bins lies past the cut
     sim.close()
+
+
+@pytest.mark.parametrize("arith", ARITH)
+def test_ray_lanes_per_ray_agree(nb, arith):
+    """every lanes-per-ray shape of the ionizing rays (1 .. 32) gives the same fronts up to the
+    rounding of the column sums, and the Stromgren radius of uniform gas within a ray step"""
+    from nebulaviewer_gb300 import autotune as at, ics
+    _lib, S = nb
+    ic = ics.sheet(res=64, nstars=3)
+    sim = S.Sim.from_state(ic["shape"], ic["dx"], ic["rho"], ic["stars"], ic["kinds"], ic["jets"], ic["jkinds"],
+                           ic["P"], mom=ic["mom"], rays=(64, 128), fuv_grid=(16, 16, 32), arith=arith)
+    st = sim.stars_absolute()[0]
+    fronts = {}
+    for g in (1, 2, 4, 8, 16, 32):
+        at.put(sim, "ray_group", g)
+        rf = torch.zeros((len(st), 128, 64), device="cuda")
+        for i, s in enumerate(st):
+            xyz = (C.c_double * 3)(*[float(v) for v in s[:3]])
+            _lib.check(sim._lib.nb_cast_rays(sim._h, xyz, float(s[3]), C.c_void_p(rf[i].data_ptr())), sim._h, "rays")
+        fronts[g] = rf.cpu().numpy()
+    for g, rf in fronts.items():
+        assert rel_linf(rf, fronts[4]) < 1e-5, g
+    sim.close()
+    n, dens = 64, 2.0
+    Q = 4.0 * 0.2 ** 3 / 3.0
+    uni = S.Sim.from_state((n, n, n), 1.0 / n, torch.full((n, n, n), dens, device="cuda"), [(0.5, 0.5, 0.5, 1.0, 0.0)],
+                           ["main"], [(0, 0, 1.0)], ["none"], dict(q_main=Q, q_ramp=0.0), rays=(32, 64),
+                           start_main=False, arith=arith)
+    for g in (1, 2):
+        at.put(uni, "ray_group", g)
+        rf = torch.zeros((32, 64), device="cuda")
+        xyz = (C.c_double * 3)(0.5, 0.5, 0.5)
+        _lib.check(uni._lib.nb_cast_rays(uni._h, xyz, Q, C.c_void_p(rf.data_ptr())), uni._h, "rays")
+        assert np.abs(rf.cpu().numpy() - 0.2).max() < 0.5 / n
+    uni.close()
