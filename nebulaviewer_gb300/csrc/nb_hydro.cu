@@ -108,6 +108,14 @@ __device__ __forceinline__ F2 nmsub2(F2 c, F2 a, F2 b) {
 }
 __device__ __forceinline__ F2 splat2(float a) { return mk2(a, a); }
 
+// The fast build's reciprocal: one approximate reciprocal (<= 1 ulp) that the three divisions
+// by one density share (the exact build divides, as the reference does).
+__device__ __forceinline__ float rcp_fast(float x) {
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
 // minmod given the product a*b (nebula3d.py:40-46)
 __device__ __forceinline__ float minmod_p(float a, float b, float ab) {
     if (ab <= 0.0f) return 0.0f;
@@ -218,7 +226,7 @@ __device__ __forceinline__ float4 face_flux_paired(const float4 qa, const float4
     const F2 T0 = madd2(slsr, sub2(UR0, UL0), madd2(SR2, FL0, mul2(nSL, FR0)));
     const F2 T1 = madd2(slsr, sub2(UR1, UL1), madd2(SR2, FL1, mul2(nSL, FR1)));
 #if NB_ARITH_FAST
-    const F2 inv = splat2(1.0f / den);
+    const F2 inv = splat2(rcp_fast(den));
     const F2 F0 = mul2(T0, inv), F1 = mul2(T1, inv);
     return make_float4(lo(F0), hi(F0), lo(F1), hi(F1));
 #else
@@ -399,8 +407,14 @@ __device__ __forceinline__ void hydro_tile(const HydroLaunch& L, int tile, unsig
             const float r = fmaxr(rb[o], floor_);
             const float xv = rb[4 * SM::RAW_FIELD + o];
             const float c2 = cn2 + xv * (ci2 - cn2);
+#if NB_ARITH_FAST
+            const float ri = rcp_fast(r);
+            pp[jj * PW + kk] = make_float4(r, rb[SM::RAW_FIELD + o] * ri, rb[2 * SM::RAW_FIELD + o] * ri,
+                                           rb[3 * SM::RAW_FIELD + o] * ri);
+#else
             pp[jj * PW + kk] = make_float4(r, rb[SM::RAW_FIELD + o] / r, rb[2 * SM::RAW_FIELD + o] / r,
                                            rb[3 * SM::RAW_FIELD + o] / r);
+#endif
             cp[jj * PW + kk] = make_float2(c2, sqrtf(c2));
         }
         __syncthreads();                         // every thread is done with the raw slot
@@ -520,12 +534,24 @@ __device__ __forceinline__ void hydro_tile(const HydroLaunch& L, int tile, unsig
         const float o0 = a * u00 + b * un0, o1 = a * u01 + b * un1, o2 = a * u02 + b * un2, o3 = a * u03 + b * un3;
 #endif
         const float r = fmaxr(o0, floor_);
+#if NB_ARITH_FAST
+        // one reciprocal for the three velocities and the max speed; the speed cap compares the
+        // squared speed and takes a root only for the capped cells
+        const float ri = rcp_fast(r);
+        float vx = o1 * ri, vy = o2 * ri, vz = o3 * ri;
+        const float s2 = (vx * vx + vy * vy) + vz * vz;
+        if (s2 > vmax * vmax) {
+            const float f = vmax * rsqrtf(s2);
+            vx = vx * f; vy = vy * f; vz = vz * f;
+        }
+#else
         float vx = o1 / r, vy = o2 / r, vz = o3 / r;
         const float sp = sqrtf((vx * vx + vy * vy) + vz * vz);
         if (sp > vmax) {
             const float f = vmax / sp;
             vx = vx * f; vy = vy * f; vz = vz * f;
         }
+#endif
         const float m1 = r * vx, m2 = r * vy, m3 = r * vz;
         if (inside) {
             L.out[0][cell] = r;
@@ -533,7 +559,11 @@ __device__ __forceinline__ void hydro_tile(const HydroLaunch& L, int tile, unsig
             L.out[2][cell] = m2;
             L.out[3][cell] = m3;
             if (STAGE2 && L.smax_bits) {         // nebula3d.py:158-162 on the new state
+#if NB_ARITH_FAST
+                const float v = fabsf(m1 * ri) + fabsf(m2 * ri) + fabsf(m3 * ri) + c[own].y;
+#else
                 const float v = fabsf(m1 / r) + fabsf(m2 / r) + fabsf(m3 / r) + c[own].y;
+#endif
                 vmax_local = fmaxr(v, vmax_local);
             }
         }
