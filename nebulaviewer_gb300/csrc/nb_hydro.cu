@@ -259,8 +259,11 @@ struct HydroSmem {
     static int bytes(int nstars) { return jet_list_offset(nstars) + 16 + ((nstars + 15) & ~15); }
 };
 
+#ifndef NB_HYDRO_TJ
+#define NB_HYDRO_TJ 8                 // tile rows along j (one warp per row; 16 measured 2% slower)
+#endif
 #ifndef NB_HYDRO_MINB
-#define NB_HYDRO_MINB 4               // resident blocks per SM the register budget is sized for (64 regs)
+#define NB_HYDRO_MINB (32 / NB_HYDRO_TJ)  // resident blocks per SM the register budget is sized for (64 regs)
 #endif
 
 // One (j,k) tile column of one instance, marched over its i-chunk.  Called once per block by
@@ -685,11 +688,11 @@ cudaError_t run_batch(const HydroLaunch* Ls, const int2* work, int n_work, unsig
 
 }  // namespace
 
-int nb_hydro_tile_j() { return 8; }
+int nb_hydro_tile_j() { return NB_HYDRO_TJ; }
 
 // resident blocks per SM of the persistent stage kernel (sizes its grid)
 int nb_hydro_batch_blocks_per_sm(int solver, int limiter, int max_stars) {
-    constexpr int TJ = 8;
+    constexpr int TJ = NB_HYDRO_TJ;
     const int smem = HydroSmem<TJ>::bytes(max_stars);
     auto occ = [&](auto kern) {
         int n = 0;
@@ -711,7 +714,7 @@ int nb_hydro_batch_blocks_per_sm(int solver, int limiter, int max_stars) {
 }
 
 cudaError_t nb_launch_hydro(const HydroLaunch& L, int solver, int limiter, cudaStream_t s) {
-    constexpr int TJ = 8;
+    constexpr int TJ = NB_HYDRO_TJ;
     if (solver == NB_SOLVER_RUSANOV) return run_stage<NB_SOLVER_RUSANOV, 0, TJ>(L, s);
     switch (limiter) {
         case NB_LIM_VANLEER: return run_stage<NB_SOLVER_HLL, NB_LIM_VANLEER, TJ>(L, s);
@@ -722,7 +725,7 @@ cudaError_t nb_launch_hydro(const HydroLaunch& L, int solver, int limiter, cudaS
 
 cudaError_t nb_launch_hydro_batch(const HydroLaunch* Ls, const int2* work, int n_work, unsigned* counter,
                                   int max_stars, int stage2, int solver, int limiter, int grid, cudaStream_t s) {
-    constexpr int TJ = 8;
+    constexpr int TJ = NB_HYDRO_TJ;
     if (solver == NB_SOLVER_RUSANOV)
         return run_batch<NB_SOLVER_RUSANOV, 0, TJ>(Ls, work, n_work, counter, max_stars, stage2, grid, s);
     switch (limiter) {
