@@ -403,3 +403,97 @@ def test_ray_lanes_per_ray_agree(nb, arith):
         _lib.check(uni._lib.nb_cast_rays(uni._h, xyz, Q, C.c_void_p(rf.data_ptr())), uni._h, "rays")
         assert np.abs(rf.cpu().numpy() - 0.2).max() < 0.5 / n
     uni.close()
+
+
+@pytest.mark.parametrize("solver,lim", (("hll", "minmod"), ("hll", "vanleer"), ("hll", "mc"), ("rusanov", "minmod")))
+def test_ragged_grid_many_stars_stage_bit_identical(nb, solver, lim):
+    """a 37 x 45 x 100 grid (partial j and k tiles, uneven i-chunks), dx = 0.01 (not a power of
+    two), 40 stars with jets, proto-jets and wind (the per-tile jet list takes two ballot rounds):
+    both RK2 stages bit-identical to the oracle's restatement of the reference kernel"""
+    import math
+    import oracle as O
+    from nebulaviewer_gb300 import autotune as at
+    from nebulaviewer_gb300.params import make_params, sound_speeds
+    _lib, S = nb
+    shape, dx = (37, 45, 100), 0.01
+    rng = np.random.default_rng(11)
+    rho = (0.5 + rng.random(shape)).astype(np.float32)
+    mom = [(0.4 * rng.standard_normal(shape)).astype(np.float32) for _ in range(3)]
+    xi = rng.random(shape).astype(np.float32)
+    L = np.array(shape) * dx
+    pos = rng.random((40, 3)) * L
+    stars = [(float(p[0]), float(p[1]), float(p[2]), float(0.5 + rng.random()), 0.0) for p in pos]
+    d = rng.standard_normal((40, 3))
+    jets = [tuple(float(v) for v in a / np.linalg.norm(a)) for a in d]
+    jkinds = [("jet", "proto", "none")[i % 3] for i in range(40)]
+    P = dict(q_main=1.0, q_ramp=0.0, wind=0.5, jet=3.0, jet_proto=2.0, jet_r=0.12, jet_angle=35.0, max_stars=64,
+             solver=solver, limiter=lim, floor=2e-3, cfl=0.3)
+    sim = S.Sim.from_state(shape, dx, torch.as_tensor(rho, device="cuda"), stars, ["main"] * 40, jets, jkinds, P,
+                           mom=[torch.as_tensor(m, device="cuda") for m in mom], rays=(16, 32), fuv_grid=(8, 8, 16),
+                           start_main=False, arith="exact")
+    at.put(sim, "chunk_i", 10)                            # 4 chunks of 9 or 10 planes
+    sim._xi.copy_(t32(xi))
+    Pm = make_params(base=P)
+    cn2, ci2, vmax = sound_speeds(Pm)
+    o = O.OracleSim(shape, dx, rho, stars, ["main"] * 40, jets, jkinds, Pm, rays=(16, 32), fuv_grid=(8, 8, 16),
+                    mom=mom, start_main=False, cn2=cn2, ci2=ci2, vmax=vmax)
+    o._set_star_weights()
+    assert float((o.jet_arr[:40, 3] > 0).sum()) > 20
+    dt, pulse = 2e-4, 1.3
+    U = [t32(rho)] + [t32(m) for m in mom]
+    g1 = [torch.zeros_like(U[0]) for _ in range(4)]
+    g2 = [torch.zeros_like(U[0]) for _ in range(4)]
+    F = lambda ts: _lib.f4([t.data_ptr() for t in ts])  # noqa: E731
+    _lib.check(sim._lib.nb_hydro_stage(sim._h, F(U), F(U), F(g1), 0.0, 1.0, dt, pulse), sim._h, "stage 1")
+    _lib.check(sim._lib.nb_hydro_stage(sim._h, F(g1), F(U), F(g2), 0.5, 0.5, dt, pulse), sim._h, "stage 2")
+    torch.cuda.synchronize()
+    Un = [rho] + mom
+    o1 = [np.zeros(shape, np.float32) for _ in range(4)]
+    o2 = [np.zeros(shape, np.float32) for _ in range(4)]
+    common = dict(stars=o.star_arr, nstars=40, wind=0.5, jets=o.jet_arr, jet_cos=math.cos(math.radians(35.0)),
+                  jet_r=0.12, pulse=pulse, dt=dt, dx=dx, floor_=2e-3, cn2=cn2, ci2=ci2, vmax=vmax,
+                  solver=1 if solver == "hll" else 0, lim={"minmod": 0, "vanleer": 1, "mc": 2}[lim])
+    o.K.hydro_stage(Un, xi, Un, o1, a=0.0, b=1.0, **common)
+    o.K.hydro_stage(o1, xi, Un, o2, a=0.5, b=0.5, **common)
+    assert bits_equal(torch.stack(g1).cpu().numpy(), np.stack(o1))
+    assert bits_equal(torch.stack(g2).cpu().numpy(), np.stack(o2))
+    sim.close()
+
+
+@pytest.mark.parametrize("arith", ARITH)
+@pytest.mark.parametrize("nstars", (0, 36))
+def test_star_count_edges_against_oracle(nb, arith, nstars):
+    """no stars at all (no rays, no fronts, no FUV sources), and 36 stars (more than a row table
+    holds: the per-cell front and FUV forms, no culling) on a 40 x 24 x 44 grid, stepped and
+    ionized against the oracle"""
+    import oracle as O
+    from nebulaviewer_gb300.params import make_params, sound_speeds
+    _, S = nb
+    shape, dx = (40, 24, 44), 1.0 / 48
+    rng = np.random.default_rng(5 + nstars)
+    rho = (0.05 + 0.5 * rng.random(shape) ** 4).astype(np.float32)
+    L = np.array(shape) * dx
+    pos = rng.random((nstars, 3)) * L * 0.9 + 0.05 * L
+    stars = [(float(p[0]), float(p[1]), float(p[2]), float(0.5 + rng.random()), 0.0) for p in pos]
+    P = dict(q_main=4e-6, q_ramp=0.0, wind=0.5, max_stars=64, solver="hll", limiter="minmod", cfl=0.3)
+    g = S.Sim.from_state(shape, dx, torch.as_tensor(rho, device="cuda"), stars, ["main"] * nstars,
+                         [(0.0, 0.0, 1.0)] * nstars, ["none"] * nstars, P, rays=(32, 64), fuv_grid=(16, 16, 32),
+                         arith=arith)
+    Pm = make_params(base=P)
+    cn2, ci2, vmax = sound_speeds(Pm)
+    o = O.OracleSim(shape, dx, rho, stars, ["main"] * nstars, [(0.0, 0.0, 1.0)] * nstars, ["none"] * nstars, Pm,
+                    rays=(32, 64), fuv_grid=(16, 16, 32), cn2=cn2, ci2=ci2, vmax=vmax)
+    _compare(g, o, 1e-6)
+    for _ in range(4):
+        g.step(1)
+        o.step(1)
+        _compare(g, o, 1e-5)
+    g.update_render_fields(force=True)
+    o.update_render_fields(force=True)
+    g0 = g.g0.numpy().astype(np.float32)
+    if nstars == 0:
+        assert not g0.any() and not g.xi.numpy().any()
+    else:
+        assert rel_linf(g0, o.g0.astype(np.float32)) < 5e-3
+        assert 0.0 < float((g.xi.numpy() > 0.5).mean()) < 0.9
+    g.close()
