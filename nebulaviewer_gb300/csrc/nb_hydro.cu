@@ -126,17 +126,27 @@ __device__ __forceinline__ float minmod_p(float a, float b, float ab) {
 // component normal to the face).  cs = (c^2, c) of a cell.
 //   dot((0, L1, L2, L3), e_AX) == 0 + L_AX exactly (the other products are +-0 and the
 //   velocities are finite), and e_c * (rho c^2) == +0 for c != AX.
-template <int SOLVER, int LIM, int AX>
-__device__ __forceinline__ float4 face_flux_scalar(const float4 qa, const float4 qb, const float4 qc, const float4 qd,
-                                            const float2 csb, const float2 csc, const float floor_) {
-    constexpr int LM = SOLVER == NB_SOLVER_HLL ? LIM : 0;
+// The limited slope (4 components) of cell b between its neighbours a and c along one axis:
+// slope_lim(b - a, c - b).  A face's right slope is the next face's left slope along the same
+// axis (same operands, same bits), which the x march carries from face to face.
+template <int LM>
+__device__ __forceinline__ float4 slopes_scalar(const float4 qa, const float4 qb, const float4 qc) {
+    float sl[4];
+#pragma unroll
+    for (int c = 0; c < 4; ++c) sl[c] = slope_lim<LM>(comp(qb, c) - comp(qa, c), comp(qc, c) - comp(qb, c));
+    return make_float4(sl[0], sl[1], sl[2], sl[3]);
+}
+
+// the face flux from the two cells and their limited slopes
+template <int SOLVER, int AX>
+__device__ __forceinline__ float4 face_flux_scalar_sl(const float4 qb, const float4 qc, const float4 sl,
+                                                      const float4 sr, const float2 csb, const float2 csc,
+                                                      const float floor_) {
     float L[4], R[4];
 #pragma unroll
     for (int c = 0; c < 4; ++c) {
-        const float a = comp(qa, c), b = comp(qb, c), cc = comp(qc, c), d = comp(qd, c);
-        const float d1 = b - a, d2 = cc - b, d3 = d - cc;
-        L[c] = b + 0.5f * slope_lim<LM>(d1, d2);
-        R[c] = cc - 0.5f * slope_lim<LM>(d2, d3);
+        L[c] = comp(qb, c) + 0.5f * comp(sl, c);
+        R[c] = comp(qc, c) - 0.5f * comp(sr, c);
     }
     const float rL = fmaxr(L[0], floor_), rR = fmaxr(R[0], floor_);
     const float unL = 0.0f + L[AX], unR = 0.0f + R[AX];
@@ -166,31 +176,40 @@ __device__ __forceinline__ float4 face_flux_scalar(const float4 qa, const float4
     return make_float4(F[0], F[1], F[2], F[3]);
 }
 
-// The same face flux on component pairs: the float operations and operands of face_flux_scalar
-// (the minmod sign test multiplies the same two differences), with a*b+c fused.
 template <int SOLVER, int LIM, int AX>
-__device__ __forceinline__ float4 face_flux_paired(const float4 qa, const float4 qb, const float4 qc, const float4 qd,
+__device__ __forceinline__ float4 face_flux_scalar(const float4 qa, const float4 qb, const float4 qc, const float4 qd,
                                                    const float2 csb, const float2 csc, const float floor_) {
     constexpr int LM = SOLVER == NB_SOLVER_HLL ? LIM : 0;
+    return face_flux_scalar_sl<SOLVER, AX>(qb, qc, slopes_scalar<LM>(qa, qb, qc), slopes_scalar<LM>(qb, qc, qd), csb,
+                                           csc, floor_);
+}
+
+// The same face flux on component pairs: the float operations and operands of face_flux_scalar
+// (the minmod sign test multiplies the same two differences), with a*b+c fused.
+// slopes_scalar on component pairs (the minmod sign test multiplies the same two differences)
+template <int LM>
+__device__ __forceinline__ float4 slopes_paired(const float4 qa, const float4 qb, const float4 qc) {
     const F2 a0 = mk2(qa.x, qa.y), a1 = mk2(qa.z, qa.w), b0 = mk2(qb.x, qb.y), b1 = mk2(qb.z, qb.w);
-    const F2 c0 = mk2(qc.x, qc.y), c1 = mk2(qc.z, qc.w), e0 = mk2(qd.x, qd.y), e1 = mk2(qd.z, qd.w);
+    const F2 c0 = mk2(qc.x, qc.y), c1 = mk2(qc.z, qc.w);
     const F2 d1_0 = sub2(b0, a0), d1_1 = sub2(b1, a1);
     const F2 d2_0 = sub2(c0, b0), d2_1 = sub2(c1, b1);
-    const F2 d3_0 = sub2(e0, c0), d3_1 = sub2(e1, c1);
-    F2 sl0, sl1, sr0, sr1;
     if (LM == 0) {
-        const F2 p12_0 = mul2(d1_0, d2_0), p12_1 = mul2(d1_1, d2_1);
-        const F2 p23_0 = mul2(d2_0, d3_0), p23_1 = mul2(d2_1, d3_1);
-        sl0 = mk2(minmod_p(lo(d1_0), lo(d2_0), lo(p12_0)), minmod_p(hi(d1_0), hi(d2_0), hi(p12_0)));
-        sl1 = mk2(minmod_p(lo(d1_1), lo(d2_1), lo(p12_1)), minmod_p(hi(d1_1), hi(d2_1), hi(p12_1)));
-        sr0 = mk2(minmod_p(lo(d2_0), lo(d3_0), lo(p23_0)), minmod_p(hi(d2_0), hi(d3_0), hi(p23_0)));
-        sr1 = mk2(minmod_p(lo(d2_1), lo(d3_1), lo(p23_1)), minmod_p(hi(d2_1), hi(d3_1), hi(p23_1)));
-    } else {
-        sl0 = mk2(slope_lim<LM>(lo(d1_0), lo(d2_0)), slope_lim<LM>(hi(d1_0), hi(d2_0)));
-        sl1 = mk2(slope_lim<LM>(lo(d1_1), lo(d2_1)), slope_lim<LM>(hi(d1_1), hi(d2_1)));
-        sr0 = mk2(slope_lim<LM>(lo(d2_0), lo(d3_0)), slope_lim<LM>(hi(d2_0), hi(d3_0)));
-        sr1 = mk2(slope_lim<LM>(lo(d2_1), lo(d3_1)), slope_lim<LM>(hi(d2_1), hi(d3_1)));
+        const F2 p_0 = mul2(d1_0, d2_0), p_1 = mul2(d1_1, d2_1);
+        return make_float4(minmod_p(lo(d1_0), lo(d2_0), lo(p_0)), minmod_p(hi(d1_0), hi(d2_0), hi(p_0)),
+                           minmod_p(lo(d1_1), lo(d2_1), lo(p_1)), minmod_p(hi(d1_1), hi(d2_1), hi(p_1)));
     }
+    return make_float4(slope_lim<LM>(lo(d1_0), lo(d2_0)), slope_lim<LM>(hi(d1_0), hi(d2_0)),
+                       slope_lim<LM>(lo(d1_1), lo(d2_1)), slope_lim<LM>(hi(d1_1), hi(d2_1)));
+}
+
+// The same face flux on component pairs: the float operations and operands of face_flux_scalar_sl,
+// with a*b+c fused.
+template <int SOLVER, int AX>
+__device__ __forceinline__ float4 face_flux_paired_sl(const float4 qb, const float4 qc, const float4 sl,
+                                                      const float4 sr, const float2 csb, const float2 csc,
+                                                      const float floor_) {
+    const F2 b0 = mk2(qb.x, qb.y), b1 = mk2(qb.z, qb.w), c0 = mk2(qc.x, qc.y), c1 = mk2(qc.z, qc.w);
+    const F2 sl0 = mk2(sl.x, sl.y), sl1 = mk2(sl.z, sl.w), sr0 = mk2(sr.x, sr.y), sr1 = mk2(sr.z, sr.w);
     const F2 half = splat2(0.5f);
     const F2 L0 = madd2(half, sl0, b0), L1 = madd2(half, sl1, b1);      // b + 0.5 * slope
     const F2 R0 = nmsub2(c0, half, sr0), R1 = nmsub2(c1, half, sr1);    // c - 0.5 * slope
@@ -235,12 +254,44 @@ __device__ __forceinline__ float4 face_flux_paired(const float4 qa, const float4
 }
 
 template <int SOLVER, int LIM, int AX>
+__device__ __forceinline__ float4 face_flux_paired(const float4 qa, const float4 qb, const float4 qc, const float4 qd,
+                                                   const float2 csb, const float2 csc, const float floor_) {
+    constexpr int LM = SOLVER == NB_SOLVER_HLL ? LIM : 0;
+    return face_flux_paired_sl<SOLVER, AX>(qb, qc, slopes_paired<LM>(qa, qb, qc), slopes_paired<LM>(qb, qc, qd), csb,
+                                           csc, floor_);
+}
+
+template <int SOLVER, int LIM, int AX>
 __device__ __forceinline__ float4 face_flux(const float4 qa, const float4 qb, const float4 qc, const float4 qd,
                                             const float2 csb, const float2 csc, const float floor_) {
 #if NB_PAIRED
     return face_flux_paired<SOLVER, LIM, AX>(qa, qb, qc, qd, csb, csc, floor_);
 #else
     return face_flux_scalar<SOLVER, LIM, AX>(qa, qb, qc, qd, csb, csc, floor_);
+#endif
+}
+
+template <int SOLVER, int LIM>
+__device__ __forceinline__ float4 cell_slopes(const float4 qa, const float4 qb, const float4 qc) {
+    constexpr int LM = SOLVER == NB_SOLVER_HLL ? LIM : 0;
+#if NB_PAIRED
+    return slopes_paired<LM>(qa, qb, qc);
+#else
+    return slopes_scalar<LM>(qa, qb, qc);
+#endif
+}
+
+// The x face between cells b and c of the march: `slope` holds cell b's limited slope on entry
+// (the previous face's right slope) and cell c's on return.
+template <int SOLVER, int LIM>
+__device__ __forceinline__ float4 face_flux_x(const float4 qb, const float4 qc, const float4 qd, const float2 csb,
+                                              const float2 csc, const float floor_, float4& slope) {
+    const float4 sl = slope;
+    slope = cell_slopes<SOLVER, LIM>(qb, qc, qd);
+#if NB_PAIRED
+    return face_flux_paired_sl<SOLVER, 1>(qb, qc, sl, slope, csb, csc, floor_);
+#else
+    return face_flux_scalar_sl<SOLVER, 1>(qb, qc, sl, slope, csb, csc, floor_);
 #endif
 }
 
@@ -356,6 +407,7 @@ __device__ __forceinline__ void hydro_tile(const HydroLaunch& L, int tile, unsig
     }
 
     float4 fx_prev = make_float4(0.f, 0.f, 0.f, 0.f);
+    float4 xslope = make_float4(0.f, 0.f, 0.f, 0.f);    // limited x slope of the march's cell p-2
     float vmax_local = 0.0f;
 
     // clamped global -> raw-tile coordinates
@@ -380,7 +432,7 @@ __device__ __forceinline__ void hydro_tile(const HydroLaunch& L, int tile, unsig
         if (work && inside) {
             ur = L.in[0][cell]; umx = L.in[1][cell]; umy = L.in[2][cell]; umz = L.in[3][cell];
             uxi = L.xi[cell];
-            if (STAGE2) {
+            if (STAGE2) {                        // early: read only at the end, 4 more live registers
                 u00 = L.u0[0][cell]; u01 = L.u0[1][cell]; u02 = L.u0[2][cell]; u03 = L.u0[3][cell];
             }
         }
@@ -423,12 +475,11 @@ __device__ __forceinline__ void hydro_tile(const HydroLaunch& L, int tile, unsig
         __syncthreads();                         // every thread is done with the raw slot
         if (tid == 0 && p + 1 <= P1) issue(p + 1);
         if (p < P0 + 3) continue;
-        // x face (p-2)+1/2 from the own column of planes p-3..p
-        const float4 fx_new = face_flux<SOLVER, LIM, 1>(prim[((p - 3 - P0) & 3) * PSLOT + own],
-                                                        prim[((p - 2 - P0) & 3) * PSLOT + own],
-                                                        prim[((p - 1 - P0) & 3) * PSLOT + own], pp[own],
-                                                        cs[((p - 2 - P0) % 3) * PSLOT + own],
-                                                        cs[((p - 1 - P0) % 3) * PSLOT + own], floor_);
+        // x face (p-2)+1/2 from the own column of planes p-2..p and the carried slope of p-2
+        const float4 qx1 = prim[((p - 2 - P0) & 3) * PSLOT + own], qx2 = prim[((p - 1 - P0) & 3) * PSLOT + own];
+        if (p == P0 + 3) xslope = cell_slopes<SOLVER, LIM>(prim[((p - 3 - P0) & 3) * PSLOT + own], qx1, qx2);
+        const float4 fx_new = face_flux_x<SOLVER, LIM>(qx1, qx2, pp[own], cs[((p - 2 - P0) % 3) * PSLOT + own],
+                                                       cs[((p - 1 - P0) % 3) * PSLOT + own], floor_, xslope);
         if (!work) { fx_prev = fx_new; continue; }
         // ---- cell plane i = p - 2
         const int si = (i - P0) & 3;
