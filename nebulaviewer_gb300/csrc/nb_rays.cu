@@ -177,6 +177,9 @@ __device__ __forceinline__ void apply_front_row(const NbConst& C, const float4* 
     const int i = row / ny, j = row - (row / ny) * ny;
     const long long base = (long long)row * nz;
     const float dx = C.dx, width = C.width;
+#if NB_ARITH_FAST
+    const float inv_width = 1.0f / width;
+#endif
     const float two_pi = 2.0f * pi_f();
     const float px = ((float)i + 0.5f) * dx, py = ((float)j + 0.5f) * dx;
     const long long rstride = (long long)nu * nphi;
@@ -207,9 +210,7 @@ __device__ __forceinline__ void apply_front_row(const NbConst& C, const float4* 
                     s = s0 + e;
                     on[e] = s < nstars && act[s];
                 }
-                r[e] = tu[e] = tp[e] = 0.0f;
-                g00[e] = g01[e] = g10[e] = g11[e] = 0.0f;
-                if (!on[e]) continue;
+                if (!on[e]) continue;                   // an empty slot's values are never read
                 const float4 sp = st[s];
                 const float* rfs = rfront + (long long)s * rstride;
                 const float rz = pz - sp.z;
@@ -231,7 +232,11 @@ __device__ __forceinline__ void apply_front_row(const NbConst& C, const float4* 
                     c0 = wrap_index(ip, nphi) * nu;
                     c1 = wrap_index(ip + 1, nphi) * nu;
                 }
+#if NB_ARITH_FAST
+                const float u = rz * rcp_approx(r[e]);
+#else
                 const float u = rz / r[e];
+#endif
                 const float fu = (u + 1.0f) * 0.5f * (float)nu - 0.5f;
                 const int iu = (int)floorf(fu);
                 tu[e] = fu - (float)iu;
@@ -247,7 +252,11 @@ __device__ __forceinline__ void apply_front_row(const NbConst& C, const float4* 
                 const float ra = g00[e] * (1.0f - tp[e]) + g01[e] * tp[e];
                 const float rb = g10[e] * (1.0f - tp[e]) + g11[e] * tp[e];
                 const float rf = ra * (1.0f - tu[e]) + rb * tu[e];
+#if NB_ARITH_FAST
+                const float val = fminr(fmaxr(0.0f, (rf - r[e]) * inv_width + 0.5f), 1.0f);
+#else
                 const float val = fminr(fmaxr(0.0f, (rf - r[e]) / width + 0.5f), 1.0f);
+#endif
                 if (val > xi) xi = val;              // in star order, as the reference merges
                 df = fminr(df, r[e] - rf);
             }

@@ -35,6 +35,13 @@ __device__ __forceinline__ float sample_n(const float* __restrict__ a, int nx, i
     return c0 + (c1 - c0) * fz;
 }
 
+// an approximate reciprocal (<= 1 ulp), for the fast build's divisions by a clamped distance
+__device__ __forceinline__ float rcp_approx(float x) {
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
 // sample_n of two fields stored interleaved ((rho, xi) pairs): the same corners, weights and
 // float operations per field as two sample_n calls, with one 8-byte load per corner.
 __device__ __forceinline__ float2 sample_n2(const float2* __restrict__ a, int nx, int ny, int nz, float px, float py,

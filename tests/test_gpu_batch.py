@@ -48,6 +48,11 @@ def same(a, b, exact=True):
     for x, y in zip(a[:6], b[:6]):
         if exact:
             assert torch.equal(x, y)
+        elif x.dtype == torch.float16:
+            # an fp16 field (dfront): the fast build's last-bit float32 differences may cross an
+            # fp16 rounding boundary; within 2 fp16 ulps (2^-9 relative, above the subnormals)
+            xd, yd = x.double(), y.double()
+            assert bool(((xd - yd).abs() <= 2.0 ** -9 * torch.clamp(yd.abs(), min=2.0 ** -14)).all())
         else:
             xd, yd = x.double(), y.double()
             assert float((xd - yd).abs().max()) <= 1e-5 * max(float(yd.abs().max()), 1e-30)
