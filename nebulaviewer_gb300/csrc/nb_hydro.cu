@@ -674,8 +674,11 @@ __global__ void __launch_bounds__(TK * TJ, NB_HYDRO_MINB) hydro_stage_kernel(con
 // Persistent batched stage: blocks take (instance, tile) work items from a list spanning many
 // instances of different sizes, in list order, through one atomic counter (reset by the
 // batched control kernel before every step).
+#ifndef NB_HYDRO_BATCH_MINB
+#define NB_HYDRO_BATCH_MINB 3            // the persistent kernel's loop state needs the 80-register budget
+#endif
 template <int SOLVER, int LIM, int TJ, bool STAGE2>
-__global__ void __launch_bounds__(TK * TJ, NB_HYDRO_MINB)
+__global__ void __launch_bounds__(TK * TJ, NB_HYDRO_BATCH_MINB)
 hydro_batch_kernel(const HydroLaunch* __restrict__ Ls, const int2* __restrict__ work, int n_work,
                    unsigned* counter) {
     extern __shared__ __align__(128) unsigned char smem[];
@@ -761,7 +764,7 @@ int nb_hydro_batch_blocks_per_sm(int solver, int limiter, int max_stars) {
     else if (limiter == NB_LIM_VANLEER) n = occ(hydro_batch_kernel<NB_SOLVER_HLL, NB_LIM_VANLEER, TJ, true>);
     else if (limiter == NB_LIM_MC) n = occ(hydro_batch_kernel<NB_SOLVER_HLL, NB_LIM_MC, TJ, true>);
     else n = occ(hydro_batch_kernel<NB_SOLVER_HLL, NB_LIM_MINMOD, TJ, true>);
-    return n > 0 ? n : NB_HYDRO_MINB;
+    return n > 0 ? n : NB_HYDRO_BATCH_MINB;
 }
 
 cudaError_t nb_launch_hydro(const HydroLaunch& L, int solver, int limiter, cudaStream_t s) {
