@@ -967,6 +967,8 @@ NbRayJob ray_job(nb_instance* h) {
     J.smax = &h->st->smax_bits;
     J.nstars = h->nstars;
     J.half = h->d.fields_fp32 ? 0 : 1;
+    J.front_parts = (h->front_cull && h->nstars >= 1 && h->nstars <= NB_ROW_STARS) ? h->front_parts : nullptr;
+    J.nray = (long long)h->d.nu * h->d.nphi;
     return J;
 }
 
@@ -994,7 +996,7 @@ int batch_hydro(nb_batch_s* b) {
 
 int batch_ionize(nb_batch_s* b, const NbRayJob* jobs, int n_jobs, long long groups, long long blocks,
                  const std::vector<int>& listed) {
-    b->launches += 4;
+    b->launches += 5;                       // control, rays, front ranges, front apply, smoothing
     BCK(b, nb_launch_ctrl_batch(b->d_inst, (int)b->inst.size(), 0, nullptr, b->bs));
     for (int i : listed) {
         nb_instance* h = b->inst[i];

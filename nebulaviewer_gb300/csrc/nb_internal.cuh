@@ -136,6 +136,8 @@ struct NbRayJob {
     long long blk0;       // first row block of this job (8 rows per block)
     int nstars;
     int half;
+    float2* front_parts;  // the instance's front-radius partials when apply_front culls, else null
+    long long nray;       // rays per star (nu * nphi)
 };
 
 // ------------------------------------------------------------------ helpers

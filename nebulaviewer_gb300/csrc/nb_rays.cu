@@ -278,10 +278,8 @@ __device__ __forceinline__ void apply_front_row(const NbConst& C, const float4* 
 // Each active star's least and largest front radius over its rays, as NB_FRONT_PARTS partial
 // (least, largest) pairs per star: block (b, s) reduces the b-th slice of star s.  The largest is
 // NaN when a NaN radius was seen (the least skips NaNs).
-__global__ void __launch_bounds__(256) front_bounds_kernel(const NbStarW* __restrict__ sw,
-                                                           const float* __restrict__ rfront, long long nray,
-                                                           float2* __restrict__ parts) {
-    const int s = blockIdx.y, b = blockIdx.x;
+__device__ __forceinline__ void front_bounds_block(const NbStarW* __restrict__ sw, const float* __restrict__ rfront,
+                                                   long long nray, float2* __restrict__ parts, int s, int b) {
     if (!sw[s].active) return;                  // uniform over the block
     const float* r = rfront + (long long)s * nray;
     const long long per = (nray + NB_FRONT_PARTS - 1) / NB_FRONT_PARTS;
@@ -310,6 +308,19 @@ __global__ void __launch_bounds__(256) front_bounds_kernel(const NbStarW* __rest
         }
         parts[s * NB_FRONT_PARTS + b] = make_float2(mn, any_nan ? __int_as_float(0x7fc00000) : mx);
     }
+}
+
+__global__ void __launch_bounds__(256) front_bounds_kernel(const NbStarW* __restrict__ sw,
+                                                           const float* __restrict__ rfront, long long nray,
+                                                           float2* __restrict__ parts) {
+    front_bounds_block(sw, rfront, nray, parts, blockIdx.y, blockIdx.x);
+}
+
+// the same for every listed instance that culls: block (b, job, star)
+__global__ void __launch_bounds__(256) front_bounds_batch_kernel(const NbRayJob* __restrict__ jobs) {
+    const NbRayJob& J = jobs[blockIdx.y];
+    if (!J.front_parts || (int)blockIdx.z >= J.nstars) return;      // uniform over the block
+    front_bounds_block(J.sw, J.rfront, J.nray, J.front_parts, blockIdx.z, blockIdx.x);
 }
 
 // the partials into (least, largest) per star in shared memory (after load_stars' barrier)
@@ -360,6 +371,7 @@ __global__ void __launch_bounds__(256) apply_front_batch_kernel(const NbRayJob* 
     __shared__ float4 st[NB_MAX_STARS];
     __shared__ int act[NB_MAX_STARS];
     __shared__ float4 tab[8][NB_ROW_STARS];
+    __shared__ float2 bnd[NB_ROW_STARS];
     int lo = 0, hi = n_jobs - 1;
     while (lo < hi) {
         const int mid = (lo + hi + 1) >> 1;
@@ -369,8 +381,9 @@ __global__ void __launch_bounds__(256) apply_front_batch_kernel(const NbRayJob* 
     const int lb = (int)(blockIdx.x - J.blk0);
     const int tlin = load_stars(J.sw, J.nstars, st, act);
     if (lb == 0 && tlin == 0) *J.smax = 0u;
+    if (J.front_parts) load_front_bounds(J.front_parts, J.nstars, bnd, tlin);     // uniform over the block
     apply_front_row(*J.c, st, act, J.nstars, J.rfront, J.xi_raw, J.dfront, J.half != 0, lb * blockDim.y + threadIdx.y,
-                    tab[threadIdx.y], nullptr);
+                    tab[threadIdx.y], J.front_parts ? bnd : nullptr);
 }
 
 // nebula3d.py:310-315 smooth_xi (+ sim.py:941 copy back) of one row, then the CFL max speed
@@ -530,6 +543,7 @@ cudaError_t nb_launch_ionize_batch(const NbRayJob* jobs, int n_jobs, long long n
             default: cast_rays_batch_kernel<32><<<(unsigned)blocks, 256, 0, s>>>(jobs, n_jobs, n_groups); break;
         }
     }
+    front_bounds_batch_kernel<<<dim3(NB_FRONT_PARTS, n_jobs, NB_ROW_STARS), 256, 0, s>>>(jobs);
     apply_front_batch_kernel<<<(unsigned)n_blocks, dim3(32, 8), 0, s>>>(jobs, n_jobs);
     smooth_batch_kernel<<<(unsigned)n_blocks, dim3(32, 8), 0, s>>>(jobs, n_jobs);
     return cudaGetLastError();
