@@ -128,7 +128,8 @@ __global__ void __launch_bounds__(256) drive_kernel(const NbConst* __restrict__ 
             }
         }
         if (STAGED) __syncwarp();
-        for (int k = w.k0; k < C.nz; k += 32) {
+#pragma unroll 4
+        for (int k = w.k0; k < C.nz; k += 32) {     // unrolled: four cells' loads in flight per lane
             const long long q = w.base + k;
             const float r = rho[q];
             float m0 = mx[q], m1 = my[q], m2 = mz[q];
@@ -163,7 +164,12 @@ __global__ void __launch_bounds__(256) drive_kernel(const NbConst* __restrict__ 
             }
             if (smax_bits) {                     // nebula3d.py:158-162 on the stirred state
                 const float cc = sqrtf(cn2 + xi[q] * (ci2 - cn2));
+#if NB_ARITH_FAST
+                const float ri = 1.0f / r;           // one division for the three velocities
+                const float v = fabsf(m0 * ri) + fabsf(m1 * ri) + fabsf(m2 * ri) + cc;
+#else
                 const float v = fabsf(m0 / r) + fabsf(m1 / r) + fabsf(m2 / r) + cc;
+#endif
                 vm = fmaxr(v, vm);
             }
         }
