@@ -36,16 +36,6 @@ __device__ __forceinline__ float slope_lim(float a, float b) {
     return b;
 }
 
-__device__ __forceinline__ float comp(const float4& v, int c) {
-    return c == 0 ? v.x : (c == 1 ? v.y : (c == 2 ? v.z : v.w));
-}
-
-// ---- paired FP32 arithmetic (sm_100+ add/sub/mul/fma.rn.f32x2): a state's four components are
-// handled as the pairs (0,1) and (2,3), one instruction issue for two float operations.  Used in
-// the fast build only: each paired operation alone rounds as the scalar one, but the assembler
-// fuses a dependent mul.rn.f32x2 -> add.rn.f32x2 into one fused multiply-add even with explicit
-// round-to-nearest modifiers and -fmad=false (measured on random operands: 13% differ by an ulp),
-// which the exact build cannot allow.  The fast build contracts a*b+c anyway.
 #ifndef NB_PAIRED
 #if defined(NB_ARITH_FAST) && NB_ARITH_FAST
 #define NB_PAIRED 1
@@ -53,6 +43,20 @@ __device__ __forceinline__ float comp(const float4& v, int c) {
 #define NB_PAIRED 0
 #endif
 #endif
+
+#if !NB_PAIRED
+__device__ __forceinline__ float comp(const float4& v, int c) {
+    return c == 0 ? v.x : (c == 1 ? v.y : (c == 2 ? v.z : v.w));
+}
+#endif
+
+// ---- paired FP32 arithmetic (sm_100+ add/sub/mul/fma.rn.f32x2): a state's four components are
+// handled as the pairs (0,1) and (2,3), one instruction issue for two float operations.  Used in
+// the fast build only: each paired operation alone rounds as the scalar one, but the assembler
+// fuses a dependent mul.rn.f32x2 -> add.rn.f32x2 into one fused multiply-add even with explicit
+// round-to-nearest modifiers and -fmad=false (measured on random operands: 13% differ by an ulp),
+// which the exact build cannot allow.  The fast build contracts a*b+c anyway.
+#if NB_PAIRED
 struct F2 {
     unsigned long long v;
 };
@@ -61,6 +65,8 @@ __device__ __forceinline__ F2 mk2(float a, float b) {
     asm("mov.b64 %0, {%1, %2};" : "=l"(r.v) : "f"(a), "f"(b));
     return r;
 }
+// one register move unpacks a pair; the unused half is a discarded output of it
+#pragma nv_diag_suppress 550
 __device__ __forceinline__ float lo(F2 a) {
     float x, y;
     asm("mov.b64 {%0, %1}, %2;" : "=f"(x), "=f"(y) : "l"(a.v));
@@ -71,6 +77,7 @@ __device__ __forceinline__ float hi(F2 a) {
     asm("mov.b64 {%0, %1}, %2;" : "=f"(x), "=f"(y) : "l"(a.v));
     return y;
 }
+#pragma nv_diag_default 550
 __device__ __forceinline__ F2 add2(F2 a, F2 b) {
     F2 r;
     asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r.v) : "l"(a.v), "l"(b.v));
@@ -108,6 +115,14 @@ __device__ __forceinline__ F2 nmsub2(F2 c, F2 a, F2 b) {
 }
 __device__ __forceinline__ F2 splat2(float a) { return mk2(a, a); }
 
+// minmod given the product a*b (nebula3d.py:40-46)
+__device__ __forceinline__ float minmod_p(float a, float b, float ab) {
+    if (ab <= 0.0f) return 0.0f;
+    return fabsf(a) < fabsf(b) ? a : b;
+}
+#endif  // NB_PAIRED
+
+#if NB_ARITH_FAST
 // The fast build's reciprocal: one approximate reciprocal (<= 1 ulp) that the three divisions
 // by one density share (the exact build divides, as the reference does).
 __device__ __forceinline__ float rcp_fast(float x) {
@@ -115,17 +130,13 @@ __device__ __forceinline__ float rcp_fast(float x) {
     asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
     return r;
 }
-
-// minmod given the product a*b (nebula3d.py:40-46)
-__device__ __forceinline__ float minmod_p(float a, float b, float ab) {
-    if (ab <= 0.0f) return 0.0f;
-    return fabsf(a) < fabsf(b) ? a : b;
-}
+#endif
 
 // Face flux between cells b and c along axis AX (1 = x, 2 = y, 3 = z: the velocity
 // component normal to the face).  cs = (c^2, c) of a cell.
 //   dot((0, L1, L2, L3), e_AX) == 0 + L_AX exactly (the other products are +-0 and the
 //   velocities are finite), and e_c * (rho c^2) == +0 for c != AX.
+#if !NB_PAIRED
 // The limited slope (4 components) of cell b between its neighbours a and c along one axis:
 // slope_lim(b - a, c - b).  A face's right slope is the next face's left slope along the same
 // axis (same operands, same bits), which the x march carries from face to face.
@@ -186,6 +197,7 @@ __device__ __forceinline__ float4 face_flux_scalar(const float4 qa, const float4
 
 // The same face flux on component pairs: the float operations and operands of face_flux_scalar
 // (the minmod sign test multiplies the same two differences), with a*b+c fused.
+#else
 // slopes_scalar on component pairs (the minmod sign test multiplies the same two differences)
 template <int LM>
 __device__ __forceinline__ float4 slopes_paired(const float4 qa, const float4 qb, const float4 qc) {
@@ -260,6 +272,7 @@ __device__ __forceinline__ float4 face_flux_paired(const float4 qa, const float4
     return face_flux_paired_sl<SOLVER, AX>(qb, qc, slopes_paired<LM>(qa, qb, qc), slopes_paired<LM>(qb, qc, qd), csb,
                                            csc, floor_);
 }
+#endif  // NB_PAIRED
 
 template <int SOLVER, int LIM, int AX>
 __device__ __forceinline__ float4 face_flux(const float4 qa, const float4 qb, const float4 qc, const float4 qd,
