@@ -15,13 +15,20 @@ __device__ __forceinline__ float sample_n(const float* __restrict__ a, int nx, i
     if (gx > (float)nx - 0.5f || gy > (float)ny - 0.5f || gz > (float)nz - 0.5f) return 0.0f;
     const int i0 = (int)floorf(gx), j0 = (int)floorf(gy), k0 = (int)floorf(gz);
     const float fx = gx - (float)i0, fy = gy - (float)j0, fz = gz - (float)k0;
-    const int ia = iclampd(i0, 0, nx - 1), ib = iclampd(i0 + 1, 0, nx - 1);
-    const int ja = iclampd(j0, 0, ny - 1), jb = iclampd(j0 + 1, 0, ny - 1);
-    const int ka = iclampd(k0, 0, nz - 1), kb = iclampd(k0 + 1, 0, nz - 1);
     // corner (ia, ja, ka) once in 64 bits, the other seven as 32-bit steps from it (a plane
-    // ny * nz below 2^31 cells, which nb_create requires)
-    const float* p = a + (((long long)ia * ny + ja) * nz + ka);
-    const int dk = kb - ka, dj = (jb - ja) * nz, di = (ib - ia) * (ny * nz);
+    // ny * nz below 2^31 cells, which nb_create requires); all eight corners inside: no clamps
+    const float* p;
+    int dk, dj, di;
+    if ((unsigned)i0 < (unsigned)(nx - 1) && (unsigned)j0 < (unsigned)(ny - 1) && (unsigned)k0 < (unsigned)(nz - 1)) {
+        p = a + (((long long)i0 * ny + j0) * nz + k0);
+        dk = 1; dj = nz; di = ny * nz;
+    } else {
+        const int ia = iclampd(i0, 0, nx - 1), ib = iclampd(i0 + 1, 0, nx - 1);
+        const int ja = iclampd(j0, 0, ny - 1), jb = iclampd(j0 + 1, 0, ny - 1);
+        const int ka = iclampd(k0, 0, nz - 1), kb = iclampd(k0 + 1, 0, nz - 1);
+        p = a + (((long long)ia * ny + ja) * nz + ka);
+        dk = kb - ka; dj = (jb - ja) * nz; di = (ib - ia) * (ny * nz);
+    }
     const float c000 = __ldg(p), c100 = __ldg(p + di);
     const float c010 = __ldg(p + dj), c110 = __ldg(p + (di + dj));
     const float c001 = __ldg(p + dk), c101 = __ldg(p + (di + dk));
@@ -56,7 +63,8 @@ __device__ __forceinline__ float2 sample_n2(const float2* __restrict__ a, int nx
     const int ia = iclampd(i0, 0, nx - 1), ib = iclampd(i0 + 1, 0, nx - 1);
     const int ja = iclampd(j0, 0, ny - 1), jb = iclampd(j0 + 1, 0, ny - 1);
     const int ka = iclampd(k0, 0, nz - 1), kb = iclampd(k0 + 1, 0, nz - 1);
-    const float2* p = a + (((long long)ia * ny + ja) * nz + ka);      // as sample_n
+    // as sample_n, always in the clamped form (an all-inside fast path measured slower in the FUV rays)
+    const float2* p = a + (((long long)ia * ny + ja) * nz + ka);
     const int dk = kb - ka, dj = (jb - ja) * nz, di = (ib - ia) * (ny * nz);
     const float2 c000 = __ldg(p), c100 = __ldg(p + di);
     const float2 c010 = __ldg(p + dj), c110 = __ldg(p + (di + dj));
