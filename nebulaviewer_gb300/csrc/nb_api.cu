@@ -174,6 +174,7 @@ int launch_stage(nb_instance* h, const float* const in[4], const float* const u0
     L.nstars_host = h->nstars;
     L.order = h->tile_order;
     L.no_sources = no_sources ? 1 : 0;
+    L.idx32 = h->ncell < (1LL << 31) ? 1 : 0;
     Prof pf(h, (smax || stage2) ? NB_PROF_STAGE2 : NB_PROF_STAGE1, 1);
     CK(h, nb_launch_hydro(L, h->d.solver, h->d.limiter, h->stream));
     return NB_OK;

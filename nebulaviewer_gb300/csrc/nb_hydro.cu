@@ -335,9 +335,10 @@ struct HydroSmem {
 // One (j,k) tile column of one instance, marched over its i-chunk.  Called once per block by
 // the single-instance kernel and once per work item by the persistent batched kernel.  The
 // two mbarriers and their phases persist across calls: every load a call issues, it waits for.
-template <int SOLVER, int LIM, int TJ, bool STAGE2>
+template <int SOLVER, int LIM, int TJ, bool STAGE2, bool I32 = false>
 __device__ __forceinline__ void hydro_tile(const HydroLaunch& L, int tile, unsigned char* smem, unsigned& ph0,
                                            bool& failed) {
+    using Idx = typename std::conditional<I32, int, long long>::type;     // the own cell's offset
     using SM = HydroSmem<TJ>;
     float* raw = reinterpret_cast<float*>(smem);                                   // [5][TJ+4][40]
     float4* prim = reinterpret_cast<float4*>(smem + SM::RAW_BYTES);                // [4][TJ+4][36]
@@ -442,7 +443,7 @@ __device__ __forceinline__ void hydro_tile(const HydroLaunch& L, int tile, unsig
         const int cq = (p - P0) % 3;                 // cs slot of plane p (3 slots: p-2..p)
         // own-cell values of plane i = p - 2 the epilogue needs, issued before the flux work
         const int i = p - 2;
-        const long long cell = ((long long)i * ny + j) * nz + k;
+        const Idx cell = ((Idx)i * ny + j) * nz + k;
         const bool work = p >= i0 + 2;
         float u00 = 0.f, u01 = 0.f, u02 = 0.f, u03 = 0.f, ur = 0.f, umx = 0.f, umy = 0.f, umz = 0.f, uxi = 0.f;
         if (work && inside) {
@@ -685,13 +686,13 @@ __device__ __forceinline__ void hydro_init_bars(unsigned char* smem) {
     __syncthreads();
 }
 
-template <int SOLVER, int LIM, int TJ, bool STAGE2>
+template <int SOLVER, int LIM, int TJ, bool STAGE2, bool I32>
 __global__ void __launch_bounds__(TK * TJ, NB_HYDRO_MINB) hydro_stage_kernel(const HydroLaunch L) {
     extern __shared__ __align__(128) unsigned char smem[];
     hydro_init_bars<TJ>(smem);
     unsigned ph0 = 0;
     bool failed = false;
-    hydro_tile<SOLVER, LIM, TJ, STAGE2>(L, blockIdx.x, smem, ph0, failed);
+    hydro_tile<SOLVER, LIM, TJ, STAGE2, I32>(L, blockIdx.x, smem, ph0, failed);
     if (failed) hydro_abort<TJ>(smem, L.status, ph0);
 }
 
@@ -725,9 +726,9 @@ hydro_batch_kernel(const HydroLaunch* __restrict__ Ls, const int2* __restrict__ 
     if (failed && last) hydro_abort<TJ>(smem, last->status, ph0);
 }
 
-template <int SOLVER, int LIM, int TJ, bool STAGE2>
+template <int SOLVER, int LIM, int TJ, bool STAGE2, bool I32>
 cudaError_t run_kernel(const HydroLaunch& L, cudaStream_t s) {
-    auto kern = hydro_stage_kernel<SOLVER, LIM, TJ, STAGE2>;
+    auto kern = hydro_stage_kernel<SOLVER, LIM, TJ, STAGE2, I32>;
     const int smem = HydroSmem<TJ>::bytes(L.nstars_host);
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (e == cudaSuccess)                        // the largest shared-memory carveout: 4 blocks of ~57 KB per SM
@@ -740,8 +741,9 @@ cudaError_t run_kernel(const HydroLaunch& L, cudaStream_t s) {
 
 template <int SOLVER, int LIM, int TJ>
 cudaError_t run_stage(const HydroLaunch& L, cudaStream_t s) {
-    return L.smax_bits || L.u0[0] != L.in[0] ? run_kernel<SOLVER, LIM, TJ, true>(L, s)
-                                             : run_kernel<SOLVER, LIM, TJ, false>(L, s);
+    const bool s2 = L.smax_bits || L.u0[0] != L.in[0];
+    if (L.idx32) return s2 ? run_kernel<SOLVER, LIM, TJ, true, true>(L, s) : run_kernel<SOLVER, LIM, TJ, false, true>(L, s);
+    return s2 ? run_kernel<SOLVER, LIM, TJ, true, false>(L, s) : run_kernel<SOLVER, LIM, TJ, false, false>(L, s);
 }
 
 template <int SOLVER, int LIM, int TJ, bool STAGE2>

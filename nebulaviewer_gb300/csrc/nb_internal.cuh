@@ -106,6 +106,7 @@ struct HydroLaunch {
     int nstars_host;             // == c->nstars (sizes the dynamic shared memory)
     int no_sources;              // stirring-phase hydro: no stars, wind or jets (sim.py:1046)
     int order;                   // tile sweep order (NB_TUNE_TILE_ORDER)
+    int idx32;                   // fewer than 2^31 cells: 32-bit cell offsets (single-instance stage)
 };
 
 // One instance of a batch, as the batched control kernel sees it.
