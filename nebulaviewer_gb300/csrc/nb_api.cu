@@ -889,6 +889,7 @@ struct nb_batch_s {
     cudaStream_t bs = nullptr;          // the batch's own stream (capturable)
     cudaEvent_t ev_in = nullptr, ev_out = nullptr;
     int solver = 0, limiter = 0, max_stars = 1, grid = 0, ray_group = 4;
+    int idx32 = 1;                      // every instance below 2^31 cells: 32-bit cell offsets
     NbBatchInst* d_inst = nullptr;
     HydroLaunch* d_L1 = nullptr;
     HydroLaunch* d_L2 = nullptr;
@@ -988,10 +989,10 @@ void job_prefix(std::vector<NbRayJob>& jobs, const std::vector<nb_instance*>& hs
 int batch_hydro(nb_batch_s* b) {
     b->launches += 3;
     BCK(b, nb_launch_ctrl_batch(b->d_inst, (int)b->inst.size(), 1, b->d_counters, b->bs));
-    BCK(b, nb_launch_hydro_batch(b->d_L1, b->d_work, b->n_work, b->d_counters + 0, b->max_stars, 0, b->solver,
-                                 b->limiter, b->grid, b->bs));
-    BCK(b, nb_launch_hydro_batch(b->d_L2, b->d_work, b->n_work, b->d_counters + 1, b->max_stars, 1, b->solver,
-                                 b->limiter, b->grid, b->bs));
+    BCK(b, nb_launch_hydro_batch(b->d_L1, b->d_work, b->n_work, b->d_counters + 0, b->max_stars, 0, b->idx32,
+                                 b->solver, b->limiter, b->grid, b->bs));
+    BCK(b, nb_launch_hydro_batch(b->d_L2, b->d_work, b->n_work, b->d_counters + 1, b->max_stars, 1, b->idx32,
+                                 b->solver, b->limiter, b->grid, b->bs));
     return NB_OK;
 }
 
@@ -1069,11 +1070,12 @@ NB_EXPORT int nb_batch_create(const nb_handle* hs, const int* ion_every, int n, 
     for (auto* h : b->inst) {
         b->max_stars = std::max(b->max_stars, h->nstars);
         b->n_plane += h->hc.plane_on ? 1 : 0;
+        if (h->ncell >= (1LL << 31)) b->idx32 = 0;
     }
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    b->grid = (sms > 0 ? sms : 152) * nb_hydro_batch_blocks_per_sm(b->solver, b->limiter, b->max_stars);
+    b->grid = (sms > 0 ? sms : 152) * nb_hydro_batch_blocks_per_sm(b->solver, b->limiter, b->max_stars, b->idx32);
     if (cudaStreamCreateWithFlags(&b->bs, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreateWithFlags(&b->ev_in, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&b->ev_out, cudaEventDisableTiming) != cudaSuccess)

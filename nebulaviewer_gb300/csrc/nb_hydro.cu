@@ -702,7 +702,7 @@ __global__ void __launch_bounds__(TK * TJ, NB_HYDRO_MINB) hydro_stage_kernel(con
 #ifndef NB_HYDRO_BATCH_MINB
 #define NB_HYDRO_BATCH_MINB 3            // the persistent kernel's loop state needs the 80-register budget
 #endif
-template <int SOLVER, int LIM, int TJ, bool STAGE2>
+template <int SOLVER, int LIM, int TJ, bool STAGE2, bool I32>
 __global__ void __launch_bounds__(TK * TJ, NB_HYDRO_BATCH_MINB)
 hydro_batch_kernel(const HydroLaunch* __restrict__ Ls, const int2* __restrict__ work, int n_work,
                    unsigned* counter) {
@@ -719,7 +719,7 @@ hydro_batch_kernel(const HydroLaunch* __restrict__ Ls, const int2* __restrict__ 
         if (it >= n_work) break;
         const int2 w = work[it];
         last = &Ls[w.x];
-        hydro_tile<SOLVER, LIM, TJ, STAGE2>(*last, w.y, smem, ph0, failed);
+        hydro_tile<SOLVER, LIM, TJ, STAGE2, I32>(*last, w.y, smem, ph0, failed);
         if (failed) break;
         __syncthreads();
     }
@@ -746,10 +746,10 @@ cudaError_t run_stage(const HydroLaunch& L, cudaStream_t s) {
     return s2 ? run_kernel<SOLVER, LIM, TJ, true, false>(L, s) : run_kernel<SOLVER, LIM, TJ, false, false>(L, s);
 }
 
-template <int SOLVER, int LIM, int TJ, bool STAGE2>
+template <int SOLVER, int LIM, int TJ, bool STAGE2, bool I32>
 cudaError_t run_batch_kernel(const HydroLaunch* Ls, const int2* work, int n_work, unsigned* counter,
                              int max_stars, int grid, cudaStream_t s) {
-    auto kern = hydro_batch_kernel<SOLVER, LIM, TJ, STAGE2>;
+    auto kern = hydro_batch_kernel<SOLVER, LIM, TJ, STAGE2, I32>;
     const int smem = HydroSmem<TJ>::bytes(max_stars);
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (e == cudaSuccess)
@@ -761,9 +761,12 @@ cudaError_t run_batch_kernel(const HydroLaunch* Ls, const int2* work, int n_work
 
 template <int SOLVER, int LIM, int TJ>
 cudaError_t run_batch(const HydroLaunch* Ls, const int2* work, int n_work, unsigned* counter, int max_stars,
-                      int stage2, int grid, cudaStream_t s) {
-    return stage2 ? run_batch_kernel<SOLVER, LIM, TJ, true>(Ls, work, n_work, counter, max_stars, grid, s)
-                  : run_batch_kernel<SOLVER, LIM, TJ, false>(Ls, work, n_work, counter, max_stars, grid, s);
+                      int stage2, int idx32, int grid, cudaStream_t s) {
+    if (idx32)
+        return stage2 ? run_batch_kernel<SOLVER, LIM, TJ, true, true>(Ls, work, n_work, counter, max_stars, grid, s)
+                      : run_batch_kernel<SOLVER, LIM, TJ, false, true>(Ls, work, n_work, counter, max_stars, grid, s);
+    return stage2 ? run_batch_kernel<SOLVER, LIM, TJ, true, false>(Ls, work, n_work, counter, max_stars, grid, s)
+                  : run_batch_kernel<SOLVER, LIM, TJ, false, false>(Ls, work, n_work, counter, max_stars, grid, s);
 }
 
 }  // namespace
@@ -771,7 +774,7 @@ cudaError_t run_batch(const HydroLaunch* Ls, const int2* work, int n_work, unsig
 int nb_hydro_tile_j() { return NB_HYDRO_TJ; }
 
 // resident blocks per SM of the persistent stage kernel (sizes its grid)
-int nb_hydro_batch_blocks_per_sm(int solver, int limiter, int max_stars) {
+int nb_hydro_batch_blocks_per_sm(int solver, int limiter, int max_stars, int idx32) {
     constexpr int TJ = NB_HYDRO_TJ;
     const int smem = HydroSmem<TJ>::bytes(max_stars);
     auto occ = [&](auto kern) {
@@ -786,10 +789,18 @@ int nb_hydro_batch_blocks_per_sm(int solver, int limiter, int max_stars) {
         return n;
     };
     int n;
-    if (solver == NB_SOLVER_RUSANOV) n = occ(hydro_batch_kernel<NB_SOLVER_RUSANOV, 0, TJ, true>);
-    else if (limiter == NB_LIM_VANLEER) n = occ(hydro_batch_kernel<NB_SOLVER_HLL, NB_LIM_VANLEER, TJ, true>);
-    else if (limiter == NB_LIM_MC) n = occ(hydro_batch_kernel<NB_SOLVER_HLL, NB_LIM_MC, TJ, true>);
-    else n = occ(hydro_batch_kernel<NB_SOLVER_HLL, NB_LIM_MINMOD, TJ, true>);
+    if (solver == NB_SOLVER_RUSANOV)
+        n = idx32 ? occ(hydro_batch_kernel<NB_SOLVER_RUSANOV, 0, TJ, true, true>)
+                  : occ(hydro_batch_kernel<NB_SOLVER_RUSANOV, 0, TJ, true, false>);
+    else if (limiter == NB_LIM_VANLEER)
+        n = idx32 ? occ(hydro_batch_kernel<NB_SOLVER_HLL, NB_LIM_VANLEER, TJ, true, true>)
+                  : occ(hydro_batch_kernel<NB_SOLVER_HLL, NB_LIM_VANLEER, TJ, true, false>);
+    else if (limiter == NB_LIM_MC)
+        n = idx32 ? occ(hydro_batch_kernel<NB_SOLVER_HLL, NB_LIM_MC, TJ, true, true>)
+                  : occ(hydro_batch_kernel<NB_SOLVER_HLL, NB_LIM_MC, TJ, true, false>);
+    else
+        n = idx32 ? occ(hydro_batch_kernel<NB_SOLVER_HLL, NB_LIM_MINMOD, TJ, true, true>)
+                  : occ(hydro_batch_kernel<NB_SOLVER_HLL, NB_LIM_MINMOD, TJ, true, false>);
     return n > 0 ? n : NB_HYDRO_BATCH_MINB;
 }
 
@@ -804,16 +815,17 @@ cudaError_t nb_launch_hydro(const HydroLaunch& L, int solver, int limiter, cudaS
 }
 
 cudaError_t nb_launch_hydro_batch(const HydroLaunch* Ls, const int2* work, int n_work, unsigned* counter,
-                                  int max_stars, int stage2, int solver, int limiter, int grid, cudaStream_t s) {
+                                  int max_stars, int stage2, int idx32, int solver, int limiter, int grid,
+                                  cudaStream_t s) {
     constexpr int TJ = NB_HYDRO_TJ;
     if (solver == NB_SOLVER_RUSANOV)
-        return run_batch<NB_SOLVER_RUSANOV, 0, TJ>(Ls, work, n_work, counter, max_stars, stage2, grid, s);
+        return run_batch<NB_SOLVER_RUSANOV, 0, TJ>(Ls, work, n_work, counter, max_stars, stage2, idx32, grid, s);
     switch (limiter) {
         case NB_LIM_VANLEER:
-            return run_batch<NB_SOLVER_HLL, NB_LIM_VANLEER, TJ>(Ls, work, n_work, counter, max_stars, stage2, grid, s);
+            return run_batch<NB_SOLVER_HLL, NB_LIM_VANLEER, TJ>(Ls, work, n_work, counter, max_stars, stage2, idx32, grid, s);
         case NB_LIM_MC:
-            return run_batch<NB_SOLVER_HLL, NB_LIM_MC, TJ>(Ls, work, n_work, counter, max_stars, stage2, grid, s);
+            return run_batch<NB_SOLVER_HLL, NB_LIM_MC, TJ>(Ls, work, n_work, counter, max_stars, stage2, idx32, grid, s);
         default:
-            return run_batch<NB_SOLVER_HLL, NB_LIM_MINMOD, TJ>(Ls, work, n_work, counter, max_stars, stage2, grid, s);
+            return run_batch<NB_SOLVER_HLL, NB_LIM_MINMOD, TJ>(Ls, work, n_work, counter, max_stars, stage2, idx32, grid, s);
     }
 }

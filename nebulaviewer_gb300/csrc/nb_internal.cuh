@@ -191,9 +191,11 @@ __device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, i
 // ------------------------------------------------------------------ launchers (nb_*.cu)
 cudaError_t nb_launch_hydro(const HydroLaunch& L, int solver, int limiter, cudaStream_t s);
 int nb_hydro_tile_j();
-int nb_hydro_batch_blocks_per_sm(int solver, int limiter, int max_stars);
+// idx32: every listed instance has fewer than 2^31 cells (32-bit cell offsets)
+int nb_hydro_batch_blocks_per_sm(int solver, int limiter, int max_stars, int idx32);
 cudaError_t nb_launch_hydro_batch(const HydroLaunch* Ls, const int2* work, int n_work, unsigned* counter,
-                                  int max_stars, int stage2, int solver, int limiter, int grid, cudaStream_t s);
+                                  int max_stars, int stage2, int idx32, int solver, int limiter, int grid,
+                                  cudaStream_t s);
 cudaError_t nb_launch_ctrl(const NbConst* c, NbState* st, const NbStarDev* stars, NbStarW* sw, int nstars,
                            int advance, cudaStream_t s);
 cudaError_t nb_launch_ctrl_batch(const NbBatchInst* insts, int n, int advance, unsigned* counters, cudaStream_t s);
