@@ -433,7 +433,29 @@ __device__ __forceinline__ void hydro_tile(const HydroLaunch& L, int tile, unsig
         return jc * RAWW + kc;
     };
     const int own = (tj + 2) * PW + tk + 2;          // this thread's cell in a prim / cs tile
+    // the cells this thread converts in every plane: its own, and one of the 4 TK + 4 TJ cells of
+    // the halo strips (corners are never read); offsets in the raw tile clamp at the domain faces.
+    // Stage 1 keeps them from plane to plane; stage 2, short of registers, recomputes them per
+    // plane (without the clamps on a tile two or more cells inside the j and k faces).
     const bool interior_tile = j0 >= 2 && j0 + TJ + 2 <= ny && k0 >= 2 && k0 + TK + 2 <= nz;
+    const bool has_halo = tid < 4 * TK + 4 * TJ;
+    int raw_own = 0, prim_halo = 0, raw_halo = 0;
+    if (!STAGE2) raw_own = raw_at(tj + 2, tk + 2);
+    if (!STAGE2 && has_halo) {
+        int jj, kk;
+        if (tid < 4 * TK) {
+            const int rr = tid >> 5;
+            jj = rr < 2 ? rr : TJ + rr;
+            kk = 2 + (tid & 31);
+        } else {
+            const int hh = tid - 4 * TK;
+            jj = 2 + (hh >> 2);
+            const int q = hh & 3;
+            kk = q < 2 ? q : 32 + q;
+        }
+        prim_halo = jj * PW + kk;
+        raw_halo = raw_at(jj, kk);
+    }
     const int j = j0 + tj, k = k0 + tk;
     const bool inside = j < ny && k < nz;
     constexpr int PSLOT = (TJ + 4) * PW;
@@ -459,44 +481,51 @@ __device__ __forceinline__ void hydro_tile(const HydroLaunch& L, int tile, unsig
         const float* rb = raw;
         float4* pp = prim + ps * PSLOT;
         float2* cp = cs + cq * PSLOT;
-        // ---- convert plane p: own cell, then the halo strips (corners are never read); a tile two
-        // cells or more inside the j and k faces reads the raw tile without the edge clamps
-        auto convert = [&](auto interior_tag) {
-            constexpr bool INTERIOR = decltype(interior_tag)::value;
-            for (int h = tid - TK * TJ; h < 4 * TK + 4 * TJ; h += TK * TJ) {
-                int jj, kk;
-                if (h < 0) {
-                    jj = tj + 2;
-                    kk = tk + 2;
-                } else if (h < 4 * TK) {
-                    const int rr = h >> 5;
-                    jj = rr < 2 ? rr : TJ + rr;
-                    kk = 2 + (h & 31);
-                } else {
-                    const int hh = h - 4 * TK;
-                    jj = 2 + (hh >> 2);
-                    const int q = hh & 3;
-                    kk = q < 2 ? q : 32 + q;
-                }
-                const int o = INTERIOR ? jj * RAWW + kk + 2 : raw_at(jj, kk);
-                const float r = fmaxr(rb[o], floor_);
-                const float xv = rb[4 * SM::RAW_FIELD + o];
-                const float c2 = cn2 + xv * (ci2 - cn2);
+        // ---- convert plane p: the own cell, then (tid < 4 TK + 4 TJ) one cell of the halo strips;
+        // their raw-tile and prim-tile offsets are the same in every plane (computed once per tile)
+        auto convert = [&](int o, int pi) {
+            const float r = fmaxr(rb[o], floor_);
+            const float xv = rb[4 * SM::RAW_FIELD + o];
+            const float c2 = cn2 + xv * (ci2 - cn2);
 #if NB_ARITH_FAST
-                const float ri = rcp_fast(r);
-                pp[jj * PW + kk] = make_float4(r, rb[SM::RAW_FIELD + o] * ri, rb[2 * SM::RAW_FIELD + o] * ri,
-                                               rb[3 * SM::RAW_FIELD + o] * ri);
+            const float ri = rcp_fast(r);
+            pp[pi] = make_float4(r, rb[SM::RAW_FIELD + o] * ri, rb[2 * SM::RAW_FIELD + o] * ri,
+                                 rb[3 * SM::RAW_FIELD + o] * ri);
 #else
-                pp[jj * PW + kk] = make_float4(r, rb[SM::RAW_FIELD + o] / r, rb[2 * SM::RAW_FIELD + o] / r,
-                                               rb[3 * SM::RAW_FIELD + o] / r);
+            pp[pi] = make_float4(r, rb[SM::RAW_FIELD + o] / r, rb[2 * SM::RAW_FIELD + o] / r,
+                                 rb[3 * SM::RAW_FIELD + o] / r);
 #endif
-                cp[jj * PW + kk] = make_float2(c2, sqrtf(c2));
-            }
+            cp[pi] = make_float2(c2, sqrtf(c2));
         };
-        if (interior_tile)
-            convert(std::true_type{});
-        else
-            convert(std::false_type{});
+        if constexpr (!STAGE2) {
+            convert(raw_own, own);
+            if (has_halo) convert(raw_halo, prim_halo);
+        } else {
+            auto convert_all = [&](auto interior_tag) {
+                constexpr bool INTERIOR = decltype(interior_tag)::value;
+                for (int h = tid - TK * TJ; h < 4 * TK + 4 * TJ; h += TK * TJ) {
+                    int jj, kk;
+                    if (h < 0) {
+                        jj = tj + 2;
+                        kk = tk + 2;
+                    } else if (h < 4 * TK) {
+                        const int rr = h >> 5;
+                        jj = rr < 2 ? rr : TJ + rr;
+                        kk = 2 + (h & 31);
+                    } else {
+                        const int hh = h - 4 * TK;
+                        jj = 2 + (hh >> 2);
+                        const int q = hh & 3;
+                        kk = q < 2 ? q : 32 + q;
+                    }
+                    convert(INTERIOR ? jj * RAWW + kk + 2 : raw_at(jj, kk), jj * PW + kk);
+                }
+            };
+            if (interior_tile)
+                convert_all(std::true_type{});
+            else
+                convert_all(std::false_type{});
+        }
         __syncthreads();                         // every thread is done with the raw slot
         if (tid == 0 && p + 1 <= P1) issue(p + 1);
         if (p < P0 + 3) continue;
