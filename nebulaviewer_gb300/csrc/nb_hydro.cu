@@ -339,6 +339,9 @@ template <int SOLVER, int LIM, int TJ, bool STAGE2, bool I32 = false>
 __device__ __forceinline__ void hydro_tile(const HydroLaunch& L, int tile, unsigned char* smem, unsigned& ph0,
                                            bool& failed) {
     using Idx = typename std::conditional<I32, int, long long>::type;     // the own cell's offset
+    // register budget choices per stage: stage 1 carries the x slope from face to face; both keep
+    // each thread's conversion offsets from plane to plane
+    constexpr bool CARRY = !STAGE2, HOIST = true;
     using SM = HydroSmem<TJ>;
     float* raw = reinterpret_cast<float*>(smem);                                   // [5][TJ+4][40]
     float4* prim = reinterpret_cast<float4*>(smem + SM::RAW_BYTES);                // [4][TJ+4][36]
@@ -440,8 +443,8 @@ __device__ __forceinline__ void hydro_tile(const HydroLaunch& L, int tile, unsig
     const bool interior_tile = j0 >= 2 && j0 + TJ + 2 <= ny && k0 >= 2 && k0 + TK + 2 <= nz;
     const bool has_halo = tid < 4 * TK + 4 * TJ;
     int raw_own = 0, prim_halo = 0, raw_halo = 0;
-    if (!STAGE2) raw_own = raw_at(tj + 2, tk + 2);
-    if (!STAGE2 && has_halo) {
+    if (HOIST) raw_own = raw_at(tj + 2, tk + 2);
+    if (HOIST && has_halo) {
         int jj, kk;
         if (tid < 4 * TK) {
             const int rr = tid >> 5;
@@ -497,7 +500,7 @@ __device__ __forceinline__ void hydro_tile(const HydroLaunch& L, int tile, unsig
 #endif
             cp[pi] = make_float2(c2, sqrtf(c2));
         };
-        if constexpr (!STAGE2) {
+        if constexpr (HOIST) {
             convert(raw_own, own);
             if (has_halo) convert(raw_halo, prim_halo);
         } else {
@@ -531,9 +534,16 @@ __device__ __forceinline__ void hydro_tile(const HydroLaunch& L, int tile, unsig
         if (p < P0 + 3) continue;
         // x face (p-2)+1/2 from the own column of planes p-2..p and the carried slope of p-2
         const float4 qx1 = prim[((p - 2 - P0) & 3) * PSLOT + own], qx2 = prim[((p - 1 - P0) & 3) * PSLOT + own];
-        if (p == P0 + 3) xslope = cell_slopes<SOLVER, LIM>(prim[((p - 3 - P0) & 3) * PSLOT + own], qx1, qx2);
-        const float4 fx_new = face_flux_x<SOLVER, LIM>(qx1, qx2, pp[own], cs[((p - 2 - P0) % 3) * PSLOT + own],
-                                                       cs[((p - 1 - P0) % 3) * PSLOT + own], floor_, xslope);
+        float4 fx_new;
+        if constexpr (CARRY) {
+            if (p == P0 + 3) xslope = cell_slopes<SOLVER, LIM>(prim[((p - 3 - P0) & 3) * PSLOT + own], qx1, qx2);
+            fx_new = face_flux_x<SOLVER, LIM>(qx1, qx2, pp[own], cs[((p - 2 - P0) % 3) * PSLOT + own],
+                                              cs[((p - 1 - P0) % 3) * PSLOT + own], floor_, xslope);
+        } else {
+            fx_new = face_flux<SOLVER, LIM, 1>(prim[((p - 3 - P0) & 3) * PSLOT + own], qx1, qx2, pp[own],
+                                               cs[((p - 2 - P0) % 3) * PSLOT + own],
+                                               cs[((p - 1 - P0) % 3) * PSLOT + own], floor_);
+        }
         if (!work) { fx_prev = fx_new; continue; }
         // ---- cell plane i = p - 2
         const int si = (i - P0) & 3;
