@@ -339,9 +339,9 @@ template <int SOLVER, int LIM, int TJ, bool STAGE2, bool I32 = false>
 __device__ __forceinline__ void hydro_tile(const HydroLaunch& L, int tile, unsigned char* smem, unsigned& ph0,
                                            bool& failed) {
     using Idx = typename std::conditional<I32, int, long long>::type;     // the own cell's offset
-    // register budget choices per stage: stage 1 carries the x slope from face to face; both keep
-    // each thread's conversion offsets from plane to plane
-    constexpr bool CARRY = !STAGE2, HOIST = true;
+    // register budget: stage 1 carries the x slope from face to face; stage 2 (U^n, the RK
+    // combination, the CFL speed) recomputes it
+    constexpr bool CARRY = !STAGE2;
     using SM = HydroSmem<TJ>;
     float* raw = reinterpret_cast<float*>(smem);                                   // [5][TJ+4][40]
     float4* prim = reinterpret_cast<float4*>(smem + SM::RAW_BYTES);                // [4][TJ+4][36]
@@ -437,14 +437,12 @@ __device__ __forceinline__ void hydro_tile(const HydroLaunch& L, int tile, unsig
     };
     const int own = (tj + 2) * PW + tk + 2;          // this thread's cell in a prim / cs tile
     // the cells this thread converts in every plane: its own, and one of the 4 TK + 4 TJ cells of
-    // the halo strips (corners are never read); offsets in the raw tile clamp at the domain faces.
-    // Stage 1 keeps them from plane to plane; stage 2, short of registers, recomputes them per
-    // plane (without the clamps on a tile two or more cells inside the j and k faces).
-    const bool interior_tile = j0 >= 2 && j0 + TJ + 2 <= ny && k0 >= 2 && k0 + TK + 2 <= nz;
+    // the halo strips (corners are never read); their offsets, computed once per tile, clamp to
+    // the domain in the raw tile
     const bool has_halo = tid < 4 * TK + 4 * TJ;
-    int raw_own = 0, prim_halo = 0, raw_halo = 0;
-    if (HOIST) raw_own = raw_at(tj + 2, tk + 2);
-    if (HOIST && has_halo) {
+    const int raw_own = raw_at(tj + 2, tk + 2);
+    int prim_halo = 0, raw_halo = 0;
+    if (has_halo) {
         int jj, kk;
         if (tid < 4 * TK) {
             const int rr = tid >> 5;
@@ -484,8 +482,7 @@ __device__ __forceinline__ void hydro_tile(const HydroLaunch& L, int tile, unsig
         const float* rb = raw;
         float4* pp = prim + ps * PSLOT;
         float2* cp = cs + cq * PSLOT;
-        // ---- convert plane p: the own cell, then (tid < 4 TK + 4 TJ) one cell of the halo strips;
-        // their raw-tile and prim-tile offsets are the same in every plane (computed once per tile)
+        // ---- convert plane p: the own cell, then (tid < 4 TK + 4 TJ) one cell of the halo strips
         auto convert = [&](int o, int pi) {
             const float r = fmaxr(rb[o], floor_);
             const float xv = rb[4 * SM::RAW_FIELD + o];
@@ -500,35 +497,8 @@ __device__ __forceinline__ void hydro_tile(const HydroLaunch& L, int tile, unsig
 #endif
             cp[pi] = make_float2(c2, sqrtf(c2));
         };
-        if constexpr (HOIST) {
-            convert(raw_own, own);
-            if (has_halo) convert(raw_halo, prim_halo);
-        } else {
-            auto convert_all = [&](auto interior_tag) {
-                constexpr bool INTERIOR = decltype(interior_tag)::value;
-                for (int h = tid - TK * TJ; h < 4 * TK + 4 * TJ; h += TK * TJ) {
-                    int jj, kk;
-                    if (h < 0) {
-                        jj = tj + 2;
-                        kk = tk + 2;
-                    } else if (h < 4 * TK) {
-                        const int rr = h >> 5;
-                        jj = rr < 2 ? rr : TJ + rr;
-                        kk = 2 + (h & 31);
-                    } else {
-                        const int hh = h - 4 * TK;
-                        jj = 2 + (hh >> 2);
-                        const int q = hh & 3;
-                        kk = q < 2 ? q : 32 + q;
-                    }
-                    convert(INTERIOR ? jj * RAWW + kk + 2 : raw_at(jj, kk), jj * PW + kk);
-                }
-            };
-            if (interior_tile)
-                convert_all(std::true_type{});
-            else
-                convert_all(std::false_type{});
-        }
+        convert(raw_own, own);
+        if (has_halo) convert(raw_halo, prim_halo);
         __syncthreads();                         // every thread is done with the raw slot
         if (tid == 0 && p + 1 <= P1) issue(p + 1);
         if (p < P0 + 3) continue;
