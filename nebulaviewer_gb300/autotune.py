@@ -15,7 +15,7 @@ import torch
 from . import _lib
 
 CANDIDATES = {
-    "chunk_i": (16, 32, 64),
+    "chunk_i": (16, 20, 24, 32, 64),
     "tile_order": (0, 1),
     "ray_group": (2, 4, 8, 16),
     "fuv_group": (8, 16, 32),
