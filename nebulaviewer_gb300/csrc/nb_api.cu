@@ -36,7 +36,7 @@ struct nb_instance {
     int nstars = 0, star_alloc = 0;
     long long host_it = 0;
     int smax_valid = 0;
-    int chunk_i = 32, ray_group = 4, fuv_group = 16;      // measured best at 256^3 (nb_set_tuning)
+    int chunk_i = 20, ray_group = 4, fuv_group = 16;      // measured best at 256^3 (nb_set_tuning)
     int tile_order = 0;
     int front_cull = 1;                 // apply_front skips the stars that cannot change a segment
     int fuv_cut = 1;                    // FUV rays stop where exp(-tau) has reached 0.0f
