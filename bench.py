@@ -298,23 +298,31 @@ def run_gb300(args):
     # from pinned host memory and the result fields (rho, xi) read back to pinned memory.
     out_host = [torch.empty(sim.shape, dtype=torch.float32).pin_memory() for _ in range(2)]
     e2e_steps = args.steps
-    if dist:
-        dist.barrier()
-    torch.cuda.synchronize(dev)
-    t0 = time.perf_counter()
-    for dst, src in zip((sim._rho, sim._mx, sim._my, sim._mz), pinned0):
-        dst.copy_(src, non_blocking=True)
-    sim.invalidate()
     h2d_live = C.sizeof(_lib.NbLive)
-    for _ in range(e2e_steps):
-        sim._live_key = None                               # force the H2D push of the live block
-        sim.step(1)
-        sim.update_render_fields()
-        _ = sim.t
-    out_host[0].copy_(sim._rho, non_blocking=True)
-    out_host[1].copy_(sim._xi, non_blocking=True)
-    torch.cuda.synchronize(dev)
-    e2e_s = time.perf_counter() - t0
+
+    def e2e_pass():
+        """one end-to-end pass: the same initial state uploaded, K blocking steps, results read back"""
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        for dst, src in zip((sim._rho, sim._mx, sim._my, sim._mz), pinned0):
+            dst.copy_(src, non_blocking=True)
+        sim.invalidate()
+        for _ in range(e2e_steps):
+            sim._live_key = None                           # force the H2D push of the live block
+            sim.step(1)
+            sim.update_render_fields()
+            _ = sim.t
+        out_host[0].copy_(sim._rho, non_blocking=True)
+        out_host[1].copy_(sim._xi, non_blocking=True)
+        torch.cuda.synchronize(dev)
+        return time.perf_counter() - t0
+
+    # three identical passes (each restarts from the same uploaded state); the median is reported:
+    # a single host-timed pass swings with the host's scheduling
+    e2e_runs = [e2e_pass() for _ in range(3)]
+    e2e_s = sorted(e2e_runs)[1]
     if dist:
         t = torch.tensor([e2e_s], device=dev, dtype=torch.float64)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
@@ -357,7 +365,8 @@ def run_gb300(args):
                            for k, v in kinds.items()},
             "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "how": "Sim.step(1) + update_render_fields + clock read per step; state upload from pinned "
-                           "host memory and rho/xi read-back inside the timed region"},
+                           "host memory and rho/xi read-back inside the timed region; median of 3 passes",
+                    "passes": [ws * ncell * e2e_steps / t / 1e9 for t in e2e_runs]},
             "gpu_launches": launches,
             "clocks": clocks,
         }
