@@ -187,7 +187,7 @@ __device__ __forceinline__ void apply_front_row(const NbConst& C, const float4* 
     if (!tab) bnd = nullptr;
     if (tab) star_row_table(st, act, nstars, px, py, nphi, nu, tab);
     const unsigned row_stars = tab ? __ballot_sync(0xffffffffu, (int)threadIdx.x < nstars && act[threadIdx.x]) : 0u;
-    constexpr int SG = 4;                       // stars whose gathers are in flight together
+    constexpr int SG = 2;                       // stars whose gathers are in flight together
     for (int kb = 0; kb < nz; kb += 32) {
         const unsigned seg = bnd ? segment_stars(st, act, tab, bnd, nstars, kb, nz, dx, width) : row_stars;
         const int k = kb + (int)threadIdx.x;
@@ -412,7 +412,12 @@ __device__ __forceinline__ float smooth_row(const NbConst& C, const float* __res
         xi[q] = x;
         if (smax) {
             const float r = rho[q];
+#if NB_ARITH_FAST
+            const float ri = 1.0f / r;               // one division for the three velocities
+            const float v = fabsf(mx[q] * ri) + fabsf(my[q] * ri) + fabsf(mz[q] * ri) + sqrtf(cn2 + x * (ci2 - cn2));
+#else
             const float v = fabsf(mx[q] / r) + fabsf(my[q] / r) + fabsf(mz[q] / r) + sqrtf(cn2 + x * (ci2 - cn2));
+#endif
             m = fmaxr(v, m);
         }
     }
