@@ -3,19 +3,24 @@
 // convex RK combination a*U0 + b*(U + dt*dU), density floor and velocity cap.
 //
 // Follows nebula3d.py:76-151 (hydro_stage, Rusanov) and sim.py:423-498 (hydro_stage_hll)
-// with the face fluxes of nebula3d.py:54-72 / sim.py:397-420.  Every float operation is
-// the reference's, in the reference's order (the library is built with -fmad=false), so a
-// stage is bit-identical to the float32 oracle.
+// with the face fluxes of nebula3d.py:54-72 / sim.py:397-420.  In the exact build every float
+// operation is the reference's, in the reference's order (-fmad=false), so a stage is
+// bit-identical to the float32 oracle; the fast build contracts a*b+c, evaluates the fluxes on
+// paired FP32 and shares one approximate reciprocal per density.
 //
-// GB300 layout: a block owns a 32 (k) x TJ (j) column of cells and marches along i.  Each
-// (j,k) plane tile with a 2-cell halo is brought into shared memory by TMA (five 3-D tiled
-// loads: rho, mx, my, mz, xi; mbarrier-tracked).  One raw slot: plane p+1 is requested as soon
-// as plane p has been converted, and lands while plane p's faces and update are computed
-// (microseconds of work against a load latency of about one), which keeps a block at ~56 KB
-// of shared memory and 4 blocks resident per SM.  A plane is converted once to primitives (rho, u, v, w) and (c^2, c) in
-// shared memory; every face flux is then evaluated once (the reference evaluates each face
-// twice) and shared through shared memory (y, z faces) or registers (x faces).  Stage 2
-// also reduces the CFL max speed of the new state (nebula3d.py:154-162) into one atomic.
+// GB300 layout: a block owns a 32 (k) x TJ (j) column of cells and marches along i over an
+// i-chunk.  Each (j,k) plane tile with a 2-cell halo is brought into shared memory by TMA (five
+// 3-D tiled loads: rho, mx, my, mz, xi; mbarrier-tracked, bounded waits).  One raw slot: plane
+// p+1 is requested as soon as plane p has been converted, and lands while plane p's faces and
+// update are computed, which keeps a block at ~56 KB of shared memory and 4 blocks resident per
+// SM.  A plane is converted once to primitives (rho, u, v, w) and (c^2, c) in shared memory (each
+// thread's own and halo cell, at offsets computed once per tile); every face flux is then
+// evaluated once (the reference evaluates each face twice) and shared through shared memory
+// (y, z faces) or registers (x faces; stage 1 also carries each cell's limited x slope to the
+// next face).  Sources: the wind loop over the active stars in ionized cells, the jet loop over
+// the tile's list of stars whose jet can reach it.  Cell offsets are 32-bit on grids below 2^31
+// cells.  Stage 2 also reduces the CFL max speed of the new state (nebula3d.py:154-162) into
+// one atomic.
 #include <type_traits>
 
 #include "nb_internal.cuh"
