@@ -4,13 +4,15 @@
 // apply_front, smooth_xi) as driven by sim.py:927-947 (ionize).
 //
 // GB300 design:
-//  * cast_rays: a group of G lanes (G = 32: one warp) marches one ray, G consecutive samples
-//    at a time; the recombination column sum(n^2 r^2 dr) is an inclusive group scan on top
-//    of a Kahan-compensated carry, and the first sample whose column passes Q is found with
+//  * cast_rays: a group of G lanes (1 to 32; 4 at 256^3) marches one ray, G consecutive
+//    samples at a time; the recombination column sum(n^2 r^2 dr) is an inclusive group scan on
+//    top of a Kahan-compensated carry, and the first sample whose column passes Q is found with
 //    one ballot.  All rays of all active stars are one launch.
-//  * apply_front: every active star merges into one register pair per cell (max / min are
-//    exact and order-free, so one pass over the grid equals the reference's S passes); the
-//    float32 front distance is rounded once to the fp16 dfront (sim.py:980-985, 511-514).
+//  * apply_front: one pass over the grid merges the active stars, in star order, into one
+//    register pair per cell (the reference makes S passes).  With up to 32 stars, each star's
+//    front-radius range (front_bounds_kernel) lets a 32-cell row segment leave out the stars that
+//    cannot change its xi or front distance (the same bits).  The float32 front distance is
+//    rounded once to the fp16 dfront (sim.py:980-985, 511-514).
 //  * smooth_xi writes the final xi and reduces the CFL max speed of the step from it
 //    (nebula3d.py:154-162), so an ionizing step needs no separate max-speed pass.
 #include "nb_rayutil.cuh"
