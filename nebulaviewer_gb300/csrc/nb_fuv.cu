@@ -5,7 +5,8 @@
 //
 // GB300 design: cast_fuv marches a ray with a group of G lanes, the optical depth being an
 // inclusive group scan over a Kahan-compensated carry; a lane that crosses into new radial
-// bins writes them.  Density and ionized fraction are sampled at the same corners, so they
+// bins writes them, and a ray stops once its optical depth passes 120 (exp(-tau) is 0.0f from
+// there on: its remaining bins are written as 0).  Density and ionized fraction are sampled at the same corners, so they
 // are first packed as (rho, xi) pairs into free scratch: one 8-byte gather per corner.  All rays of all active stars are one launch, into one attenuation grid
 // per star laid out [star][u][phi][r] (r fastest: a ray's bins are contiguous).  apply_fuv
 // then accumulates every active star for a cell in one register, in the reference's star
