@@ -10,8 +10,6 @@ knobs; the ray sums only through rounding.  Results are cached per problem shape
 """
 import ctypes as C
 
-import torch
-
 from . import _lib
 
 CANDIDATES = {

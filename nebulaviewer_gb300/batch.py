@@ -9,8 +9,6 @@ parameters, and its results are bit-identical to stepping it alone.
 import ctypes as C
 import time
 
-import torch
-
 from . import _lib
 from . import ics as _ics
 from .sim import Sim

@@ -21,7 +21,6 @@ Random fields are sums of seeded random plane waves (resolution independent, so 
 and a large grid of the same scenario share their large scales) evaluated with torch on
 the requested device.
 """
-import math
 
 import numpy as np
 import torch

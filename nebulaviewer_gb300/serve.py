@@ -11,11 +11,9 @@ while others run overlaps with them on the device.  Each request's result is bit
 running it alone.
 """
 import collections
-import math
 import time
 
 import numpy as np
-import torch
 
 from .batch import BatchSim
 from .sim import Sim

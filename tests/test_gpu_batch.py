@@ -3,7 +3,6 @@ control and ionization, CUDA graphs): every instance's result equals stepping it
 the batch composition, cadence mix or graph use -- bit for bit with the exact build, within the
 path's tolerance (rel-L_inf 1e-5) with the fast build, whose batched and single-instance
 kernels may contract multiply-adds differently."""
-import numpy as np
 import pytest
 
 torch = pytest.importorskip("torch")

@@ -3,7 +3,6 @@ slots / HBM budget free up, overlap on the device in one batch, and each result 
 running the request alone: bit-identical with the exact build; within the path's tolerance
 (rel-L_inf 1e-5) with the fast build, whose batched and single-instance kernels may contract
 multiply-adds differently."""
-import numpy as np
 import pytest
 
 torch = pytest.importorskip("torch")
