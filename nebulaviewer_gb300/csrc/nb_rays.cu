@@ -352,7 +352,7 @@ __device__ __forceinline__ int load_stars(const NbStarW* sw, int nstars, float4*
 }
 
 template <bool HALF>
-__global__ void __launch_bounds__(256, 3) apply_front_kernel(const NbConst* __restrict__ c,
+__global__ void __launch_bounds__(256, 4) apply_front_kernel(const NbConst* __restrict__ c,
                                                           const NbStarW* __restrict__ sw,
                                                           const float* __restrict__ rfront, int nstars,
                                                           float* __restrict__ xi_raw, void* __restrict__ dfront,
