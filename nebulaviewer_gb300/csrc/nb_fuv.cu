@@ -22,7 +22,7 @@ __global__ void __launch_bounds__(256) pack_rx_kernel(const float* __restrict__ 
 }
 
 template <int G, bool REF_LAYOUT>
-__global__ void __launch_bounds__(256) cast_fuv_kernel(const NbConst* __restrict__ c, const NbStarW* __restrict__ sw,
+__global__ void __launch_bounds__(256, 5) cast_fuv_kernel(const NbConst* __restrict__ c, const NbStarW* __restrict__ sw,
                                                        const float4* __restrict__ dirs,
                                                        const float2* __restrict__ rx,
                                                        float* __restrict__ att, int nstars,
@@ -115,7 +115,7 @@ __global__ void __launch_bounds__(256) cast_fuv_kernel(const NbConst* __restrict
 }
 
 template <bool HALF>
-__global__ void __launch_bounds__(256) apply_fuv_kernel(const NbConst* __restrict__ c, const NbStarW* __restrict__ sw,
+__global__ void __launch_bounds__(256, 6) apply_fuv_kernel(const NbConst* __restrict__ c, const NbStarW* __restrict__ sw,
                                                         const float* __restrict__ att, int nstars,
                                                         void* __restrict__ g0) {
     __shared__ float4 st[NB_MAX_STARS];

@@ -85,7 +85,7 @@ __device__ __forceinline__ void cast_ray(const NbConst& C, const float4* __restr
 }
 
 template <int G>
-__global__ void __launch_bounds__(256) cast_rays_kernel(const NbConst* __restrict__ c, const NbStarW* __restrict__ sw,
+__global__ void __launch_bounds__(256, 6) cast_rays_kernel(const NbConst* __restrict__ c, const NbStarW* __restrict__ sw,
                                                         const float4* __restrict__ dirs,
                                                         const float* __restrict__ rho, float* __restrict__ rfront,
                                                         int nstars, const float* star_override, float q_override) {
