@@ -331,7 +331,7 @@ struct HydroSmem {
 };
 
 #ifndef NB_HYDRO_TJ
-#define NB_HYDRO_TJ 8                 // tile rows along j (one warp per row; 16 measured 2% slower)
+#define NB_HYDRO_TJ 8                 // tile rows along j (one warp per row; 16 measured 2% slower; hydro_tile assumes 8)
 #endif
 #ifndef NB_HYDRO_MINB
 #define NB_HYDRO_MINB (32 / NB_HYDRO_TJ)  // resident blocks per SM the register budget is sized for (64 regs)
@@ -340,9 +340,15 @@ struct HydroSmem {
 // One (j,k) tile column of one instance, marched over its i-chunk.  Called once per block by
 // the single-instance kernel and once per work item by the persistent batched kernel.  The
 // two mbarriers and their phases persist across calls: every load a call issues, it waits for.
+// `rot` (0-3, the same in every thread of the block) spreads the per-plane work that only some
+// warps do -- the y faces below the tile, the z faces before it, the z-halo conversion and the TMA
+// issue -- over warps of four different schedulers (warp w is issued by scheduler w mod 4 when a
+// block's warp slots start at a multiple of 4), rotated from block to block; any value gives the
+// same results.
 template <int SOLVER, int LIM, int TJ, bool STAGE2, bool I32 = false>
 __device__ __forceinline__ void hydro_tile(const HydroLaunch& L, int tile, unsigned char* smem, unsigned& ph0,
-                                           bool& failed) {
+                                           bool& failed, int rot) {
+    static_assert(TJ == 8, "the halo and edge-face warp assignment assumes 8 warps of 32 threads");
     using Idx = typename std::conditional<I32, int, long long>::type;     // the own cell's offset
     // register budget: stage 1 carries the x slope from face to face; stage 2 (U^n, the RK
     // combination, the CFL speed) recomputes it
@@ -400,7 +406,13 @@ __device__ __forceinline__ void hydro_tile(const HydroLaunch& L, int tile, unsig
             tma_load_3d(raw + f * SM::RAW_FIELD, &L.maps[L.map_in + f], k0 - 4, j0 - 2, pc, &bar[0]);
         tma_load_3d(raw + 4 * SM::RAW_FIELD, &L.maps[NB_MAP_XI], k0 - 4, j0 - 2, pc, &bar[0]);
     };
-    if (tid == 0) issue(P0);
+    // the per-plane extra work, on warps of schedulers rot, rot+1, rot+2 and rot+3 (mod 4): the y
+    // faces below the tile (role bit 1), the z faces before it (bit 2), the z-halo conversion,
+    // the TMA issue (bit 4)
+    const int w_zhalo = 4 + ((rot + 2) & 3);
+    const unsigned role = (tj == rot ? 1u : 0u) | (tj == ((rot + 1) & 3) && tk < TJ ? 2u : 0u) |
+                          (tid == (4 + ((rot + 3) & 3)) * 32 ? 4u : 0u);
+    if (role & 4u) issue(P0);
     if (tj == 0) {
         // The stars whose jet (nebula3d.py:131-149: strength > 0, an active star, r < jet_r) can reach
         // a cell centre of this tile, in star order: the distance from the star to the box of the
@@ -442,19 +454,18 @@ __device__ __forceinline__ void hydro_tile(const HydroLaunch& L, int tile, unsig
     };
     const int own = (tj + 2) * PW + tk + 2;          // this thread's cell in a prim / cs tile
     // the cells this thread converts in every plane: its own, and one of the 4 TK + 4 TJ cells of
-    // the halo strips (corners are never read); their offsets, computed once per tile, clamp to
-    // the domain in the raw tile
-    const bool has_halo = tid < 4 * TK + 4 * TJ;
+    // the halo strips (corners are never read): warps 0-3 one row of the y strips each, warp
+    // w_zhalo the z strips; their offsets, computed once per tile, clamp to the domain in the raw tile
+    const bool has_halo = tj < 4 || tj == w_zhalo;
     const int raw_own = raw_at(tj + 2, tk + 2);
     int prim_halo = 0, raw_halo = 0;
     if (has_halo) {
         int jj, kk;
-        if (tid < 4 * TK) {
-            const int rr = tid >> 5;
-            jj = rr < 2 ? rr : TJ + rr;
-            kk = 2 + (tid & 31);
+        if (tj < 4) {
+            jj = tj < 2 ? tj : TJ + tj;
+            kk = 2 + tk;
         } else {
-            const int hh = tid - 4 * TK;
+            const int hh = tk;
             jj = 2 + (hh >> 2);
             const int q = hh & 3;
             kk = q < 2 ? q : 32 + q;
@@ -487,7 +498,7 @@ __device__ __forceinline__ void hydro_tile(const HydroLaunch& L, int tile, unsig
         const float* rb = raw;
         float4* pp = prim + ps * PSLOT;
         float2* cp = cs + cq * PSLOT;
-        // ---- convert plane p: the own cell, then (tid < 4 TK + 4 TJ) one cell of the halo strips
+        // ---- convert plane p: the own cell, then (has_halo) one cell of the halo strips
         auto convert = [&](int o, int pi) {
             const float r = fmaxr(rb[o], floor_);
             const float xv = rb[4 * SM::RAW_FIELD + o];
@@ -505,7 +516,7 @@ __device__ __forceinline__ void hydro_tile(const HydroLaunch& L, int tile, unsig
         convert(raw_own, own);
         if (has_halo) convert(raw_halo, prim_halo);
         __syncthreads();                         // every thread is done with the raw slot
-        if (tid == 0 && p + 1 <= P1) issue(p + 1);
+        if ((role & 4u) && p + 1 <= P1) issue(p + 1);
         if (p < P0 + 3) continue;
         // x face (p-2)+1/2 from the own column of planes p-2..p and the carried slope of p-2
         const float4 qx1 = prim[((p - 2 - P0) & 3) * PSLOT + own], qx2 = prim[((p - 1 - P0) & 3) * PSLOT + own];
@@ -533,10 +544,10 @@ __device__ __forceinline__ void hydro_tile(const HydroLaunch& L, int tile, unsig
                                                      floor_);
         fy[(tj + 1) * TK + tk] = fyp;
         fz[tj * (TK + 1) + tk + 1] = fzp;
-        if (tj == 0) {                          // the y face below the tile: (j0-1)+1/2
+        if (role & 1u) {                        // the y face below the tile: (j0-1)+1/2
             fy[tk] = face_flux<SOLVER, LIM, 2>(q[0 * PW + kk], q[1 * PW + kk], q[2 * PW + kk], q[3 * PW + kk],
                                                c[1 * PW + kk], c[2 * PW + kk], floor_);
-        } else if (tj == 1 && tk < TJ) {        // the z face before the tile in row tk: (k0-1)+1/2
+        } else if (role & 2u) {                 // the z face before the tile in row tk: (k0-1)+1/2
             const int r2 = (tk + 2) * PW;
             fz[tk * (TK + 1)] = face_flux<SOLVER, LIM, 3>(q[r2 + 0], q[r2 + 1], q[r2 + 2], q[r2 + 3], c[r2 + 1],
                                                           c[r2 + 2], floor_);
@@ -688,14 +699,17 @@ __device__ __forceinline__ void hydro_abort(unsigned char* smem, unsigned* statu
     __syncthreads();
 }
 
+// the barriers, and the block's work rotation (hydro_tile) from the slot of its first warp: the
+// blocks resident on an SM occupy different groups of 8 slots and so take different rotations
 template <int TJ>
-__device__ __forceinline__ void hydro_init_bars(unsigned char* smem) {
+__device__ __forceinline__ void hydro_init_bars(unsigned char* smem, int* rot) {
     using SM = HydroSmem<TJ>;
     uint64_t* bar = reinterpret_cast<uint64_t*>(smem + SM::FIXED - SM::BAR_BYTES);
     if (threadIdx.x == 0) {
         mbar_init(&bar[0], 1);
         mbar_init(&bar[1], 1);
         fence_mbar_init();
+        *rot = (int)((warp_slot() >> 3) & 3u);
     }
     __syncthreads();
 }
@@ -703,10 +717,11 @@ __device__ __forceinline__ void hydro_init_bars(unsigned char* smem) {
 template <int SOLVER, int LIM, int TJ, bool STAGE2, bool I32>
 __global__ void __launch_bounds__(TK * TJ, NB_HYDRO_MINB) hydro_stage_kernel(const HydroLaunch L) {
     extern __shared__ __align__(128) unsigned char smem[];
-    hydro_init_bars<TJ>(smem);
+    __shared__ int rot;
+    hydro_init_bars<TJ>(smem, &rot);
     unsigned ph0 = 0;
     bool failed = false;
-    hydro_tile<SOLVER, LIM, TJ, STAGE2, I32>(L, blockIdx.x, smem, ph0, failed);
+    hydro_tile<SOLVER, LIM, TJ, STAGE2, I32>(L, blockIdx.x, smem, ph0, failed, rot);
     if (failed) hydro_abort<TJ>(smem, L.status, ph0);
 }
 
@@ -721,8 +736,8 @@ __global__ void __launch_bounds__(TK * TJ, NB_HYDRO_BATCH_MINB)
 hydro_batch_kernel(const HydroLaunch* __restrict__ Ls, const int2* __restrict__ work, int n_work,
                    unsigned* counter) {
     extern __shared__ __align__(128) unsigned char smem[];
-    __shared__ int item;
-    hydro_init_bars<TJ>(smem);
+    __shared__ int item, rot;
+    hydro_init_bars<TJ>(smem, &rot);
     unsigned ph0 = 0;
     bool failed = false;
     const HydroLaunch* last = nullptr;
@@ -733,7 +748,7 @@ hydro_batch_kernel(const HydroLaunch* __restrict__ Ls, const int2* __restrict__ 
         if (it >= n_work) break;
         const int2 w = work[it];
         last = &Ls[w.x];
-        hydro_tile<SOLVER, LIM, TJ, STAGE2, I32>(*last, w.y, smem, ph0, failed);
+        hydro_tile<SOLVER, LIM, TJ, STAGE2, I32>(*last, w.y, smem, ph0, failed, rot);
         if (failed) break;
         __syncthreads();
     }

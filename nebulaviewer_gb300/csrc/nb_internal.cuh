@@ -148,6 +148,13 @@ __device__ __forceinline__ unsigned smem_u32(const void* p) {
 __device__ __forceinline__ float fmaxr(float a, float b) { return a > b ? a : b; }   // Warp max
 __device__ __forceinline__ float fminr(float a, float b) { return a < b ? a : b; }   // Warp min
 __device__ __forceinline__ int iclampd(int x, int lo, int hi) { return x < lo ? lo : (x > hi ? hi : x); }
+// The calling warp's slot on its SM (%warpid).  Slot w is issued by scheduler w mod 4; the slot
+// may change on preemption, so it only ever steers work placement, never correctness.
+__device__ __forceinline__ unsigned warp_slot() {
+    unsigned w;
+    asm volatile("mov.u32 %0, %%warpid;" : "=r"(w));
+    return w;
+}
 
 // ---- mbarrier / TMA (sm_90+ PTX; every wait is bounded)
 __device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count) {
