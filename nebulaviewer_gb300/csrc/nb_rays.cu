@@ -84,8 +84,15 @@ __device__ __forceinline__ void cast_ray(const NbConst& C, const float4* __restr
     if (lane == 0) *out = rf;
 }
 
+// Resident blocks per SM of the ray kernel: 6 (40 registers) in the fast build, 5 (48) in the exact
+// one, whose IEEE divisions would spill 60 bytes at 40 registers.
+#if NB_ARITH_FAST
+#define NB_CAST_RAYS_MINB 6
+#else
+#define NB_CAST_RAYS_MINB 5
+#endif
 template <int G>
-__global__ void __launch_bounds__(256, 6) cast_rays_kernel(const NbConst* __restrict__ c, const NbStarW* __restrict__ sw,
+__global__ void __launch_bounds__(256, NB_CAST_RAYS_MINB) cast_rays_kernel(const NbConst* __restrict__ c, const NbStarW* __restrict__ sw,
                                                         const float4* __restrict__ dirs,
                                                         const float* __restrict__ rho, float* __restrict__ rfront,
                                                         int nstars, const float* star_override, float q_override) {
