@@ -63,6 +63,8 @@ class Snapshot:
 
 class Request:
     def __init__(self, rid, t_arrive, snap, mod, nsteps):
+        if int(nsteps) < 0:
+            raise ValueError(f"a request runs nsteps >= 0 steps, not {nsteps}")
         self.rid, self.t_arrive, self.snap, self.mod, self.nsteps = rid, t_arrive, snap, mod, int(nsteps)
         self.sim = None
         self.left = self.nsteps
@@ -114,6 +116,9 @@ class Server:
         return self.snaps[req.snap].cells * self.bpc
 
     def run(self, requests, realtime=True):
+        """serve `requests` (in arrival order; realtime=False admits each as soon as it fits);
+        returns (stats, the finished requests in completion order).  On an error every instance and
+        batch still open is closed before it propagates."""
         pending = collections.deque(sorted(requests, key=lambda r: r.t_arrive))
         queue = collections.deque()
         active, done = [], []
@@ -121,57 +126,73 @@ class Server:
         batch = None
         t0 = time.perf_counter()
         cell_steps = 0
-        while pending or queue or active:
-            now = time.perf_counter() - t0
-            while pending and (pending[0].t_arrive <= now or not realtime):
-                queue.append(pending.popleft())
-            changed = False
-            while queue and len(active) < self.max_slots and used + self._cost(queue[0]) <= self.budget:
-                r = queue.popleft()
-                r.sim = self.snaps[r.snap].branch(r.mod)
-                r.t_admit = time.perf_counter() - t0
-                used += self._cost(r)
-                active.append(r)
-                changed = True
-            if queue and not active:
-                raise RuntimeError("a request does not fit the HBM budget on its own")
-            if not active:
-                if pending:
-                    time.sleep(max(0.0, min(pending[0].t_arrive - now, 0.01)))
-                continue
-            if changed or batch is None:
-                if batch is not None:
+
+        def finish(r):                       # the result, then the instance is closed whatever happens
+            try:
+                r.result = result_of(r.sim)
+                if not self.keep_state:
+                    r.result.pop("state")
+            finally:
+                r.sim.close()
+                r.sim = None
+            r.t_done = time.perf_counter() - t0
+            done.append(r)
+
+        try:
+            while pending or queue or active:
+                now = time.perf_counter() - t0
+                while pending and (pending[0].t_arrive <= now or not realtime):
+                    queue.append(pending.popleft())
+                changed = False
+                while queue and len(active) < self.max_slots and used + self._cost(queue[0]) <= self.budget:
+                    r = queue.popleft()
+                    r.sim = self.snaps[r.snap].branch(r.mod)
+                    r.t_admit = time.perf_counter() - t0
+                    if r.left == 0:                    # nothing to run: the branched state is the result
+                        finish(r)
+                        continue
+                    used += self._cost(r)
+                    active.append(r)
+                    changed = True
+                if queue and not active:
+                    raise RuntimeError("a request does not fit the HBM budget on its own")
+                if not active:
+                    if pending:
+                        time.sleep(max(0.0, min(pending[0].t_arrive - now, 0.01)))
+                    continue
+                if changed or batch is None:
+                    if batch is not None:
+                        batch.close()
+                        batch = None
+                    batch = BatchSim([r.sim for r in active])
+                    self.rebuilds += 1
+                batch.step(1)                          # one tick: every active request advances one step
+                self.ticks += 1
+                fin = []
+                for r in active:
+                    r.left -= 1
+                    cell_steps += r.sim._n
+                    if r.left == 0:
+                        fin.append(r)
+                if fin:
                     batch.close()
-                batch = BatchSim([r.sim for r in active])
-                self.rebuilds += 1
-            batch.step(1)                          # one tick: every active request advances one step
-            self.ticks += 1
-            fin = []
-            for r in active:
-                r.left -= 1
-                cell_steps += r.sim._n
-                if r.left == 0:
-                    fin.append(r)
-            if fin:
+                    batch = None
+                    for r in fin:
+                        active.remove(r)
+                        used -= self._cost(r)
+                        finish(r)
+        finally:
+            if batch is not None:
                 batch.close()
-                batch = None
-                for r in fin:
-                    r.result = result_of(r.sim)
-                    if not self.keep_state:
-                        r.result.pop("state")
-                    r.t_done = time.perf_counter() - t0
-                    active.remove(r)
-                    used -= self._cost(r)
+            for r in active:
+                if r.sim is not None:
                     r.sim.close()
                     r.sim = None
-                    done.append(r)
-        if batch is not None:
-            batch.close()
         wall = time.perf_counter() - t0
         lat = np.array([r.t_done - r.t_arrive for r in done])
+        pct = (lambda q: float(np.percentile(lat, q) * 1e3)) if len(lat) else (lambda q: None)
         return dict(requests=len(done), wall_s=wall, cell_steps=cell_steps, gcells_per_s=cell_steps / wall / 1e9,
-                    p50_ms=float(np.percentile(lat, 50) * 1e3), p99_ms=float(np.percentile(lat, 99) * 1e3),
-                    ticks=self.ticks, batch_rebuilds=self.rebuilds), done
+                    p50_ms=pct(50), p99_ms=pct(99), ticks=self.ticks, batch_rebuilds=self.rebuilds), done
 
 
 def run_alone(snapshot, req):
