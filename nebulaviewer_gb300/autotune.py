@@ -81,20 +81,30 @@ def autotune(sim, knobs=None, steps=4, use_cache=True):
         for k, v in book.items():
             setattr(sim, k, v)
 
+    knobs = list(knobs or CANDIDATES)
+    orig = {k: get(sim, k) for k in knobs}
     out = {}
-    for knob in knobs or CANDIDATES:
-        best = None
-        for v in CANDIDATES[knob]:
-            put(sim, knob, v)
-            restore()
-            _measure(sim, knob, 1)                     # warm the launch path
-            restore()
-            t = _measure(sim, knob, steps)
-            if best is None or t < best[1]:
-                best = (v, t)
-        put(sim, knob, best[0])
-        out[knob] = best
-    restore()
-    sim._sync()
+    ok = False
+    try:
+        for knob in knobs:
+            best = None
+            for v in CANDIDATES[knob]:
+                put(sim, knob, v)
+                restore()
+                _measure(sim, knob, 1)                 # warm the launch path
+                restore()
+                t = _measure(sim, knob, steps)
+                if best is None or t < best[1]:
+                    best = (v, t)
+            put(sim, knob, best[0])
+            out[knob] = best
+        ok = True
+    finally:                                           # a failed candidate leaves no trace
+        sim._lib.nb_profile(sim._h, 0)
+        if not ok:
+            for k, v in orig.items():
+                put(sim, k, v)
+        restore()
+        sim._sync()
     _CACHE[key] = dict(out)
     return out
