@@ -176,15 +176,23 @@ class Sim:
             raise ValueError("nz must be a multiple of 4 (16-byte rows for the TMA tiles)")
         self.dx = float(ic["dx"])
         self.L = (nx * self.dx, ny * self.dx, nz * self.dx)
+        if min(self.shape) < 1 or not self.dx > 0.0:
+            raise ValueError(f"a grid needs positive sizes and dx, not {self.shape}, dx = {self.dx}")
         dev = self.device
         f32 = dict(device=dev, dtype=torch.float32)
-        self._rho = torch.as_tensor(ic["rho"]).to(**f32).contiguous().clone()
+
+        def field(x, what):                      # the kernels index every field by the grid's shape
+            t = x if torch.is_tensor(x) else torch.as_tensor(np.asarray(x, np.float32))
+            if tuple(t.shape) != self.shape:
+                raise ValueError(f"{what} has shape {tuple(t.shape)}; the grid is {self.shape}")
+            return t.to(**f32).contiguous()
+
+        self._rho = field(ic["rho"], "rho").clone()
         pre = float(P.get("pre_t", 0.0) or 0.0) > 0.0
         torus = ic.get("torus")
         self.torus = None
         if torus is not None:                                                       # sim.py:669-671, 737
-            torus = (torus if torch.is_tensor(torus) else torch.as_tensor(np.asarray(torus, np.float32)))
-            torus = torus.to(**f32).contiguous()
+            torus = field(torus, "torus")
             if pre:
                 self.torus = torus
             else:
@@ -193,7 +201,9 @@ class Sim:
         if ic.get("mom") is None:
             m = [torch.zeros(self.shape, **f32) for _ in range(3)]
         else:
-            m = [torch.as_tensor(v).to(**f32).contiguous().clone() for v in ic["mom"]]
+            if len(ic["mom"]) != 3:
+                raise ValueError("mom holds the three momentum fields (mx, my, mz)")
+            m = [field(v, name).clone() for v, name in zip(ic["mom"], ("mx", "my", "mz"))]
         self._mx, self._my, self._mz = m
         self._xi = torch.zeros(self.shape, **f32)
         self._stage = torch.zeros((4,) + self.shape, **f32)
@@ -561,13 +571,20 @@ class Sim:
             st = copy.deepcopy(self.rng.bit_generator.state)
             self._forcing.append((self._mkF(), st))
 
+    def _push_forcing(self, buf):
+        """copy n forcing fields ([n][3][sx][sy][sz] float32, host) into the device ring: the library
+        reads n whole fields of the forcing grid from the buffer, so its shape is checked here"""
+        want = (3,) + tuple(self.sshape)
+        if buf.dtype != np.float32 or buf.ndim != 5 or tuple(buf.shape[1:]) != want or not buf.flags.c_contiguous:
+            raise ValueError(f"forcing fields must be float32 [n]{list(want)}, not {buf.dtype} {list(buf.shape)}")
+        self._chk(self._lib.nb_drive_push(self._h, C.c_void_p(buf.ctypes.data), len(buf)), "nb_drive_push")
+
     def _drive_fill(self, upto):
         """push forcing fields until `upto` fields were pushed since the ring reset"""
         self._drive_make(upto)
         new = [f for f, _ in self._forcing[self._pushed:upto]]
         if new:
-            buf = np.ascontiguousarray(np.stack(new))
-            self._chk(self._lib.nb_drive_push(self._h, C.c_void_p(buf.ctypes.data), len(new)), "nb_drive_push")
+            self._push_forcing(np.ascontiguousarray(np.stack(new), np.float32))
             self._pushed += len(new)
 
     def _drive_new(self, clock, fields=None):
@@ -580,8 +597,8 @@ class Sim:
         self._pushed = 0
         if fields is not None:
             buf = np.ascontiguousarray(np.stack([np.asarray(f, np.float32) for f in fields]))
+            self._push_forcing(buf)
             self._forcing = [(f, None) for f in buf]
-            self._chk(self._lib.nb_drive_push(self._h, C.c_void_p(buf.ctypes.data), len(buf)), "nb_drive_push")
             self._pushed = len(buf)
         else:
             self._drive_fill(2)

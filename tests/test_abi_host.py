@@ -112,3 +112,34 @@ def test_product_path_does_not_import_the_oracle():
                 src = open(os.path.join(dirpath, f)).read()
                 assert not re.search(r"^\s*(import|from)\s+oracle\b", src, re.M), f
                 assert "liboracle" not in src and "ref_cpu" not in src, f
+
+
+def _state_kwargs(shape, rho_shape=None, mom_shape=None, torus_shape=None):
+    rho = np.ones(rho_shape or shape, np.float32)
+    mom = None if mom_shape is None else [np.zeros(mom_shape, np.float32)] * 3
+    torus = None if torus_shape is None else np.zeros(torus_shape, np.float32)
+    return dict(shape=shape, dx=0.01, rho=rho, stars=[(0.1, 0.1, 0.1, 1.0)], kinds=["main"], jets=[(0.0, 0.0, 1.0)],
+                jkinds=[None], P={}, mom=mom, torus=torus, device="cpu")
+
+
+@pytest.mark.parametrize("bad", ("rho", "mom", "torus", "dims"))
+def test_fields_of_another_shape_are_refused_before_the_library(bad):
+    """every field the kernels index by the grid shape must have that shape (no library call yet)"""
+    from nebulaviewer_gb300.sim import Sim
+    g = (8, 8, 8)
+    kw = {"rho": _state_kwargs(g, rho_shape=(8, 8, 4)), "mom": _state_kwargs(g, mom_shape=(8, 8 * 8)),
+          "torus": _state_kwargs(g, torus_shape=(4, 8, 8)), "dims": _state_kwargs((0, 8, 8))}[bad]
+    with pytest.raises(ValueError):
+        Sim.from_state(**kw)
+
+
+def test_forcing_fields_of_another_shape_are_refused():
+    """the library copies whole forcing fields of the forcing grid from the host buffer"""
+    from nebulaviewer_gb300.sim import Sim
+    s = Sim.__new__(Sim)
+    s.sshape = (4, 5, 6)
+    s._h = None
+    for buf in (np.zeros((2, 3, 4, 5, 5), np.float32), np.zeros((2, 3, 4, 5, 6), np.float64),
+                np.zeros((3, 4, 5, 6), np.float32)):
+        with pytest.raises(ValueError):
+            s._push_forcing(buf)
