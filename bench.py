@@ -82,8 +82,10 @@ def ncu_traffic():
 
 
 class ClockSampler:
-    """nvidia-smi clocks / throttle reasons sampled every 50 ms during the timed region, which
-    is also marked as the NVTX range "timed" (ncu --nvtx --nvtx-include timed/ captures only it)"""
+    """nvidia-smi clocks / throttle reasons sampled every 20 ms; the summary keeps the samples that
+    arrived while the timed region ran.  `start()` may launch the sampler ahead of the region (before
+    the warm-up), so that it is already sampling when a short region begins.  The region is also
+    marked as the NVTX range "timed" (ncu --nvtx --nvtx-include timed/ captures only it)."""
 
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
          "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
@@ -92,30 +94,57 @@ class ClockSampler:
     def __init__(self, index):
         self.index = index
         self.p = None
+        self.arrived = []                        # (monotonic arrival time, csv line)
+        self.window = None
 
-    def __enter__(self):
+    def start(self):
+        if self.p is not None:
+            return self
         try:
             self.p = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
-                                       "--format=csv,noheader,nounits", "-lms", "50"],
-                                      stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+                                       "--format=csv,noheader,nounits", "-lms", "20"],
+                                      stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True, bufsize=1)
         except OSError:
             self.p = None
+            return self
+        import atexit
+        import threading
+        atexit.register(self._stop)              # never outlive the process, whatever happens
+
+        def read(out):
+            for ln in out:
+                if ln.strip():
+                    self.arrived.append((time.monotonic(), ln))
+        self.reader = threading.Thread(target=read, args=(self.p.stdout,), daemon=True)
+        self.reader.start()
+        return self
+
+    def _stop(self):
+        if self.p is not None and self.p.poll() is None:
+            self.p.terminate()
+            try:
+                self.p.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.p.kill()
+                self.p.wait()
+        if getattr(self, "reader", None) is not None:
+            self.reader.join(timeout=5)
+
+    def __enter__(self):
+        self.start()
         import torch
         torch.cuda.nvtx.range_push("timed")
+        self.t_enter = time.monotonic()
         return self
 
     def __exit__(self, *a):
         import torch
+        t_exit = time.monotonic()
         torch.cuda.nvtx.range_pop()
-        self.lines = []
-        if self.p is not None:
-            self.p.terminate()
-            try:
-                out, _ = self.p.communicate(timeout=5)
-            except subprocess.TimeoutExpired:
-                self.p.kill()
-                out, _ = self.p.communicate()
-            self.lines = [ln for ln in out.splitlines() if ln.strip()]
+        time.sleep(0.03)                         # the sample taken at the end of the region arrives
+        self._stop()
+        self.window = (self.t_enter, t_exit + 0.03)
+        self.lines = [ln for t, ln in list(self.arrived) if self.window[0] <= t <= self.window[1]]
 
     def summary(self):
         sm, mx, reasons = [], 0.0, set()
@@ -264,6 +293,7 @@ def run_gb300(args):
 
     from nebulaviewer_gb300.autotune import autotune
     tuning = {k: v[0] for k, v in autotune(sim).items()}       # untimed: launch shapes for this problem
+    clk = ClockSampler(local).start()          # sampling before the timed region begins
     device_steps(args.warmup)
     torch.cuda.synchronize(dev)
     # ---------------- device-resident throughput (the metric's value)
@@ -277,7 +307,7 @@ def run_gb300(args):
     if dist:
         dist.barrier()
     torch.cuda.synchronize(dev)
-    with ClockSampler(local) as clk:
+    with clk:
         ev0.record(stream)
         device_steps(args.steps)
         ev1.record(stream)
@@ -428,11 +458,12 @@ def run_batch(args):
     plain_s = time.perf_counter() - t0
     plain = cells * plain_steps / plain_s / 1e9
     B = BatchSim(sims, graphs=True)
+    clk = ClockSampler(0).start()              # sampling before the timed region begins
     B.step(args.warmup)
     torch.cuda.synchronize(dev)
     l0 = B.launches()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    with ClockSampler(0) as clk:
+    with clk:
         ev0.record()
         B.step(args.steps, sync=False)
         ev1.record()
@@ -506,13 +537,14 @@ def run_stirred(args):
     res = (args.res if args.res != RES else 256) // 2
     sim = Sim("torus_stirred", res=res, device=dev, verbose=False, arith=args.arith, params=dict(pre_t=1e9))
     lib = sim._lib
+    clk = ClockSampler(0).start()              # sampling before the timed region begins
     sim.step(args.warmup)
     torch.cuda.synchronize(dev)
     lib.nb_profile(sim._h, 1)
     prof_ms, prof_n = (C.c_double * 16)(), (C.c_longlong * 16)()
     lib.nb_profile_read(sim._h, prof_ms, prof_n)
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    with ClockSampler(0) as clk:
+    with clk:
         ev0.record()
         sim.step(args.steps, sync=False)
         ev1.record()
@@ -564,6 +596,7 @@ def run_render(args):
     pp = {"c_ha": (0.33, 0.675, 1.5), "c_o3": (0.45, 1.125, 1.5), "c_s2": (1.2, 0.66, 0.3), "c_dg": (0.07, 0.035, 0.01),
           "c_sh": (0.02, 0.007, 0.009), "gs": 12.0, "ambient": 0.1, "edge": 0.08, "inv_L": [1.0 / v for v in L],
           "dx": sim.dx}
+    clk = ClockSampler(0).start()              # sampling before the timed region begins
     for _ in range(args.warmup):
         sim.render_pack(pp)
     torch.cuda.synchronize(dev)
@@ -572,7 +605,7 @@ def run_render(args):
     prof_ms, prof_n = (C.c_double * 16)(), (C.c_longlong * 16)()
     lib.nb_profile_read(sim._h, prof_ms, prof_n)
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    with ClockSampler(0) as clk:
+    with clk:
         ev0.record()
         for _ in range(args.steps):
             sim.render_pack(pp)
@@ -609,11 +642,12 @@ def run_cliff(args):
     res = args.res if args.res != RES else 1024
     sim = Sim("cliffwall", res=res, device=dev, verbose=False, arith=args.arith)
     m0 = sim.conservation()
+    clk = ClockSampler(0).start()              # sampling before the timed region begins
     sim.step(args.warmup)
     torch.cuda.synchronize(dev)
     m1 = sim.conservation()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    with ClockSampler(0) as clk:
+    with clk:
         ev0.record()
         for _ in range(args.steps):
             sim.step(1, sync=False)
