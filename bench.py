@@ -223,7 +223,6 @@ def run_reference(args):
     from nebulaviewer_gb300 import ics
     dev = "cuda" if torch.cuda.is_available() else "cpu"
     ic = ics.sheet(res=args.res, device=dev)
-    import numpy as np
     ic_host = dict(ic, rho=ic["rho"].cpu().numpy(), mom=[m.cpu().numpy() for m in ic["mom"]])
     del ic
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
