@@ -1,7 +1,7 @@
 """CPU oracle of the simulation step: TEST INFRASTRUCTURE ONLY.
 
 Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use this module, as
-the checker; the product (nebulaviewer_gb300) never imports it.
+the reference to check against; the product (nebulaviewer_gb300) never imports it.
 
 * `Kernels(dtype)`: ctypes access to oracle/ref_cpu.cpp, a line-by-line C++ restatement
   of the reference's Warp kernels (nebula3d.py / sim.py; each function cites its lines),

@@ -1,7 +1,7 @@
 // CPU oracle: a line-by-line restatement of the reference's simulation-step kernels.
 //
 // TEST INFRASTRUCTURE ONLY.  Nothing in the product links, loads or calls this file;
-// tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use it as the checker.
+// tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use it to check results.
 //
 // Each function follows one NVIDIA-Warp kernel of the reference (file:line cited) with
 // the same operation order, evaluated op by op (built with -ffp-contract=off, no
