@@ -88,7 +88,6 @@ class Kernels:
                     cn2, ci2, vmax, solver, lim):
         nx, ny, nz = U[0].shape
         ins = [self._a(x) for x in U] + [self._a(xi)]
-        u0 = [x if x is not None else None for x in U0]
         u0 = [self._a(x) for x in U0]
         for o in out:
             assert o.dtype == self.dt and o.flags.c_contiguous
