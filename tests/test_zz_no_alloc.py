@@ -9,8 +9,6 @@ give the totals of the handle-based nb_reduce_fp64 (which allocates its scratch 
 and that a size beyond the array's limit is refused.  Collected last (file name) so that a run
 stopping at its first failure has already run every other test.
 """
-import ctypes as C
-
 import numpy as np
 import pytest
 
