@@ -187,6 +187,69 @@ def algorithmic_bytes(kind, ncell, nstars):
     return per.get(kind, 0) * ncell
 
 
+def ray_march_samples(star, L, dr, nsteps, nu, nphi, rfront=None, rcap=None, rstop=None):
+    """Samples the reference's ray loops evaluate for one star's (nu, nphi) rays.
+
+    Each ray runs n over [int(t_in / dr), min(nsteps, int(t_out / dr) + 2)) with (t_in, t_out)
+    the slab test against [0, L] (box_range, nebula3d.py:229-244).  cast_rays (nebula3d.py:247-270)
+    leaves the loop at the front crossing: a front rf < rcap lies in [n dr, (n + 1) dr) of the
+    crossing sample n, which is the last one evaluated.  cast_fuv (nebula3d.py:320-352) leaves it
+    once r = (n + 1/2) dr reaches rstop = nr * binr (its last radial bin).  Geometry in float64:
+    a ray whose bound falls on a sample boundary in float32 may count one sample more or less."""
+    import numpy as np
+    u = -1.0 + (np.arange(nu) + 0.5) * 2.0 / nu
+    s = np.sqrt(np.maximum(1.0 - u * u, 0.0))
+    phi = (np.arange(nphi) + 0.5) * 2.0 * np.pi / nphi
+    d = np.stack([s[:, None] * np.cos(phi)[None, :], s[:, None] * np.sin(phi)[None, :],
+                  np.broadcast_to(u[:, None], (nu, nphi))])
+    t0 = np.zeros((nu, nphi))
+    t1 = np.full((nu, nphi), 1e9)
+    for a in range(3):
+        o, da = float(star[a]), d[a]
+        flat = np.abs(da) < 1e-9
+        with np.errstate(divide="ignore", invalid="ignore"):
+            ta = np.where(flat, 0.0, (0.0 - o) / da)
+            tb = np.where(flat, 0.0, (float(L[a]) - o) / da)
+        t0 = np.where(flat, t0, np.maximum(t0, np.minimum(ta, tb)))
+        t1 = np.where(flat, np.where((o < 0.0) | (o > L[a]), -1.0, t1), np.minimum(t1, np.maximum(ta, tb)))
+    n0 = np.trunc(t0 / dr)
+    n1 = np.minimum(nsteps, np.trunc(t1 / dr) + 2)
+    if rfront is not None:
+        rf = np.asarray(rfront, np.float64).reshape(nu, nphi)
+        n1 = np.where(rf < rcap, np.minimum(n1, np.floor(rf / dr) + 1), n1)
+    if rstop is not None:
+        n1 = np.minimum(n1, math.ceil(rstop / dr - 0.5) + 1)
+    return int(np.maximum(n1 - n0, 0).sum())
+
+
+def ray_rates(sim, lib, kinds):
+    """Ray samples per second of the ionizing and FUV ray kernels: the samples the reference's
+    loops evaluate for the active stars (ray_march_samples; the ionizing fronts re-cast from the
+    final state) over the mean launch time of each kernel.  Our kernels may evaluate a few more
+    (G lanes step G samples at a time) or fewer (the FUV rays stop once exp(-tau) is 0.0f)."""
+    import ctypes as C
+    import torch
+    from nebulaviewer_gb300 import _lib
+    act = sim.active_stars()
+    nu, nphi = sim.rfront.shape
+    rf = torch.empty((nu, nphi), dtype=torch.float32, device=sim._rho.device)
+    ion = fuv = 0
+    for x, y, z, qf, _ in act:
+        xyz = (C.c_double * 3)(x, y, z)
+        _lib.check(lib.nb_cast_rays(sim._h, xyz, qf * sim.P["q_main"], C.c_void_p(rf.data_ptr())), sim._h,
+                   "nb_cast_rays")
+        ion += ray_march_samples((x, y, z), sim.L, sim.dr, sim.nsteps, nu, nphi, rfront=rf.cpu().numpy(),
+                                 rcap=sim.diag)
+        fuv += ray_march_samples((x, y, z), sim.L, sim.dr, sim.nsteps, sim.att.shape[1], sim.att.shape[2],
+                                 rstop=sim.diag)       # nr * binr, binr = diag / nr (sim.py:957-958)
+    out = {"stars": len(act)}
+    for kind, n in (("cast_rays", ion), ("cast_fuv", fuv)):
+        if kind in kinds:
+            ms, launches = kinds[kind]
+            out[kind] = {"samples_per_launch": n, "gsamples_per_s": n / (ms / launches * 1e-3) / 1e9}
+    return out
+
+
 def cpu_sample(ic_host, steps=3):
     """the oracle (reference scheme, CPU restatement) on a bounded sample of the workload"""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
@@ -376,6 +439,10 @@ def run_gb300(args):
     clocks = clk.summary()
     res = None
     if rank == 0:
+        try:
+            rays = ray_rates(sim, lib, kinds)
+        except Exception as e:        # an auxiliary figure: its failure must not cost the bench line
+            rays = {"error": f"{type(e).__name__}: {e}"}
         res = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True, "scaling": "weak",
@@ -398,6 +465,7 @@ def run_gb300(args):
                     "passes": [ws * ncell * e2e_steps / t / 1e9 for t in e2e_runs]},
             "gpu_launches": launches,
             "clocks": clocks,
+            "ray_samples": rays,
         }
     sim.close()
     if rank == 0:
