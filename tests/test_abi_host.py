@@ -103,6 +103,33 @@ def test_synthetic_ics_are_seeded_and_shaped():
     assert r[:4].max() < 3.0 and r[-4:].min() > 150.0
 
 
+def test_sheet_and_torus_follow_their_stated_distributions():
+    """the turbulent sheet: slab profile 1 + 49 exp(-(y/0.1)^2) (n = 50 at the mid-plane) times a
+    log-normal of sigma 0.5, a divergence-free velocity of rms Mach 5 at cs_n = 1, six stars in the
+    slab with photon rates inside one decade; the torus: background n = 1 and Q = n^2 R^3 / 3 of a
+    Stromgren radius 0.25"""
+    from nebulaviewer_gb300 import ics
+    n = 64
+    s = ics.sheet(res=n)
+    rho = s["rho"].numpy().astype(np.float64)
+    dx = s["dx"]
+    y = (np.arange(n) + 0.5) * dx
+    prof = np.exp(-((y - 0.5) / 0.1) ** 2)[None, :, None]
+    ln = np.log(rho / (1.0 + 49.0 * prof))
+    assert 0.45 < ln.std() < 0.55 and abs(ln.mean() + 0.125) < 0.05       # exp(sigma g - sigma^2 / 2)
+    v = np.stack([m.numpy() / s["rho"].numpy() for m in s["mom"]]).astype(np.float64)
+    assert 4.5 < np.sqrt((v ** 2).sum(0).mean()) < 5.5
+    div = sum(np.gradient(v[a], dx, axis=a) for a in range(3))
+    grad = np.sqrt(sum(np.gradient(v[c], dx, axis=a) ** 2 for c in range(3) for a in range(3)))
+    assert np.abs(div).mean() < 0.05 * grad.mean()
+    assert len(s["stars"]) == 6
+    for x, sy, z, qf, ton in s["stars"]:
+        assert abs(sy - 0.5) <= 0.03 and 0.2 <= x <= 0.8 and 0.2 <= z <= 0.8 and 1.0 <= qf <= 10.0 and ton == 0.0
+    t = ics.torus(res=32)
+    assert 0.9 < float(np.median(t["rho"].numpy())) < 1.1
+    assert abs(t["P"]["q_main"] - 5.208e-3) < 1e-6
+
+
 def test_product_path_does_not_import_the_oracle():
     """the package must never route through the CPU oracle"""
     pkg = os.path.join(ROOT, "nebulaviewer_gb300")
