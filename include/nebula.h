@@ -142,7 +142,9 @@ int nb_set_live(nb_handle h, const nb_live* live);
 int nb_set_stars(nb_handle h, const nb_star* stars, int n);
 /* Sim.t / dt / it, as written by set_state_meta (sim.py:1185-1211). */
 int nb_set_clock(nb_handle h, const nb_clock* c);
-int nb_get_clock(nb_handle h, nb_clock* c);          /* synchronizes the stream */
+/* Synchronizes the stream.  Both clock reads return NB_ERR_TIMEOUT (the clock still filled in)
+ * once a hydro stage's bounded TMA wait has given up on the device: the fields are incomplete. */
+int nb_get_clock(nb_handle h, nb_clock* c);
 /* Enqueues a copy of the clock into pinned host memory, in stream order (asynchronous). */
 int nb_mirror_clock(nb_handle h);
 /* The clock as of the last nb_mirror_clock (once the stream has passed it: the caller

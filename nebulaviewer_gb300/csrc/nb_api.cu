@@ -479,6 +479,16 @@ NB_EXPORT int nb_set_clock(nb_handle h, const nb_clock* c) {
     return NB_OK;
 }
 
+// A hydro stage whose bounded TMA wait gave up left the rest of its tile unwritten, so every
+// clock read after it reports NB_ERR_TIMEOUT (the clock itself is still returned).  The device
+// status bit stays set for the life of the handle.
+static int clock_status(nb_instance* h, const NbState& s) {
+    if (s.status & NB_DEV_TMA_TIMEOUT)
+        return fail(h, NB_ERR_TIMEOUT, "a bounded TMA wait in a hydro stage gave up on the device: the fields "
+                                       "are incomplete since then (nb_device_status)");
+    return NB_OK;
+}
+
 NB_EXPORT int nb_mirror_clock(nb_handle h) {
     if (!h) return fail(h, NB_ERR_ARG, "null handle");
     return mirror_state(h);
@@ -492,7 +502,7 @@ NB_EXPORT int nb_peek_clock(nb_handle h, nb_clock* c) {
     c->it = s.it;
     c->tp = s.tp;
     c->ip = s.ip;
-    return NB_OK;
+    return clock_status(h, s);
 }
 
 NB_EXPORT int nb_get_clock(nb_handle h, nb_clock* c) {
@@ -505,7 +515,7 @@ NB_EXPORT int nb_get_clock(nb_handle h, nb_clock* c) {
     c->it = s.it;
     c->tp = s.tp;
     c->ip = s.ip;
-    return NB_OK;
+    return clock_status(h, s);
 }
 
 NB_EXPORT int nb_device_status(nb_handle h, int* status) {

@@ -486,6 +486,7 @@ class Sim:
             self._chk(self._lib.nb_mirror_clock(self._h), "nb_mirror_clock")
             self._sync()
             self._clock_fresh = True                 # the stream passed the clock's copy to host memory
+            self._clock()                            # host read; raises if a hydro stage's TMA wait gave up
             if self._drv_on:
                 self._drive_info()                 # raises if a stirred step found no forcing field
         self._tick("step", t0)
