@@ -310,9 +310,16 @@ int nb_profile_read(nb_handle h, double ms[NB_PROF_KINDS], long long count[NB_PR
  * leaves out, per 32-cell segment of a row, the stars that cannot change its ionized fraction or
  * front distance; NB_TUNE_FUV_CUT (default 1): a FUV ray stops once its optical depth passes 120,
  * where exp(-tau) is 0.0f for good, and writes 0 to its remaining bins.  The result is the same
- * either way, bit for bit. */
+ * either way, bit for bit.
+ * Failure-path test keys (no reference counterpart; the reference blocks on a host read instead,
+ * sim.py:1009-1012): NB_TUNE_WAIT_LIMIT (default and maximum 2^22) is the number of polls after
+ * which a hydro stage's bounded TMA wait gives up; NB_TUNE_STALL_TEST = 1 makes the hydro stages
+ * issue no tile copy at all, so the first wait of every tile runs out with nothing in flight: the
+ * stage records NB_DEV_TMA_TIMEOUT, writes nothing and returns, and every later clock read returns
+ * NB_ERR_TIMEOUT.  The handle's fields are then incomplete for good (destroy it).  A batch takes
+ * both from its instances when it is created. */
 enum { NB_TUNE_CHUNK_I = 0, NB_TUNE_RAY_GROUP = 1, NB_TUNE_FUV_GROUP = 2, NB_TUNE_TILE_ORDER = 3,
-       NB_TUNE_FRONT_CULL = 4, NB_TUNE_FUV_CUT = 5 };
+       NB_TUNE_FRONT_CULL = 4, NB_TUNE_FUV_CUT = 5, NB_TUNE_WAIT_LIMIT = 6, NB_TUNE_STALL_TEST = 7 };
 int nb_set_tuning(nb_handle h, int key, int value);
 int nb_get_tuning(nb_handle h, int key, int* value);
 /* Number of kernels the handle has launched (a claim the benchmark reports). */
@@ -328,8 +335,12 @@ int nb_counters(nb_handle h, long long* launches);
  * until the process exits), which caps n at 2^30 cells: larger n returns NB_ERR_LIMIT with a
  * message in nb_static_last_error().  It calls no cudaMalloc / cudaFree.  The first call on a
  * device looks up that array's device address (cudaGetSymbolAddress, with the device current);
- * make that first call before any stream capture.  Every call shares the one array: calls
- * that overlap on the GPU (different streams without ordering) race.  Asynchronous on
+ * make that first call before any stream capture.  The address belongs to the context it was
+ * looked up in: a call made in another context (after a cudaDeviceReset, or with another context
+ * current on the thread) looks it up again, so the first call after such a change is a set-up
+ * call too.  An error that an earlier CUDA call left pending on the thread is returned as
+ * NB_ERR_CUDA before any work is enqueued, and left pending.  Every call shares the one array:
+ * calls that overlap on the GPU (different streams without ordering) race.  Asynchronous on
  * `stream` (0 = legacy default stream). */
 int nb_reduce_fp64_static(const float* rho, const float* mx, const float* my, const float* mz, long long n,
                           double* out4, void* stream);

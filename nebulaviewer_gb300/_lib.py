@@ -17,6 +17,8 @@ DEFAULT_ARITH = os.environ.get("NEBULA_ARITH", "fast")
 
 NB_ABI_VERSION = 2
 NB_OK = 0
+NB_DEV_TMA_TIMEOUT = 1      # nb_device_status bit: a hydro stage's bounded TMA wait gave up
+NB_DEV_DRIVE_EMPTY = 2      # nb_device_status bit: a stirred step found no forcing field B
 ERRORS = {-1: "NB_ERR_ARG", -2: "NB_ERR_CUDA", -3: "NB_ERR_STATE", -4: "NB_ERR_LIMIT", -5: "NB_ERR_TIMEOUT",
           -6: "NB_ERR_NOMEM"}
 SOLVERS = {"rusanov": 0, "hll": 1}
@@ -122,7 +124,8 @@ SIGNATURES = {
     "nb_reduce_fp64_static": (C.c_int, [_P, _P, _P, _P, C.c_longlong, _P, _P]),
     "nb_static_last_error": (C.c_char_p, []),
 }
-TUNE = {"chunk_i": 0, "ray_group": 1, "fuv_group": 2, "tile_order": 3, "front_cull": 4, "fuv_cut": 5}
+TUNE = {"chunk_i": 0, "ray_group": 1, "fuv_group": 2, "tile_order": 3, "front_cull": 4, "fuv_cut": 5,
+        "wait_limit": 6, "stall_test": 7}
 PROF_KINDS = ["ctrl", "stage1", "stage2", "cast_rays", "apply_front", "smooth", "cast_fuv", "apply_fuv", "max_speed",
               "snapshot", "drive", "render"]
 

@@ -64,8 +64,23 @@ class BatchSim:
             s.version += int(k)
         if sync:
             self.sims[0]._sync()
+            self.check_status()
         self.prof["step"] = self.prof.get("step", 0.0) + time.perf_counter() - t0
         return time.perf_counter() - t0
+
+    def check_status(self):
+        """raise if a batched hydro stage's bounded TMA wait gave up on the device for any instance
+        (its fields are incomplete from then on), as a synchronized Sim.step does; step(sync=True)
+        calls it after the batch's steps"""
+        st = C.c_int()
+        bad = []
+        for i, s in enumerate(self.sims):
+            s._chk(s._lib.nb_device_status(s._h, C.byref(st)), "nb_device_status")
+            if st.value & _lib.NB_DEV_TMA_TIMEOUT:
+                bad.append(i)
+        if bad:
+            raise _lib.NebulaError(f"nb_batch_step: NB_ERR_TIMEOUT: a bounded TMA wait in a batched hydro stage "
+                                   f"gave up on the device; instances {bad} have incomplete fields")
 
     def launches(self):
         v = C.c_longlong()

@@ -40,6 +40,8 @@ struct nb_instance {
     int tile_order = 0;
     int front_cull = 1;                 // apply_front skips the stars that cannot change a segment
     int fuv_cut = 1;                    // FUV rays stop where exp(-tau) has reached 0.0f
+    unsigned wait_limit = NB_WAIT_LIMIT; // polls of each bounded TMA wait in the hydro stages
+    int stall_test = 0;                 // failure-path test: the hydro stages issue no tile copies
     long long ncell = 0;
     long long launches = 0;             // kernels this handle launched (nb_counters)
     int profiling = 0;                  // CUDA-event timing per kernel kind (nb_profile)
@@ -175,6 +177,8 @@ int launch_stage(nb_instance* h, const float* const in[4], const float* const u0
     L.order = h->tile_order;
     L.no_sources = no_sources ? 1 : 0;
     L.idx32 = h->ncell < (1LL << 31) ? 1 : 0;
+    L.wait_limit = h->wait_limit;
+    if (h->stall_test) L.maps = nullptr;
     Prof pf(h, (smax || stage2) ? NB_PROF_STAGE2 : NB_PROF_STAGE1, 1);
     CK(h, nb_launch_hydro(L, h->d.solver, h->d.limiter, h->stream));
     return NB_OK;
@@ -852,6 +856,8 @@ NB_EXPORT int nb_get_tuning(nb_handle h, int key, int* value) {
         case NB_TUNE_TILE_ORDER: *value = h->tile_order; return NB_OK;
         case NB_TUNE_FRONT_CULL: *value = h->front_cull; return NB_OK;
         case NB_TUNE_FUV_CUT: *value = h->fuv_cut; return NB_OK;
+        case NB_TUNE_WAIT_LIMIT: *value = (int)h->wait_limit; return NB_OK;
+        case NB_TUNE_STALL_TEST: *value = h->stall_test; return NB_OK;
         default: return fail(h, NB_ERR_ARG, "unknown tuning key");
     }
 }
@@ -874,6 +880,15 @@ NB_EXPORT int nb_set_tuning(nb_handle h, int key, int value) {
         case NB_TUNE_FUV_CUT:
             if (value != 0 && value != 1) return fail(h, NB_ERR_ARG, "FUV cut must be 0 or 1");
             h->fuv_cut = value;
+            return NB_OK;
+        case NB_TUNE_WAIT_LIMIT:
+            if (value < 1 || (unsigned)value > NB_WAIT_LIMIT)
+                return fail(h, NB_ERR_ARG, "the wait limit must be in [1, 2^22] polls");
+            h->wait_limit = (unsigned)value;
+            return NB_OK;
+        case NB_TUNE_STALL_TEST:
+            if (value != 0 && value != 1) return fail(h, NB_ERR_ARG, "the stall test switch must be 0 or 1");
+            h->stall_test = value;
             return NB_OK;
         case NB_TUNE_RAY_GROUP:
         case NB_TUNE_FUV_GROUP:
@@ -959,6 +974,8 @@ HydroLaunch stage_desc(nb_instance* h, bool stage2) {
     L.n_chunks = (h->d.nx + L.chunk_i - 1) / L.chunk_i;
     L.nstars_host = h->nstars;
     L.order = h->tile_order;
+    L.wait_limit = h->wait_limit;
+    if (h->stall_test) L.maps = nullptr;
     return L;
 }
 

@@ -398,6 +398,7 @@ __device__ __forceinline__ void hydro_tile(const HydroLaunch& L, int tile, unsig
     }
     constexpr unsigned TX_BYTES = 5u * SM::RAW_FIELD * 4u;
     auto issue = [&](int p) {                    // plane p into the raw slot, tracked by bar[0]
+        if (!L.maps) return;                     // failure-path test: the wait for it runs out
         const int pc = iclampd(p, 0, nx - 1);
         fence_proxy_async();                     // the slot's previous contents were read by this block
         mbar_expect_tx(&bar[0], TX_BYTES);
@@ -492,7 +493,7 @@ __device__ __forceinline__ void hydro_tile(const HydroLaunch& L, int tile, unsig
                 u00 = L.u0[0][cell]; u01 = L.u0[1][cell]; u02 = L.u0[2][cell]; u03 = L.u0[3][cell];
             }
         }
-        const bool ok = mbar_wait_bounded(&bar[0], ph0);
+        const bool ok = mbar_wait_limited(&bar[0], ph0, &L.wait_limit);
         if (ok) ph0 ^= 1u;                       // a timed-out wait keeps its parity for the abort wait
         if (__syncthreads_or(!ok)) { failed = true; break; }
         const float* rb = raw;
@@ -689,12 +690,12 @@ __device__ __forceinline__ void hydro_tile(const HydroLaunch& L, int tile, unsig
 
 // a TMA wait gave up: record it, let both slots' copies land (bounded waits), leave
 template <int TJ>
-__device__ __forceinline__ void hydro_abort(unsigned char* smem, unsigned* status, unsigned ph0) {
+__device__ __forceinline__ void hydro_abort(unsigned char* smem, unsigned* status, unsigned ph0, unsigned limit) {
     using SM = HydroSmem<TJ>;
     uint64_t* bar = reinterpret_cast<uint64_t*>(smem + SM::FIXED - SM::BAR_BYTES);
     if (threadIdx.x == 0) {                      // the one load that may still be in flight
         atomicOr(status, NB_DEV_TMA_TIMEOUT);
-        mbar_wait_bounded(&bar[0], ph0);
+        mbar_wait_limited(&bar[0], ph0, &limit);
     }
     __syncthreads();
 }
@@ -722,12 +723,14 @@ __global__ void __launch_bounds__(TK * TJ, NB_HYDRO_MINB) hydro_stage_kernel(con
     unsigned ph0 = 0;
     bool failed = false;
     hydro_tile<SOLVER, LIM, TJ, STAGE2, I32>(L, blockIdx.x, smem, ph0, failed, rot);
-    if (failed) hydro_abort<TJ>(smem, L.status, ph0);
+    if (failed) hydro_abort<TJ>(smem, L.status, ph0, L.wait_limit);
 }
 
 // Persistent batched stage: blocks take (instance, tile) work items from a list spanning many
 // instances of different sizes, in list order, through one atomic counter (reset by the
-// batched control kernel before every step).
+// batched control kernel before every step).  A block whose bounded wait gave up computes nothing
+// more: it keeps taking items and flags the instance of each one it leaves undone, so every
+// instance with an unwritten tile reports NB_DEV_TMA_TIMEOUT.
 #ifndef NB_HYDRO_BATCH_MINB
 #define NB_HYDRO_BATCH_MINB 3            // the persistent kernel's loop state needs the 80-register budget
 #endif
@@ -739,7 +742,7 @@ hydro_batch_kernel(const HydroLaunch* __restrict__ Ls, const int2* __restrict__ 
     __shared__ int item, rot;
     hydro_init_bars<TJ>(smem, &rot);
     unsigned ph0 = 0;
-    bool failed = false;
+    bool failed = false;                         // block-uniform (hydro_tile sets it after a barrier)
     const HydroLaunch* last = nullptr;
     for (;;) {
         if (threadIdx.x == 0) item = (int)atomicAdd(counter, 1u);
@@ -752,7 +755,14 @@ hydro_batch_kernel(const HydroLaunch* __restrict__ Ls, const int2* __restrict__ 
         if (failed) break;
         __syncthreads();
     }
-    if (failed && last) hydro_abort<TJ>(smem, last->status, ph0);
+    if (failed && last) {
+        hydro_abort<TJ>(smem, last->status, ph0, last->wait_limit);
+        // the items this block would still have taken are left undone: flag their instances (the
+        // counter grows by one per turn, so the loop ends)
+        if (threadIdx.x == 0)
+            for (unsigned it; (it = atomicAdd(counter, 1u)) < (unsigned)n_work;)
+                atomicOr(Ls[work[it].x].status, NB_DEV_TMA_TIMEOUT);
+    }
 }
 
 template <int SOLVER, int LIM, int TJ, bool STAGE2, bool I32>

@@ -91,7 +91,9 @@ struct HydroLaunch {
     const NbConst* c;
     const NbState* st;
     const NbStarW* sw;
-    const CUtensorMap* maps;     // device array of NB_NMAPS maps
+    const CUtensorMap* maps;     // device array of NB_NMAPS maps; null: the failure-path test
+                                 // (NB_TUNE_STALL_TEST) -- no tile copy is issued, so the first wait
+                                 // of every tile runs out with nothing in flight
     int map_in;                  // NB_MAP_RHO (stage 1) or NB_MAP_S0 (stage 2)
     const float* in[4];
     const float* u0[4];
@@ -107,6 +109,7 @@ struct HydroLaunch {
     int no_sources;              // stirring-phase hydro: no stars, wind or jets (sim.py:1046)
     int order;                   // tile sweep order (NB_TUNE_TILE_ORDER)
     int idx32;                   // fewer than 2^31 cells: 32-bit cell offsets (single-instance stage)
+    unsigned wait_limit;         // polls of each bounded TMA wait (NB_TUNE_WAIT_LIMIT)
 };
 
 // One instance of a batch, as the batched control kernel sees it.
@@ -179,6 +182,16 @@ __device__ __forceinline__ bool mbar_test(uint64_t* bar, unsigned parity) {
 __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, unsigned parity) {
     for (unsigned n = 0; n < NB_WAIT_LIMIT; ++n)
         if (mbar_test(bar, parity)) return true;
+    return false;
+}
+// The same wait with a lower limit read from memory (a handle's NB_TUNE_WAIT_LIMIT): the limit is
+// read only on the slow path, after each 64 polls that found the phase still open, so a wait that
+// completes at once keeps no register for it.
+__device__ __forceinline__ bool mbar_wait_limited(uint64_t* bar, unsigned parity, const unsigned* limit) {
+    for (unsigned n = 0; n < NB_WAIT_LIMIT; ++n) {
+        if (mbar_test(bar, parity)) return true;
+        if ((n & 63u) == 63u && n + 1u >= *limit) return false;
+    }
     return false;
 }
 __device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }

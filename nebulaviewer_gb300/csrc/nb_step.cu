@@ -230,10 +230,45 @@ static __device__ __align__(256) double g_static_red[NB_STATIC_RED_MAX_BLOCKS * 
 namespace {
 
 #define NB_MAX_DEVICES 64
+// The device address of g_static_red per device, with the ID of the context it was looked up in:
+// an address belongs to one context (a cudaDeviceReset destroys it), so a call made in another
+// context (a different one current on this thread, or the device's primary context re-created
+// after a reset) looks it up again.
+struct StaticSlot {
+    unsigned long long ctx_id;
+    double* ptr;
+};
 std::mutex g_static_mu;
-double* g_static_ptr[NB_MAX_DEVICES];     // device address of g_static_red, per device (set up once)
+StaticSlot g_static_slot[NB_MAX_DEVICES];
 
 thread_local std::string g_static_err;
+
+using CtxGetCurrentFn = CUresult (*)(CUcontext*);
+using CtxGetIdFn = CUresult (*)(CUcontext, unsigned long long*);
+
+// The process-unique ID of the context current on this thread (cuCtxGetId, through the runtime's
+// driver entry points); 0 when no context is current or the driver cannot tell, which makes the
+// caller look the address up again.
+unsigned long long current_ctx_id() {
+    static CtxGetCurrentFn get_cur = nullptr;
+    static CtxGetIdFn get_id = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_cur = reinterpret_cast<CtxGetCurrentFn>(p);
+        p = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_id = reinterpret_cast<CtxGetIdFn>(p);
+    });
+    CUcontext c = nullptr;
+    unsigned long long id = 0;
+    if (!get_cur || !get_id || get_cur(&c) != CUDA_SUCCESS || !c || get_id(c, &id) != CUDA_SUCCESS) return 0;
+    return id;
+}
 
 }  // namespace
 
@@ -255,24 +290,42 @@ extern "C" __attribute__((visibility("default"))) int nb_reduce_fp64_static(cons
     }
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess || dev < 0 || dev >= NB_MAX_DEVICES) {
+    if (e != cudaSuccess) {
         g_static_err = std::string("nb_reduce_fp64_static: cudaGetDevice: ") + cudaGetErrorString(e);
+        return NB_ERR_CUDA;
+    }
+    if (dev < 0 || dev >= NB_MAX_DEVICES) {
+        g_static_err = "nb_reduce_fp64_static: device index " + std::to_string(dev) + " beyond the " +
+                       std::to_string(NB_MAX_DEVICES) + " devices this entry point keeps an address for";
+        return NB_ERR_LIMIT;
+    }
+    // an error left by an earlier call on this thread is the caller's, not this call's: report it
+    // without clearing it, before any work is enqueued
+    e = cudaPeekAtLastError();
+    if (e != cudaSuccess) {
+        g_static_err = std::string("nb_reduce_fp64_static: an earlier CUDA call left an error pending: ") +
+                       cudaGetErrorString(e);
         return NB_ERR_CUDA;
     }
     double* part = nullptr;
     {
-        // set-up, once per device, with that device current: the device address of the array
+        // set-up, once per device and context, with that device current: the device address of the
+        // array (the lookup itself makes the device's primary context current if none was)
         std::lock_guard<std::mutex> lock(g_static_mu);
-        if (!g_static_ptr[dev]) {
+        StaticSlot& slot = g_static_slot[dev];
+        const unsigned long long id = current_ctx_id();
+        if (!slot.ptr || id == 0 || slot.ctx_id != id) {
             void* p = nullptr;
             e = cudaGetSymbolAddress(&p, g_static_red);
             if (e != cudaSuccess || !p) {
+                slot.ptr = nullptr;
                 g_static_err = std::string("nb_reduce_fp64_static: cudaGetSymbolAddress: ") + cudaGetErrorString(e);
                 return NB_ERR_CUDA;
             }
-            g_static_ptr[dev] = static_cast<double*>(p);
+            slot.ptr = static_cast<double*>(p);
+            slot.ctx_id = current_ctx_id();
         }
-        part = g_static_ptr[dev];
+        part = slot.ptr;
     }
     const int blocks = (int)((n + NB_STATIC_RED_CELLS_PER_BLOCK - 1) / NB_STATIC_RED_CELLS_PER_BLOCK);
     cudaStream_t s = static_cast<cudaStream_t>(stream);

@@ -34,6 +34,7 @@ from . import stir as _stir
 from .params import LIVE, make_params, sound_speeds
 
 DRIVE_SLOTS = 16          # forcing fields the device ring holds
+REFERENCE_PRESETS = ("bipolar", "bubbles", "cliff")      # sim.py:50-59 PRESETS
 DRIVE_LOOKAHEAD = 2       # fields pushed beyond B before a chunk of stirred steps
 
 
@@ -145,9 +146,79 @@ class Sim:
         self._setup(ic, dict(P), start_main=start_main)
         return self
 
+    @classmethod
+    def from_reference(cls, ref, params=None, arith=None, device="cuda:0", verbose=False):
+        """The drop-in taking over a reference `Sim` instance (sim.py:543-1222) as it stands: one
+        built by the reference's own reset() from its presets and initial conditions
+        (sim.py:50-59, 591-795), in the stirring phase or the main phase.  It copies the fields
+        (rho, mx, my, mz, xi, dfront, g0), the star and jet lists, the parameters P, the ray / FUV
+        budgets, the cadences, the clocks, the live-event log, the render-field bookkeeping and
+        the stirring state (fields A and B, the cross-fade clock, the forcing generator: the
+        Generator state, or the matched spectrum's seed and call count, sim.py:270-337), so that
+        stepping the drop-in continues the reference's run.
+
+        The reference package is never imported: `ref` is read through its attributes and
+        get_state_meta() alone, and every field through .numpy() (a Warp array, a NumPy array or
+        anything with that method).  `params` overrides entries of P, e.g. {"trigger": 0.0} as
+        bake.py sets it after construction (bake.py:61-63); triggered star formation and cropped
+        domains are outside this package and are refused."""
+        def host(x):
+            return np.asarray(x.numpy() if hasattr(x, "numpy") else x)
+
+        P = dict(ref.P)
+        P.update(params or {})
+        meta = dict(ref.get_state_meta())
+        meta["P"] = dict(P)
+        d = meta.get("drv")
+        if d is not None:
+            meta["drv"] = {"A": [host(c) for c in d["A"]], "B": [host(c) for c in d["B"]], "clock": float(d["clock"])}
+        noise = getattr(ref, "noise", None)
+        if noise is not None and not hasattr(noise, "seed"):
+            raise NotImplementedError("the reference's noise generator is not the matched one (a cropped domain?)")
+        noise = None if noise is None else {"seed": int(noise.seed), "calls": int(noise.calls),
+                                            "modes": int(getattr(noise, "K", _stir.MATCHED_MODES))}
+        torus0 = getattr(ref, "torus0", None)
+        self = cls.__new__(cls)
+        self.arith = _lib.arith_of(arith)
+        self.device = torch.device(device)
+        self.fast = bool(ref.fast)
+        self.verbose = verbose
+        self.ic_mode = getattr(ref, "ic_mode", "matched")
+        self.rays_override = tuple(int(v) for v in ref.rfront.shape)
+        self.fuv_override = tuple(int(v) for v in ref.att.shape)
+        self.ion_every_override = int(ref.ion_every)
+        self.prof = {}
+        self._h = None
+        self.scenario = getattr(ref, "scenario", "reference")
+        self.res = getattr(ref, "res", None)
+        ic = dict(shape=tuple(int(v) for v in ref.shape), dx=float(ref.dx), rho=host(ref.rho),
+                  mom=[host(ref.mx), host(ref.my), host(ref.mz)], stars=ref.stars, kinds=ref.kinds, jets=ref.jets,
+                  jkinds=ref.jkinds, P={}, torus=host(torus0) if (torus0 is not None and ref.phase == "pre") else None,
+                  stir_grid=(tuple(int(v) for v in ref.sshape), float(ref.dxs)), noise=noise)
+        self._setup(ic, P, start_main=False)
+        if torus0 is not None:
+            self.torus0 = torch.as_tensor(host(torus0), dtype=torch.float32, device=self.device)
+        self._xi.copy_(torch.as_tensor(host(ref.xi)).to(self._xi.dtype))
+        self._dfront.copy_(torch.as_tensor(host(ref.dfront)).to(self._dfront.dtype))
+        self._g0.copy_(torch.as_tensor(host(ref.g0)).to(self._g0.dtype))
+        self.events = [tuple(e) for e in ref.events]
+        self.set_state_meta(meta)
+        # the render-field bookkeeping continues the reference's cadence (sim.py:989-1007)
+        for k in ("version", "rf_version", "fuv_version"):
+            setattr(self, k, int(getattr(ref, k)))
+        self.fuv_nstars = getattr(ref, "fuv_nstars", -1)
+        self.fuv_phase = getattr(ref, "fuv_phase", None)
+        self.dt_cap = getattr(ref, "dt_cap", None)
+        self._sync()
+        return self
+
     def reset(self, scenario=None, res=None, params=None, seed=None):
         if scenario is not None:
             self.scenario = scenario
+        if self.scenario in REFERENCE_PRESETS:
+            raise ValueError(f"{self.scenario!r} is one of the reference's preset scenes, whose initial conditions the "
+                             f"reference's own reset() builds (sim.py:591-795): build the reference Sim and hand it "
+                             f"over with Sim.from_reference(ref_sim); synthetic scenarios: {sorted(_ics.SCENARIOS)}")
         if self.scenario not in _ics.SCENARIOS:
             raise ValueError(f"unknown scenario {self.scenario!r}; synthetic scenarios: {sorted(_ics.SCENARIOS)}")
         gen = _ics.SCENARIOS[self.scenario]
@@ -271,6 +342,11 @@ class Sim:
         self.q_main0 = P["q_main"]
         # stirring (sim.py:760-768, 786-790): the forcing grid, the Generator, the ring
         self.rng = np.random.default_rng(P["seed"])
+        # the reference's "matched" mode draws forcing fields from a per-call seeded spectrum
+        # (sim.py:648, 802) instead of the Generator: {"seed", "calls", "modes"}, or None
+        nz_ = ic.get("noise")
+        self.noise = None if nz_ is None else {"seed": int(nz_["seed"]), "calls": int(nz_["calls"]),
+                                               "modes": int(nz_.get("modes", _stir.MATCHED_MODES))}
         src = ic.get("stir_fields")
         self._stir_src = None if src is None else collections.deque(np.asarray(f, np.float32) for f in src)
         grid = ic.get("stir_grid")
@@ -560,8 +636,25 @@ class Sim:
             if not self._stir_src:
                 raise _lib.NebulaError("the given forcing fields are used up")
             return np.ascontiguousarray(self._stir_src.popleft(), np.float32)
-        return np.ascontiguousarray(np.stack(_stir.solenoidal(self.sshape, self.rng, 1.0,
-                                                              float(self.P["pre_kmax"]))), np.float32)
+        kmax = float(self.P["pre_kmax"])
+        if self.noise is not None:
+            c = self.noise["calls"]
+            self.noise["calls"] = c + 3                      # one call per component (sim.py:330)
+            return np.ascontiguousarray(np.stack(_stir.matched_solenoidal(self.sshape, self.noise["seed"], c, 1.0, kmax,
+                                                                          self.noise["modes"])), np.float32)
+        return np.ascontiguousarray(np.stack(_stir.solenoidal(self.sshape, self.rng, 1.0, kmax)), np.float32)
+
+    def _gen_state(self):
+        """the forcing generator's state: the Generator's, or the matched spectrum's call count"""
+        if self.noise is not None:
+            return ("calls", self.noise["calls"])
+        return copy.deepcopy(self.rng.bit_generator.state)
+
+    def _gen_restore(self, st):
+        if self.noise is not None:
+            self.noise["calls"] = int(st[1])
+        else:
+            self.rng.bit_generator.state = st
 
     def _drive_make(self, upto):
         """draw forcing fields on the host until `upto` exist since the ring reset (a given, finite
@@ -569,7 +662,7 @@ class Sim:
         while len(self._forcing) < upto:
             if self._stir_src is not None and not self._stir_src:
                 break
-            st = copy.deepcopy(self.rng.bit_generator.state)
+            st = self._gen_state()
             self._forcing.append((self._mkF(), st))
 
     def _push_forcing(self, buf):
@@ -618,7 +711,7 @@ class Sim:
             if self._stir_src is not None:
                 self._stir_src.extendleft(f for f, _ in reversed(extra))
             elif extra[0][1] is not None:
-                self.rng.bit_generator.state = extra[0][1]
+                self._gen_restore(extra[0][1])
         self._forcing = self._forcing[:used]
         self._pushed = min(self._pushed, used)
 
@@ -701,17 +794,20 @@ class Sim:
         """sim.py:1173-1183: everything but the big fields needed to resume from this moment.
         The Generator state is the one after the fields in use (A and B), as the reference's."""
         c = self._clock()
-        drv, rng = None, copy.deepcopy(self.rng.bit_generator.state)
+        drv, gen = None, self._gen_state()
         if self._drv_on:
             info = self._drive_info()
             sw = int(info.swaps)
             drv = {"A": list(self._forcing[sw][0]), "B": list(self._forcing[sw + 1][0]), "clock": float(info.clock)}
             if sw + 2 < len(self._forcing) and self._forcing[sw + 2][1] is not None:
-                rng = copy.deepcopy(self._forcing[sw + 2][1])
+                gen = copy.deepcopy(self._forcing[sw + 2][1])
+        matched = self.noise is not None
+        rng = copy.deepcopy(self.rng.bit_generator.state) if matched else gen
         return dict(t=c.t, it=int(c.it), tp=c.tp, ip=int(c.ip), dt=c.dt, phase=self.phase, mach=self.mach,
                     stars=list(self.stars), kinds=list(self.kinds), jets=list(self.jets), jkinds=list(self.jkinds),
                     births=list(self.births), n_born=self.n_born, last_birth=self.last_birth, P=dict(self.P),
-                    n_events=len(self.events), sm0=self.sm0, drv=drv, rng=rng, noise_calls=0)
+                    n_events=len(self.events), sm0=self.sm0, drv=drv, rng=rng,
+                    noise_calls=int(gen[1]) if matched else 0)
 
     def set_state_meta(self, m):
         """sim.py:1185-1211: after the fields were restored"""
@@ -731,6 +827,8 @@ class Sim:
             self._drive_new(d["clock"], fields=[np.stack(d["A"]), np.stack(d["B"])])
         if m.get("rng") is not None:
             self.rng.bit_generator.state = copy.deepcopy(m["rng"])
+        if self.noise is not None:
+            self.noise["calls"] = int(m.get("noise_calls", 0))                       # sim.py:1198-1199
         self.torus = self.torus0 if self.phase == "pre" else None
         self._chk(self._lib.nb_invalidate(self._h), "nb_invalidate")
         self._push(force=True)

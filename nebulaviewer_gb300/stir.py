@@ -45,3 +45,47 @@ def solenoidal(shape, rng, kmin=1.0, kmax=6.0):
     comps = [np.fft.ifftn(c).real for c in coef]
     rms = np.sqrt(sum((v * v).mean() for v in comps))
     return [np.ascontiguousarray(v / rms, dtype=np.float32) for v in comps]
+
+
+MATCHED_MODES = 32                   # sim.py:276: the matched spectrum covers |m| <= 32
+
+
+def _matched_coefficients(shape, seed, call, modes):
+    """Complex Gaussian coefficients on the full FFT grid of `shape` whose low modes |m| <= modes
+    come from a master spectrum that depends only on (seed, call) -- so every grid size gets the
+    same large-scale coefficients -- and whose other modes depend on the grid size as well
+    (sim.py:282-304 for a grid without a half-spectrum axis).  Draw order: the master real
+    parts then imaginary parts on a (2 modes + 1)^3 grid from a Generator seeded with
+    [seed, 7919, call]; then the grid's own real and imaginary parts from one seeded with
+    [seed, 104729, call, *shape]; the master values replace the grid's at the matched modes."""
+    side = 2 * modes + 1
+    g = np.random.default_rng([seed, 7919, call])
+    master = g.standard_normal((side,) * len(shape)) + 1j * g.standard_normal((side,) * len(shape))
+    g = np.random.default_rng([seed, 104729, call, *shape])
+    out = g.standard_normal(shape) + 1j * g.standard_normal(shape)
+    grid_ix, master_ix = [], []
+    for n in shape:
+        top = min(modes, (n - 1) // 2)
+        m = np.arange(-top, top + 1)
+        grid_ix.append(m % n)
+        master_ix.append(m % side)
+    out[np.ix_(*grid_ix)] = master[np.ix_(*master_ix)]
+    return out
+
+
+def matched_solenoidal(shape, seed, calls, kmin=1.0, kmax=6.0, modes=MATCHED_MODES):
+    """The forcing field the reference draws in its default "matched" initial-condition mode
+    (sim.py:327-337 MatchedNoise.solenoidal, used by sim.py:801-804): the construction of
+    `solenoidal` with each component's coefficients taken from _matched_coefficients instead of
+    the Generator.  `calls` is the generator's call count before this field; the field uses the
+    next three (one per component).  Returns the three float32 components, bit-identical to the
+    reference's for the same seed, count and shape."""
+    waves = np.meshgrid(*[np.fft.fftfreq(n) * n for n in shape], indexing="ij")
+    kmag = np.sqrt(sum(w * w for w in waves))
+    weight = np.where((kmag >= kmin) & (kmag <= kmax), 1.0 / np.maximum(kmag, 1e-6), 0.0)
+    coef = [weight * _matched_coefficients(shape, seed, calls + 1 + c, modes) for c in range(3)]
+    along = sum(w * c for w, c in zip(waves, coef)) / np.maximum(kmag * kmag, 1e-12)
+    coef = [c - w * along for w, c in zip(waves, coef)]
+    comps = [np.fft.ifftn(c).real for c in coef]
+    rms = np.sqrt(sum((v * v).mean() for v in comps))
+    return [np.ascontiguousarray(v / rms, dtype=np.float32) for v in comps]

@@ -1,7 +1,9 @@
 """Generate the golden fixtures under tests/golden/ by running the REFERENCE's own
 kernel source and its `Sim` driver on small seeded inputs.
 
-    python tests/golden/make_golden.py [--ref /root/reference]
+    python tests/golden/make_golden.py --ref <reference checkout>
+
+(or set NEBULA_REFERENCE to the checkout instead of passing --ref)
 
 The reference is NVIDIA-Warp Python; `warp` is absent here, so `warp_stub` supplies
 a float32 restatement of the Warp builtins its kernels call (see that module's
@@ -22,6 +24,9 @@ Fixtures (all small, committed):
   sim_bipolar_pre.npz  a reference `Sim` run through the pre-turbulence (stirring) phase,
                    its end (torus added, first ionization) and main-phase stirring, with
                    every forcing field the run drew.
+  bake_bipolar.npz bake.py's loop run by the reference on a bipolar scene in the default
+                   matched mode (stirring phase, replace_stars, live events, dt_cap, frames),
+                   with the reference Sim as constructed (what Sim.from_reference reads).
 Test infrastructure only: nothing in the product reads these files.
 """
 import argparse
@@ -321,6 +326,99 @@ def sim_pre_case(S, scenario, res, overrides, nsteps, rays, fuv, ic_mode):
     return out
 
 
+# ----------------------------------------------------------------------------- bake.py's loop
+def _json_safe(v):
+    if isinstance(v, dict):
+        return {k: _json_safe(x) for k, x in v.items()}
+    if isinstance(v, (list, tuple)):
+        return [_json_safe(x) for x in v]
+    if isinstance(v, (np.floating, np.integer)):
+        return v.item()
+    return v
+
+
+def ref_state(sim):
+    """everything Sim.from_reference reads from a reference Sim: arrays apart, the rest as JSON"""
+    meta = sim.get_state_meta()
+    d = meta.pop("drv")
+    arrays = {"rho": sim.rho.numpy(), "mx": sim.mx.numpy(), "my": sim.my.numpy(), "mz": sim.mz.numpy(),
+              "xi": sim.xi.numpy(), "dfront": sim.dfront.numpy(), "g0": sim.g0.numpy()}
+    if sim.torus0 is not None:
+        arrays["torus0"] = np.asarray(sim.torus0, np.float32)
+    if d is not None:
+        arrays["drv_A"] = np.stack([c.numpy() for c in d["A"]])
+        arrays["drv_B"] = np.stack([c.numpy() for c in d["B"]])
+    attrs = dict(scenario=sim.scenario, res=sim.res, shape=list(sim.shape), dx=sim.dx, fast=sim.fast,
+                 ic_mode=sim.ic_mode, phase=sim.phase, rfront_shape=list(sim.rfront.shape),
+                 att_shape=list(sim.att.shape), ion_every=sim.ion_every, fuv_every=sim.fuv_every,
+                 sshape=list(sim.sshape), dxs=sim.dxs, stars=[list(map(float, x)) for x in sim.stars],
+                 kinds=list(sim.kinds), jets=[list(map(float, j)) for j in sim.jets], jkinds=list(sim.jkinds),
+                 P=dict(sim.P), events=[list(e) for e in sim.events], version=sim.version,
+                 rf_version=sim.rf_version, fuv_version=sim.fuv_version,
+                 fuv_nstars=getattr(sim, "fuv_nstars", -1), fuv_phase=getattr(sim, "fuv_phase", None),
+                 dt_cap=sim.dt_cap,
+                 noise=None if sim.noise is None else dict(seed=sim.noise.seed, calls=sim.noise.calls, K=sim.noise.K),
+                 drv_clock=None if d is None else d["clock"], meta=meta)
+    return arrays, _json_safe(attrs)
+
+
+def bake_case(S, res=8):
+    """bake.py:59-114 run by the reference on a small bipolar scene: Sim(..., fast=False) in the
+    default matched mode (forcing fields from the matched spectrum) with a short stirring phase;
+    the stirring steps; replace_stars with the preview's list plus a later birth; the live events
+    replayed into P at their times; at each frame time update_render_fields(force=True) and the
+    frame expressions of bake.py:95-102; dt_cap landing the steps on the frame times.  Saves the
+    reference Sim as constructed (what Sim.from_reference reads) and every frame."""
+    P = S.make_params("bipolar", dict(pre_t=0.49, pre_corr=0.02, pre_amp=7.0, seed=21, jet_r=0.35, jet_angle=35.0,
+                                      clumps=0))
+    t_end, frames = 0.12, 4
+    sim = S.Sim("bipolar", res=res, params=P, ic_mode="matched", rays=(8, 16), fuv_grid=(6, 8, 16), fast=False,
+                device="cpu", verbose=False)
+    arrays, attrs = ref_state(sim)
+    print(f"  bipolar {sim.shape} phase {sim.phase}, {len(sim.stars)} stars, noise calls {sim.noise.calls}", flush=True)
+    sim.P["trigger"] = 0.0                                                    # bake.py:61-63
+    while sim.phase == "pre":                                                 # bake.py:67-68
+        sim.step(1)
+    pre_steps = sim.ip
+    stars = [list(map(float, x)) for x in sim.stars]
+    L = sim.L
+    stars.append([0.55 * L[0], 0.45 * L[1], 0.5 * L[2], 2.0e-4, 0.03])          # a later birth, absolute Q
+    kinds = list(sim.kinds) + ["abs"]
+    jets = [list(map(float, j)) for j in sim.jets] + [[0.0, 0.6, 0.8]]
+    jkinds = list(sim.jkinds) + ["proto"]
+    sim.replace_stars(stars, kinds, jets, jkinds)                             # bake.py:69
+    events = [[0.02, "wind", 0.6], [0.05, "q_main", float(P["q_main"]) * 1.5], [0.08, "jet", 2.0]]
+    out = {f"s_{k}": v for k, v in arrays.items()}
+    dt_frame = t_end / max(frames - 1, 1)
+    next_frame, frame, ev_i, times = 0.0, 0, 0, []
+    while True:                                                               # bake.py:87-114
+        while ev_i < len(events) and events[ev_i][0] <= sim.t + 1e-12:
+            _, name, val = events[ev_i]
+            sim.P[name] = val
+            sim._wkey = None
+            ev_i += 1
+        if sim.t >= next_frame - 1e-9:
+            sim.update_render_fields(force=True)
+            out[f"f{frame}_g0"] = np.minimum(sim.g0.numpy(), 6e4).astype(np.float16)
+            out[f"f{frame}_rho"] = sim.rho.numpy().astype(np.float16)
+            out[f"f{frame}_xi"] = np.round(np.clip(sim.xi.numpy(), 0, 1) * 255).astype(np.uint8)
+            out[f"f{frame}_df"] = np.clip(sim.dfront.numpy(), -4, 4).astype(np.float16)
+            out[f"f{frame}_sh"] = np.minimum(sim.shock.numpy(), 6e4).astype(np.float16)
+            times.append(sim.t)
+            print(f"    frame {frame} t={sim.t:.5f} step {sim.it}", flush=True)
+            frame += 1
+            next_frame += dt_frame
+            if frame >= frames:
+                break
+        sim.dt_cap = next_frame - sim.t + 1e-7
+        sim.step(1)
+    attrs["bake"] = dict(t_end=t_end, frames=frames, stars=stars, kinds=kinds, jets=jets, jkinds=jkinds, events=events,
+                         times=times, steps=sim.it, pre_steps=pre_steps, mach=sim.mach)
+    out["meta"] = np.array(json.dumps(_json_safe(attrs)))
+    print(f"  bake: {pre_steps} stirring steps, {sim.it} main steps, {frame} frames", flush=True)
+    return out
+
+
 # ----------------------------------------------------------------------------- renderer pack
 def render_cases(ref, rng):
     """render.py:176-205 pack_volume_lm (RGBA16F voxel: emission rgb + dust, shock proxy inline,
@@ -363,9 +461,12 @@ def render_cases(ref, rng):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=os.environ.get("NEBULA_REFERENCE"),
+                    help="the reference checkout (default: $NEBULA_REFERENCE)")
     ap.add_argument("--only", default=None)
     a = ap.parse_args()
+    if not a.ref:
+        ap.error("give the reference checkout with --ref or NEBULA_REFERENCE")
     N, S = import_reference(a.ref)
     rng = np.random.default_rng(20261203)
     if a.only in (None, "kernels"):
@@ -383,6 +484,9 @@ def main():
                                                             seed=13, jet_r=0.35, jet_angle=35.0, clumps=0),
                  nsteps=14, rays=(8, 16), fuv=(6, 8, 16), ic_mode="nebula3d")   # 6-cell forcing grid
         np.savez_compressed(os.path.join(HERE, "sim_bipolar_pre.npz"), **sim_pre_case(S, **c))
+    if a.only in (None, "bake"):
+        print("bake:", flush=True)
+        np.savez_compressed(os.path.join(HERE, "bake_bipolar.npz"), **bake_case(S))
     if a.only in (None, "timeline"):
         print("timeline:", flush=True)
         np.savez_compressed(os.path.join(HERE, "timeline.npz"), **timeline_cases(a.ref, np.random.default_rng(99)))

@@ -29,10 +29,10 @@ def test_static_totals_match_handle_totals_twice():
     from nebulaviewer_gb300.sim import Sim
     assert torch.cuda.is_available()
     stream = torch.cuda.current_stream()
-    # 1.97 M cells = 30 full blocks of 65536 cells and a partial one
-    shape = (160, 128, 96)
-    n = int(np.prod(shape))
-    for seed in (11, 12):                                     # two calls in a row, different inputs
+    # two calls in a row per shape, different inputs: 161 x 128 x 96 = 1,978,368 cells = 30 full
+    # blocks of 65536 cells and a partial one of 12,288; 7 x 9 x 12 = 756 cells, one partial block
+    for shape, seed in (((161, 128, 96), 11), ((161, 128, 96), 12), ((7, 9, 12), 13), ((7, 9, 12), 14)):
+        n = int(np.prod(shape))
         g = torch.Generator(device="cuda").manual_seed(seed)
         rho = torch.rand(shape, device="cuda", generator=g) * 10 + 0.01
         mom = [torch.randn(shape, device="cuda", generator=g) for _ in range(3)]
