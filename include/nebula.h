@@ -131,6 +131,13 @@ typedef struct nb_clock {
 int nb_create(const nb_desc* desc, nb_handle* out);
 /* Releases library scratch and graphs (never the caller's fields). */
 void nb_destroy(nb_handle h);
+/* No reference counterpart (the reference allocates through Warp and charges 40 B/cell of fields,
+ * sim.py:79-87): the device bytes the library holds for an instance -- control blocks, tensor
+ * maps, ray directions, the ray-front and FUV tables sized for the star table, the reduction and
+ * culling scratch, the stirring ring -- beyond the caller's fields.  With h: what h holds now.
+ * Without (h = NULL): what nb_create(d) followed by nb_set_stars(nstars) will allocate, for an
+ * admission decision made before any allocation. */
+int nb_instance_bytes(nb_handle h, const nb_desc* d, int nstars, long long* out);
 const char* nb_last_error(nb_handle h);
 int nb_device_status(nb_handle h, int* status);     /* bounded-wait failures seen on device */
 
@@ -244,6 +251,12 @@ typedef struct nb_batch_s* nb_batch;
 enum { NB_BATCH_GRAPHS = 0, NB_BATCH_GRID = 1, NB_BATCH_RAY_GROUP = 2 };
 int nb_batch_create(const nb_handle* instances, const int* ion_every, int n, nb_batch* out);
 int nb_batch_step(nb_batch b, int k);
+/* Slots of a batch (no reference counterpart; a server keeps a pool of instances in one batch): n
+ * flags, one per instance in nb_batch_create's order; an idle slot (0) is not stepped -- no weights,
+ * clock, rays or tiles -- and is left as it is, so instances can join and leave the stepping set
+ * without rebuilding the batch or its graphs.  All slots start active.  Synchronizes the batch's
+ * stream. */
+int nb_batch_set_active(nb_batch b, const int* active, int n);
 int nb_batch_set_option(nb_batch b, int key, int value);
 int nb_batch_counters(nb_batch b, long long* launches);
 void nb_batch_destroy(nb_batch b);
@@ -317,9 +330,16 @@ int nb_profile_read(nb_handle h, double ms[NB_PROF_KINDS], long long count[NB_PR
  * issue no tile copy at all, so the first wait of every tile runs out with nothing in flight: the
  * stage records NB_DEV_TMA_TIMEOUT, writes nothing and returns, and every later clock read returns
  * NB_ERR_TIMEOUT.  The handle's fields are then incomplete for good (destroy it).  A batch takes
- * both from its instances when it is created. */
+ * both from its instances when it is created.
+ * NB_TUNE_FRONT_PAIRS (default 0) and NB_TUNE_FUV_PAIRS (default 1): the ray-front table (fronts,
+ * nebula3d.py:273-307) or the FUV attenuation table (nebula3d.py:355-388) holds each entry with its
+ * next neighbour along u (fronts) or r (attenuation) as one float2 pair, so the bilinear or
+ * trilinear lookup makes half as many gathers, for twice the table bytes and a second write per
+ * entry in the ray kernel; 0 keeps one float per entry.  The result is the same either way, bit for
+ * bit.  A batch takes the front layout from its instances when it is created. */
 enum { NB_TUNE_CHUNK_I = 0, NB_TUNE_RAY_GROUP = 1, NB_TUNE_FUV_GROUP = 2, NB_TUNE_TILE_ORDER = 3,
-       NB_TUNE_FRONT_CULL = 4, NB_TUNE_FUV_CUT = 5, NB_TUNE_WAIT_LIMIT = 6, NB_TUNE_STALL_TEST = 7 };
+       NB_TUNE_FRONT_CULL = 4, NB_TUNE_FUV_CUT = 5, NB_TUNE_WAIT_LIMIT = 6, NB_TUNE_STALL_TEST = 7,
+       NB_TUNE_FRONT_PAIRS = 8, NB_TUNE_FUV_PAIRS = 9 };
 int nb_set_tuning(nb_handle h, int key, int value);
 int nb_get_tuning(nb_handle h, int key, int* value);
 /* Number of kernels the handle has launched (a claim the benchmark reports). */

@@ -80,6 +80,7 @@ _F4 = C.c_void_p * 4
 SIGNATURES = {
     "nb_create": (C.c_int, [C.POINTER(NbDesc), C.POINTER(_P)]),
     "nb_destroy": (None, [_P]),
+    "nb_instance_bytes": (C.c_int, [_P, C.POINTER(NbDesc), C.c_int, C.POINTER(C.c_longlong)]),
     "nb_last_error": (C.c_char_p, [_P]),
     "nb_device_status": (C.c_int, [_P, C.POINTER(C.c_int)]),
     "nb_set_live": (C.c_int, [_P, C.POINTER(NbLive)]),
@@ -120,12 +121,13 @@ SIGNATURES = {
     "nb_batch_set_option": (C.c_int, [_P, C.c_int, C.c_int]),
     "nb_batch_counters": (C.c_int, [_P, C.POINTER(C.c_longlong)]),
     "nb_batch_destroy": (None, [_P]),
+    "nb_batch_set_active": (C.c_int, [_P, C.POINTER(C.c_int), C.c_int]),
     "nb_batch_last_error": (C.c_char_p, [_P]),
     "nb_reduce_fp64_static": (C.c_int, [_P, _P, _P, _P, C.c_longlong, _P, _P]),
     "nb_static_last_error": (C.c_char_p, []),
 }
 TUNE = {"chunk_i": 0, "ray_group": 1, "fuv_group": 2, "tile_order": 3, "front_cull": 4, "fuv_cut": 5,
-        "wait_limit": 6, "stall_test": 7}
+        "wait_limit": 6, "stall_test": 7, "front_pairs": 8, "fuv_pairs": 9}
 PROF_KINDS = ["ctrl", "stage1", "stage2", "cast_rays", "apply_front", "smooth", "cast_fuv", "apply_fuv", "max_speed",
               "snapshot", "drive", "render"]
 

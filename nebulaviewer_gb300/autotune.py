@@ -1,8 +1,10 @@
 """A launch-shape autotuner for one simulation instance.
 
 Knobs (nb_set_tuning): the tile depth along i of the hydro march (`chunk_i`: the tile shape of
-the persistent 2.5-D sweep), the tile sweep order (`tile_order`), and the lanes per ray of the
-ionizing and FUV ray kernels (`ray_group`, `fuv_group`).  Each knob is tuned in turn
+the persistent 2.5-D sweep), the tile sweep order (`tile_order`), the lanes per ray of the
+ionizing and FUV ray kernels (`ray_group`, `fuv_group`), and the layouts of the ray-front and FUV
+attenuation tables (`front_pairs`, `fuv_pairs`: neighbour pairs or single entries; the same bits
+either way).  Each knob is tuned in turn
 (coordinate descent) on the instance's own state: the state and clock are saved, every
 candidate runs a few steps (or FUV passes) timed by the library's per-kernel CUDA events, the
 state is restored, and the fastest candidate is kept.  The hydro result never depends on these
@@ -17,10 +19,13 @@ CANDIDATES = {
     "tile_order": (0, 1),
     "ray_group": (2, 4, 8, 16),
     "fuv_group": (8, 16, 32),
+    "front_pairs": (0, 1),
+    "fuv_pairs": (0, 1),
 }
 # which kernel kinds a knob moves (names of _lib.PROF_KINDS)
 AFFECTS = {"chunk_i": ("stage1", "stage2"), "tile_order": ("stage1", "stage2"), "ray_group": ("cast_rays",),
-           "fuv_group": ("cast_fuv",)}
+           "fuv_group": ("cast_fuv",), "front_pairs": ("cast_rays", "apply_front"),
+           "fuv_pairs": ("cast_fuv", "apply_fuv")}
 
 _CACHE = {}
 
@@ -46,10 +51,10 @@ def _measure(sim, knob, steps):
     n = (C.c_longlong * 16)()
     lib.nb_profile(sim._h, 1)
     lib.nb_profile_read(sim._h, ms, n)
-    if knob == "fuv_group":
+    if knob in ("fuv_group", "fuv_pairs"):
         for _ in range(steps):
             sim.fuv_field()
-    elif knob == "ray_group":
+    elif knob in ("ray_group", "front_pairs"):
         for _ in range(steps):
             sim.ionize()
     else:
@@ -57,12 +62,12 @@ def _measure(sim, knob, steps):
     lib.nb_profile_read(sim._h, ms, n)
     lib.nb_profile(sim._h, 0)
     idx = [_lib.PROF_KINDS.index(k) for k in AFFECTS[knob]]
-    return sum(ms[i] for i in idx) / max(1, max(n[i] for i in idx))
+    return sum(ms[i] for i in idx) / steps
 
 
 def autotune(sim, knobs=None, steps=4, use_cache=True):
     """pick the fastest launch shapes for `sim` (its state and clock are left unchanged);
-    returns {knob: (value, ms per launch)}"""
+    returns {knob: (value, ms per step or pass of the kernels it moves)}"""
     key = _key(sim)
     if use_cache and key in _CACHE:
         for k, (v, _) in _CACHE[key].items():

@@ -24,8 +24,8 @@ struct nb_instance {
     CUtensorMap* tmp_maps = nullptr;    // maps for nb_hydro_stage on foreign planes
     float4* dirs = nullptr;             // ionizing-ray directions (nu * nphi)
     float4* dirs_fuv = nullptr;         // FUV-ray directions (fnu * fnphi)
-    float* rfront = nullptr;            // [star][nu][nphi]
-    float* att = nullptr;               // [star][fnu][fnphi][fnr]
+    float* rfront = nullptr;            // [star][nphi][nu] (float2 (u, u + 1) pairs with front_pairs)
+    float* att = nullptr;               // [star][fnu][fnphi][fnr] (float2 (r, r + 1) pairs with fuv_pairs)
     float* scratch3 = nullptr;          // 3 floats: a single star position for the one-star kernels
     float* plane_xf = nullptr;          // [ny][nz] front of the -x plane source
     double* red = nullptr;              // FP64 reduction partials
@@ -42,6 +42,8 @@ struct nb_instance {
     int fuv_cut = 1;                    // FUV rays stop where exp(-tau) has reached 0.0f
     unsigned wait_limit = NB_WAIT_LIMIT; // polls of each bounded TMA wait in the hydro stages
     int stall_test = 0;                 // failure-path test: the hydro stages issue no tile copies
+    int front_pairs = 0;                // ray-front table as float2 (u, u + 1) pairs (measured: no gain at 256^3)
+    int fuv_pairs = 1;                  // FUV attenuation table as float2 (r, r + 1) pairs
     long long ncell = 0;
     long long launches = 0;             // kernels this handle launched (nb_counters)
     int profiling = 0;                  // CUDA-event timing per kernel kind (nb_profile)
@@ -193,7 +195,7 @@ int do_ionize(nb_instance* h) {
     if (h->nstars > 0) {
         Prof pf(h, NB_PROF_CAST_RAYS, 1);
         CK(h, nb_launch_cast_rays(h->c, h->sw, h->dirs, f.rho, h->rfront, h->nstars, h->ray_group, nullptr, 0.0f,
-                                  h->stream, h->d.nu, h->d.nphi));
+                                  h->stream, h->d.nu, h->d.nphi, h->front_pairs));
     }
     if (h->hc.plane_on) {
         Prof pf(h, NB_PROF_CAST_RAYS, 1);
@@ -206,7 +208,7 @@ int do_ionize(nb_instance* h) {
         CK(h, nb_launch_apply_front(h->c, h->sw, h->rfront, h->nstars, xi_raw, f.dfront, &h->st->smax_bits,
                                     h->stream, h->d.nx, h->d.ny, h->d.fields_fp32 ? 0 : 1,
                                     cull ? h->front_parts : nullptr,
-                                    (long long)h->d.nu * h->d.nphi));
+                                    (long long)h->d.nu * h->d.nphi, h->front_pairs));
     }
     {
         Prof pf(h, NB_PROF_SMOOTH, 1);
@@ -388,6 +390,34 @@ NB_EXPORT int nb_create(const nb_desc* d, nb_handle* out) {
     return NB_OK;
 }
 
+// Device bytes an instance of `d` holds with a star table for `star_alloc` stars and a stirring ring
+// of `ring_bytes`: the allocations of nb_create, nb_set_stars and nb_drive_config (not the caller's
+// fields).  One formula for the estimate and for the live count, so they agree by construction.
+static long long instance_bytes(const nb_desc& d, long long star_alloc, long long ring_bytes) {
+    const long long ncell_plane = (long long)d.ny * d.nz;
+    long long b = 0;
+    b += sizeof(NbConst) + sizeof(NbState);
+    b += (long long)(sizeof(NbStarDev) + sizeof(NbStarW)) * d.max_stars;
+    b += 2LL * sizeof(CUtensorMap) * NB_NMAPS;
+    b += (long long)sizeof(float4) * ((long long)d.nu * d.nphi + (long long)d.fnu * d.fnphi);
+    b += 4 * sizeof(float) + sizeof(float) * ncell_plane;
+    b += (long long)sizeof(double) * nb_reduce_scratch_doubles();
+    b += (long long)sizeof(float2) * NB_ROW_STARS * NB_FRONT_PARTS;
+    b += 2LL * sizeof(float) * star_alloc * ((long long)d.nu * d.nphi + (long long)d.fnr * d.fnu * d.fnphi);
+    return b + ring_bytes;
+}
+
+NB_EXPORT int nb_instance_bytes(nb_handle h, const nb_desc* d, int nstars, long long* out) {
+    if (!out || (!h && !d)) return fail(h, NB_ERR_ARG, "null argument");
+    if (h) {
+        *out = instance_bytes(h->d, h->star_alloc, (long long)sizeof(float) * h->drive_field * h->hc.drive_slots);
+        return NB_OK;
+    }
+    if (nstars < 0 || nstars > d->max_stars) return fail(nullptr, NB_ERR_LIMIT, "nstars must be in [0, max_stars]");
+    *out = instance_bytes(*d, nstars, 0);
+    return NB_OK;
+}
+
 NB_EXPORT void nb_destroy(nb_handle h) {
     if (!h) return;
     if (h->stream) cudaStreamSynchronize(h->stream);
@@ -444,8 +474,9 @@ NB_EXPORT int nb_set_stars(nb_handle h, const nb_star* s, int n) {
         h->rfront = nullptr;
         h->att = nullptr;
         h->star_alloc = 0;
-        const size_t rf = sizeof(float) * (size_t)n * h->d.nu * h->d.nphi;
-        const size_t at = sizeof(float) * (size_t)n * h->d.fnr * h->d.fnu * h->d.fnphi;
+        // room for the float2 pair layouts (NB_TUNE_FRONT_PAIRS / NB_TUNE_FUV_PAIRS may switch at any time)
+        const size_t rf = 2 * sizeof(float) * (size_t)n * h->d.nu * h->d.nphi;
+        const size_t at = 2 * sizeof(float) * (size_t)n * h->d.fnr * h->d.fnu * h->d.fnphi;
         if (cudaMalloc(&h->rfront, rf) != cudaSuccess || cudaMalloc(&h->att, at) != cudaSuccess) {
             cudaGetLastError();
             return fail(h, NB_ERR_NOMEM, "ray scratch allocation refused");
@@ -704,7 +735,7 @@ NB_EXPORT int nb_fuv(nb_handle h) {
         Prof pf(h, NB_PROF_CAST_FUV, 2);                // the (rho, xi) pack into stage planes 0-1 + the rays
         CK(h, nb_launch_cast_fuv(h->c, h->sw, h->dirs_fuv, h->d.f.rho, h->d.f.xi, h->att, h->nstars, h->fuv_group,
                                  nullptr, 0, h->stream, h->d.fnu, h->d.fnphi, plane(h, 0), h->ncell,
-                                 h->fuv_cut ? NB_FUV_TAU_CUT : 0.0f));
+                                 h->fuv_cut ? NB_FUV_TAU_CUT : 0.0f, h->fuv_pairs));
     }
     if (h->hc.plane_on) {
         Prof pf(h, NB_PROF_CAST_FUV, 1);
@@ -713,7 +744,7 @@ NB_EXPORT int nb_fuv(nb_handle h) {
     {
         Prof pf(h, NB_PROF_APPLY_FUV, 1);
         CK(h, nb_launch_apply_fuv(h->c, h->sw, h->att, h->nstars, h->d.f.g0, h->stream, h->d.nx,
-                                  h->d.ny, h->d.fields_fp32 ? 0 : 1));
+                                  h->d.ny, h->d.fields_fp32 ? 0 : 1, h->fuv_pairs));
     }
     return NB_OK;
 }
@@ -753,7 +784,7 @@ NB_EXPORT int nb_cast_rays(nb_handle h, const double xyz[3], double Q, float* rf
     float s3[4] = {(float)xyz[0], (float)xyz[1], (float)xyz[2], 0.f};
     CK(h, cudaMemcpyAsync(h->scratch3, s3, sizeof(s3), cudaMemcpyHostToDevice, h->stream));
     CK(h, nb_launch_cast_rays(h->c, h->sw, h->dirs, h->d.f.rho, rfront_out, 1, h->ray_group, h->scratch3, (float)Q,
-                              h->stream, h->d.nu, h->d.nphi));
+                              h->stream, h->d.nu, h->d.nphi, 0));
     CK(h, cudaStreamSynchronize(h->stream));
     return NB_OK;
 }
@@ -763,7 +794,8 @@ NB_EXPORT int nb_cast_fuv(nb_handle h, const double xyz[3], float* att_out) {
     float s3[4] = {(float)xyz[0], (float)xyz[1], (float)xyz[2], 0.f};
     CK(h, cudaMemcpyAsync(h->scratch3, s3, sizeof(s3), cudaMemcpyHostToDevice, h->stream));
     CK(h, nb_launch_cast_fuv(h->c, h->sw, h->dirs_fuv, h->d.f.rho, h->d.f.xi, att_out, 1, 32, h->scratch3, 1,
-                             h->stream, h->d.fnu, h->d.fnphi, plane(h, 0), h->ncell, h->fuv_cut ? NB_FUV_TAU_CUT : 0.0f));
+                             h->stream, h->d.fnu, h->d.fnphi, plane(h, 0), h->ncell, h->fuv_cut ? NB_FUV_TAU_CUT : 0.0f,
+                             0));
     CK(h, cudaStreamSynchronize(h->stream));
     return NB_OK;
 }
@@ -858,6 +890,8 @@ NB_EXPORT int nb_get_tuning(nb_handle h, int key, int* value) {
         case NB_TUNE_FUV_CUT: *value = h->fuv_cut; return NB_OK;
         case NB_TUNE_WAIT_LIMIT: *value = (int)h->wait_limit; return NB_OK;
         case NB_TUNE_STALL_TEST: *value = h->stall_test; return NB_OK;
+        case NB_TUNE_FRONT_PAIRS: *value = h->front_pairs; return NB_OK;
+        case NB_TUNE_FUV_PAIRS: *value = h->fuv_pairs; return NB_OK;
         default: return fail(h, NB_ERR_ARG, "unknown tuning key");
     }
 }
@@ -889,6 +923,11 @@ NB_EXPORT int nb_set_tuning(nb_handle h, int key, int value) {
         case NB_TUNE_STALL_TEST:
             if (value != 0 && value != 1) return fail(h, NB_ERR_ARG, "the stall test switch must be 0 or 1");
             h->stall_test = value;
+            return NB_OK;
+        case NB_TUNE_FRONT_PAIRS:
+        case NB_TUNE_FUV_PAIRS:
+            if (value != 0 && value != 1) return fail(h, NB_ERR_ARG, "a pair-table switch must be 0 or 1");
+            (key == NB_TUNE_FRONT_PAIRS ? h->front_pairs : h->fuv_pairs) = value;
             return NB_OK;
         case NB_TUNE_RAY_GROUP:
         case NB_TUNE_FUV_GROUP:
@@ -925,6 +964,10 @@ struct nb_batch_s {
     long long all_groups = 0, all_blocks = 0;
     NbRayJob* d_jobs = nullptr;         // a per-step subset
     std::vector<NbRayJob> h_all;
+    std::vector<NbBatchInst> h_inst;    // host copies of the descriptors (nb_batch_set_active re-uploads them)
+    std::vector<HydroLaunch> h_L1, h_L2;
+    std::vector<int> active;            // per instance: 1 = its slot steps, 0 = idle
+    int n_active = 0;
     std::vector<const float*> rfront0;  // each instance's ray scratch when the batch was built
     std::vector<int> nstars0;
     int use_graphs = 1;
@@ -976,6 +1019,7 @@ HydroLaunch stage_desc(nb_instance* h, bool stage2) {
     L.order = h->tile_order;
     L.wait_limit = h->wait_limit;
     if (h->stall_test) L.maps = nullptr;
+    L.active = 1;
     return L;
 }
 
@@ -998,6 +1042,8 @@ NbRayJob ray_job(nb_instance* h) {
     J.half = h->d.fields_fp32 ? 0 : 1;
     J.front_parts = (h->front_cull && h->nstars >= 1 && h->nstars <= NB_ROW_STARS) ? h->front_parts : nullptr;
     J.nray = (long long)h->d.nu * h->d.nphi;
+    J.pairs = h->front_pairs;
+    J.active = 1;
     return J;
 }
 
@@ -1108,11 +1154,17 @@ NB_EXPORT int nb_batch_create(const nb_handle* hs, const int* ion_every, int n, 
         cudaEventCreateWithFlags(&b->ev_out, cudaEventDisableTiming) != cudaSuccess)
         return bail(NB_ERR_CUDA, "nb_batch_create: stream / event creation failed");
     // descriptors
-    std::vector<NbBatchInst> bi(n);
-    std::vector<HydroLaunch> L1(n), L2(n);
+    std::vector<NbBatchInst>& bi = b->h_inst;
+    std::vector<HydroLaunch>& L1 = b->h_L1;
+    std::vector<HydroLaunch>& L2 = b->h_L2;
+    bi.resize(n);
+    L1.resize(n);
+    L2.resize(n);
+    b->active.assign(n, 1);
+    b->n_active = n;
     for (int i = 0; i < n; ++i) {
         nb_instance* h = b->inst[i];
-        bi[i] = NbBatchInst{h->c, h->st, h->stars, h->sw, h->nstars, 0};
+        bi[i] = NbBatchInst{h->c, h->st, h->stars, h->sw, h->nstars, 1};
         L1[i] = stage_desc(h, false);
         L2[i] = stage_desc(h, true);
     }
@@ -1190,21 +1242,47 @@ NB_EXPORT int nb_batch_set_option(nb_batch b, int key, int value) {
     return NB_OK;
 }
 
+NB_EXPORT int nb_batch_set_active(nb_batch b, const int* active, int n) {
+    if (!b || !active) return fail(nullptr, NB_ERR_ARG, "null argument");
+    if (n != (int)b->inst.size()) return bfail(b, NB_ERR_ARG, "one flag per instance of the batch");
+    int na = 0;
+    for (int i = 0; i < n; ++i) {
+        const int a = active[i] ? 1 : 0;
+        b->active[i] = a;
+        b->h_inst[i].active = a;
+        b->h_L1[i].active = a;
+        b->h_L2[i].active = a;
+        b->h_all[i].active = a;
+        na += a;
+    }
+    b->n_active = na;
+    // in stream order before the next step; the captured graphs read these arrays when they run
+    cudaStream_t s = b->bs;
+    BCK(b, cudaMemcpyAsync(b->d_inst, b->h_inst.data(), sizeof(NbBatchInst) * n, cudaMemcpyHostToDevice, s));
+    BCK(b, cudaMemcpyAsync(b->d_L1, b->h_L1.data(), sizeof(HydroLaunch) * n, cudaMemcpyHostToDevice, s));
+    BCK(b, cudaMemcpyAsync(b->d_L2, b->h_L2.data(), sizeof(HydroLaunch) * n, cudaMemcpyHostToDevice, s));
+    BCK(b, cudaMemcpyAsync(b->d_jobs_all, b->h_all.data(), sizeof(NbRayJob) * n, cudaMemcpyHostToDevice, s));
+    BCK(b, cudaStreamSynchronize(s));            // the host arrays may change again at once
+    return NB_OK;
+}
+
 NB_EXPORT int nb_batch_step(nb_batch b, int k) {
     if (!b) return fail(nullptr, NB_ERR_ARG, "null batch");
     if (k < 0) return bfail(b, NB_ERR_ARG, "k >= 0 required");
     const int n = (int)b->inst.size();
     for (int i = 0; i < n; ++i)
-        if (b->inst[i]->rfront != b->rfront0[i] || b->inst[i]->nstars != b->nstars0[i])
+        if (b->active[i] && (b->inst[i]->rfront != b->rfront0[i] || b->inst[i]->nstars != b->nstars0[i]))
             return bfail(b, NB_ERR_STATE, "an instance's star table changed size since nb_batch_create: rebuild the batch");
     for (int i = 0; i < n; ++i)
-        if (!b->inst[i]->hc.phase_main || stirring_main(b->inst[i]))
+        if (b->active[i] && (!b->inst[i]->hc.phase_main || stirring_main(b->inst[i])))
             return bfail(b, NB_ERR_STATE, "batched steps are main-phase steps without stirring: step stirred instances alone");
+    if (b->n_active == 0) return NB_OK;          // every slot idle: nothing to step
     BCK(b, cudaEventRecord(b->ev_in, b->user));
     BCK(b, cudaStreamWaitEvent(b->bs, b->ev_in, 0));
     // an instance whose CFL max speed is stale and that does not ionize first needs a fresh one
     for (int i = 0; i < n; ++i) {
         nb_instance* h = b->inst[i];
+        if (!b->active[i]) continue;
         if (!h->smax_valid && h->host_it % b->ion_every[i] != 0) {
             const nb_fields& f = h->d.f;
             BCK(b, nb_launch_max_speed(h->c, f.rho, f.mx, f.my, f.mz, f.xi, &h->st->smax_bits, h->ncell, b->bs));
@@ -1215,13 +1293,14 @@ NB_EXPORT int nb_batch_step(nb_batch b, int k) {
     for (int s = 0; s < k; ++s) {
         std::vector<int> due;
         for (int i = 0; i < n; ++i)
-            if (b->inst[i]->host_it % b->ion_every[i] == 0) due.push_back(i);
+            if (b->active[i] && b->inst[i]->host_it % b->ion_every[i] == 0) due.push_back(i);
         int rc = NB_OK;
-        const bool all = (int)due.size() == n, none = due.empty();
+        // every active slot or none ionizes: the captured graphs (idle slots skip themselves)
+        const bool all = (int)due.size() == b->n_active, none = due.empty();
         if (b->use_graphs && (all || none) && (all ? b->warm_ion : b->warm_plain)) {
             rc = batch_run_graph(b, all ? &b->g_ion : &b->g_plain, all ? 1 : 0);
         } else {
-            if (all) {
+            if (all) {                           // every active slot: the whole job list (idle slots skip)
                 rc = batch_ionize(b, b->d_jobs_all, n, b->all_groups, b->all_blocks, due);
                 b->warm_ion = 1;
             } else if (!none) {
@@ -1242,9 +1321,10 @@ NB_EXPORT int nb_batch_step(nb_batch b, int k) {
             if (rc == NB_OK) rc = batch_hydro(b);
         }
         if (rc != NB_OK) return rc;
-        for (auto* h : b->inst) {
-            h->host_it += 1;
-            h->smax_valid = 1;
+        for (int i = 0; i < n; ++i) {
+            if (!b->active[i]) continue;
+            b->inst[i]->host_it += 1;
+            b->inst[i]->smax_valid = 1;
         }
     }
     BCK(b, cudaEventRecord(b->ev_out, b->bs));

@@ -8,9 +8,13 @@
 // bins writes them, and a ray stops once its optical depth passes 120 (exp(-tau) is 0.0f from
 // there on: its remaining bins are written as 0).  Density and ionized fraction are sampled at the same corners, so they
 // are first packed as (rho, xi) pairs into free scratch: one 8-byte gather per corner.  All rays of all active stars are one launch, into one attenuation grid
-// per star laid out [star][u][phi][r] (r fastest: a ray's bins are contiguous).  apply_fuv
-// then accumulates every active star for a cell in one register, in the reference's star
-// order (so the float32 sum is the reference's), and stores G0 once as fp16.
+// per star laid out [star][u][phi][r] (r fastest: a ray's bins are contiguous).  Each entry is
+// the pair (att(r), att(min(r + 1, nr - 1))) as one float2 (the ray writes each bin into its own
+// pair and its lower neighbour's), so a trilinear sample of apply_fuv is four 8-byte gathers
+// instead of eight 4-byte ones; values and arithmetic are those of the plain table
+// (NB_TUNE_FUV_PAIRS = 0), bit for bit.  apply_fuv accumulates every active star for a cell in
+// one register, in the reference's star order (so the float32 sum is the reference's), and
+// stores G0 once as fp16.
 #include "nb_rayutil.cuh"
 
 namespace {
@@ -21,7 +25,7 @@ __global__ void __launch_bounds__(256) pack_rx_kernel(const float* __restrict__ 
         rx[q] = make_float2(rho[q], xi[q]);
 }
 
-template <int G, bool REF_LAYOUT>
+template <int G, bool REF_LAYOUT, bool PAIRS>
 __global__ void __launch_bounds__(256, 5) cast_fuv_kernel(const NbConst* __restrict__ c, const NbStarW* __restrict__ sw,
                                                        const float4* __restrict__ dirs,
                                                        const float2* __restrict__ rx,
@@ -45,9 +49,17 @@ __global__ void __launch_bounds__(256, 5) cast_fuv_kernel(const NbConst* __restr
     // bin b of this ray: the reference layout [b][iu][ip], or the instance's [star][u][phi][b] (a ray's
     // bins contiguous; a u-fastest layout makes the apply's gathers contiguous but scatters these writes,
     // a net loss measured at 256^3)
-    auto at = [&](int b) -> float& {
-        return REF_LAYOUT ? att[((long long)b * nu + iu) * nphi + ip]
-                          : att[((long long)s * nray + ray) * nr + b];
+    auto put = [&](int b, float v) {
+        if (REF_LAYOUT) {
+            att[((long long)b * nu + iu) * nphi + ip] = v;
+        } else if (!PAIRS) {
+            att[((long long)s * nray + ray) * nr + b] = v;
+        } else {                                 // bin b is pair b's .x and pair b-1's .y
+            float* p = att + 2 * (((long long)s * nray + ray) * nr + b);
+            p[0] = v;
+            if (b > 0) p[-1] = v;
+            if (b == nr - 1) p[1] = v;
+        }
     };
     const int nx = c->nx, ny = c->ny, nz = c->nz;
     const float dx = c->dx, inv_dx = c->inv_dx, dr = c->dr_f, binr = c->binr_f, kappa = c->kappa_f;
@@ -92,11 +104,11 @@ __global__ void __launch_bounds__(256, 5) cast_fuv_kernel(const NbConst* __restr
         if (valid && lane <= first_stop && nb > prev) {
             const float v = expf(-tau);
             const int e = min(nb, nr);
-            for (int b = prev; b < e; ++b) at(b) = v;
+            for (int b = prev; b < e; ++b) put(b, v);
         }
         if (mine) {                              // a lane ran out of bins or into the dark
             const int e_first = __shfl_sync(gmask, min(nb, nr), first_stop, G);
-            for (int b = e_first + lane; b < nr; b += G) at(b) = 0.0f;
+            for (int b = e_first + lane; b < nr; b += G) put(b, 0.0f);
             stopped = true;
             break;
         }
@@ -110,11 +122,11 @@ __global__ void __launch_bounds__(256, 5) cast_fuv_kernel(const NbConst* __restr
     }
     if (!stopped) {
         const float v = expf(-(hi - comp));
-        for (int b = ib + lane; b < nr; b += G) at(b) = v;
+        for (int b = ib + lane; b < nr; b += G) put(b, v);
     }
 }
 
-template <bool HALF>
+template <bool HALF, bool PAIRS>
 __global__ void __launch_bounds__(256, 6) apply_fuv_kernel(const NbConst* __restrict__ c, const NbStarW* __restrict__ sw,
                                                         const float* __restrict__ att, int nstars,
                                                         void* __restrict__ g0) {
@@ -179,7 +191,35 @@ __global__ void __launch_bounds__(256, 6) apply_fuv_kernel(const NbConst* __rest
             const float fu = (u + 1.0f) * 0.5f * (float)nu - 0.5f;
             const int ir = (int)floorf(fr), iu = (int)floorf(fu);
             const float tr = fr - (float)ir, tu = fu - (float)iu;
-            const float* as = att + (long long)s * nu * nphi * nr;
+            const long long tab0 = (long long)s * nu * nphi * nr;
+            float v[2][2][2];                    // [r corner][u corner][phi corner]
+            if (PAIRS) {
+                // pair rc = (att(rc), att(min(rc + 1, nr - 1))): the two r corners, except at ir = -1,
+                // where both clamp to r = 0 (the pair's .x)
+                const float2* ap = reinterpret_cast<const float2*>(att) + tab0;
+                const int rc = iclampd(ir, 0, nr - 1);
+#pragma unroll
+                for (int bb = 0; bb < 2; ++bb)
+#pragma unroll
+                    for (int cc = 0; cc < 2; ++cc) {
+                        const int uu = iclampd(iu + bb, 0, nu - 1);
+                        const float2 pr = __ldg(ap + ((uu * nphi + pw[cc]) * nr + rc));      // < 2^31 per star
+                        v[0][bb][cc] = pr.x;
+                        v[1][bb][cc] = ir < 0 ? pr.x : pr.y;
+                    }
+            } else {
+                const float* as = att + tab0;
+#pragma unroll
+                for (int aa = 0; aa < 2; ++aa)
+#pragma unroll
+                    for (int bb = 0; bb < 2; ++bb)
+#pragma unroll
+                        for (int cc = 0; cc < 2; ++cc) {
+                            const int rr = iclampd(ir + aa, 0, nr - 1);
+                            const int uu = iclampd(iu + bb, 0, nu - 1);
+                            v[aa][bb][cc] = __ldg(as + ((uu * nphi + pw[cc]) * nr + rr));   // < 2^31 per star
+                        }
+            }
             float acc = 0.0f;
 #pragma unroll
             for (int aa = 0; aa < 2; ++aa)
@@ -188,9 +228,7 @@ __global__ void __launch_bounds__(256, 6) apply_fuv_kernel(const NbConst* __rest
 #pragma unroll
                     for (int cc = 0; cc < 2; ++cc) {
                         const float wgt = (aa == 0 ? 1.0f - tr : tr) * (bb == 0 ? 1.0f - tu : tu) * (cc == 0 ? 1.0f - tp : tp);
-                        const int rr = iclampd(ir + aa, 0, nr - 1);
-                        const int uu = iclampd(iu + bb, 0, nu - 1);
-                        acc = acc + wgt * __ldg(as + ((uu * nphi + pw[cc]) * nr + rr));   // < 2^31 per star
+                        acc = acc + wgt * v[aa][bb][cc];
                     }
             const float r2 = fmaxr(r * r, 0.0004f);
             term[e] = lum[s] * acc / r2;
@@ -237,7 +275,7 @@ cudaError_t nb_launch_plane_fuv(const NbConst* c, const float* rho, const float*
 cudaError_t nb_launch_cast_fuv(const NbConst* c, const NbStarW* sw, const float4* dirs, const float* rho,
                                const float* xi, float* att, int nstars, int group, const float* star_override,
                                int ref_layout, cudaStream_t s, int fnu, int fnphi, void* rx_scratch, long long ncell,
-                               float tau_cut) {
+                               float tau_cut, int pairs) {
     float2* rx = static_cast<float2*>(rx_scratch);
     {
         const long long b = (ncell + 255) / 256;
@@ -245,15 +283,21 @@ cudaError_t nb_launch_cast_fuv(const NbConst* c, const NbStarW* sw, const float4
     }
     const long long threads = (long long)fnu * fnphi * nstars * group;
     const int blocks = (int)((threads + 255) / 256);
-#define NB_FUV_LAUNCH(G, R) \
-    cast_fuv_kernel<G, R><<<blocks, 256, 0, s>>>(c, sw, dirs, rx, att, nstars, star_override, tau_cut)
+#define NB_FUV_LAUNCH(G, R, PR) \
+    cast_fuv_kernel<G, R, PR><<<blocks, 256, 0, s>>>(c, sw, dirs, rx, att, nstars, star_override, tau_cut)
     if (ref_layout) {
-        NB_FUV_LAUNCH(32, true);
+        NB_FUV_LAUNCH(32, true, false);
+    } else if (pairs) {
+        switch (group) {
+            case 8: NB_FUV_LAUNCH(8, false, true); break;
+            case 16: NB_FUV_LAUNCH(16, false, true); break;
+            default: NB_FUV_LAUNCH(32, false, true); break;
+        }
     } else {
         switch (group) {
-            case 8: NB_FUV_LAUNCH(8, false); break;
-            case 16: NB_FUV_LAUNCH(16, false); break;
-            default: NB_FUV_LAUNCH(32, false); break;
+            case 8: NB_FUV_LAUNCH(8, false, false); break;
+            case 16: NB_FUV_LAUNCH(16, false, false); break;
+            default: NB_FUV_LAUNCH(32, false, false); break;
         }
     }
 #undef NB_FUV_LAUNCH
@@ -261,11 +305,15 @@ cudaError_t nb_launch_cast_fuv(const NbConst* c, const NbStarW* sw, const float4
 }
 
 cudaError_t nb_launch_apply_fuv(const NbConst* c, const NbStarW* sw, const float* att, int nstars, void* g0,
-                                cudaStream_t s, int nx, int ny, int half) {
+                                cudaStream_t s, int nx, int ny, int half, int pairs) {
     const int blocks = rowwalk_blocks(nx, ny);
-    if (half)
-        apply_fuv_kernel<true><<<blocks, dim3(32, 8), 0, s>>>(c, sw, att, nstars, g0);
+    if (half && pairs)
+        apply_fuv_kernel<true, true><<<blocks, dim3(32, 8), 0, s>>>(c, sw, att, nstars, g0);
+    else if (half)
+        apply_fuv_kernel<true, false><<<blocks, dim3(32, 8), 0, s>>>(c, sw, att, nstars, g0);
+    else if (pairs)
+        apply_fuv_kernel<false, true><<<blocks, dim3(32, 8), 0, s>>>(c, sw, att, nstars, g0);
     else
-        apply_fuv_kernel<false><<<blocks, dim3(32, 8), 0, s>>>(c, sw, att, nstars, g0);
+        apply_fuv_kernel<false, false><<<blocks, dim3(32, 8), 0, s>>>(c, sw, att, nstars, g0);
     return cudaGetLastError();
 }

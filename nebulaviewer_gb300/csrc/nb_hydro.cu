@@ -750,6 +750,10 @@ hydro_batch_kernel(const HydroLaunch* __restrict__ Ls, const int2* __restrict__ 
         const int it = item;
         if (it >= n_work) break;
         const int2 w = work[it];
+        if (!Ls[w.x].active) {                   // an idle slot of the batch: nothing to do
+            __syncthreads();
+            continue;
+        }
         last = &Ls[w.x];
         hydro_tile<SOLVER, LIM, TJ, STAGE2, I32>(*last, w.y, smem, ph0, failed, rot);
         if (failed) break;

@@ -110,6 +110,7 @@ struct HydroLaunch {
     int order;                   // tile sweep order (NB_TUNE_TILE_ORDER)
     int idx32;                   // fewer than 2^31 cells: 32-bit cell offsets (single-instance stage)
     unsigned wait_limit;         // polls of each bounded TMA wait (NB_TUNE_WAIT_LIMIT)
+    int active;                  // batched stage: 0 = the instance's slot is idle (its tiles are skipped)
 };
 
 // One instance of a batch, as the batched control kernel sees it.
@@ -119,7 +120,7 @@ struct NbBatchInst {
     const NbStarDev* stars;
     NbStarW* sw;
     int nstars;
-    int pad;
+    int active;           // 0: an idle slot of the batch (no weights, no clock advance)
 };
 
 // One instance of a batched ionization (nebula3d.py:247-315 over many instances in 3 launches).
@@ -142,6 +143,8 @@ struct NbRayJob {
     int half;
     float2* front_parts;  // the instance's front-radius partials when apply_front culls, else null
     long long nray;       // rays per star (nu * nphi)
+    int pairs;            // the front table holds (u, u + 1) pairs (NB_TUNE_FRONT_PAIRS)
+    int active;           // 0: an idle slot of the batch (its rays, fronts and smoothing are skipped)
 };
 
 // ------------------------------------------------------------------ helpers
@@ -238,15 +241,17 @@ cudaError_t nb_launch_render_pack(const NbConst* c, const float* rho, const floa
                                   const nb_pack_params& pp, int shock_on, int smooth, void* out8, void* tmp8, int nx,
                                   int ny, cudaStream_t s);
 cudaError_t nb_launch_ray_dirs(int nu, int nphi, float4* dirs, cudaStream_t s);
+// pairs: the instance's front table holds (rf(u), rf(u + 1)) float2 pairs (2 * nu * nphi floats per
+// star); a star_override launch writes the reference layout [u][phi] (pairs = 0)
 cudaError_t nb_launch_cast_rays(const NbConst* c, const NbStarW* sw, const float4* dirs, const float* rho,
                                 float* rfront, int nstars, int group, const float* star_override, float q_override,
-                                cudaStream_t s, int nu, int nphi);
+                                cudaStream_t s, int nu, int nphi, int pairs);
 // with front_parts (NB_ROW_STARS * NB_FRONT_PARTS float2 scratch) and 1 <= nstars <= NB_ROW_STARS:
 // first each star's front-radius range (one more launch), then segments skip the stars that
 // cannot change them
 cudaError_t nb_launch_apply_front(const NbConst* c, const NbStarW* sw, const float* rfront, int nstars,
                                   float* xi_raw, void* dfront, unsigned* smax_reset, cudaStream_t s, int nx, int ny,
-                                  int half, float2* front_parts = nullptr, long long nray = 0);
+                                  int half, float2* front_parts, long long nray, int pairs);
 cudaError_t nb_launch_smooth(const NbConst* c, const float* xi_raw, float* xi, const float* rho, const float* mx,
                              const float* my, const float* mz, unsigned* smax_bits, cudaStream_t s, int nx, int ny);
 cudaError_t nb_launch_ionize_batch(const NbRayJob* jobs, int n_jobs, long long n_groups, long long n_blocks, int group,
@@ -258,10 +263,10 @@ cudaError_t nb_launch_plane_fuv(const NbConst* c, const float* rho, const float*
 cudaError_t nb_launch_cast_fuv(const NbConst* c, const NbStarW* sw, const float4* dirs, const float* rho,
                                const float* xi, float* att, int nstars, int group, const float* star_override,
                                int ref_layout, cudaStream_t s, int fnu, int fnphi, void* rx_scratch, long long ncell,
-                               float tau_cut);
+                               float tau_cut, int pairs);
 #define NB_FUV_TAU_CUT 120.0f            // optical depth past which a FUV ray's remaining bins are 0
 cudaError_t nb_launch_apply_fuv(const NbConst* c, const NbStarW* sw, const float* att, int nstars, void* g0,
-                                cudaStream_t s, int nx, int ny, int half);
+                                cudaStream_t s, int nx, int ny, int half, int pairs);
 cudaError_t nb_launch_pack(const NbConst* c, const float* rho, const float* mx, const float* my, const float* mz,
                            const float* xi, const void* df, const void* g0, int half, void* out, long long n,
                            cudaStream_t s);

@@ -8,6 +8,10 @@
 //    samples at a time; the recombination column sum(n^2 r^2 dr) is an inclusive group scan on
 //    top of a Kahan-compensated carry, and the first sample whose column passes Q is found with
 //    one ballot.  All rays of all active stars are one launch.
+//  * The front table holds, per (star, phi, u), the pair (rf(u), rf(min(u + 1, nu - 1))) as one
+//    float2 (cast_rays writes each front into its own pair and its lower neighbour's), so the
+//    bilinear lookup of apply_front is two 8-byte gathers instead of four 4-byte ones; the values
+//    and the arithmetic are those of the plain table (NB_TUNE_FRONT_PAIRS = 0), bit for bit.
 //  * apply_front: one pass over the grid merges the active stars, in star order, into one
 //    register pair per cell (the reference makes S passes).  With up to 32 stars, each star's
 //    front-radius range (front_bounds_kernel) lets a 32-cell row segment leave out the stars that
@@ -33,11 +37,14 @@ __global__ void ray_dirs_kernel(int nu, int nphi, float4* __restrict__ dirs) {
     dirs[id] = make_float4(s * cph, s * sph, u, 0.0f);
 }
 
-// nebula3d.py:247-270 cast_rays: ray `ray` of star (sx, sy, sz, Q), G lanes per ray.
+// nebula3d.py:247-270 cast_rays: ray `ray` of star (sx, sy, sz, Q), G lanes per ray.  `out` is where
+// the front radius goes (a float pointer, 4-byte aligned) with two flags in its low bits: bit 0 also
+// writes out[-1] and bit 1 out[1] (the pair layout's neighbour copies, front_slot); one 64-bit
+// value stays live across the march, as a plain pointer would.
 template <int G>
 __device__ __forceinline__ void cast_ray(const NbConst& C, const float4* __restrict__ dirs,
-                                         const float* __restrict__ rho, float* __restrict__ out, int ray, float sx,
-                                         float sy, float sz, float Q, int lane, unsigned gmask) {
+                                         const float* __restrict__ rho, uintptr_t out, int ray, float sx, float sy,
+                                         float sz, float Q, int lane, unsigned gmask) {
     const int nx = C.nx, ny = C.ny, nz = C.nz;
     const float dx = C.dx, inv_dx = C.inv_dx, dr = C.dr_f;
     const bool pow2 = C.dx_pow2 != 0;
@@ -81,7 +88,22 @@ __device__ __forceinline__ void cast_ray(const NbConst& C, const float4* __restr
         comp = (tsum - hi) - y;
         hi = tsum;
     }
-    if (lane == 0) *out = rf;
+    if (lane == 0) {
+        float* p = reinterpret_cast<float*>(out & ~(uintptr_t)3);
+        p[0] = rf;
+        if (out & 1) p[-1] = rf;
+        if (out & 2) p[1] = rf;
+    }
+}
+
+// Where the front of ray (iu, ip) of star s goes in an instance's table [star][phi][u]: one float,
+// or (pairs) the .x of its own float2 pair, flagged to write the .y of the pair below it too (and
+// of its own at the last u).
+__device__ __forceinline__ uintptr_t front_slot(float* rfront, bool pairs, int s, long long nray, int nu, int iu,
+                                                int ip) {
+    const long long e = (long long)s * nray + (long long)ip * nu + iu;
+    if (!pairs) return reinterpret_cast<uintptr_t>(rfront + e);
+    return reinterpret_cast<uintptr_t>(rfront + 2 * e) | (iu > 0 ? 1u : 0u) | (iu == nu - 1 ? 2u : 0u);
 }
 
 // Resident blocks per SM of the ray kernel: 6 (40 registers) in the fast build, 5 (48) in the exact
@@ -91,7 +113,7 @@ __device__ __forceinline__ void cast_ray(const NbConst& C, const float4* __restr
 #else
 #define NB_CAST_RAYS_MINB 5
 #endif
-template <int G>
+template <int G, bool PAIRS>
 __global__ void __launch_bounds__(256, NB_CAST_RAYS_MINB) cast_rays_kernel(const NbConst* __restrict__ c, const NbStarW* __restrict__ sw,
                                                         const float4* __restrict__ dirs,
                                                         const float* __restrict__ rho, float* __restrict__ rfront,
@@ -103,16 +125,16 @@ __global__ void __launch_bounds__(256, NB_CAST_RAYS_MINB) cast_rays_kernel(const
     if (gid >= (long long)nray * nstars) return;
     const int s = (int)(gid / nray), ray = (int)(gid % nray);
     if (star_override) {
-        cast_ray<G>(*c, dirs, rho, rfront + ray, ray, star_override[0], star_override[1], star_override[2],
-                    q_override, lane, gmask);
+        cast_ray<G>(*c, dirs, rho, reinterpret_cast<uintptr_t>(rfront + ray), ray, star_override[0], star_override[1],
+                    star_override[2], q_override, lane, gmask);
         return;
     }
     const NbStarW w = sw[s];
     if (!w.active) return;
     // the instance's table is [star][phi][u] (u fastest: the cells of a warp share phi)
     const int iu = ray / c->nphi, ip = ray - iu * c->nphi;
-    cast_ray<G>(*c, dirs, rho, rfront + (long long)s * nray + (long long)ip * c->nu + iu, ray, w.w.x, w.w.y, w.w.z,
-                w.q_f, lane, gmask);
+    cast_ray<G>(*c, dirs, rho, front_slot(rfront, PAIRS, s, nray, c->nu, iu, ip), ray, w.w.x, w.w.y, w.w.z, w.q_f,
+                lane, gmask);
 }
 
 // Rays of every star of every listed instance: job e owns groups [job[e].ray0, job[e+1].ray0).
@@ -133,11 +155,11 @@ __global__ void __launch_bounds__(256) cast_rays_batch_kernel(const NbRayJob* __
     const int nray = C.nu * C.nphi;
     const long long local = gid - J.ray0;
     const int s = (int)(local / nray), ray = (int)(local % nray);
-    if (s >= J.nstars) return;
+    if (s >= J.nstars || !J.active) return;
     const NbStarW w = J.sw[s];
     if (!w.active) return;
     const int iu = ray / C.nphi, ip = ray - iu * C.nphi;
-    cast_ray<G>(C, J.dirs, J.rho, J.rfront + (long long)s * nray + (long long)ip * C.nu + iu, ray, w.w.x, w.w.y, w.w.z,
+    cast_ray<G>(C, J.dirs, J.rho, front_slot(J.rfront, J.pairs != 0, s, nray, C.nu, iu, ip), ray, w.w.x, w.w.y, w.w.z,
                 w.q_f, lane, gmask);
 }
 
@@ -176,7 +198,9 @@ __device__ __forceinline__ unsigned segment_stars(const float4* st, const int* a
 // nebula3d.py:273-307 rf_at + apply_front over one row (i, j), fused over the active stars,
 // with the fp16 store of the front distance (sim.py:942, 980-985).  `tab`: this warp's row
 // table (NB_ROW_STARS entries) or null for the per-cell form; `bnd`: each star's (least, largest)
-// front radius, or null to merge every active star in every segment.
+// front radius, or null to merge every active star in every segment.  PAIRS: the front table
+// holds (u, u + 1) pairs.
+template <bool PAIRS>
 __device__ __forceinline__ void apply_front_row(const NbConst& C, const float4* st, const int* act, int nstars,
                                                 const float* __restrict__ rfront, float* __restrict__ xi_raw,
                                                 void* __restrict__ dfront, bool half, int row, float4* tab,
@@ -250,10 +274,21 @@ __device__ __forceinline__ void apply_front_row(const NbConst& C, const float4* 
                 const int iu = (int)floorf(fu);
                 tu[e] = fu - (float)iu;
                 const int u0 = max(iu, 0), u1 = min(iu + 1, nu - 1);    // u in [-1, 1]: iu in [-1, nu - 1]
-                g00[e] = __ldg(rfs + c0 + u0);
-                g01[e] = __ldg(rfs + c1 + u0);
-                g10[e] = __ldg(rfs + c0 + u1);
-                g11[e] = __ldg(rfs + c1 + u1);
+                if (PAIRS) {
+                    // pair u0 = (rf(u0), rf(min(u0 + 1, nu - 1))): the two u corners, except at iu = -1,
+                    // where both corners clamp to u = 0 (the pair's .x)
+                    const float2* rp = reinterpret_cast<const float2*>(rfront) + (long long)s * rstride;
+                    const float2 p0 = __ldg(rp + c0 + u0), p1 = __ldg(rp + c1 + u0);
+                    g00[e] = p0.x;
+                    g01[e] = p1.x;
+                    g10[e] = iu < 0 ? p0.x : p0.y;
+                    g11[e] = iu < 0 ? p1.x : p1.y;
+                } else {
+                    g00[e] = __ldg(rfs + c0 + u0);
+                    g01[e] = __ldg(rfs + c1 + u0);
+                    g10[e] = __ldg(rfs + c0 + u1);
+                    g11[e] = __ldg(rfs + c1 + u1);
+                }
             }
 #pragma unroll
             for (int e = 0; e < SG; ++e) {
@@ -287,6 +322,8 @@ __device__ __forceinline__ void apply_front_row(const NbConst& C, const float4* 
 // Each active star's least and largest front radius over its rays, as NB_FRONT_PARTS partial
 // (least, largest) pairs per star: block (b, s) reduces the b-th slice of star s.  The largest is
 // NaN when a NaN radius was seen (the least skips NaNs).
+// With pair tables a star's slice holds every front twice (as a .x and as a .y): the same set of
+// values, so the same bounds.
 __device__ __forceinline__ void front_bounds_block(const NbStarW* __restrict__ sw, const float* __restrict__ rfront,
                                                    long long nray, float2* __restrict__ parts, int s, int b) {
     if (!sw[s].active) return;                  // uniform over the block
@@ -328,8 +365,8 @@ __global__ void __launch_bounds__(256) front_bounds_kernel(const NbStarW* __rest
 // the same for every listed instance that culls: block (b, job, star)
 __global__ void __launch_bounds__(256) front_bounds_batch_kernel(const NbRayJob* __restrict__ jobs) {
     const NbRayJob& J = jobs[blockIdx.y];
-    if (!J.front_parts || (int)blockIdx.z >= J.nstars) return;      // uniform over the block
-    front_bounds_block(J.sw, J.rfront, J.nray, J.front_parts, blockIdx.z, blockIdx.x);
+    if (!J.front_parts || !J.active || (int)blockIdx.z >= J.nstars) return;      // uniform over the block
+    front_bounds_block(J.sw, J.rfront, J.pairs ? 2 * J.nray : J.nray, J.front_parts, blockIdx.z, blockIdx.x);
 }
 
 // the partials into (least, largest) per star in shared memory (after load_stars' barrier)
@@ -358,7 +395,7 @@ __device__ __forceinline__ int load_stars(const NbStarW* sw, int nstars, float4*
     return tlin;
 }
 
-template <bool HALF>
+template <bool HALF, bool PAIRS>
 __global__ void __launch_bounds__(256, 4) apply_front_kernel(const NbConst* __restrict__ c,
                                                           const NbStarW* __restrict__ sw,
                                                           const float* __restrict__ rfront, int nstars,
@@ -371,8 +408,8 @@ __global__ void __launch_bounds__(256, 4) apply_front_kernel(const NbConst* __re
     const int tlin = load_stars(sw, nstars, st, act);
     if (smax_reset && blockIdx.x == 0 && tlin == 0) *smax_reset = 0u;
     if (parts) load_front_bounds(parts, nstars, bnd, tlin);      // parts only with nstars <= NB_ROW_STARS
-    apply_front_row(*c, st, act, nstars, rfront, xi_raw, dfront, HALF, blockIdx.x * blockDim.y + threadIdx.y,
-                    tab[threadIdx.y], parts ? bnd : nullptr);
+    apply_front_row<PAIRS>(*c, st, act, nstars, rfront, xi_raw, dfront, HALF, blockIdx.x * blockDim.y + threadIdx.y,
+                           tab[threadIdx.y], parts ? bnd : nullptr);
 }
 
 // Rows of every listed instance; job e owns blocks [job[e].blk0, job[e+1].blk0) (8 rows each).
@@ -387,12 +424,17 @@ __global__ void __launch_bounds__(256) apply_front_batch_kernel(const NbRayJob* 
         if (jobs[mid].blk0 <= (long long)blockIdx.x) lo = mid; else hi = mid - 1;
     }
     const NbRayJob& J = jobs[lo];
+    if (!J.active) return;                       // uniform over the block
     const int lb = (int)(blockIdx.x - J.blk0);
     const int tlin = load_stars(J.sw, J.nstars, st, act);
     if (lb == 0 && tlin == 0) *J.smax = 0u;
     if (J.front_parts) load_front_bounds(J.front_parts, J.nstars, bnd, tlin);     // uniform over the block
-    apply_front_row(*J.c, st, act, J.nstars, J.rfront, J.xi_raw, J.dfront, J.half != 0, lb * blockDim.y + threadIdx.y,
-                    tab[threadIdx.y], J.front_parts ? bnd : nullptr);
+    if (J.pairs)
+        apply_front_row<true>(*J.c, st, act, J.nstars, J.rfront, J.xi_raw, J.dfront, J.half != 0,
+                              lb * blockDim.y + threadIdx.y, tab[threadIdx.y], J.front_parts ? bnd : nullptr);
+    else
+        apply_front_row<false>(*J.c, st, act, J.nstars, J.rfront, J.xi_raw, J.dfront, J.half != 0,
+                               lb * blockDim.y + threadIdx.y, tab[threadIdx.y], J.front_parts ? bnd : nullptr);
 }
 
 // nebula3d.py:310-315 smooth_xi (+ sim.py:941 copy back) of one row, then the CFL max speed
@@ -461,6 +503,7 @@ __global__ void __launch_bounds__(256) smooth_batch_kernel(const NbRayJob* __res
         if (jobs[mid].blk0 <= (long long)blockIdx.x) lo = mid; else hi = mid - 1;
     }
     const NbRayJob& J = jobs[lo];
+    if (!J.active) return;                       // uniform over the block
     const int lb = (int)(blockIdx.x - J.blk0);
     const float m = smooth_row(*J.c, J.xi_raw, J.xi, J.rho, J.mx, J.my, J.mz, true, lb * blockDim.y + threadIdx.y);
     block_max_to(m, J.smax);
@@ -505,34 +548,45 @@ cudaError_t nb_launch_ray_dirs(int nu, int nphi, float4* dirs, cudaStream_t s) {
 
 cudaError_t nb_launch_cast_rays(const NbConst* c, const NbStarW* sw, const float4* dirs, const float* rho,
                                 float* rfront, int nstars, int group, const float* star_override, float q_override,
-                                cudaStream_t s, int nu, int nphi) {
+                                cudaStream_t s, int nu, int nphi, int pairs) {
     const long long threads = (long long)nu * nphi * nstars * group;
     const int blocks = (int)((threads + 255) / 256);
+#define NB_RAYS_LAUNCH(G)                                                                                      \
+    (pairs ? cast_rays_kernel<G, true><<<blocks, 256, 0, s>>>(c, sw, dirs, rho, rfront, nstars, star_override,  \
+                                                              q_override)                                       \
+           : cast_rays_kernel<G, false><<<blocks, 256, 0, s>>>(c, sw, dirs, rho, rfront, nstars, star_override, \
+                                                               q_override))
     switch (group) {
-        case 1: cast_rays_kernel<1><<<blocks, 256, 0, s>>>(c, sw, dirs, rho, rfront, nstars, star_override, q_override); break;
-        case 2: cast_rays_kernel<2><<<blocks, 256, 0, s>>>(c, sw, dirs, rho, rfront, nstars, star_override, q_override); break;
-        case 4: cast_rays_kernel<4><<<blocks, 256, 0, s>>>(c, sw, dirs, rho, rfront, nstars, star_override, q_override); break;
-        case 8: cast_rays_kernel<8><<<blocks, 256, 0, s>>>(c, sw, dirs, rho, rfront, nstars, star_override, q_override); break;
-        case 16: cast_rays_kernel<16><<<blocks, 256, 0, s>>>(c, sw, dirs, rho, rfront, nstars, star_override, q_override); break;
-        default: cast_rays_kernel<32><<<blocks, 256, 0, s>>>(c, sw, dirs, rho, rfront, nstars, star_override, q_override); break;
+        case 1: NB_RAYS_LAUNCH(1); break;
+        case 2: NB_RAYS_LAUNCH(2); break;
+        case 4: NB_RAYS_LAUNCH(4); break;
+        case 8: NB_RAYS_LAUNCH(8); break;
+        case 16: NB_RAYS_LAUNCH(16); break;
+        default: NB_RAYS_LAUNCH(32); break;
     }
+#undef NB_RAYS_LAUNCH
     return cudaGetLastError();
 }
 
 cudaError_t nb_launch_apply_front(const NbConst* c, const NbStarW* sw, const float* rfront, int nstars,
                                   float* xi_raw, void* dfront, unsigned* smax_reset, cudaStream_t s, int nx, int ny,
-                                  int half, float2* front_parts, long long nray) {
+                                  int half, float2* front_parts, long long nray, int pairs) {
     const dim3 blk(32, 8);
     const int blocks = rowwalk_blocks(nx, ny);
     const float2* parts = nullptr;
     if (front_parts && nstars >= 1 && nstars <= NB_ROW_STARS) {
-        front_bounds_kernel<<<dim3(NB_FRONT_PARTS, nstars), 256, 0, s>>>(sw, rfront, nray, front_parts);
+        front_bounds_kernel<<<dim3(NB_FRONT_PARTS, nstars), 256, 0, s>>>(sw, rfront, pairs ? 2 * nray : nray,
+                                                                          front_parts);
         parts = front_parts;
     }
-    if (half)
-        apply_front_kernel<true><<<blocks, blk, 0, s>>>(c, sw, rfront, nstars, xi_raw, dfront, smax_reset, parts);
+    if (half && pairs)
+        apply_front_kernel<true, true><<<blocks, blk, 0, s>>>(c, sw, rfront, nstars, xi_raw, dfront, smax_reset, parts);
+    else if (half)
+        apply_front_kernel<true, false><<<blocks, blk, 0, s>>>(c, sw, rfront, nstars, xi_raw, dfront, smax_reset, parts);
+    else if (pairs)
+        apply_front_kernel<false, true><<<blocks, blk, 0, s>>>(c, sw, rfront, nstars, xi_raw, dfront, smax_reset, parts);
     else
-        apply_front_kernel<false><<<blocks, blk, 0, s>>>(c, sw, rfront, nstars, xi_raw, dfront, smax_reset, parts);
+        apply_front_kernel<false, false><<<blocks, blk, 0, s>>>(c, sw, rfront, nstars, xi_raw, dfront, smax_reset, parts);
     return cudaGetLastError();
 }
 

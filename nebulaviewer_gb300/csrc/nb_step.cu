@@ -113,6 +113,7 @@ __global__ void ctrl_batch_kernel(const NbBatchInst* __restrict__ insts, int n, 
         counters[0] = 0u;
         counters[1] = 0u;
     }
+    if (!I.active) return;                       // an idle slot: its clock stays
     ctrl_body(I.c, I.st, I.stars, I.sw, I.nstars, advance);
 }
 

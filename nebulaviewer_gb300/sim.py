@@ -95,6 +95,53 @@ def _ray_budget(nz, fast, rays, fuv_grid):
     return (int(nu), int(nphi)), tuple(int(v) for v in fg)
 
 
+def instance_desc(shape, dx, P, rays, fuv, fast, cap):
+    """the library's description of an instance (nb_desc, without field pointers or stream): the
+    values sim.py:Sim.reset computes for the grid, the physics and the ray / FUV budgets
+    (sim.py:718-759)"""
+    nx, ny, nz = (int(v) for v in shape)
+    cn2, ci2, vmax = sound_speeds(P)
+    L = (nx * dx, ny * dx, nz * dx)
+    diag = math.sqrt(L[0] ** 2 + L[1] ** 2 + L[2] ** 2) + 0.6                          # sim.py:742
+    dr = (1.0 if fast else 0.5) * dx                                                  # sim.py:743
+    d = _lib.NbDesc()
+    d.abi_version = _lib.NB_ABI_VERSION
+    d.nx, d.ny, d.nz = nx, ny, nz
+    d.dx = float(dx)
+    d.cn2, d.ci2, d.vmax = cn2, ci2, vmax
+    d.floor_rho = float(P["floor"])
+    d.cfl = float(P["cfl"])
+    d.solver = _lib.SOLVERS[P.get("solver", "rusanov")]
+    d.limiter = _lib.LIMITERS[P.get("limiter", "minmod")]
+    d.nu, d.nphi = (int(v) for v in rays)
+    d.dr = dr
+    d.nsteps = int(diag / dr) + 1                                                     # sim.py:744
+    d.diag = diag
+    d.fnr, d.fnu, d.fnphi = (int(v) for v in fuv)
+    d.fields_fp32 = 1 if P.get("fp32_fields") else 0
+    d.max_stars = min(256, max(int(cap), 1))
+    return d
+
+
+def field_bytes(shape, P):
+    """device bytes of an instance's fields: rho, mx, my, mz, xi and the 4-plane stage block in
+    float32, dfront and g0 in float16 (float32 with fp32_fields) -- the reference's 40 B/cell
+    (sim.py:718-735)"""
+    n = int(np.prod(shape))
+    return n * (9 * 4 + 2 * (4 if P.get("fp32_fields") else 2))
+
+
+def footprint_bytes(shape, dx, P, rays, fuv, fast, nstars, arith=None):
+    """device bytes an instance of this description holds once built with `nstars` stars: its fields
+    plus the library's scratch (nb_instance_bytes), known before anything is allocated"""
+    lib = _lib.load(arith)
+    cap = max(int(nstars), int(P["max_stars"]))
+    d = instance_desc(shape, dx, P, rays, fuv, fast, cap)
+    out = C.c_longlong()
+    _lib.check(lib.nb_instance_bytes(None, C.byref(d), int(nstars), C.byref(out)), None, "nb_instance_bytes", lib)
+    return field_bytes(shape, P) + int(out.value)
+
+
 class Sim:
     """GPU-resident simulation on the GB300 kernels.
 
@@ -298,22 +345,7 @@ class Sim:
         self.fuv_every = (8 if nz <= 160 else 16) if self.fast else 8               # sim.py:759
         self._stream = torch.cuda.current_stream(dev) if dev.type == "cuda" else None
         lib = _lib.load(self.arith)
-        d = _lib.NbDesc()
-        d.abi_version = _lib.NB_ABI_VERSION
-        d.nx, d.ny, d.nz = nx, ny, nz
-        d.dx = self.dx
-        d.cn2, d.ci2, d.vmax = self.cn2, self.ci2, self.vmax
-        d.floor_rho = float(P["floor"])
-        d.cfl = float(P["cfl"])
-        d.solver = _lib.SOLVERS[P.get("solver", "rusanov")]
-        d.limiter = _lib.LIMITERS[P.get("limiter", "minmod")]
-        d.nu, d.nphi = rays
-        d.dr = self.dr
-        d.nsteps = self.nsteps
-        d.diag = self.diag
-        d.fnr, d.fnu, d.fnphi = fuv
-        d.fields_fp32 = 1 if P.get("fp32_fields") else 0
-        d.max_stars = min(256, max(self.cap, 1))
+        d = instance_desc(self.shape, self.dx, P, rays, fuv, self.fast, self.cap)
         st = self._stage
         n = nx * ny * nz
         d.f = _lib.NbFields(self._rho.data_ptr(), self._mx.data_ptr(), self._my.data_ptr(), self._mz.data_ptr(),
@@ -923,6 +955,14 @@ class Sim:
         self._chk(self._lib.nb_reduce_fp64(self._h, out), "nb_reduce_fp64")
         v = self.dx ** 3
         return tuple(float(x) * v for x in out)
+
+    def footprint(self):
+        """device bytes this instance holds: its fields and the library's scratch for it"""
+        out = C.c_longlong()
+        self._chk(self._lib.nb_instance_bytes(self._h, None, 0, C.byref(out)), "nb_instance_bytes")
+        fields = sum(t.numel() * t.element_size() for t in (self._rho, self._mx, self._my, self._mz, self._xi,
+                                                            self._stage, self._dfront, self._g0))
+        return fields + int(out.value)
 
     def invalidate(self):
         """call after writing rho / m / xi directly: the next step recomputes the CFL max speed"""

@@ -1,0 +1,153 @@
+"""The drop-in constructed the way the reference's callers construct theirs, and driven by the
+reference caller's own loop.
+
+bake.py builds a reference `Sim` from a preset (bake.py:59), runs its stirring phase, replaces the
+stars with the preview's list, replays the live events into P at their times, writes a frame at
+each frame time after update_render_fields(force=True), and lands the steps on the frame times
+with dt_cap (bake.py:67-114).  tests/golden/bake_bipolar.npz holds a reference `Sim` as its
+constructor left it (bipolar preset, the default matched initial conditions, fast=False budgets)
+and the frames the reference wrote running that loop.  Here a stand-in object carrying exactly the
+attributes and get_state_meta() of that reference `Sim` is handed to `Sim.from_reference`, and the
+same loop runs on the drop-in; its frames must match the reference's within the path's tolerances.
+"""
+import json
+import os
+import types
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def S():
+    from nebulaviewer_gb300 import build
+    build.build(verbose=False)
+    from nebulaviewer_gb300 import sim
+    assert torch.cuda.is_available(), "the gpu tests need a CUDA device"
+    return sim
+
+
+@pytest.fixture(scope="module")
+def bake():
+    d = np.load(os.path.join(GOLDEN, "bake_bipolar.npz"))
+    return d, json.loads(str(d["meta"]))
+
+
+class _Field:
+    """an array with the .numpy() of a Warp array"""
+
+    def __init__(self, a):
+        self.a = a
+        self.shape = a.shape
+
+    def numpy(self):
+        return self.a.copy()
+
+
+def reference_standin(d, m):
+    """an object with the attributes and get_state_meta() of the reference Sim in the fixture"""
+    meta = dict(m["meta"])
+    meta["drv"] = None if m["drv_clock"] is None else {
+        "A": [_Field(c) for c in d["s_drv_A"]], "B": [_Field(c) for c in d["s_drv_B"]], "clock": m["drv_clock"]}
+    noise = None if m["noise"] is None else types.SimpleNamespace(**m["noise"])
+    return types.SimpleNamespace(
+        scenario=m["scenario"], res=m["res"], shape=tuple(m["shape"]), dx=m["dx"], fast=m["fast"], ic_mode=m["ic_mode"],
+        phase=m["phase"], rfront=types.SimpleNamespace(shape=tuple(m["rfront_shape"])),
+        att=types.SimpleNamespace(shape=tuple(m["att_shape"])), ion_every=m["ion_every"], fuv_every=m["fuv_every"],
+        sshape=tuple(m["sshape"]), dxs=m["dxs"], stars=[tuple(s) for s in m["stars"]], kinds=m["kinds"],
+        jets=[tuple(j) for j in m["jets"]], jkinds=m["jkinds"], P=dict(m["P"]), events=[tuple(e) for e in m["events"]],
+        version=m["version"], rf_version=m["rf_version"], fuv_version=m["fuv_version"], fuv_nstars=m["fuv_nstars"],
+        fuv_phase=m["fuv_phase"], dt_cap=m["dt_cap"], noise=noise,
+        torus0=d["s_torus0"] if "s_torus0" in d.files else None,
+        **{k: _Field(d[f"s_{k}"]) for k in ("rho", "mx", "my", "mz", "xi", "dfront", "g0")},
+        get_state_meta=lambda: dict(meta))
+
+
+def run_bake_loop(sim, b):
+    """bake.py:67-114 on a Sim-like object: stirring phase, replace_stars, events, frames, dt_cap"""
+    sim.P["trigger"] = 0.0
+    while sim.phase == "pre":
+        sim.step(1)
+    pre_steps = sim.ip
+    sim.replace_stars(b["stars"], b["kinds"], b["jets"], b["jkinds"])
+    events = b["events"]
+    dt_frame = b["t_end"] / max(b["frames"] - 1, 1)
+    next_frame, frame, ev_i, frames, times = 0.0, 0, 0, [], []
+    while True:
+        while ev_i < len(events) and events[ev_i][0] <= sim.t + 1e-12:
+            _, name, val = events[ev_i]
+            sim.P[name] = val
+            sim._wkey = None
+            ev_i += 1
+        if sim.t >= next_frame - 1e-9:
+            sim.update_render_fields(force=True)
+            frames.append(dict(g0=np.minimum(sim.g0.numpy(), 6e4).astype(np.float16),
+                               rho=sim.rho.numpy().astype(np.float16),
+                               xi=np.round(np.clip(sim.xi.numpy(), 0, 1) * 255).astype(np.uint8),
+                               df=np.clip(sim.dfront.numpy(), -4, 4).astype(np.float16),
+                               sh=np.minimum(sim.shock.numpy(), 6e4).astype(np.float16),
+                               device=sim.frame()))
+            times.append(sim.t)
+            frame += 1
+            next_frame += dt_frame
+            if frame >= b["frames"]:
+                break
+        sim.dt_cap = next_frame - sim.t + 1e-7
+        sim.step(1)
+    return frames, times, pre_steps
+
+
+def _f16_close(a, b, ulps, slack=0.0):
+    a, b = a.astype(np.float32), b.astype(np.float32)
+    return np.all(np.abs(a - b) <= ulps * np.abs(b) * 2.0 ** -10 + slack)
+
+
+def test_preset_names_point_to_from_reference(S):
+    with pytest.raises(ValueError, match="from_reference"):
+        S.Sim("bipolar", res=8)
+
+
+@pytest.mark.parametrize("arith", ("exact", "fast"))
+def test_bake_loop_through_the_dropin_matches_the_reference(S, bake, arith):
+    d, m = bake
+    ref = reference_standin(d, m)
+    sim = S.Sim.from_reference(ref, arith=arith)
+    # the hand-over itself: fields, clocks, phase, budgets, the stirring state
+    assert sim.phase == m["phase"] == "pre" and sim.shape == tuple(m["shape"])
+    assert sim.rfront.shape == tuple(m["rfront_shape"]) and sim.att.shape == tuple(m["att_shape"])
+    assert sim.ion_every == m["ion_every"] and sim.fuv_every == m["fuv_every"]
+    assert np.array_equal(sim.rho.numpy(), d["s_rho"]) and np.array_equal(sim.dfront.numpy(), d["s_dfront"])
+    assert sim.noise == {"seed": m["noise"]["seed"], "calls": m["noise"]["calls"], "modes": m["noise"]["K"]}
+    drv = sim.drv
+    assert np.array_equal(np.stack(drv["A"]), d["s_drv_A"]) and np.array_equal(np.stack(drv["B"]), d["s_drv_B"])
+    b = m["bake"]
+    frames, times, pre_steps = run_bake_loop(sim, b)
+    assert pre_steps == b["pre_steps"] and sim.it == b["steps"]
+    assert np.allclose(times, b["times"], rtol=1e-6, atol=1e-9)
+    assert abs(sim.mach - b["mach"]) <= 1e-5 * b["mach"]
+    n = frames[0]["rho"].size
+    for k, f in enumerate(frames):
+        ref_f = {x: d[f"f{k}_{x}"] for x in ("g0", "rho", "xi", "df", "sh")}
+        assert _f16_close(f["rho"], ref_f["rho"], 1), k
+        # xi as uint8: within one level, the ionized mask identical but for <= 0.1% of the cells
+        dxi = np.abs(f["xi"].astype(int) - ref_f["xi"].astype(int))
+        assert dxi.max() <= 1 or np.mean(dxi > 1) <= 1e-3, (k, dxi.max())
+        assert np.mean((f["xi"] > 127) != (ref_f["xi"] > 127)) <= 1e-3, k
+        assert _f16_close(f["df"], ref_f["df"], 2, slack=1e-5 * 4.0), k
+        g, gr = f["g0"].astype(np.float32), ref_f["g0"].astype(np.float32)
+        assert np.abs(g - gr).max() <= 2e-3 * np.abs(gr).max(), k
+        sh, shr = f["sh"].astype(np.float32), ref_f["sh"].astype(np.float32)
+        assert np.abs(sh - shr).max() <= 1e-3 * max(np.abs(shr).max(), 1e-30), k
+        # the device-quantized frame (Sim.frame) is byte-identical to the host expressions
+        dev = f["device"]
+        for x in ("g0", "rho", "df", "sh"):
+            assert np.array_equal(dev[x].view(np.uint16), f[x].view(np.uint16)), (k, x)
+        # rounding of xi * 255: the device rounds half to even as np.round does
+        assert np.array_equal(dev["xi"], f["xi"]), k
+        assert dev["rho"].size == n
+    sim.close()

@@ -407,6 +407,52 @@ def test_front_culling_changes_no_bit(nb, arith, case):
 
 
 @pytest.mark.parametrize("arith", ARITH)
+def test_pair_tables_change_no_bit(nb, arith):
+    """the front and attenuation tables stored as neighbour pairs (one 8-byte gather for two
+    corners) give the same xi, front distance and G0, bit for bit, as the plain tables: a 12-star
+    sheet (cells next to a star, where a corner index clamps below 0, included) and the batched
+    ionization of two instances"""
+    from nebulaviewer_gb300 import autotune as at, ics
+    from nebulaviewer_gb300.batch import BatchSim
+    _, S = nb
+
+    def sheet(res, seed):
+        ic = ics.sheet(res=res, nstars=12, seed=seed)
+        s = S.Sim.from_state(ic["shape"], ic["dx"], ic["rho"], ic["stars"], ic["kinds"], ic["jets"], ic["jkinds"],
+                             ic["P"], mom=ic["mom"], rays=(128, 256), fuv_grid=(32, 32, 64), arith=arith)
+        s.step(4)
+        return s
+
+    sim = sheet(128, 2)
+    out = {}
+    for pairs in (0, 1):
+        at.put(sim, "front_pairs", pairs)
+        at.put(sim, "fuv_pairs", pairs)
+        xi, df = _front_fields(sim)
+        sim.update_render_fields(force=True)
+        torch.cuda.synchronize()
+        out[pairs] = (xi, df, sim._g0.clone().view(torch.int16))
+    assert at.get(sim, "front_pairs") == 1 and at.get(sim, "fuv_pairs") == 1
+    for a, b in zip(out[0], out[1]):
+        assert torch.equal(a, b)
+    sim.close()
+    # the batched ionization reads and writes the same layouts
+    res = {}
+    for pairs in (0, 1):
+        sims = [sheet(64, 3), sheet(48, 4)]
+        for s in sims:
+            at.put(s, "front_pairs", pairs)
+        B = BatchSim(sims, graphs=False)
+        B.step(3)                                   # it = 4, 5, 6: the third step ionizes (ion_every 3)
+        res[pairs] = [(s._xi.clone().view(torch.int32), s._rho.clone().view(torch.int32)) for s in sims]
+        B.close()
+        for s in sims:
+            s.close()
+    for (x0, r0), (x1, r1) in zip(res[0], res[1]):
+        assert torch.equal(x0, x1) and torch.equal(r0, r1)
+
+
+@pytest.mark.parametrize("arith", ARITH)
 def test_fuv_cut_changes_no_bit(nb, arith):
     """a FUV ray that stops once its optical depth passes the cut (exp(-tau) is 0.0f from there
     on) leaves the same attenuation bins and the same G0, bit for bit, as marching to the edge;

@@ -102,5 +102,5 @@ def test_timeline_capture_restore_branch(S):
     assert outs[0][3] == outs[1][3]
     tl.truncate_after(tau)
     assert all(x <= tau + 1e-12 for x in tl.taus())
-    assert "frames" in tl.status()
+    assert "snapshots" in tl.status()
     s.close()

@@ -165,6 +165,22 @@ def test_forcing_generator_reproduces_reference_draws(tag, shape, kmax):
     assert np.array_equal(g.standard_normal(4), z[f"sol_{tag}_next"])
 
 
+def test_matched_forcing_reproduces_reference_fields():
+    """the reference's default "matched" mode draws its forcing fields from a per-call seeded
+    spectrum (sim.py:270-337); the reference Sim of the bake fixture drew A and B that way right
+    after its initial conditions (one call) -- three calls per field, so A used calls 2-4 and B 5-7"""
+    import json
+    from conftest import golden
+    from nebulaviewer_gb300 import stir
+    z = golden("bake_bipolar.npz")
+    m = json.loads(str(z["meta"]))
+    seed, calls, kmax = m["noise"]["seed"], m["noise"]["calls"], float(m["P"]["pre_kmax"])
+    shape = tuple(m["sshape"])
+    a = np.stack(stir.matched_solenoidal(shape, seed, calls - 6, 1.0, kmax, m["noise"]["K"]))
+    b = np.stack(stir.matched_solenoidal(shape, seed, calls - 3, 1.0, kmax, m["noise"]["K"]))
+    assert bits_equal(a, z["s_drv_A"]) and bits_equal(b, z["s_drv_B"])
+
+
 def test_forcing_grid_rules():
     """sim.py:761-768: 24 cells per unit + 2 (resolution independent), or one per 6 cells + 2"""
     from nebulaviewer_gb300 import stir
