@@ -589,7 +589,7 @@ def served_result(args, requests):
         del ic
     torch.cuda.synchronize(dev)
     reqs = serve.poisson_requests(snaps, requests, rate=args.rate, seed=1)
-    srv = serve.Server(snaps, budget_bytes=150e9, bytes_per_cell=48, max_slots=64)
+    srv = serve.Server(snaps, budget_bytes=150e9, max_slots=64)
     clk = ClockSampler(0).start()
     with clk:
         stats, done = srv.run(reqs, realtime=True)
@@ -597,7 +597,9 @@ def served_result(args, requests):
            "n_gpus": 1, "higher_is_better": True, "dtype": "f32", "data": "synthetic",
            "p50_ms": stats["p50_ms"], "p99_ms": stats["p99_ms"],
            "config": {"workload": f"{requests} requests, Poisson {args.rate:g}/s, snapshots 96^3/160^3/256^3/320^3, "
-                                  "+-50% on a star's Q or the wind, 10-100 steps, 150 GB budget at 48 B/cell"},
+                                  "+-50% on a star's Q or the wind, 10-100 steps, 150 GB budget charging each pooled "
+                                  "instance its device footprint (fields + library scratch)",
+                      "footprint_bytes_per_cell": {f"{s.shape[0]}^3": s.footprint / s.cells for s in snaps}},
            "stats": stats, "clocks": clk.summary(), "arith": snaps[0].arith}
     return res
 
@@ -786,8 +788,10 @@ def added_forms(args):
         d = {k: r[k] for k in keep if k in r}
         d["workload"] = r["config"]["workload"]
         if key == "served":
-            d["requests"] = r["stats"]["requests"]
-            d["wall_s"] = r["stats"]["wall_s"]
+            for k in ("requests", "wall_s", "instances_built", "branches_in_place", "evicted", "batch_rebuilds",
+                      "peak_pool_bytes"):
+                d[k] = r["stats"][k]
+            d["footprint_bytes_per_cell"] = r["config"]["footprint_bytes_per_cell"]
         d["run_s"] = time.perf_counter() - t0
         out[key] = d
     return out

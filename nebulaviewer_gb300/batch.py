@@ -37,6 +37,7 @@ class BatchSim:
             raise _lib.NebulaError(f"nb_batch_create: {_lib.ERRORS.get(rc, rc)}: "
                                    f"{self._lib.nb_batch_last_error(None).decode()}")
         self._b = b
+        self.active = [True] * n
         self.set_option("graphs", 1 if graphs else 0)
         self.prof = {}
 
@@ -50,16 +51,29 @@ class BatchSim:
 
     @property
     def cells(self):
-        return sum(s._n for s in self.sims)
+        """cells of the active instances (those a step advances)"""
+        return sum(s._n for s, a in zip(self.sims, self.active) if a)
+
+    def set_active(self, active):
+        """which instances step (one flag per Sim, in the batch's order): an idle one is left as it
+        is, so instances join and leave the stepping set without rebuilding the batch or its graphs"""
+        flags = [bool(a) for a in active]
+        if len(flags) != len(self.sims):
+            raise ValueError(f"one flag per instance ({len(self.sims)}), not {len(flags)}")
+        arr = (C.c_int * len(flags))(*[int(a) for a in flags])
+        self._chk(self._lib.nb_batch_set_active(self._b, arr, len(flags)), "nb_batch_set_active")
+        self.active = flags
 
     def step(self, k=1, sync=True):
-        """advance every instance k steps (the live parameters / stars of each Sim are pushed first)"""
+        """advance every active instance k steps (the live parameters / stars of each Sim are pushed
+        first)"""
         t0 = time.perf_counter()
-        for s in self.sims:
+        live = [s for s, a in zip(self.sims, self.active) if a]
+        for s in live:
             s._push()
             s._clock_fresh = False               # the batch advances the clocks: read them from the device
         self._chk(self._lib.nb_batch_step(self._b, int(k)), "nb_batch_step")
-        for s in self.sims:
+        for s in live:
             s._it += int(k)
             s.version += int(k)
         if sync:

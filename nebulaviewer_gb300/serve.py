@@ -2,13 +2,21 @@
 
 A request branches from a device snapshot of an instance (the state the reference keeps in
 its timeline, timeline.py:95-203, restored through Sim.set_state_meta, sim.py:1185-1211,
-then advanced as viewer.py's branch-and-play does), changes one star's photon rate or the
-wind by a factor, and runs a number of steps.  The server admits queued requests whenever a
-slot and HBM (under a byte budget at a stated cost per cell) are free, advances every admitted
-request together in one batch (BatchSim: persistent kernels, CUDA graphs) one step per tick,
-retires finished requests at once and admits new ones at the next tick, so work that arrives
-while others run overlaps with them on the device.  Each request's result is bit-identical to
-running it alone.
+then advanced as viewer.py's branch-and-play does, viewer.py:257-266), changes one star's
+photon rate or the wind by a factor, and runs a number of steps.
+
+The server keeps a pool of instances.  A request for a snapshot takes an idle instance built
+from that snapshot if there is one and branches into it by device copies (no allocation);
+otherwise a new instance is built, if its true device footprint -- its fields and the
+library's scratch for it (nb_instance_bytes: ray and FUV tables sized for its stars, tensor
+maps, ...) -- fits the HBM budget next to every instance already pooled, busy or idle; idle
+instances of other snapshots are closed first, least recently used first, when that makes
+room.  All pooled instances live in one BatchSim (persistent kernels, CUDA graphs): a request
+joins the stepping set when it is admitted and leaves it when it has run its steps, through
+the batch's slot flags, so admissions and retirements rebuild nothing; the batch and its
+graphs are rebuilt only when the pool itself changes.  Every tick advances all busy instances
+one step together, so work that arrives while others run overlaps with them on the device.
+Each request's result is the same as running it alone (bit-identical with the exact build).
 """
 import collections
 import time
@@ -16,7 +24,7 @@ import time
 import numpy as np
 
 from .batch import BatchSim
-from .sim import Sim
+from .sim import Sim, footprint_bytes
 
 
 class Snapshot:
@@ -31,6 +39,9 @@ class Snapshot:
         self.ion_every, self.fast, self.arith = sim.ion_every, sim.fast, sim.arith
         self.torus = sim.torus0 if sim.phase == "pre" else None          # joins when the stirring phase ends
         self.stir_grid = (sim.sshape, sim.dxs)
+        # device bytes of an instance branched from this snapshot, known before it is built
+        self.footprint = footprint_bytes(self.shape, self.dx, self.meta["P"], self.rays, self.fuv, self.fast,
+                                         len(self.meta["stars"]), self.arith)
 
     @property
     def cells(self):
@@ -44,10 +55,23 @@ class Snapshot:
                            mom=[f["mx"], f["my"], f["mz"]], rays=self.rays, fuv_grid=self.fuv,
                            ion_every=self.ion_every, fast=self.fast, device=self.device, start_main=False,
                            torus=self.torus, stir_grid=self.stir_grid, arith=self.arith)
-        s._xi.copy_(f["xi"])
-        s._dfront.copy_(f["dfront"])
-        s._g0.copy_(f["g0"])
-        s.set_state_meta(m)
+        self._resume(s, mod)
+        return s
+
+    def branch_into(self, sim, mod=None):
+        """resume this snapshot in `sim`, an instance built from it before (Snapshot.branch) and
+        since used for another request: device copies of the fields and the state meta, no
+        allocation -- the same state a fresh branch starts from"""
+        if tuple(sim.shape) != tuple(self.shape) or len(sim.stars) != len(self.meta["stars"]):
+            raise ValueError("branch_into needs an instance built from this snapshot")
+        sim.events = []
+        self._resume(sim, mod)
+        return sim
+
+    def _resume(self, s, mod):
+        for k in ("rho", "mx", "my", "mz", "xi", "dfront", "g0"):
+            getattr(s, "_" + k).copy_(self.fields[k])
+        s.set_state_meta(self.meta)
         if mod is not None:
             if mod[0] == "q":
                 i, fac = int(mod[1]), float(mod[2])
@@ -58,7 +82,6 @@ class Snapshot:
                 s.set_param("wind", s.P["wind"] * float(mod[1]))
             else:
                 raise ValueError(f"unknown modification {mod!r}")
-        return s
 
 
 class Request:
@@ -100,20 +123,30 @@ def result_of(sim):
                 state=[t.clone() for t in (sim._rho, sim._mx, sim._my, sim._mz, sim._xi)])
 
 
-class Server:
-    """Continuous batching under an HBM budget."""
+class _Slot:
+    """a pooled instance: the snapshot it was built from, the request it serves (None: idle), and
+    the tick it was last released at"""
 
-    def __init__(self, snapshots, budget_bytes=150e9, bytes_per_cell=48, max_slots=64, keep_state=False):
+    def __init__(self, snap, sim, nbytes):
+        self.snap, self.sim, self.nbytes = snap, sim, nbytes
+        self.req = None
+        self.last = -1
+
+
+class Server:
+    """Continuous batching over a pool of instances under an HBM budget (see the module text)."""
+
+    def __init__(self, snapshots, budget_bytes=150e9, max_slots=64, keep_state=False):
         self.snaps = snapshots
         self.budget = float(budget_bytes)
-        self.bpc = float(bytes_per_cell)
         self.max_slots = int(max_slots)
         self.keep_state = keep_state
         self.ticks = 0
         self.rebuilds = 0
-
-    def _cost(self, req):
-        return self.snaps[req.snap].cells * self.bpc
+        self.built = 0               # instances built
+        self.reused = 0              # requests branched into a pooled instance
+        self.evicted = 0             # idle instances closed to make room
+        self.peak_bytes = 0
 
     def run(self, requests, realtime=True):
         """serve `requests` (in arrival order; realtime=False admits each as soon as it fits);
@@ -121,78 +154,110 @@ class Server:
         batch still open is closed before it propagates."""
         pending = collections.deque(sorted(requests, key=lambda r: r.t_arrive))
         queue = collections.deque()
-        active, done = [], []
-        used = 0.0
+        pool, done = [], []
         batch = None
+        dirty = False                # the pool changed since the batch was built
         t0 = time.perf_counter()
         cell_steps = 0
 
-        def finish(r):                       # the result, then the instance is closed whatever happens
-            try:
-                r.result = result_of(r.sim)
-                if not self.keep_state:
-                    r.result.pop("state")
-            finally:
-                r.sim.close()
-                r.sim = None
+        def pool_bytes():
+            return sum(p.nbytes for p in pool)
+
+        def finish(slot):            # the result; the instance stays in the pool, idle
+            r = slot.req
+            r.result = result_of(slot.sim)
+            if not self.keep_state:
+                r.result.pop("state")
+            r.sim = None
             r.t_done = time.perf_counter() - t0
             done.append(r)
+            slot.req = None
+            slot.last = self.ticks
+
+        def admit(r):
+            """an instance for r (reused, or built within the budget); False when r must wait"""
+            nonlocal dirty
+            snap = self.snaps[r.snap]
+            idle = [p for p in pool if p.req is None and p.snap == r.snap]
+            if idle:
+                slot = max(idle, key=lambda p: p.last)
+                snap.branch_into(slot.sim, r.mod)
+                self.reused += 1
+            else:
+                cost = snap.footprint
+                others = sorted((p for p in pool if p.req is None), key=lambda p: p.last)
+                if pool_bytes() + cost > self.budget and pool_bytes() - sum(p.nbytes for p in others) + cost > self.budget:
+                    return False                     # even closing every idle instance makes no room
+                while pool_bytes() + cost > self.budget:
+                    p = others.pop(0)                # least recently used idle instance
+                    pool.remove(p)
+                    p.sim.close()
+                    self.evicted += 1
+                    dirty = True
+                sim = snap.branch(r.mod)
+                slot = _Slot(r.snap, sim, sim.footprint())
+                pool.append(slot)
+                self.built += 1
+                dirty = True
+                if slot.nbytes > cost:
+                    raise RuntimeError(f"an instance holds {slot.nbytes} bytes, more than the {cost} it was admitted for")
+            slot.req = r
+            r.sim = slot.sim
+            r.t_admit = time.perf_counter() - t0
+            self.peak_bytes = max(self.peak_bytes, pool_bytes())
+            return slot
 
         try:
-            while pending or queue or active:
+            while pending or queue or any(p.req is not None for p in pool):
                 now = time.perf_counter() - t0
                 while pending and (pending[0].t_arrive <= now or not realtime):
                     queue.append(pending.popleft())
-                changed = False
-                while queue and len(active) < self.max_slots and used + self._cost(queue[0]) <= self.budget:
-                    r = queue.popleft()
-                    r.sim = self.snaps[r.snap].branch(r.mod)
-                    r.t_admit = time.perf_counter() - t0
-                    if r.left == 0:                    # nothing to run: the branched state is the result
-                        finish(r)
-                        continue
-                    used += self._cost(r)
-                    active.append(r)
-                    changed = True
-                if queue and not active:
+                while queue and sum(p.req is not None for p in pool) < self.max_slots:
+                    slot = admit(queue[0])
+                    if not slot:
+                        break
+                    queue.popleft()
+                    if slot.req.left == 0:             # nothing to run: the branched state is the result
+                        finish(slot)
+                busy = [p for p in pool if p.req is not None]
+                if queue and not busy:
                     raise RuntimeError("a request does not fit the HBM budget on its own")
-                if not active:
+                if not busy:
                     if pending:
                         time.sleep(max(0.0, min(pending[0].t_arrive - now, 0.01)))
                     continue
-                if changed or batch is None:
+                if dirty or batch is None:
                     if batch is not None:
                         batch.close()
                         batch = None
-                    batch = BatchSim([r.sim for r in active])
+                    batch = BatchSim([p.sim for p in pool])
+                    batch_pool = list(pool)
                     self.rebuilds += 1
-                batch.step(1)                          # one tick: every active request advances one step
+                    dirty = False
+                flags = [p.req is not None for p in batch_pool]
+                if flags != list(batch.active):
+                    batch.set_active(flags)
+                batch.step(1)                          # one tick: every busy instance advances one step
                 self.ticks += 1
-                fin = []
-                for r in active:
-                    r.left -= 1
-                    cell_steps += r.sim._n
-                    if r.left == 0:
-                        fin.append(r)
-                if fin:
-                    batch.close()
-                    batch = None
-                    for r in fin:
-                        active.remove(r)
-                        used -= self._cost(r)
-                        finish(r)
+                for p in busy:
+                    p.req.left -= 1
+                    cell_steps += p.sim._n
+                    if p.req.left == 0:
+                        finish(p)
         finally:
             if batch is not None:
                 batch.close()
-            for r in active:
-                if r.sim is not None:
-                    r.sim.close()
-                    r.sim = None
+            for p in pool:
+                if p.req is not None:
+                    p.req.sim = None
+                p.sim.close()
         wall = time.perf_counter() - t0
         lat = np.array([r.t_done - r.t_arrive for r in done])
         pct = (lambda q: float(np.percentile(lat, q) * 1e3)) if len(lat) else (lambda q: None)
         return dict(requests=len(done), wall_s=wall, cell_steps=cell_steps, gcells_per_s=cell_steps / wall / 1e9,
-                    p50_ms=pct(50), p99_ms=pct(99), ticks=self.ticks, batch_rebuilds=self.rebuilds), done
+                    p50_ms=pct(50), p99_ms=pct(99), ticks=self.ticks, batch_rebuilds=self.rebuilds,
+                    instances_built=self.built, branches_in_place=self.reused, evicted=self.evicted,
+                    peak_pool_bytes=self.peak_bytes, budget_bytes=self.budget), done
 
 
 def run_alone(snapshot, req):

@@ -107,3 +107,55 @@ def test_batch_instances_remain_usable_alone(nb):
     b[0].update_render_fields(force=True)
     assert torch.equal(a[0]._g0, b[0]._g0)
     B.close()
+
+
+@pytest.mark.parametrize("graphs", (True, False))
+def test_idle_slots_are_left_untouched(nb, graphs):
+    """a batch whose slots go idle and active again (nb_batch_set_active, as the server's pool does):
+    an idle instance keeps every bit of its state and clock; an active one ends exactly where
+    stepping it alone ends, across ionizing steps where only some active instances ionize"""
+    batch, ics, S = nb
+    ics_list = scenes(ics)
+    ie = [2, 3, 5, 1]
+    sims = [make(S, ic, e, "exact") for ic, e in zip(ics_list, ie)]
+    alone = [make(S, ic, e, "exact") for ic, e in zip(ics_list, ie)]
+    B = batch.BatchSim(sims, graphs=graphs)
+    plan = [([1, 0, 1, 1], 3), ([0, 1, 0, 1], 2), ([1, 1, 1, 1], 2), ([0, 0, 0, 0], 1), ([0, 0, 1, 0], 4)]
+    for flags, k in plan:
+        before = [state(s) for s in sims]
+        B.set_active(flags)
+        B.step(k)
+        for s, a, f, prev in zip(sims, alone, flags, before):
+            if f:
+                a.step(k)
+                same(state(s), state(a))
+            else:
+                same(state(s), prev)
+    assert B.cells == sims[2]._n
+    B.close()
+    for s in sims + alone:
+        s.close()
+
+
+def test_footprint_is_known_before_allocation_and_matches_the_device(nb):
+    """Sim.footprint (fields + nb_instance_bytes of the live handle) equals the estimate made from the
+    description alone before anything is allocated, and the device memory the instance takes"""
+    _, ics, S = nb
+    from nebulaviewer_gb300.sim import footprint_bytes
+    ic = ics.sheet(res=160, nstars=6, seed=8, device="cuda")
+    P = dict(ic["P"])
+    from nebulaviewer_gb300.params import make_params
+    est = footprint_bytes(ic["shape"], ic["dx"], make_params(base=P), (512, 1024), (128, 128, 256), True, 6)
+    torch.cuda.synchronize()
+    torch.cuda.empty_cache()
+    free0 = torch.cuda.mem_get_info()[0]
+    s = S.Sim.from_state(ic["shape"], ic["dx"], ic["rho"], ic["stars"], ic["kinds"], ic["jets"], ic["jkinds"], P,
+                         mom=ic["mom"])
+    torch.cuda.synchronize()
+    torch.cuda.empty_cache()
+    used = free0 - torch.cuda.mem_get_info()[0]
+    fp = s.footprint()
+    assert fp == est
+    assert abs(used - fp) <= 0.03 * fp + (32 << 20), (used, fp)
+    assert fp > 40 * s._n + 100e6                     # the FUV and front tables are most of it here
+    s.close()

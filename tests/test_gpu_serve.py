@@ -33,16 +33,20 @@ def _close(a, b, exact):
     return float((a - b).abs().max()) <= 1e-5 * max(float(b.abs().max()), 1e-30)
 
 
-@pytest.mark.parametrize("slots,budget_cells", ((3, None), (8, 2 * 32 * 40 * 24)))
-def test_served_results_equal_alone(env, slots, budget_cells):
+@pytest.mark.parametrize("slots,tight", ((3, False), (8, True)))
+def test_served_results_equal_alone(env, slots, tight):
+    """8 requests over two snapshots: with 3 slots the pool's instances are branched into again by
+    later requests; with a budget of one and a half instances (the two snapshots' instances are of
+    about the same size), an idle instance is closed whenever the other snapshot needs room"""
     serve, snaps = env
     exact = snaps[0].arith == "exact"
     reqs = serve.poisson_requests(snaps, 8, rate=1000.0, seed=slots, steps=(3, 9))
-    budget = 1e12 if budget_cells is None else 48.0 * budget_cells
+    budget = max(s.footprint for s in snaps) * 1.5 if tight else 1e12
     srv = serve.Server(snaps, budget_bytes=budget, max_slots=slots, keep_state=True)
     stats, done = srv.run(reqs, realtime=False)
     assert stats["requests"] == 8 and stats["ticks"] >= max(r.nsteps for r in done)
-    assert stats["batch_rebuilds"] > 1                    # admissions happened while others ran
+    assert stats["peak_pool_bytes"] <= budget
+    assert stats["branches_in_place"] > 0 if not tight else stats["evicted"] > 0
     for r in done:
         ref = serve.run_alone(snaps[r.snap], r)
         assert r.result["it"] == ref["it"]
@@ -60,4 +64,17 @@ def test_snapshot_branch_resumes_the_state(env):
     s = snaps[0].branch()
     assert torch.equal(s._rho, snaps[0].fields["rho"]) and torch.equal(s._xi, snaps[0].fields["xi"])
     assert s.it == snaps[0].meta["it"] and s.t == snaps[0].meta["t"]
+    assert s.footprint() == snaps[0].footprint
+    # a used instance branched into again starts from the same state as a fresh branch
+    mod = ("q", 1, 1.5)
+    s.step(5)
+    snaps[0].branch_into(s, mod)
+    f = snaps[0].branch(mod)
+    for k in ("rho", "mx", "xi", "dfront", "g0"):
+        assert torch.equal(getattr(s, "_" + k), getattr(f, "_" + k))
+    assert s.it == f.it and s.t == f.t and s.stars == f.stars
+    s.step(4)
+    f.step(4)
+    assert torch.equal(s._rho, f._rho) and torch.equal(s._xi, f._xi)
     s.close()
+    f.close()

@@ -1,51 +1,74 @@
 """The serving scheduler's host logic (serve.Server.run) on fake instances: admission under the
-slot and HBM limits, every request stepped exactly its step count, zero-step requests, and every
-instance and batch closed when a batch step fails.  No GPU: BatchSim and the results are faked."""
+slot limit and under the HBM budget counted with every pooled instance's true footprint (busy or
+idle), instances reused for later requests of the same snapshot, idle instances of other
+snapshots closed (least recently used first) to make room, every request stepped exactly its step
+count, zero-step requests, and every instance and batch closed when a batch step fails.  No GPU:
+BatchSim and the results are faked."""
 import pytest
 
 serve = pytest.importorskip("nebulaviewer_gb300.serve")
 
 
 class FakeSim:
-    def __init__(self, cells):
+    def __init__(self, cells, nbytes):
         self._n = cells
+        self.nbytes = nbytes
         self.steps = 0
         self.closed = False
+
+    def footprint(self):
+        return self.nbytes
 
     def close(self):
         self.closed = True
 
 
 class FakeSnap:
-    def __init__(self, cells):
+    def __init__(self, cells, nbytes=None):
         self.cells = cells
+        self.footprint = nbytes if nbytes is not None else 40 * cells + 1000     # fields + some scratch
         self.made = []
+        self.branched_into = 0
 
     def branch(self, mod):
-        s = FakeSim(self.cells)
+        s = FakeSim(self.cells, self.footprint)
         self.made.append(s)
         return s
 
+    def branch_into(self, sim, mod):
+        assert sim in self.made and not sim.closed
+        sim.steps = 0                      # the snapshot's state again
+        self.branched_into += 1
+        return sim
 
-def install(monkeypatch, max_slots=None, budget_cells=None, fail_on_tick=None):
-    log = {"batches": [], "ticks": 0}
+
+def install(monkeypatch, max_slots=None, budget=None, fail_on_tick=None):
+    log = {"batches": [], "ticks": 0, "peak": 0}
 
     class FakeBatch:
         def __init__(self, sims):
             assert all(not s.closed for s in sims)
-            if max_slots is not None:
-                assert len(sims) <= max_slots
-            if budget_cells is not None:
-                assert sum(s._n for s in sims) <= budget_cells
+            if budget is not None:
+                assert sum(s.footprint() for s in sims) <= budget          # the whole pool, idle ones too
             self.sims = sims
+            self.active = [True] * len(sims)
             self.closed = False
             log["batches"].append(self)
+
+        def set_active(self, flags):
+            assert len(flags) == len(self.sims)
+            self.active = list(flags)
 
         def step(self, k):
             log["ticks"] += 1
             if fail_on_tick is not None and log["ticks"] == fail_on_tick:
                 raise RuntimeError("injected batch-step failure")
-            for s in self.sims:
+            live = [s for s, a in zip(self.sims, self.active) if a]
+            assert live and all(not s.closed for s in live)
+            if max_slots is not None:
+                assert len(live) <= max_slots
+            log["peak"] = max(log["peak"], sum(s.footprint() for s in self.sims))
+            for s in live:
                 s.steps += k
 
         def close(self):
@@ -56,15 +79,17 @@ def install(monkeypatch, max_slots=None, budget_cells=None, fail_on_tick=None):
     return log
 
 
-def requests(snaps, steps):
-    return [serve.Request(i, 0.001 * i, i % len(snaps), None, n) for i, n in enumerate(steps)]
+def requests(snaps, steps, pick=None):
+    pick = pick or (lambda i: i % len(snaps))
+    return [serve.Request(i, 0.001 * i, pick(i), None, n) for i, n in enumerate(steps)]
 
 
 def test_every_request_runs_its_steps_within_slots_and_budget(monkeypatch):
     snaps = [FakeSnap(1000), FakeSnap(3000)]
-    log = install(monkeypatch, max_slots=3, budget_cells=5000)
-    reqs = requests(snaps, [5, 2, 7, 1, 4, 3, 6, 2])
-    srv = serve.Server(snaps, budget_bytes=5000 * 48.0, bytes_per_cell=48, max_slots=3)
+    budget = snaps[0].footprint + 2 * snaps[1].footprint
+    log = install(monkeypatch, max_slots=3, budget=budget)
+    reqs = requests(snaps, [5, 2, 7, 1, 4, 3, 6, 2, 5, 3])
+    srv = serve.Server(snaps, budget_bytes=budget, max_slots=3)
     stats, done = srv.run(reqs, realtime=False)
     assert stats["requests"] == len(reqs) and len(done) == len(reqs)
     assert sorted(r.rid for r in done) == list(range(len(reqs)))
@@ -74,6 +99,29 @@ def test_every_request_runs_its_steps_within_slots_and_budget(monkeypatch):
     assert all(b.closed for b in log["batches"])
     assert stats["cell_steps"] == sum(r.nsteps * snaps[r.snap].cells for r in reqs)
     assert stats["p50_ms"] is not None and stats["p99_ms"] >= stats["p50_ms"]
+    assert stats["peak_pool_bytes"] <= budget and log["peak"] <= budget
+
+
+def test_instances_are_reused_and_the_batch_is_not_rebuilt_per_admission(monkeypatch):
+    snaps = [FakeSnap(500)]
+    log = install(monkeypatch, max_slots=2)
+    reqs = requests(snaps, [3, 3, 4, 2, 5, 1, 3, 2])
+    stats, done = serve.Server(snaps, max_slots=2).run(reqs, realtime=False)
+    assert stats["requests"] == 8 and stats["instances_built"] == 2 == len(snaps[0].made)
+    assert stats["branches_in_place"] == 6 == snaps[0].branched_into
+    assert stats["batch_rebuilds"] == len(log["batches"]) <= 2          # only when the pool grew
+    assert {r.rid: r.result["it"] for r in done} == {r.rid: r.nsteps for r in reqs}
+
+
+def test_idle_instances_of_other_snapshots_make_room(monkeypatch):
+    snaps = [FakeSnap(1000), FakeSnap(2000)]
+    budget = snaps[1].footprint + 10                 # one instance at a time
+    log = install(monkeypatch, budget=budget)
+    reqs = requests(snaps, [3, 2, 4, 1, 2])          # snapshots 0, 1, 0, 1, 0
+    stats, done = serve.Server(snaps, budget_bytes=budget).run(reqs, realtime=False)
+    assert stats["requests"] == 5 and stats["evicted"] == 4 and stats["instances_built"] == 5
+    assert stats["peak_pool_bytes"] <= budget and log["peak"] <= budget
+    assert all(s.closed for sn in snaps for s in sn.made)
 
 
 def test_zero_step_requests_finish_at_admission(monkeypatch):
@@ -105,5 +153,5 @@ def test_a_request_beyond_the_budget_is_refused(monkeypatch):
     snaps = [FakeSnap(100), FakeSnap(10 ** 6)]
     install(monkeypatch)
     with pytest.raises(RuntimeError, match="budget"):
-        serve.Server(snaps, budget_bytes=48.0 * 1000).run(requests(snaps, [2, 2]), realtime=False)
+        serve.Server(snaps, budget_bytes=snaps[0].footprint * 2).run(requests(snaps, [2, 2]), realtime=False)
     assert all(s.closed for sn in snaps for s in sn.made)
