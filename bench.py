@@ -12,7 +12,7 @@ photon rates, winds on, ionization every 3 steps with 512 x 1024 rays (dr = dx),
 
 The step runs on the package's default library build (libnebula_fast.so: FMA contraction,
 approximate division / square root, within the path's tolerance of the exact build); the same
-line reports the exact build (libnebula.so, bit-identical to the reference kernels) on the same
+line reports the exact build (libnebula.so, bit-identical to the reference's kernel source in float32) on the same
 workload under "arith_exact".  --arith picks the build of the headline.
 
 --impl reference times the reference scheme's CPU implementation (the CPU restatement of its
@@ -813,7 +813,7 @@ def main():
     ap.add_argument("--rate", type=float, default=200.0)
     ap.add_argument("--instances", type=int, default=32)
     ap.add_argument("--arith", default=None, choices=["exact", "fast"],
-                    help="library build: exact (bit-identical to the reference kernels) or fast (FMA, approximate "
+                    help="library build: exact (bit-identical to the reference's kernel source in float32) or fast (FMA, approximate "
                          "division / square root); default: the package default")
     args = ap.parse_args()
     if args.warmup < 3:

@@ -5,7 +5,8 @@ Both export the same C ABI (include/nebula.h) and differ only in floating-point 
 generation:
   libnebula.so       exact: no contraction of a*b+c, IEEE division and square root, no
                      flush-to-zero -- every float operation is the reference's, so results are
-                     bit-identical to the reference's kernels;
+                     bit-identical to the reference's kernel source evaluated in
+                     IEEE float32 without contraction;
   libnebula_fast.so  fast: a*b+c contracted to FMA, approximate division and square root,
                      denormals flushed to zero in the compute kernels (the snapshot / frame
                      formats and the renderer's voxel pack keep the exact flags, their bytes
