@@ -24,9 +24,10 @@ Fixtures (all small, committed):
   sim_bipolar_pre.npz  a reference `Sim` run through the pre-turbulence (stirring) phase,
                    its end (torus added, first ionization) and main-phase stirring, with
                    every forcing field the run drew.
-  bake_bipolar.npz bake.py's loop run by the reference on a bipolar scene in the default
-                   matched mode (stirring phase, replace_stars, live events, dt_cap, frames),
-                   with the reference Sim as constructed (what Sim.from_reference reads).
+  bake_<scene>.npz bake.py's loop run by the reference on the bipolar (stirring phase) and
+                   bubbles (main phase, winds, triggered formation switched off) presets in the
+                   default matched mode (replace_stars, live events, dt_cap, frames), with the
+                   reference Sim as constructed (what Sim.from_reference reads).
 Test infrastructure only: nothing in the product reads these files.
 """
 import argparse
@@ -340,6 +341,7 @@ def _json_safe(v):
 def ref_state(sim):
     """everything Sim.from_reference reads from a reference Sim: arrays apart, the rest as JSON"""
     meta = sim.get_state_meta()
+    meta["sm0"] = None          # the triggered-formation reference field: unused with the trigger off
     d = meta.pop("drv")
     arrays = {"rho": sim.rho.numpy(), "mx": sim.mx.numpy(), "my": sim.my.numpy(), "mz": sim.mz.numpy(),
               "xi": sim.xi.numpy(), "dfront": sim.dfront.numpy(), "g0": sim.g0.numpy()}
@@ -362,32 +364,48 @@ def ref_state(sim):
     return arrays, _json_safe(attrs)
 
 
-def bake_case(S, res=8):
-    """bake.py:59-114 run by the reference on a small bipolar scene: Sim(..., fast=False) in the
-    default matched mode (forcing fields from the matched spectrum) with a short stirring phase;
-    the stirring steps; replace_stars with the preview's list plus a later birth; the live events
-    replayed into P at their times; at each frame time update_render_fields(force=True) and the
-    frame expressions of bake.py:95-102; dt_cap landing the steps on the frame times.  Saves the
-    reference Sim as constructed (what Sim.from_reference reads) and every frame."""
-    P = S.make_params("bipolar", dict(pre_t=0.49, pre_corr=0.02, pre_amp=7.0, seed=21, jet_r=0.35, jet_angle=35.0,
-                                      clumps=0))
-    t_end, frames = 0.12, 4
-    sim = S.Sim("bipolar", res=res, params=P, ic_mode="matched", rays=(8, 16), fuv_grid=(6, 8, 16), fast=False,
+BAKE_CASES = {
+    # stirring phase (matched forcing spectrum), jets, a later proto-star birth with a jet
+    "bipolar": dict(overrides=dict(pre_t=0.49, pre_corr=0.02, pre_amp=7.0, seed=21, jet_r=0.35, jet_angle=35.0,
+                                   clumps=0),
+                    t_end=0.12, frames=4, birth=([0.55, 0.45, 0.5], 2.0e-4, 0.03, [0.0, 0.6, 0.8], "proto"),
+                    events=[[0.02, "wind", 0.6], [0.05, "q_main", 1.5], [0.08, "jet", 2.0]]),
+    # straight into the main phase, six stars with winds, the preset's triggered formation on at
+    # construction (bake.py turns it off), a later birth without a jet
+    "bubbles": dict(overrides=dict(seed=5, min_sep=0.2), t_end=0.16, frames=5,
+                    birth=([0.3, 0.6, 0.4], 5.0e-5, 0.05, [0.0, 0.0, 1.0], "none"),
+                    events=[[0.03, "wind", 0.8], [0.09, "q_main", 0.7]]),
+}
+
+
+def bake_case(S, scen="bipolar", res=8):
+    """bake.py:59-114 run by the reference on a small preset scene: Sim(..., fast=False) in the
+    default matched mode (forcing fields from the matched spectrum); the stirring steps if the
+    preset has a stirring phase; replace_stars with the preview's list plus a later birth; the live
+    events replayed into P at their times (q_main as a factor of the preset's); at each frame time
+    update_render_fields(force=True) and the frame expressions of bake.py:95-102; dt_cap landing
+    the steps on the frame times.  Saves the reference Sim as constructed (what
+    Sim.from_reference reads) and every frame."""
+    c = BAKE_CASES[scen]
+    P = S.make_params(scen, c["overrides"])
+    t_end, frames = c["t_end"], c["frames"]
+    sim = S.Sim(scen, res=res, params=P, ic_mode="matched", rays=(8, 16), fuv_grid=(6, 8, 16), fast=False,
                 device="cpu", verbose=False)
     arrays, attrs = ref_state(sim)
-    print(f"  bipolar {sim.shape} phase {sim.phase}, {len(sim.stars)} stars, noise calls {sim.noise.calls}", flush=True)
+    print(f"  {scen} {sim.shape} phase {sim.phase}, {len(sim.stars)} stars, noise calls {sim.noise.calls}", flush=True)
     sim.P["trigger"] = 0.0                                                    # bake.py:61-63
     while sim.phase == "pre":                                                 # bake.py:67-68
         sim.step(1)
     pre_steps = sim.ip
     stars = [list(map(float, x)) for x in sim.stars]
     L = sim.L
-    stars.append([0.55 * L[0], 0.45 * L[1], 0.5 * L[2], 2.0e-4, 0.03])          # a later birth, absolute Q
+    pos, q_abs, t_on, axis, jkind = c["birth"]
+    stars.append([pos[0] * L[0], pos[1] * L[1], pos[2] * L[2], q_abs, t_on])  # a later birth, absolute Q
     kinds = list(sim.kinds) + ["abs"]
-    jets = [list(map(float, j)) for j in sim.jets] + [[0.0, 0.6, 0.8]]
-    jkinds = list(sim.jkinds) + ["proto"]
+    jets = [list(map(float, j)) for j in sim.jets] + [list(axis)]
+    jkinds = list(sim.jkinds) + [jkind]
     sim.replace_stars(stars, kinds, jets, jkinds)                             # bake.py:69
-    events = [[0.02, "wind", 0.6], [0.05, "q_main", float(P["q_main"]) * 1.5], [0.08, "jet", 2.0]]
+    events = [[t, name, float(P["q_main"]) * v if name == "q_main" else v] for t, name, v in c["events"]]
     out = {f"s_{k}": v for k, v in arrays.items()}
     dt_frame = t_end / max(frames - 1, 1)
     next_frame, frame, ev_i, times = 0.0, 0, 0, []
@@ -484,9 +502,10 @@ def main():
                                                             seed=13, jet_r=0.35, jet_angle=35.0, clumps=0),
                  nsteps=14, rays=(8, 16), fuv=(6, 8, 16), ic_mode="nebula3d")   # 6-cell forcing grid
         np.savez_compressed(os.path.join(HERE, "sim_bipolar_pre.npz"), **sim_pre_case(S, **c))
-    if a.only in (None, "bake"):
-        print("bake:", flush=True)
-        np.savez_compressed(os.path.join(HERE, "bake_bipolar.npz"), **bake_case(S))
+    for scen in BAKE_CASES:
+        if a.only in (None, "bake", f"bake_{scen}"):
+            print(f"bake {scen}:", flush=True)
+            np.savez_compressed(os.path.join(HERE, f"bake_{scen}.npz"), **bake_case(S, scen))
     if a.only in (None, "timeline"):
         print("timeline:", flush=True)
         np.savez_compressed(os.path.join(HERE, "timeline.npz"), **timeline_cases(a.ref, np.random.default_rng(99)))
