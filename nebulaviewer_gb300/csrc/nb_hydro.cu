@@ -127,6 +127,23 @@ __device__ __forceinline__ float minmod_p(float a, float b, float ab) {
     if (ab <= 0.0f) return 0.0f;
     return fabsf(a) < fabsf(b) ? a : b;
 }
+
+#if NB_ARITH_FAST
+// min.xorsign.abs: min(|a|, |b|) with the sign sign(a) xor sign(b)
+__device__ __forceinline__ float min_xorsign(float a, float b) {
+    float r;
+    asm("min.xorsign.abs.f32 %0, %1, %2;" : "=f"(r) : "f"(a), "f"(b));
+    return r;
+}
+// minmod in three ALU operations and no product: m = min_xorsign(a, b) is min(|a|, |b|) when a and b
+// have the same sign, <= 0 otherwise; min_xorsign(a, max(m, 0)) puts a's sign on it.  The value is
+// the one minmod_p returns (a or b, the smaller magnitude; ties pick equal values), except that a
+// zero result may be -0 (a < 0, or a zero of either sign) where minmod_p returns +0: -0 and +0
+// give the same reconstruction b + 0.5 s and c - 0.5 s but for an operand of exactly -0.
+__device__ __forceinline__ float minmod_xs(float a, float b) {
+    return min_xorsign(a, fmaxf(min_xorsign(a, b), 0.0f));
+}
+#endif
 #endif  // NB_PAIRED
 
 #if NB_ARITH_FAST
@@ -213,6 +230,10 @@ __device__ __forceinline__ float4 slopes_paired(const float4 qa, const float4 qb
     const F2 d1_0 = sub2(b0, a0), d1_1 = sub2(b1, a1);
     const F2 d2_0 = sub2(c0, b0), d2_1 = sub2(c1, b1);
     if (LM == 0) {
+#if NB_ARITH_FAST
+        return make_float4(minmod_xs(lo(d1_0), lo(d2_0)), minmod_xs(hi(d1_0), hi(d2_0)),
+                           minmod_xs(lo(d1_1), lo(d2_1)), minmod_xs(hi(d1_1), hi(d2_1)));
+#endif
         const F2 p_0 = mul2(d1_0, d2_0), p_1 = mul2(d1_1, d2_1);
         return make_float4(minmod_p(lo(d1_0), lo(d2_0), lo(p_0)), minmod_p(hi(d1_0), hi(d2_0), hi(p_0)),
                            minmod_p(lo(d1_1), lo(d2_1), lo(p_1)), minmod_p(hi(d1_1), hi(d2_1), hi(p_1)));
@@ -354,6 +375,14 @@ __device__ __forceinline__ void hydro_tile(const HydroLaunch& L, int tile, unsig
     // combination, the CFL speed) recomputes it
     constexpr bool CARRY = !STAGE2;
     using SM = HydroSmem<TJ>;
+    {
+        // an opaque zero added to the shared-memory base: the compiler then derives the tiles'
+        // addresses from one register rather than holding several precomputed bases (measured at
+        // 256^3: stage spills 4 -> 0 bytes, stages -3%, the same code otherwise)
+        unsigned zero = 0;
+        asm volatile("" : "+r"(zero));
+        smem += zero;
+    }
     float* raw = reinterpret_cast<float*>(smem);                                   // [5][TJ+4][40]
     float4* prim = reinterpret_cast<float4*>(smem + SM::RAW_BYTES);                // [4][TJ+4][36]
     float2* cs = reinterpret_cast<float2*>(smem + SM::RAW_BYTES + SM::PRIM_BYTES); // [3][TJ+4][36]
