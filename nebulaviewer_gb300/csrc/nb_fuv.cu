@@ -171,13 +171,13 @@ __global__ void __launch_bounds__(256, 6) apply_fuv_kernel(const NbConst* __rest
             int pw[2];
             if (tab) {
                 const float4 tb = tab[s];
-                r = fmaxr(sqrtf(tb.x + rz * rz), 1e-6f);                          // (rx^2 + ry^2) + rz^2
+                r = fmaxq(sqrtf(tb.x + rz * rz), 1e-6f);                          // (rx^2 + ry^2) + rz^2
                 tp = tb.y;
                 pw[0] = __float_as_int(tb.z);
                 pw[1] = __float_as_int(tb.w);
             } else {
                 const float rx = px - sp.x, ry = py - sp.y;
-                r = fmaxr(sqrtf((rx * rx + ry * ry) + rz * rz), 1e-6f);             // 0 + x*x == x*x
+                r = fmaxq(sqrtf((rx * rx + ry * ry) + rz * rz), 1e-6f);             // 0 + x*x == x*x
                 float phi = atan2f(ry, rx);
                 if (phi < 0.0f) phi = phi + two_pi;
                 const float fp = phi / two_pi * (float)nphi - 0.5f;
@@ -230,7 +230,7 @@ __global__ void __launch_bounds__(256, 6) apply_fuv_kernel(const NbConst* __rest
                         const float wgt = (aa == 0 ? 1.0f - tr : tr) * (bb == 0 ? 1.0f - tu : tu) * (cc == 0 ? 1.0f - tp : tp);
                         acc = acc + wgt * v[aa][bb][cc];
                     }
-            const float r2 = fmaxr(r * r, 0.0004f);
+            const float r2 = fmaxq(r * r, 0.0004f);
             term[e] = lum[s] * acc / r2;
           }
 #pragma unroll

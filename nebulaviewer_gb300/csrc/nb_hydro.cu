@@ -16,8 +16,8 @@
 // SM.  A plane is converted once to primitives (rho, u, v, w) and (c^2, c) in shared memory (each
 // thread's own and halo cell, at offsets computed once per tile); every face flux is then
 // evaluated once (the reference evaluates each face twice) and shared through shared memory
-// (y, z faces) or registers (x faces; stage 1 also carries each cell's limited x slope to the
-// next face).  Sources: the wind loop over the active stars in ionized cells, the jet loop over
+// (y, z faces) or registers (x faces; each cell's limited x slope is also carried to the next
+// face).  Sources: the wind loop over the active stars in ionized cells, the jet loop over
 // the tile's list of stars whose jet can reach it.  Cell offsets are 32-bit on grids below 2^31
 // cells.  Stage 2 also reduces the CFL max speed of the new state (nebula3d.py:154-162) into
 // one atomic.
@@ -183,7 +183,7 @@ __device__ __forceinline__ float4 face_flux_scalar_sl(const float4 qb, const flo
         L[c] = comp(qb, c) + 0.5f * comp(sl, c);
         R[c] = comp(qc, c) - 0.5f * comp(sr, c);
     }
-    const float rL = fmaxr(L[0], floor_), rR = fmaxr(R[0], floor_);
+    const float rL = fmaxq(L[0], floor_), rR = fmaxq(R[0], floor_);
     const float unL = 0.0f + L[AX], unR = 0.0f + R[AX];
     const float UL[4] = {rL, rL * L[1], rL * L[2], rL * L[3]};
     const float UR[4] = {rR, rR * R[1], rR * R[2], rR * R[3]};
@@ -195,14 +195,14 @@ __device__ __forceinline__ float4 face_flux_scalar_sl(const float4 qb, const flo
         FR[c] = UR[c] * unR + (c == AX ? pR : 0.0f);
     }
     if (SOLVER == NB_SOLVER_RUSANOV) {
-        const float amax = fmaxr(fabsf(unL) + csb.y, fabsf(unR) + csc.y);
+        const float amax = fmaxq(fabsf(unL) + csb.y, fabsf(unR) + csc.y);
         const float ha = 0.5f * amax;
 #pragma unroll
         for (int c = 0; c < 4; ++c) F[c] = 0.5f * (FL[c] + FR[c]) - ha * (UR[c] - UL[c]);
         return make_float4(F[0], F[1], F[2], F[3]);
     }
-    const float SL = fminr(unL - csb.y, unR - csc.y);
-    const float SR = fmaxr(unL + csb.y, unR + csc.y);
+    const float SL = fminq(unL - csb.y, unR - csc.y);
+    const float SR = fmaxq(unL + csb.y, unR + csc.y);
     if (SL >= 0.0f) return make_float4(FL[0], FL[1], FL[2], FL[3]);
     if (SR <= 0.0f) return make_float4(FR[0], FR[1], FR[2], FR[3]);
     const float slsr = SL * SR, den = SR - SL;
@@ -253,7 +253,7 @@ __device__ __forceinline__ float4 face_flux_paired_sl(const float4 qb, const flo
     const F2 half = splat2(0.5f);
     const F2 L0 = madd2(half, sl0, b0), L1 = madd2(half, sl1, b1);      // b + 0.5 * slope
     const F2 R0 = nmsub2(c0, half, sr0), R1 = nmsub2(c1, half, sr1);    // c - 0.5 * slope
-    const float rL = fmaxr(lo(L0), floor_), rR = fmaxr(lo(R0), floor_);
+    const float rL = fmaxq(lo(L0), floor_), rR = fmaxq(lo(R0), floor_);
     const float unL = 0.0f + (AX == 1 ? hi(L0) : (AX == 2 ? lo(L1) : hi(L1)));
     const float unR = 0.0f + (AX == 1 ? hi(R0) : (AX == 2 ? lo(R1) : hi(R1)));
     // U = (r, r u, r v, r w): r * 1 == r exactly
@@ -266,14 +266,14 @@ __device__ __forceinline__ float4 face_flux_paired_sl(const float4 qb, const flo
     const F2 FL0 = madd2(UL0, splat2(unL), pL0), FL1 = madd2(UL1, splat2(unL), pL1);
     const F2 FR0 = madd2(UR0, splat2(unR), pR0), FR1 = madd2(UR1, splat2(unR), pR1);
     if (SOLVER == NB_SOLVER_RUSANOV) {
-        const float amax = fmaxr(fabsf(unL) + csb.y, fabsf(unR) + csc.y);
+        const float amax = fmaxq(fabsf(unL) + csb.y, fabsf(unR) + csc.y);
         const F2 ha = splat2(0.5f * amax);
         const F2 F0 = nmsub2(mul2(half, add2(FL0, FR0)), ha, sub2(UR0, UL0));
         const F2 F1 = nmsub2(mul2(half, add2(FL1, FR1)), ha, sub2(UR1, UL1));
         return make_float4(lo(F0), hi(F0), lo(F1), hi(F1));
     }
-    const float SL = fminr(unL - csb.y, unR - csc.y);
-    const float SR = fmaxr(unL + csb.y, unR + csc.y);
+    const float SL = fminq(unL - csb.y, unR - csc.y);
+    const float SR = fmaxq(unL + csb.y, unR + csc.y);
     if (SL >= 0.0f) return make_float4(lo(FL0), hi(FL0), lo(FL1), hi(FL1));
     if (SR <= 0.0f) return make_float4(lo(FR0), hi(FR0), lo(FR1), hi(FR1));
     const F2 slsr = splat2(SL * SR);
@@ -371,9 +371,6 @@ __device__ __forceinline__ void hydro_tile(const HydroLaunch& L, int tile, unsig
                                            bool& failed, int rot) {
     static_assert(TJ == 8, "the halo and edge-face warp assignment assumes 8 warps of 32 threads");
     using Idx = typename std::conditional<I32, int, long long>::type;     // the own cell's offset
-    // register budget: stage 1 carries the x slope from face to face; stage 2 (U^n, the RK
-    // combination, the CFL speed) recomputes it
-    constexpr bool CARRY = !STAGE2;
     using SM = HydroSmem<TJ>;
     {
         // an opaque zero added to the shared-memory base: the compiler then derives the tiles'
@@ -530,7 +527,7 @@ __device__ __forceinline__ void hydro_tile(const HydroLaunch& L, int tile, unsig
         float2* cp = cs + cq * PSLOT;
         // ---- convert plane p: the own cell, then (has_halo) one cell of the halo strips
         auto convert = [&](int o, int pi) {
-            const float r = fmaxr(rb[o], floor_);
+            const float r = fmaxq(rb[o], floor_);
             const float xv = rb[4 * SM::RAW_FIELD + o];
             const float c2 = cn2 + xv * (ci2 - cn2);
 #if NB_ARITH_FAST
@@ -550,16 +547,9 @@ __device__ __forceinline__ void hydro_tile(const HydroLaunch& L, int tile, unsig
         if (p < P0 + 3) continue;
         // x face (p-2)+1/2 from the own column of planes p-2..p and the carried slope of p-2
         const float4 qx1 = prim[((p - 2 - P0) & 3) * PSLOT + own], qx2 = prim[((p - 1 - P0) & 3) * PSLOT + own];
-        float4 fx_new;
-        if constexpr (CARRY) {
-            if (p == P0 + 3) xslope = cell_slopes<SOLVER, LIM>(prim[((p - 3 - P0) & 3) * PSLOT + own], qx1, qx2);
-            fx_new = face_flux_x<SOLVER, LIM>(qx1, qx2, pp[own], cs[((p - 2 - P0) % 3) * PSLOT + own],
-                                              cs[((p - 1 - P0) % 3) * PSLOT + own], floor_, xslope);
-        } else {
-            fx_new = face_flux<SOLVER, LIM, 1>(prim[((p - 3 - P0) & 3) * PSLOT + own], qx1, qx2, pp[own],
-                                               cs[((p - 2 - P0) % 3) * PSLOT + own],
-                                               cs[((p - 1 - P0) % 3) * PSLOT + own], floor_);
-        }
+        if (p == P0 + 3) xslope = cell_slopes<SOLVER, LIM>(prim[((p - 3 - P0) & 3) * PSLOT + own], qx1, qx2);
+        const float4 fx_new = face_flux_x<SOLVER, LIM>(qx1, qx2, pp[own], cs[((p - 2 - P0) % 3) * PSLOT + own],
+                                                       cs[((p - 1 - P0) % 3) * PSLOT + own], floor_, xslope);
         if (!work) { fx_prev = fx_new; continue; }
         // ---- cell plane i = p - 2
         const int si = (i - P0) & 3;
@@ -667,7 +657,7 @@ __device__ __forceinline__ void hydro_tile(const HydroLaunch& L, int tile, unsig
         const float un0 = ur + dt * du0, un1 = umx + dt * du1, un2 = umy + dt * du2, un3 = umz + dt * du3;
         const float o0 = a * u00 + b * un0, o1 = a * u01 + b * un1, o2 = a * u02 + b * un2, o3 = a * u03 + b * un3;
 #endif
-        const float r = fmaxr(o0, floor_);
+        const float r = fmaxq(o0, floor_);
 #if NB_ARITH_FAST
         // one reciprocal for the three velocities and the max speed; the speed cap compares the
         // squared speed and takes a root only for the capped cells
@@ -698,7 +688,7 @@ __device__ __forceinline__ void hydro_tile(const HydroLaunch& L, int tile, unsig
 #else
                 const float v = fabsf(m1 / r) + fabsf(m2 / r) + fabsf(m3 / r) + c[own].y;
 #endif
-                vmax_local = fmaxr(v, vmax_local);
+                vmax_local = fmaxq(v, vmax_local);
             }
         }
     }

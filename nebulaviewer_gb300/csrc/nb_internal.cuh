@@ -153,6 +153,15 @@ __device__ __forceinline__ unsigned smem_u32(const void* p) {
 }
 __device__ __forceinline__ float fmaxr(float a, float b) { return a > b ? a : b; }   // Warp max
 __device__ __forceinline__ float fminr(float a, float b) { return a < b ? a : b; }   // Warp min
+// fmaxr / fminr in the exact build; one min / max instruction in the fast build (fmaxr is a compare
+// and a select): the same value for every operand pair without a NaN, but for the sign of a zero
+#if defined(NB_ARITH_FAST) && NB_ARITH_FAST
+__device__ __forceinline__ float fmaxq(float a, float b) { return fmaxf(a, b); }
+__device__ __forceinline__ float fminq(float a, float b) { return fminf(a, b); }
+#else
+__device__ __forceinline__ float fmaxq(float a, float b) { return fmaxr(a, b); }
+__device__ __forceinline__ float fminq(float a, float b) { return fminr(a, b); }
+#endif
 __device__ __forceinline__ int iclampd(int x, int lo, int hi) { return x < lo ? lo : (x > hi ? hi : x); }
 // The calling warp's slot on its SM (%warpid).  Slot w is issued by scheduler w mod 4; the slot
 // may change on preemption, so it only ever steers work placement, never correctness.

@@ -250,13 +250,13 @@ __device__ __forceinline__ void apply_front_row(const NbConst& C, const float4* 
                 int c0, c1;                      // phi columns times nu (table [phi][u])
                 if (tab) {
                     const float4 tb = tab[s];
-                    r[e] = fmaxr(sqrtf(tb.x + rz * rz), 1e-6f);                  // (rx^2 + ry^2) + rz^2
+                    r[e] = fmaxq(sqrtf(tb.x + rz * rz), 1e-6f);                  // (rx^2 + ry^2) + rz^2
                     tp[e] = tb.y;
                     c0 = __float_as_int(tb.z);
                     c1 = __float_as_int(tb.w);
                 } else {
                     const float rx = px - sp.x, ry = py - sp.y;
-                    r[e] = fmaxr(sqrtf((rx * rx + ry * ry) + rz * rz), 1e-6f);     // 0 + x*x == x*x
+                    r[e] = fmaxq(sqrtf((rx * rx + ry * ry) + rz * rz), 1e-6f);     // 0 + x*x == x*x
                     float phi = atan2f(ry, rx);
                     if (phi < 0.0f) phi = phi + two_pi;
                     const float fp = phi / two_pi * (float)nphi - 0.5f;
@@ -297,12 +297,13 @@ __device__ __forceinline__ void apply_front_row(const NbConst& C, const float4* 
                 const float rb = g10[e] * (1.0f - tp[e]) + g11[e] * tp[e];
                 const float rf = ra * (1.0f - tu[e]) + rb * tu[e];
 #if NB_ARITH_FAST
-                const float val = fminr(fmaxr(0.0f, (rf - r[e]) * inv_width + 0.5f), 1.0f);
+                // clamped to [0, 1] by the saturating form of the multiply-add; merged by one max
+                xi = fmaxf(xi, __saturatef((rf - r[e]) * inv_width + 0.5f));
 #else
                 const float val = fminr(fmaxr(0.0f, (rf - r[e]) / width + 0.5f), 1.0f);
-#endif
                 if (val > xi) xi = val;              // in star order, as the reference merges
-                df = fminr(df, r[e] - rf);
+#endif
+                df = fminq(df, r[e] - rf);
             }
         }
         if (C.plane_on) {                        // the -x plane-parallel source: same merge rules
