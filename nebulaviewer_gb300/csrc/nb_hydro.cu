@@ -272,10 +272,17 @@ __device__ __forceinline__ float4 face_flux_paired_sl(const float4 qb, const flo
         const F2 F1 = nmsub2(mul2(half, add2(FL1, FR1)), ha, sub2(UR1, UL1));
         return make_float4(lo(F0), hi(F0), lo(F1), hi(F1));
     }
+#if NB_ARITH_FAST
+    // branch-free: min(SL, 0) and max(SR, 0) in the general formula give FL (SL >= 0) and FR
+    // (SR <= 0) up to the rounding of SR FL / SR; SR - SL >= 2 c > 0 keeps the denominator positive
+    const float SL = fminf(fminq(unL - csb.y, unR - csc.y), 0.0f);
+    const float SR = fmaxf(fmaxq(unL + csb.y, unR + csc.y), 0.0f);
+#else
     const float SL = fminq(unL - csb.y, unR - csc.y);
     const float SR = fmaxq(unL + csb.y, unR + csc.y);
     if (SL >= 0.0f) return make_float4(lo(FL0), hi(FL0), lo(FL1), hi(FL1));
     if (SR <= 0.0f) return make_float4(lo(FR0), hi(FR0), lo(FR1), hi(FR1));
+#endif
     const F2 slsr = splat2(SL * SR);
     const float den = SR - SL;
     // (SR FL - SL FR + SL SR (UR - UL)) / den, every product feeding a sum as an explicit fused
