@@ -4,10 +4,12 @@
 // apply_front, smooth_xi) as driven by sim.py:927-947 (ionize).
 //
 // GB300 design:
-//  * cast_rays: a group of G lanes (1 to 32; 4 at 256^3) marches one ray, G consecutive
+//  * cast_rays: a group of G lanes (1 to 32; 2 at 256^3) marches one ray, G consecutive
 //    samples at a time; the recombination column sum(n^2 r^2 dr) is an inclusive group scan on
 //    top of a Kahan-compensated carry, and the first sample whose column passes Q is found with
-//    one ballot.  All rays of all active stars are one launch.
+//    one ballot.  The march is warp-uniform: a warp's groups loop together until all are done,
+//    and the trilinear sampler has no branches, so the lanes never diverge (divergent exits had
+//    made branch resolution the leading stall).  All rays of all active stars are one launch.
 //  * The front table holds, per (star, phi, u), the pair (rf(u), rf(min(u + 1, nu - 1))) as one
 //    float2 (cast_rays writes each front into its own pair and its lower neighbour's), so the
 //    bilinear lookup of apply_front is two 8-byte gathers instead of four 4-byte ones; the values
@@ -44,7 +46,10 @@ __global__ void ray_dirs_kernel(int nu, int nphi, float4* __restrict__ dirs) {
 template <int G>
 __device__ __forceinline__ void cast_ray(const NbConst& C, const float4* __restrict__ dirs,
                                          const float* __restrict__ rho, uintptr_t out, int ray, float sx, float sy,
-                                         float sz, float Q, int lane, unsigned gmask) {
+                                         float sz, float Q, int lane, unsigned gmask, bool live) {
+    // Warp-uniform march: every lane of the warp runs the loop until all of its groups are done
+    // (`live` false: the group has no ray; `ray` is then any valid index), a finished group's lanes
+    // only carry predicated-off values, so the warp never diverges inside the loop.
     const int nx = C.nx, ny = C.ny, nz = C.nz;
     const float dx = C.dx, inv_dx = C.inv_dx, dr = C.dr_f;
     const bool pow2 = C.dx_pow2 != 0;
@@ -55,15 +60,14 @@ __device__ __forceinline__ void cast_ray(const NbConst& C, const float4* __restr
     const int n1 = min(C.nsteps, trunc_i(t1 / dr) + 2);
     float hi = 0.0f, comp = 0.0f;          // Kahan-compensated column carried between segments
     float rf = C.diag_f;
-    for (int base = n0; base < n1; base += G) {
+    bool done = !live || n0 >= n1;
+    for (int base = n0;; base += G) {
+        if (__all_sync(0xffffffffu, done)) break;
         const int n = base + lane;
-        const bool valid = n < n1;
+        const bool valid = !done && n < n1;
         const float r = ((float)n + 0.5f) * dr;
-        float inc = 0.0f;
-        if (valid) {
-            const float nv = sample_n(rho, nx, ny, nz, sx + d.x * r, sy + d.y * r, sz + d.z * r, dx, inv_dx, pow2);
-            inc = nv * nv * r * r * dr;
-        }
+        const float nv = sample_n(rho, nx, ny, nz, sx + d.x * r, sy + d.y * r, sz + d.z * r, dx, inv_dx, pow2);
+        const float inc = valid ? nv * nv * r * r * dr : 0.0f;
         float incl = inc;
 #pragma unroll
         for (int o = 1; o < G; o <<= 1) {
@@ -74,21 +78,25 @@ __device__ __forceinline__ void cast_ray(const NbConst& C, const float4* __restr
         if (lane == 0) excl = 0.0f;
         const float col = hi + (excl - comp);
         const bool cross = valid && (col + inc > Q);
-        const unsigned bal = __ballot_sync(gmask, cross);
+        const unsigned bal = __ballot_sync(0xffffffffu, cross);
         const unsigned mine = G == 32 ? bal : (bal >> ((threadIdx.x & 31) / G * G)) & ((1u << G) - 1u);
-        if (mine) {
-            const int f = __ffs(mine) - 1;
-            const float rfl = r - 0.5f * dr + dr * (Q - col) / fmaxr(inc, 1e-20f);
-            rf = __shfl_sync(gmask, rfl, f, G);
-            break;
-        }
+        const float rfl = r - 0.5f * dr + dr * (Q - col) / fmaxr(inc, 1e-20f);
+        const float rfc = __shfl_sync(gmask, rfl, mine ? __ffs(mine) - 1 : 0, G);
         const float total = __shfl_sync(gmask, incl, G - 1, G);
-        const float y = total - comp;
-        const float tsum = hi + y;
-        comp = (tsum - hi) - y;
-        hi = tsum;
+        if (!done) {
+            if (mine) {
+                rf = rfc;
+                done = true;
+            } else {
+                const float y = total - comp;
+                const float tsum = hi + y;
+                comp = (tsum - hi) - y;
+                hi = tsum;
+                done = base + G >= n1;
+            }
+        }
     }
-    if (lane == 0) {
+    if (live && lane == 0) {
         float* p = reinterpret_cast<float*>(out & ~(uintptr_t)3);
         p[0] = rf;
         if (out & 1) p[-1] = rf;
@@ -106,13 +114,9 @@ __device__ __forceinline__ uintptr_t front_slot(float* rfront, bool pairs, int s
     return reinterpret_cast<uintptr_t>(rfront + 2 * e) | (iu > 0 ? 1u : 0u) | (iu == nu - 1 ? 2u : 0u);
 }
 
-// Resident blocks per SM of the ray kernel: 6 (40 registers) in the fast build, 5 (48) in the exact
-// one, whose IEEE divisions would spill 60 bytes at 40 registers.
-#if NB_ARITH_FAST
-#define NB_CAST_RAYS_MINB 6
-#else
+// Resident blocks per SM of the ray kernel: 5 (48 registers); at 6 (40 registers) the warp-uniform
+// march spills 44-84 bytes.
 #define NB_CAST_RAYS_MINB 5
-#endif
 template <int G, bool PAIRS>
 __global__ void __launch_bounds__(256, NB_CAST_RAYS_MINB) cast_rays_kernel(const NbConst* __restrict__ c, const NbStarW* __restrict__ sw,
                                                         const float4* __restrict__ dirs,
@@ -122,29 +126,31 @@ __global__ void __launch_bounds__(256, NB_CAST_RAYS_MINB) cast_rays_kernel(const
     const long long gid = (blockIdx.x * (long long)blockDim.x + threadIdx.x) / G;
     const int lane = threadIdx.x % G;
     const unsigned gmask = G == 32 ? 0xffffffffu : (((1u << G) - 1u) << ((threadIdx.x & 31) / G * G));
-    if (gid >= (long long)nray * nstars) return;
-    const int s = (int)(gid / nray), ray = (int)(gid % nray);
+    // no early exit: every lane of a warp reaches cast_ray's warp-uniform loop
+    const bool in = gid < (long long)nray * nstars;
+    const int s = in ? (int)(gid / nray) : 0, ray = in ? (int)(gid % nray) : 0;
     if (star_override) {
         cast_ray<G>(*c, dirs, rho, reinterpret_cast<uintptr_t>(rfront + ray), ray, star_override[0], star_override[1],
-                    star_override[2], q_override, lane, gmask);
+                    star_override[2], q_override, lane, gmask, in);
         return;
     }
     const NbStarW w = sw[s];
-    if (!w.active) return;
     // the instance's table is [star][phi][u] (u fastest: the cells of a warp share phi)
     const int iu = ray / c->nphi, ip = ray - iu * c->nphi;
     cast_ray<G>(*c, dirs, rho, front_slot(rfront, PAIRS, s, nray, c->nu, iu, ip), ray, w.w.x, w.w.y, w.w.z, w.q_f,
-                lane, gmask);
+                lane, gmask, in && w.active);
 }
 
 // Rays of every star of every listed instance: job e owns groups [job[e].ray0, job[e+1].ray0).
 template <int G>
 __global__ void __launch_bounds__(256) cast_rays_batch_kernel(const NbRayJob* __restrict__ jobs, int n_jobs,
                                                               long long n_groups) {
-    const long long gid = (blockIdx.x * (long long)blockDim.x + threadIdx.x) / G;
+    const long long gid0 = (blockIdx.x * (long long)blockDim.x + threadIdx.x) / G;
     const int lane = threadIdx.x % G;
     const unsigned gmask = G == 32 ? 0xffffffffu : (((1u << G) - 1u) << ((threadIdx.x & 31) / G * G));
-    if (gid >= n_groups) return;
+    // no early exit: every lane of a warp reaches cast_ray's warp-uniform loop
+    const bool in = gid0 < n_groups;
+    const long long gid = in ? gid0 : 0;
     int lo = 0, hi = n_jobs - 1;
     while (lo < hi) {                          // last job with ray0 <= gid
         const int mid = (lo + hi + 1) >> 1;
@@ -155,12 +161,12 @@ __global__ void __launch_bounds__(256) cast_rays_batch_kernel(const NbRayJob* __
     const int nray = C.nu * C.nphi;
     const long long local = gid - J.ray0;
     const int s = (int)(local / nray), ray = (int)(local % nray);
-    if (s >= J.nstars || !J.active) return;
-    const NbStarW w = J.sw[s];
-    if (!w.active) return;
+    const bool star = in && s < J.nstars && J.active;
+    NbStarW w{};
+    if (star) w = J.sw[s];
     const int iu = ray / C.nphi, ip = ray - iu * C.nphi;
     cast_ray<G>(C, J.dirs, J.rho, front_slot(J.rfront, J.pairs != 0, s, nray, C.nu, iu, ip), ray, w.w.x, w.w.y, w.w.z,
-                w.q_f, lane, gmask);
+                w.q_f, lane, gmask, star && w.active);
 }
 
 // The stars that can change xi or the front distance of the 32-cell segment [kb, kb + 32) of a

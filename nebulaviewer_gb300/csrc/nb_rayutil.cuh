@@ -4,31 +4,25 @@
 
 __device__ __forceinline__ float pi_f() { return 3.14159265358979323846f; }
 
-// nebula3d.py:195-226 sample_n (trilinear, 0 outside the domain).  With dx == 2^-m the
-// division p / dx is the exact multiplication p * 2^m.
+// nebula3d.py:195-226 sample_n (trilinear, 0 outside the domain), without branches: the corners
+// are always clamped to the grid (no-ops inside it) and 0 is selected outside the domain, so the
+// lanes of a warp never diverge here.  With dx == 2^-m the division p / dx is the exact
+// multiplication p * 2^m.  A plane ny * nz stays below 2^31 cells (nb_create requires it).
 __device__ __forceinline__ float sample_n(const float* __restrict__ a, int nx, int ny, int nz, float px, float py,
                                           float pz, float dx, float inv_dx, bool pow2) {
     const float gx = (pow2 ? px * inv_dx : px / dx) - 0.5f;
     const float gy = (pow2 ? py * inv_dx : py / dx) - 0.5f;
     const float gz = (pow2 ? pz * inv_dx : pz / dx) - 0.5f;
-    if (gx < -0.5f || gy < -0.5f || gz < -0.5f) return 0.0f;
-    if (gx > (float)nx - 0.5f || gy > (float)ny - 0.5f || gz > (float)nz - 0.5f) return 0.0f;
-    const int i0 = (int)floorf(gx), j0 = (int)floorf(gy), k0 = (int)floorf(gz);
+    const bool outside = gx < -0.5f || gy < -0.5f || gz < -0.5f || gx > (float)nx - 0.5f || gy > (float)ny - 0.5f ||
+                         gz > (float)nz - 0.5f;
+    const float fgx = floorf(gx), fgy = floorf(gy), fgz = floorf(gz);
+    const int i0 = (int)fgx, j0 = (int)fgy, k0 = (int)fgz;
     const float fx = gx - (float)i0, fy = gy - (float)j0, fz = gz - (float)k0;
-    // corner (ia, ja, ka) once in 64 bits, the other seven as 32-bit steps from it (a plane
-    // ny * nz below 2^31 cells, which nb_create requires); all eight corners inside: no clamps
-    const float* p;
-    int dk, dj, di;
-    if ((unsigned)i0 < (unsigned)(nx - 1) && (unsigned)j0 < (unsigned)(ny - 1) && (unsigned)k0 < (unsigned)(nz - 1)) {
-        p = a + (((long long)i0 * ny + j0) * nz + k0);
-        dk = 1; dj = nz; di = ny * nz;
-    } else {
-        const int ia = iclampd(i0, 0, nx - 1), ib = iclampd(i0 + 1, 0, nx - 1);
-        const int ja = iclampd(j0, 0, ny - 1), jb = iclampd(j0 + 1, 0, ny - 1);
-        const int ka = iclampd(k0, 0, nz - 1), kb = iclampd(k0 + 1, 0, nz - 1);
-        p = a + (((long long)ia * ny + ja) * nz + ka);
-        dk = kb - ka; dj = (jb - ja) * nz; di = (ib - ia) * (ny * nz);
-    }
+    const int ia = iclampd(i0, 0, nx - 1), ib = iclampd(i0 + 1, 0, nx - 1);
+    const int ja = iclampd(j0, 0, ny - 1), jb = iclampd(j0 + 1, 0, ny - 1);
+    const int ka = iclampd(k0, 0, nz - 1), kb = iclampd(k0 + 1, 0, nz - 1);
+    const float* p = a + (((long long)ia * ny + ja) * nz + ka);
+    const int dk = kb - ka, dj = (jb - ja) * nz, di = (ib - ia) * (ny * nz);
     const float c000 = __ldg(p), c100 = __ldg(p + di);
     const float c010 = __ldg(p + dj), c110 = __ldg(p + (di + dj));
     const float c001 = __ldg(p + dk), c101 = __ldg(p + (di + dk));
@@ -39,7 +33,8 @@ __device__ __forceinline__ float sample_n(const float* __restrict__ a, int nx, i
     const float c11 = c011 + (c111 - c011) * fx;
     const float c0 = c00 + (c10 - c00) * fy;
     const float c1 = c01 + (c11 - c01) * fy;
-    return c0 + (c1 - c0) * fz;
+    const float v = c0 + (c1 - c0) * fz;
+    return outside ? 0.0f : v;
 }
 
 // an approximate reciprocal (<= 1 ulp), for the fast build's divisions by a clamped distance
