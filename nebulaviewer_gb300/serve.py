@@ -11,7 +11,8 @@ otherwise a new instance is built, if its true device footprint -- its fields an
 library's scratch for it (nb_instance_bytes: ray and FUV tables sized for its stars, tensor
 maps, ...) -- fits the HBM budget next to every instance already pooled, busy or idle; idle
 instances of other snapshots are closed first, least recently used first, when that makes
-room.  All pooled instances live in one BatchSim (persistent kernels, CUDA graphs): a request
+room.  A server may also build a warm pool before traffic starts (run's `warm`: idle instances
+per snapshot, within the budget).  All pooled instances live in one BatchSim (persistent kernels, CUDA graphs): a request
 joins the stepping set when it is admitted and leaves it when it has run its steps, through
 the batch's slot flags, so admissions and retirements rebuild nothing; the batch and its
 graphs are rebuilt only when the pool itself changes.  Every tick advances all busy instances
@@ -146,19 +147,39 @@ class Server:
         self.built = 0               # instances built
         self.reused = 0              # requests branched into a pooled instance
         self.evicted = 0             # idle instances closed to make room
+        self.prewarmed = 0           # idle instances built before the clock started (run's `warm`)
         self.peak_bytes = 0
 
-    def run(self, requests, realtime=True):
+    def run(self, requests, realtime=True, warm=None):
         """serve `requests` (in arrival order; realtime=False admits each as soon as it fits);
-        returns (stats, the finished requests in completion order).  On an error every instance and
-        batch still open is closed before it propagates."""
+        returns (stats, the finished requests in completion order).  warm = {snapshot index: n}
+        builds up to n idle instances of each snapshot before the clock starts (as far as the
+        budget allows), the warm pool a server keeps for the traffic it expects, so that requests
+        branch into them by device copies.  On an error every instance and batch still open is
+        closed before it propagates."""
         pending = collections.deque(sorted(requests, key=lambda r: r.t_arrive))
         queue = collections.deque()
         pool, done = [], []
         batch = None
         dirty = False                # the pool changed since the batch was built
-        t0 = time.perf_counter()
         cell_steps = 0
+        self.prewarmed = 0
+        try:
+            for si, n in sorted((warm or {}).items()):
+                snap = self.snaps[si]
+                for _ in range(int(n)):
+                    if sum(p.nbytes for p in pool) + snap.footprint > self.budget:
+                        break
+                    sim = snap.branch(None)
+                    pool.append(_Slot(si, sim, sim.footprint()))
+                    self.prewarmed += 1
+            self.peak_bytes = max(self.peak_bytes, sum(p.nbytes for p in pool))
+        except BaseException:
+            for p in pool:
+                p.sim.close()
+            raise
+        dirty = bool(pool)
+        t0 = time.perf_counter()
 
         def pool_bytes():
             return sum(p.nbytes for p in pool)
@@ -256,8 +277,8 @@ class Server:
         pct = (lambda q: float(np.percentile(lat, q) * 1e3)) if len(lat) else (lambda q: None)
         return dict(requests=len(done), wall_s=wall, cell_steps=cell_steps, gcells_per_s=cell_steps / wall / 1e9,
                     p50_ms=pct(50), p99_ms=pct(99), ticks=self.ticks, batch_rebuilds=self.rebuilds,
-                    instances_built=self.built, branches_in_place=self.reused, evicted=self.evicted,
-                    peak_pool_bytes=self.peak_bytes, budget_bytes=self.budget), done
+                    instances_built=self.built, instances_prewarmed=self.prewarmed, branches_in_place=self.reused,
+                    evicted=self.evicted, peak_pool_bytes=self.peak_bytes, budget_bytes=self.budget), done
 
 
 def run_alone(snapshot, req):

@@ -52,5 +52,6 @@ def test_fp32_error_against_fp64_rerun_torus64(arith):
         # the GPU's FP32 result is as close to the FP64 re-run as the reference scheme's FP32 is
         assert g2 <= 3.0 * c2 + 1e-6, (k, g2, c2)
         assert g2 < 1e-3, (k, g2)
+        assert gi < 1e-3, (k, gi)                 # the stated rel-L_inf after 100 steps
     assert abs(g.t - o64.t) / o64.t < 1e-4
     g.close()

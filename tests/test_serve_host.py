@@ -1,7 +1,7 @@
 """The serving scheduler's host logic (serve.Server.run) on fake instances: admission under the
 slot limit and under the HBM budget counted with every pooled instance's true footprint (busy or
-idle), instances reused for later requests of the same snapshot, idle instances of other
-snapshots closed (least recently used first) to make room, every request stepped exactly its step
+idle), instances reused for later requests of the same snapshot, a warm pool built before traffic within
+the budget, idle instances of other snapshots closed (least recently used first) to make room, every request stepped exactly its step
 count, zero-step requests, and every instance and batch closed when a batch step fails.  No GPU:
 BatchSim and the results are faked."""
 import pytest
@@ -111,6 +111,25 @@ def test_instances_are_reused_and_the_batch_is_not_rebuilt_per_admission(monkeyp
     assert stats["branches_in_place"] == 6 == snaps[0].branched_into
     assert stats["batch_rebuilds"] == len(log["batches"]) <= 2          # only when the pool grew
     assert {r.rid: r.result["it"] for r in done} == {r.rid: r.nsteps for r in reqs}
+
+
+def test_a_warm_pool_serves_every_request_by_device_copies(monkeypatch):
+    snaps = [FakeSnap(500), FakeSnap(800)]
+    log = install(monkeypatch, max_slots=6)
+    reqs = requests(snaps, [3, 3, 4, 2, 5, 1])       # snapshots 0, 1, 0, 1, 0, 1
+    srv = serve.Server(snaps, max_slots=6)
+    stats, done = srv.run(reqs, realtime=False, warm={0: 3, 1: 3})
+    assert stats["instances_prewarmed"] == 6 and stats["instances_built"] == 0
+    assert stats["branches_in_place"] == 6 == snaps[0].branched_into + snaps[1].branched_into
+    assert stats["batch_rebuilds"] == 1 == len(log["batches"])     # the warm pool never changes
+    assert {r.rid: r.result["it"] for r in done} == {r.rid: r.nsteps for r in reqs}
+    assert all(s.closed for sn in snaps for s in sn.made)
+    # a warm pool stops at the budget
+    snaps = [FakeSnap(1000)]
+    budget = 2 * snaps[0].footprint + 10
+    install(monkeypatch, budget=budget)
+    stats, _ = serve.Server(snaps, budget_bytes=budget).run(requests(snaps, [2, 2, 2]), realtime=False, warm={0: 5})
+    assert stats["instances_prewarmed"] == 2 and stats["instances_built"] == 0 and stats["peak_pool_bytes"] <= budget
 
 
 def test_idle_instances_of_other_snapshots_make_room(monkeypatch):
