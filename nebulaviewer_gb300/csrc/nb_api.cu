@@ -6,6 +6,7 @@
 #include <cstring>
 #include <mutex>
 #include <string>
+#include <memory>
 #include <vector>
 
 #include "nb_internal.cuh"
@@ -966,6 +967,9 @@ struct nb_batch_s {
     std::vector<NbRayJob> h_all;
     std::vector<NbBatchInst> h_inst;    // host copies of the descriptors (nb_batch_set_active re-uploads them)
     std::vector<HydroLaunch> h_L1, h_L2;
+    // the stage records as the persistent kernel's parameter (at most NB_BATCH_PARAM_MAX instances,
+    // 32-bit offsets; their active flags are not read: the kernel takes those from d_L1 / d_L2)
+    std::unique_ptr<NbBatchRecords> rec1, rec2;
     std::vector<int> active;            // per instance: 1 = its slot steps, 0 = idle
     int n_active = 0;
     std::vector<const float*> rfront0;  // each instance's ray scratch when the batch was built
@@ -1062,10 +1066,10 @@ void job_prefix(std::vector<NbRayJob>& jobs, const std::vector<nb_instance*>& hs
 int batch_hydro(nb_batch_s* b) {
     b->launches += 3;
     BCK(b, nb_launch_ctrl_batch(b->d_inst, (int)b->inst.size(), 1, b->d_counters, b->bs));
-    BCK(b, nb_launch_hydro_batch(b->d_L1, b->d_work, b->n_work, b->d_counters + 0, b->max_stars, 0, b->idx32,
-                                 b->solver, b->limiter, b->grid, b->bs));
-    BCK(b, nb_launch_hydro_batch(b->d_L2, b->d_work, b->n_work, b->d_counters + 1, b->max_stars, 1, b->idx32,
-                                 b->solver, b->limiter, b->grid, b->bs));
+    BCK(b, nb_launch_hydro_batch(b->d_L1, b->rec1.get(), b->d_work, b->n_work, b->d_counters + 0, b->max_stars, 0,
+                                 b->idx32, b->solver, b->limiter, b->grid, b->bs));
+    BCK(b, nb_launch_hydro_batch(b->d_L2, b->rec2.get(), b->d_work, b->n_work, b->d_counters + 1, b->max_stars, 1,
+                                 b->idx32, b->solver, b->limiter, b->grid, b->bs));
     return NB_OK;
 }
 
@@ -1148,7 +1152,8 @@ NB_EXPORT int nb_batch_create(const nb_handle* hs, const int* ion_every, int n, 
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    b->grid = (sms > 0 ? sms : 152) * nb_hydro_batch_blocks_per_sm(b->solver, b->limiter, b->max_stars, b->idx32);
+    const int params = b->idx32 && n <= NB_BATCH_PARAM_MAX;
+    b->grid = (sms > 0 ? sms : 152) * nb_hydro_batch_blocks_per_sm(b->solver, b->limiter, b->max_stars, b->idx32, params);
     if (cudaStreamCreateWithFlags(&b->bs, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreateWithFlags(&b->ev_in, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&b->ev_out, cudaEventDisableTiming) != cudaSuccess)
@@ -1167,6 +1172,14 @@ NB_EXPORT int nb_batch_create(const nb_handle* hs, const int* ion_every, int n, 
         bi[i] = NbBatchInst{h->c, h->st, h->stars, h->sw, h->nstars, 1};
         L1[i] = stage_desc(h, false);
         L2[i] = stage_desc(h, true);
+    }
+    if (params) {                                // the records as the persistent kernel's parameter
+        b->rec1.reset(new NbBatchRecords());
+        b->rec2.reset(new NbBatchRecords());
+        for (int i = 0; i < n; ++i) {
+            b->rec1->L[i] = L1[i];
+            b->rec2->L[i] = L2[i];
+        }
     }
     // work list: largest instances first, each instance's tiles in order
     std::vector<int> order(n);

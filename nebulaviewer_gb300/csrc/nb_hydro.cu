@@ -795,6 +795,43 @@ hydro_batch_kernel(const HydroLaunch* __restrict__ Ls, const int2* __restrict__ 
     }
 }
 
+// The same persistent stage with the stage records in the kernel parameter (batches of at most
+// NB_BATCH_PARAM_MAX instances, 32-bit offsets): a record's fields come from the constant bank,
+// as the single-instance kernel's do, so it fits 64 registers and 4 blocks / SM.  The active flags
+// (changed between graph replays) and the status words are read from the device copy Lg.
+template <int SOLVER, int LIM, int TJ, bool STAGE2>
+__global__ void __launch_bounds__(TK * TJ, NB_HYDRO_MINB)
+hydro_batch_param_kernel(const __grid_constant__ NbBatchRecords R, const HydroLaunch* __restrict__ Lg,
+                         const int2* __restrict__ work, int n_work, unsigned* counter) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    __shared__ int item, rot;
+    hydro_init_bars<TJ>(smem, &rot);
+    unsigned ph0 = 0;
+    bool failed = false;                         // block-uniform (hydro_tile sets it after a barrier)
+    int last = -1;
+    for (;;) {
+        if (threadIdx.x == 0) item = (int)atomicAdd(counter, 1u);
+        __syncthreads();
+        const int it = item;
+        if (it >= n_work) break;
+        const int2 w = work[it];
+        if (!Lg[w.x].active) {                   // an idle slot of the batch: nothing to do
+            __syncthreads();
+            continue;
+        }
+        last = w.x;
+        hydro_tile<SOLVER, LIM, TJ, STAGE2, true>(R.L[w.x], w.y, smem, ph0, failed, rot);
+        if (failed) break;
+        __syncthreads();
+    }
+    if (failed && last >= 0) {
+        hydro_abort<TJ>(smem, Lg[last].status, ph0, Lg[last].wait_limit);
+        if (threadIdx.x == 0)                    // flag the instances of the items left undone
+            for (unsigned it; (it = atomicAdd(counter, 1u)) < (unsigned)n_work;)
+                atomicOr(Lg[work[it].x].status, NB_DEV_TMA_TIMEOUT);
+    }
+}
+
 template <int SOLVER, int LIM, int TJ, bool STAGE2, bool I32>
 cudaError_t run_kernel(const HydroLaunch& L, cudaStream_t s) {
     auto kern = hydro_stage_kernel<SOLVER, LIM, TJ, STAGE2, I32>;
@@ -816,10 +853,20 @@ cudaError_t run_stage(const HydroLaunch& L, cudaStream_t s) {
 }
 
 template <int SOLVER, int LIM, int TJ, bool STAGE2, bool I32>
-cudaError_t run_batch_kernel(const HydroLaunch* Ls, const int2* work, int n_work, unsigned* counter,
-                             int max_stars, int grid, cudaStream_t s) {
-    auto kern = hydro_batch_kernel<SOLVER, LIM, TJ, STAGE2, I32>;
+cudaError_t run_batch_kernel(const HydroLaunch* Ls, const NbBatchRecords* rec, const int2* work, int n_work,
+                             unsigned* counter, int max_stars, int grid, cudaStream_t s) {
     const int smem = HydroSmem<TJ>::bytes(max_stars);
+    if (I32 && rec) {
+        auto kern = hydro_batch_param_kernel<SOLVER, LIM, TJ, STAGE2>;
+        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                     cudaSharedmemCarveoutMaxShared);
+        if (e != cudaSuccess) return e;
+        kern<<<grid, TK * TJ, smem, s>>>(*rec, Ls, work, n_work, counter);
+        return cudaGetLastError();
+    }
+    auto kern = hydro_batch_kernel<SOLVER, LIM, TJ, STAGE2, I32>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (e == cudaSuccess)
         e = cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
@@ -829,13 +876,13 @@ cudaError_t run_batch_kernel(const HydroLaunch* Ls, const int2* work, int n_work
 }
 
 template <int SOLVER, int LIM, int TJ>
-cudaError_t run_batch(const HydroLaunch* Ls, const int2* work, int n_work, unsigned* counter, int max_stars,
-                      int stage2, int idx32, int grid, cudaStream_t s) {
+cudaError_t run_batch(const HydroLaunch* Ls, const NbBatchRecords* rec, const int2* work, int n_work,
+                      unsigned* counter, int max_stars, int stage2, int idx32, int grid, cudaStream_t s) {
     if (idx32)
-        return stage2 ? run_batch_kernel<SOLVER, LIM, TJ, true, true>(Ls, work, n_work, counter, max_stars, grid, s)
-                      : run_batch_kernel<SOLVER, LIM, TJ, false, true>(Ls, work, n_work, counter, max_stars, grid, s);
-    return stage2 ? run_batch_kernel<SOLVER, LIM, TJ, true, false>(Ls, work, n_work, counter, max_stars, grid, s)
-                  : run_batch_kernel<SOLVER, LIM, TJ, false, false>(Ls, work, n_work, counter, max_stars, grid, s);
+        return stage2 ? run_batch_kernel<SOLVER, LIM, TJ, true, true>(Ls, rec, work, n_work, counter, max_stars, grid, s)
+                      : run_batch_kernel<SOLVER, LIM, TJ, false, true>(Ls, rec, work, n_work, counter, max_stars, grid, s);
+    return stage2 ? run_batch_kernel<SOLVER, LIM, TJ, true, false>(Ls, nullptr, work, n_work, counter, max_stars, grid, s)
+                  : run_batch_kernel<SOLVER, LIM, TJ, false, false>(Ls, nullptr, work, n_work, counter, max_stars, grid, s);
 }
 
 }  // namespace
@@ -843,7 +890,7 @@ cudaError_t run_batch(const HydroLaunch* Ls, const int2* work, int n_work, unsig
 int nb_hydro_tile_j() { return NB_HYDRO_TJ; }
 
 // resident blocks per SM of the persistent stage kernel (sizes its grid)
-int nb_hydro_batch_blocks_per_sm(int solver, int limiter, int max_stars, int idx32) {
+int nb_hydro_batch_blocks_per_sm(int solver, int limiter, int max_stars, int idx32, int params) {
     constexpr int TJ = NB_HYDRO_TJ;
     const int smem = HydroSmem<TJ>::bytes(max_stars);
     auto occ = [&](auto kern) {
@@ -858,6 +905,17 @@ int nb_hydro_batch_blocks_per_sm(int solver, int limiter, int max_stars, int idx
         return n;
     };
     int n;
+    if (idx32 && params) {
+        if (solver == NB_SOLVER_RUSANOV)
+            n = occ(hydro_batch_param_kernel<NB_SOLVER_RUSANOV, 0, TJ, true>);
+        else if (limiter == NB_LIM_VANLEER)
+            n = occ(hydro_batch_param_kernel<NB_SOLVER_HLL, NB_LIM_VANLEER, TJ, true>);
+        else if (limiter == NB_LIM_MC)
+            n = occ(hydro_batch_param_kernel<NB_SOLVER_HLL, NB_LIM_MC, TJ, true>);
+        else
+            n = occ(hydro_batch_param_kernel<NB_SOLVER_HLL, NB_LIM_MINMOD, TJ, true>);
+        return n > 0 ? n : NB_HYDRO_MINB;
+    }
     if (solver == NB_SOLVER_RUSANOV)
         n = idx32 ? occ(hydro_batch_kernel<NB_SOLVER_RUSANOV, 0, TJ, true, true>)
                   : occ(hydro_batch_kernel<NB_SOLVER_RUSANOV, 0, TJ, true, false>);
@@ -883,18 +941,21 @@ cudaError_t nb_launch_hydro(const HydroLaunch& L, int solver, int limiter, cudaS
     }
 }
 
-cudaError_t nb_launch_hydro_batch(const HydroLaunch* Ls, const int2* work, int n_work, unsigned* counter,
-                                  int max_stars, int stage2, int idx32, int solver, int limiter, int grid,
-                                  cudaStream_t s) {
+cudaError_t nb_launch_hydro_batch(const HydroLaunch* Ls, const NbBatchRecords* rec, const int2* work, int n_work,
+                                  unsigned* counter, int max_stars, int stage2, int idx32, int solver, int limiter,
+                                  int grid, cudaStream_t s) {
     constexpr int TJ = NB_HYDRO_TJ;
     if (solver == NB_SOLVER_RUSANOV)
-        return run_batch<NB_SOLVER_RUSANOV, 0, TJ>(Ls, work, n_work, counter, max_stars, stage2, idx32, grid, s);
+        return run_batch<NB_SOLVER_RUSANOV, 0, TJ>(Ls, rec, work, n_work, counter, max_stars, stage2, idx32, grid, s);
     switch (limiter) {
         case NB_LIM_VANLEER:
-            return run_batch<NB_SOLVER_HLL, NB_LIM_VANLEER, TJ>(Ls, work, n_work, counter, max_stars, stage2, idx32, grid, s);
+            return run_batch<NB_SOLVER_HLL, NB_LIM_VANLEER, TJ>(Ls, rec, work, n_work, counter, max_stars, stage2, idx32,
+                                                                grid, s);
         case NB_LIM_MC:
-            return run_batch<NB_SOLVER_HLL, NB_LIM_MC, TJ>(Ls, work, n_work, counter, max_stars, stage2, idx32, grid, s);
+            return run_batch<NB_SOLVER_HLL, NB_LIM_MC, TJ>(Ls, rec, work, n_work, counter, max_stars, stage2, idx32, grid,
+                                                           s);
         default:
-            return run_batch<NB_SOLVER_HLL, NB_LIM_MINMOD, TJ>(Ls, work, n_work, counter, max_stars, stage2, idx32, grid, s);
+            return run_batch<NB_SOLVER_HLL, NB_LIM_MINMOD, TJ>(Ls, rec, work, n_work, counter, max_stars, stage2, idx32,
+                                                               grid, s);
     }
 }

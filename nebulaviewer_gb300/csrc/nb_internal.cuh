@@ -223,11 +223,22 @@ __device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, i
 // ------------------------------------------------------------------ launchers (nb_*.cu)
 cudaError_t nb_launch_hydro(const HydroLaunch& L, int solver, int limiter, cudaStream_t s);
 int nb_hydro_tile_j();
-// idx32: every listed instance has fewer than 2^31 cells (32-bit cell offsets)
-int nb_hydro_batch_blocks_per_sm(int solver, int limiter, int max_stars, int idx32);
-cudaError_t nb_launch_hydro_batch(const HydroLaunch* Ls, const int2* work, int n_work, unsigned* counter,
-                                  int max_stars, int stage2, int idx32, int solver, int limiter, int grid,
-                                  cudaStream_t s);
+// Batches of up to NB_BATCH_PARAM_MAX instances (32-bit cell offsets) hand the persistent stage
+// kernel their stage records as one kernel parameter (28 KB of the 32 KB parameter space): the
+// kernel then reads a record's fields from the constant bank, as the single-instance kernel reads
+// its own, and fits 64 registers (4 blocks / SM) where records read from global memory need 80.
+#define NB_BATCH_PARAM_MAX 128
+struct NbBatchRecords {
+    HydroLaunch L[NB_BATCH_PARAM_MAX];
+};
+// idx32: every listed instance has fewer than 2^31 cells (32-bit cell offsets); params: the
+// records go in the kernel parameter (idx32 and at most NB_BATCH_PARAM_MAX instances)
+int nb_hydro_batch_blocks_per_sm(int solver, int limiter, int max_stars, int idx32, int params);
+// Ls: the device copy of the records (the active flags and status words are read there); rec: the
+// same records on the host, passed as the kernel parameter, or null
+cudaError_t nb_launch_hydro_batch(const HydroLaunch* Ls, const NbBatchRecords* rec, const int2* work, int n_work,
+                                  unsigned* counter, int max_stars, int stage2, int idx32, int solver, int limiter,
+                                  int grid, cudaStream_t s);
 cudaError_t nb_launch_ctrl(const NbConst* c, NbState* st, const NbStarDev* stars, NbStarW* sw, int nstars,
                            int advance, cudaStream_t s);
 cudaError_t nb_launch_ctrl_batch(const NbBatchInst* insts, int n, int advance, unsigned* counters, cudaStream_t s);
