@@ -1073,8 +1073,8 @@ int batch_hydro(nb_batch_s* b) {
     return NB_OK;
 }
 
-int batch_ionize(nb_batch_s* b, const NbRayJob* jobs, int n_jobs, long long groups, long long blocks,
-                 const std::vector<int>& listed) {
+int batch_ionize(nb_batch_s* b, const NbRayJob* jobs, const NbRayJob* host_jobs, int n_jobs, long long groups,
+                 long long blocks, const std::vector<int>& listed) {
     b->launches += 5;                       // control, rays, front ranges, front apply, smoothing
     BCK(b, nb_launch_ctrl_batch(b->d_inst, (int)b->inst.size(), 0, nullptr, b->bs));
     for (int i : listed) {
@@ -1083,7 +1083,7 @@ int batch_ionize(nb_batch_s* b, const NbRayJob* jobs, int n_jobs, long long grou
         b->launches += 1;
         BCK(b, nb_launch_plane_front(h->c, h->d.f.rho, h->plane_xf, h->d.ny, h->d.nz, b->bs));
     }
-    BCK(b, nb_launch_ionize_batch(jobs, n_jobs, groups, blocks, b->ray_group, b->bs));
+    BCK(b, nb_launch_ionize_batch(jobs, host_jobs, n_jobs, groups, blocks, b->ray_group, b->bs));
     return NB_OK;
 }
 
@@ -1093,7 +1093,7 @@ int batch_run_graph(nb_batch_s* b, cudaGraphExec_t* g, int ion) {
         BCK(b, cudaStreamBeginCapture(b->bs, cudaStreamCaptureModeRelaxed));
         std::vector<int> all(b->inst.size());
         for (size_t i = 0; i < all.size(); ++i) all[i] = (int)i;
-        int rc = ion ? batch_ionize(b, b->d_jobs_all, (int)b->inst.size(), b->all_groups, b->all_blocks, all) : NB_OK;
+        int rc = ion ? batch_ionize(b, b->d_jobs_all, b->h_all.data(), (int)b->inst.size(), b->all_groups, b->all_blocks, all) : NB_OK;
         if (rc == NB_OK) rc = batch_hydro(b);
         cudaError_t e = cudaStreamEndCapture(b->bs, &graph);
         if (rc != NB_OK) {
@@ -1314,7 +1314,7 @@ NB_EXPORT int nb_batch_step(nb_batch b, int k) {
             rc = batch_run_graph(b, all ? &b->g_ion : &b->g_plain, all ? 1 : 0);
         } else {
             if (all) {                           // every active slot: the whole job list (idle slots skip)
-                rc = batch_ionize(b, b->d_jobs_all, n, b->all_groups, b->all_blocks, due);
+                rc = batch_ionize(b, b->d_jobs_all, b->h_all.data(), n, b->all_groups, b->all_blocks, due);
                 b->warm_ion = 1;
             } else if (!none) {
                 std::vector<NbRayJob> jobs;
@@ -1327,7 +1327,7 @@ NB_EXPORT int nb_batch_step(nb_batch b, int k) {
                 job_prefix(jobs, hs, groups, blocks);
                 BCK(b, cudaMemcpyAsync(b->d_jobs, jobs.data(), sizeof(NbRayJob) * jobs.size(), cudaMemcpyHostToDevice,
                                        b->bs));
-                rc = batch_ionize(b, b->d_jobs, (int)jobs.size(), groups, blocks, due);
+                rc = batch_ionize(b, b->d_jobs, jobs.data(), (int)jobs.size(), groups, blocks, due);
             } else {
                 b->warm_plain = 1;
             }

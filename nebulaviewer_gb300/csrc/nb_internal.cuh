@@ -274,8 +274,14 @@ cudaError_t nb_launch_apply_front(const NbConst* c, const NbStarW* sw, const flo
                                   int half, float2* front_parts, long long nray, int pairs);
 cudaError_t nb_launch_smooth(const NbConst* c, const float* xi_raw, float* xi, const float* rho, const float* mx,
                              const float* my, const float* mz, unsigned* smax_bits, cudaStream_t s, int nx, int ny);
-cudaError_t nb_launch_ionize_batch(const NbRayJob* jobs, int n_jobs, long long n_groups, long long n_blocks, int group,
-                                   cudaStream_t s);
+// The ray cast of a batch of at most NB_BATCH_PARAM_MAX jobs takes the job records as one kernel
+// parameter (host_jobs, the host copy of `jobs`), as the batched hydro stage does; the active
+// flags are read from the device copy.  host_jobs null: the records are read from `jobs`.
+struct NbRayJobs {
+    NbRayJob J[NB_BATCH_PARAM_MAX];
+};
+cudaError_t nb_launch_ionize_batch(const NbRayJob* jobs, const NbRayJob* host_jobs, int n_jobs, long long n_groups,
+                                   long long n_blocks, int group, cudaStream_t s);
 cudaError_t nb_launch_plane_front(const NbConst* c, const float* rho, float* xf, int ny, int nz, cudaStream_t s);
 cudaError_t nb_launch_plane_fuv(const NbConst* c, const float* rho, const float* xi, float* g, int ny, int nz,
                                 cudaStream_t s);

@@ -21,6 +21,8 @@
 //    rounded once to the fp16 dfront (sim.py:980-985, 511-514).
 //  * smooth_xi writes the final xi and reduces the CFL max speed of the step from it
 //    (nebula3d.py:154-162), so an ionizing step needs no separate max-speed pass.
+#include <cstring>
+
 #include "nb_rayutil.cuh"
 
 namespace {
@@ -142,9 +144,11 @@ __global__ void __launch_bounds__(256, NB_CAST_RAYS_MINB) cast_rays_kernel(const
 }
 
 // Rays of every star of every listed instance: job e owns groups [job[e].ray0, job[e+1].ray0).
-template <int G>
-__global__ void __launch_bounds__(256) cast_rays_batch_kernel(const NbRayJob* __restrict__ jobs, int n_jobs,
-                                                              long long n_groups) {
+// `J` holds the job records (global memory, or the kernel parameter of the param form); the active
+// flags always come from `Jd`, the device copy (they change between replays of a captured step).
+template <int G, typename Jobs>
+__device__ __forceinline__ void cast_rays_batch_body(const Jobs& J, const NbRayJob* __restrict__ Jd, int n_jobs,
+                                                     long long n_groups) {
     const long long gid0 = (blockIdx.x * (long long)blockDim.x + threadIdx.x) / G;
     const int lane = threadIdx.x % G;
     const unsigned gmask = G == 32 ? 0xffffffffu : (((1u << G) - 1u) << ((threadIdx.x & 31) / G * G));
@@ -154,19 +158,33 @@ __global__ void __launch_bounds__(256) cast_rays_batch_kernel(const NbRayJob* __
     int lo = 0, hi = n_jobs - 1;
     while (lo < hi) {                          // last job with ray0 <= gid
         const int mid = (lo + hi + 1) >> 1;
-        if (jobs[mid].ray0 <= gid) lo = mid; else hi = mid - 1;
+        if (J[mid].ray0 <= gid) lo = mid; else hi = mid - 1;
     }
-    const NbRayJob& J = jobs[lo];
-    const NbConst& C = *J.c;
+    const NbRayJob& job = J[lo];
+    const NbConst& C = *job.c;
     const int nray = C.nu * C.nphi;
-    const long long local = gid - J.ray0;
+    const long long local = gid - job.ray0;
     const int s = (int)(local / nray), ray = (int)(local % nray);
-    const bool star = in && s < J.nstars && J.active;
+    const bool star = in && s < job.nstars && Jd[lo].active;
     NbStarW w{};
-    if (star) w = J.sw[s];
+    if (star) w = job.sw[s];
     const int iu = ray / C.nphi, ip = ray - iu * C.nphi;
-    cast_ray<G>(C, J.dirs, J.rho, front_slot(J.rfront, J.pairs != 0, s, nray, C.nu, iu, ip), ray, w.w.x, w.w.y, w.w.z,
-                w.q_f, lane, gmask, star && w.active);
+    cast_ray<G>(C, job.dirs, job.rho, front_slot(job.rfront, job.pairs != 0, s, nray, C.nu, iu, ip), ray, w.w.x,
+                w.w.y, w.w.z, w.q_f, lane, gmask, star && w.active);
+}
+
+template <int G>
+__global__ void __launch_bounds__(256) cast_rays_batch_kernel(const NbRayJob* __restrict__ jobs, int n_jobs,
+                                                              long long n_groups) {
+    cast_rays_batch_body<G>(jobs, jobs, n_jobs, n_groups);
+}
+
+// the job records in the kernel parameter (constant bank): 48 registers, 5 blocks / SM
+template <int G>
+__global__ void __launch_bounds__(256, NB_CAST_RAYS_MINB)
+    cast_rays_batch_param_kernel(const __grid_constant__ NbRayJobs P, const NbRayJob* __restrict__ jobs, int n_jobs,
+                                 long long n_groups) {
+    cast_rays_batch_body<G>(P.J, jobs, n_jobs, n_groups);
 }
 
 // The stars that can change xi or the front distance of the 32-cell segment [kb, kb + 32) of a
@@ -603,12 +621,25 @@ cudaError_t nb_launch_smooth(const NbConst* c, const float* xi_raw, float* xi, c
     return cudaGetLastError();
 }
 
-cudaError_t nb_launch_ionize_batch(const NbRayJob* jobs, int n_jobs, long long n_groups, long long n_blocks, int group,
-                                   cudaStream_t s) {
+cudaError_t nb_launch_ionize_batch(const NbRayJob* jobs, const NbRayJob* host_jobs, int n_jobs, long long n_groups,
+                                   long long n_blocks, int group, cudaStream_t s) {
     if (n_jobs <= 0) return cudaSuccess;
     const long long threads = n_groups * group;
     const long long blocks = (threads + 255) / 256;
-    if (blocks > 0) {
+    if (blocks > 0 && host_jobs && n_jobs <= NB_BATCH_PARAM_MAX) {
+        NbRayJobs P;
+        std::memset(&P, 0, sizeof(P));
+        std::memcpy(P.J, host_jobs, sizeof(NbRayJob) * n_jobs);
+        const unsigned nb = (unsigned)blocks;
+        switch (group) {
+            case 1: cast_rays_batch_param_kernel<1><<<nb, 256, 0, s>>>(P, jobs, n_jobs, n_groups); break;
+            case 2: cast_rays_batch_param_kernel<2><<<nb, 256, 0, s>>>(P, jobs, n_jobs, n_groups); break;
+            case 4: cast_rays_batch_param_kernel<4><<<nb, 256, 0, s>>>(P, jobs, n_jobs, n_groups); break;
+            case 8: cast_rays_batch_param_kernel<8><<<nb, 256, 0, s>>>(P, jobs, n_jobs, n_groups); break;
+            case 16: cast_rays_batch_param_kernel<16><<<nb, 256, 0, s>>>(P, jobs, n_jobs, n_groups); break;
+            default: cast_rays_batch_param_kernel<32><<<nb, 256, 0, s>>>(P, jobs, n_jobs, n_groups); break;
+        }
+    } else if (blocks > 0) {
         switch (group) {
             case 1: cast_rays_batch_kernel<1><<<(unsigned)blocks, 256, 0, s>>>(jobs, n_jobs, n_groups); break;
             case 2: cast_rays_batch_kernel<2><<<(unsigned)blocks, 256, 0, s>>>(jobs, n_jobs, n_groups); break;
