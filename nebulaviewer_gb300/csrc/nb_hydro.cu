@@ -758,7 +758,7 @@ __global__ void __launch_bounds__(TK * TJ, NB_HYDRO_MINB) hydro_stage_kernel(con
 // more: it keeps taking items and flags the instance of each one it leaves undone, so every
 // instance with an unwritten tile reports NB_DEV_TMA_TIMEOUT.
 #ifndef NB_HYDRO_BATCH_MINB
-#define NB_HYDRO_BATCH_MINB 3            // the persistent kernel's loop state needs the 80-register budget
+#define NB_HYDRO_BATCH_MINB 3            // records in global memory: their loaded fields need the 80-register budget
 #endif
 template <int SOLVER, int LIM, int TJ, bool STAGE2, bool I32>
 __global__ void __launch_bounds__(TK * TJ, NB_HYDRO_BATCH_MINB)
