@@ -16,8 +16,9 @@
 // SM.  A plane is converted once to primitives (rho, u, v, w) and (c^2, c) in shared memory (each
 // thread's own and halo cell, at offsets computed once per tile); every face flux is then
 // evaluated once (the reference evaluates each face twice) and shared through shared memory
-// (y, z faces) or registers (x faces; each cell's limited x slope is also carried to the next
-// face).  Sources: the wind loop over the active stars in ionized cells, the jet loop over
+// (y, z faces; the z faces by warp shuffle where the slopes are kept per cell) or registers (x
+// faces; each cell's limited x slope is also carried to the next face).  The exact build also
+// evaluates each limited y / z slope once per cell (NB_ONCE_SLOPES).  Sources: the wind loop over the active stars in ionized cells, the jet loop over
 // the tile's list of stars whose jet can reach it.  Cell offsets are 32-bit on grids below 2^31
 // cells.  Stage 2 also reduces the CFL max speed of the new state (nebula3d.py:154-162) into
 // one atomic.
@@ -48,6 +49,18 @@ __device__ __forceinline__ float slope_lim(float a, float b) {
 #define NB_PAIRED 1
 #else
 #define NB_PAIRED 0
+#endif
+#endif
+
+// Each limited y / z slope evaluated once per cell and kept in shared memory, or once per face.
+// Once per cell pays in the exact build, whose slopes cost a product, two compares and two selects
+// per component (stages -5.5%); the fast build's three-operation minmod is cheaper than the extra
+// shared-memory traffic (+5% / +8% measured), so it evaluates them per face.  Same bits either way.
+#ifndef NB_ONCE_SLOPES
+#if NB_PAIRED
+#define NB_ONCE_SLOPES 0
+#else
+#define NB_ONCE_SLOPES 1
 #endif
 #endif
 
@@ -319,6 +332,17 @@ __device__ __forceinline__ float4 face_flux(const float4 qa, const float4 qb, co
 #endif
 }
 
+// the face flux from the face's two cells and their limited slopes along its axis
+template <int SOLVER, int AX>
+__device__ __forceinline__ float4 face_flux_sl(const float4 qb, const float4 qc, const float4 sl, const float4 sr,
+                                               const float2 csb, const float2 csc, const float floor_) {
+#if NB_PAIRED
+    return face_flux_paired_sl<SOLVER, AX>(qb, qc, sl, sr, csb, csc, floor_);
+#else
+    return face_flux_scalar_sl<SOLVER, AX>(qb, qc, sl, sr, csb, csc, floor_);
+#endif
+}
+
 template <int SOLVER, int LIM>
 __device__ __forceinline__ float4 cell_slopes(const float4 qa, const float4 qb, const float4 qc) {
     constexpr int LM = SOLVER == NB_SOLVER_HLL ? LIM : 0;
@@ -347,11 +371,20 @@ template <int TJ>
 struct HydroSmem {
     static constexpr int RAW_FIELD = (TJ + 4) * RAWW;                     // floats per field
     static constexpr int RAW_BYTES = 5 * RAW_FIELD * 4;                      // one raw slot
-    static constexpr int PRIM_BYTES = 4 * (TJ + 4) * PW * 16;
+#if NB_ONCE_SLOPES
+    static constexpr int PRIM_BYTES = 3 * (TJ + 4) * PW * 16;               // planes p-2, p-1, p
     static constexpr int CS_BYTES = 3 * (TJ + 4) * PW * 8;
-    static constexpr int FACE_BYTES = ((TJ + 1) * TK + TJ * (TK + 1)) * 16;
+    static constexpr int SY_BYTES = (TJ + 2) * TK * 16;                     // y slopes, rows j0-1 .. j0+TJ
+    static constexpr int SZ_BYTES = TJ * (TK + 2) * 16;                     // z slopes, columns k0-1 .. k0+TK
+    static constexpr int FACE_BYTES = ((TJ + 1) * TK + TJ) * 16;            // y faces; the z faces k0-1/2
+#else
+    static constexpr int PRIM_BYTES = 4 * (TJ + 4) * PW * 16;               // planes p-3 .. p
+    static constexpr int CS_BYTES = 3 * (TJ + 4) * PW * 8;
+    static constexpr int SY_BYTES = 0, SZ_BYTES = 0;
+    static constexpr int FACE_BYTES = ((TJ + 1) * TK + TJ * (TK + 1)) * 16; // y faces; z faces
+#endif
     static constexpr int BAR_BYTES = 64;
-    static constexpr int FIXED = RAW_BYTES + PRIM_BYTES + CS_BYTES + FACE_BYTES + BAR_BYTES;
+    static constexpr int FIXED = RAW_BYTES + PRIM_BYTES + CS_BYTES + SY_BYTES + SZ_BYTES + FACE_BYTES + BAR_BYTES;
     // star tables: positions / wind weights and jets (2 x float4 per star), then the tile's jet
     // list: a count and the indices (one byte each) of the stars whose jet can reach the tile
     __host__ __device__ static int jet_list_offset(int nstars) { return FIXED + nstars * 32; }
@@ -388,10 +421,17 @@ __device__ __forceinline__ void hydro_tile(const HydroLaunch& L, int tile, unsig
         smem += zero;
     }
     float* raw = reinterpret_cast<float*>(smem);                                   // [5][TJ+4][40]
-    float4* prim = reinterpret_cast<float4*>(smem + SM::RAW_BYTES);                // [4][TJ+4][36]
+    float4* prim = reinterpret_cast<float4*>(smem + SM::RAW_BYTES);                // [4 or 3][TJ+4][36]
     float2* cs = reinterpret_cast<float2*>(smem + SM::RAW_BYTES + SM::PRIM_BYTES); // [3][TJ+4][36]
+#if NB_ONCE_SLOPES
+    float4* sy = reinterpret_cast<float4*>(smem + SM::RAW_BYTES + SM::PRIM_BYTES + SM::CS_BYTES);  // [TJ+2][32]
+    float4* sz = sy + (TJ + 2) * TK;                                               // [TJ][34]
+    float4* fy = sz + TJ * (TK + 2);                                               // [TJ+1][32]
+    float4* fz0 = fy + (TJ + 1) * TK;                                              // [TJ]
+#else
     float4* fy = reinterpret_cast<float4*>(smem + SM::RAW_BYTES + SM::PRIM_BYTES + SM::CS_BYTES);  // [TJ+1][32]
     float4* fz = fy + (TJ + 1) * TK;                                               // [TJ][33]
+#endif
     uint64_t* bar = reinterpret_cast<uint64_t*>(smem + SM::FIXED - SM::BAR_BYTES);
     float4* sw_w = reinterpret_cast<float4*>(smem + SM::FIXED);
     const NbConst& C = *L.c;
@@ -442,10 +482,15 @@ __device__ __forceinline__ void hydro_tile(const HydroLaunch& L, int tile, unsig
     };
     // the per-plane extra work, on warps of schedulers rot, rot+1, rot+2 and rot+3 (mod 4): the y
     // faces below the tile (role bit 1), the z faces before it (bit 2), the z-halo conversion,
-    // the TMA issue (bit 4)
+    // the TMA issue (bit 4); with once-per-cell slopes also the slopes of the halo cells the faces
+    // read: the y slopes of row j0-1 (bit 8) and of row j0+TJ (bit 16), the z slopes of columns
+    // k0-1 and k0+TK (bit 32)
     const int w_zhalo = 4 + ((rot + 2) & 3);
     const unsigned role = (tj == rot ? 1u : 0u) | (tj == ((rot + 1) & 3) && tk < TJ ? 2u : 0u) |
-                          (tid == (4 + ((rot + 3) & 3)) * 32 ? 4u : 0u);
+                          (tid == (4 + ((rot + 3) & 3)) * 32 ? 4u : 0u) |
+                          (NB_ONCE_SLOPES && tj == 4 + (rot & 3) ? 8u : 0u) |
+                          (NB_ONCE_SLOPES && tj == 4 + ((rot + 1) & 3) ? 16u : 0u) |
+                          (NB_ONCE_SLOPES && tj == 4 + ((rot + 3) & 3) && tk < 2 * TJ ? 32u : 0u);
     if (role & 4u) issue(P0);
     if (tj == 0) {
         // The stars whose jet (nebula3d.py:131-149: strength > 0, an active star, r < jet_r) can reach
@@ -512,8 +557,16 @@ __device__ __forceinline__ void hydro_tile(const HydroLaunch& L, int tile, unsig
     constexpr int PSLOT = (TJ + 4) * PW;
 
     for (int p = P0; p <= P1; ++p) {
+#if NB_ONCE_SLOPES
+        // slots of planes p, p-1, p-2 in the three-plane rings of primitives and sound speeds
+        const int cq = (p - P0) % 3;
+        const int cq1 = cq == 0 ? 2 : cq - 1;
+        const int cq2 = cq1 == 0 ? 2 : cq1 - 1;
+        const int ps = cq;
+#else
         const int ps = (p - P0) & 3;                 // prim slot of plane p (4 slots: p-3..p)
         const int cq = (p - P0) % 3;                 // cs slot of plane p (3 slots: p-2..p)
+#endif
         // own-cell values of plane i = p - 2 the epilogue needs, issued before the flux work
         const int i = p - 2;
         const Idx cell = ((Idx)i * ny + j) * nz + k;
@@ -526,6 +579,31 @@ __device__ __forceinline__ void hydro_tile(const HydroLaunch& L, int tile, unsig
                 u00 = L.u0[0][cell]; u01 = L.u0[1][cell]; u02 = L.u0[2][cell]; u03 = L.u0[3][cell];
             }
         }
+        const int jj = tj + 2, kk = tk + 2;
+#if NB_ONCE_SLOPES
+        if (work) {
+            // ---- the limited y and z slopes of every cell of plane i that the faces read, each
+            // evaluated once (a face's two slopes are its cells' slopes along its axis: the same
+            // operands, the same bits).  Plane i was converted two planes ago and the previous
+            // plane's faces are done (its second barrier), so no barrier is needed here, and this
+            // work overlaps the wait for plane p's tile.
+            const float4* q = prim + cq2 * PSLOT;
+            const float4 qo = q[jj * PW + kk];
+            sy[(tj + 1) * TK + tk] = cell_slopes<SOLVER, LIM>(q[(jj - 1) * PW + kk], qo, q[(jj + 1) * PW + kk]);
+            sz[tj * (TK + 2) + tk + 1] = cell_slopes<SOLVER, LIM>(q[jj * PW + kk - 1], qo, q[jj * PW + kk + 1]);
+            if (role & 8u)                       // row j0-1: primitive rows 0..2
+                sy[tk] = cell_slopes<SOLVER, LIM>(q[0 * PW + kk], q[1 * PW + kk], q[2 * PW + kk]);
+            if (role & 16u)                      // row j0+TJ: primitive rows TJ+1..TJ+3
+                sy[(TJ + 1) * TK + tk] = cell_slopes<SOLVER, LIM>(q[(TJ + 1) * PW + kk], q[(TJ + 2) * PW + kk],
+                                                                  q[(TJ + 3) * PW + kk]);
+            if (role & 32u) {                    // columns k0-1 (lanes 0..TJ-1) and k0+TK (lanes TJ..2TJ-1)
+                const int r = tk & (TJ - 1);
+                const int c0 = tk < TJ ? 0 : TK + 1;
+                const int b = (r + 2) * PW + c0;
+                sz[r * (TK + 2) + c0] = cell_slopes<SOLVER, LIM>(q[b], q[b + 1], q[b + 2]);
+            }
+        }
+#endif
         const bool ok = mbar_wait_limited(&bar[0], ph0, &L.wait_limit);
         if (ok) ph0 ^= 1u;                       // a timed-out wait keeps its parity for the abort wait
         if (__syncthreads_or(!ok)) { failed = true; break; }
@@ -551,6 +629,41 @@ __device__ __forceinline__ void hydro_tile(const HydroLaunch& L, int tile, unsig
         if (has_halo) convert(raw_halo, prim_halo);
         __syncthreads();                         // every thread is done with the raw slot
         if ((role & 4u) && p + 1 <= P1) issue(p + 1);
+#if NB_ONCE_SLOPES
+        if (p < P0 + 2) continue;
+        if (p == P0 + 2) {                       // the x slope of plane P0+1 (planes P0, P0+1, P0+2)
+            xslope = cell_slopes<SOLVER, LIM>(prim[cq2 * PSLOT + own], prim[cq1 * PSLOT + own], pp[own]);
+            continue;
+        }
+        // x face (p-2)+1/2 from the own column of planes p-2..p and the carried slope of p-2
+        const float4 fx_new = face_flux_x<SOLVER, LIM>(prim[cq2 * PSLOT + own], prim[cq1 * PSLOT + own], pp[own],
+                                                       cs[cq2 * PSLOT + own], cs[cq1 * PSLOT + own], floor_, xslope);
+        if (!work) { fx_prev = fx_new; continue; }
+        // ---- the y and z faces of cell plane i, from the cells and their slopes
+        const float4* q = prim + cq2 * PSLOT;
+        const float2* c = cs + cq2 * PSLOT;
+        const float4 fyp = face_flux_sl<SOLVER, 2>(q[jj * PW + kk], q[(jj + 1) * PW + kk], sy[(tj + 1) * TK + tk],
+                                                   sy[(tj + 2) * TK + tk], c[jj * PW + kk], c[(jj + 1) * PW + kk],
+                                                   floor_);
+        const float4 fzp = face_flux_sl<SOLVER, 3>(q[jj * PW + kk], q[jj * PW + kk + 1], sz[tj * (TK + 2) + tk + 1],
+                                                   sz[tj * (TK + 2) + tk + 2], c[jj * PW + kk], c[jj * PW + kk + 1],
+                                                   floor_);
+        fy[(tj + 1) * TK + tk] = fyp;
+        if (role & 1u) {                        // the y face below the tile: (j0-1)+1/2
+            fy[tk] = face_flux_sl<SOLVER, 2>(q[1 * PW + kk], q[2 * PW + kk], sy[tk], sy[TK + tk], c[1 * PW + kk],
+                                             c[2 * PW + kk], floor_);
+        } else if (role & 2u) {                 // the z face before the tile in row tk: (k0-1)+1/2
+            const int r2 = (tk + 2) * PW;
+            fz0[tk] = face_flux_sl<SOLVER, 3>(q[r2 + 1], q[r2 + 2], sz[tk * (TK + 2)], sz[tk * (TK + 2) + 1],
+                                              c[r2 + 1], c[r2 + 2], floor_);
+        }
+        __syncthreads();
+        const float4 fym = fy[tj * TK + tk];
+        // the z face k-1/2 is the lower lane's k+1/2; lane 0 takes the face before the tile
+        float4 fzm = make_float4(__shfl_up_sync(0xffffffffu, fzp.x, 1), __shfl_up_sync(0xffffffffu, fzp.y, 1),
+                                 __shfl_up_sync(0xffffffffu, fzp.z, 1), __shfl_up_sync(0xffffffffu, fzp.w, 1));
+        if (tk == 0) fzm = fz0[tj];
+#else
         if (p < P0 + 3) continue;
         // x face (p-2)+1/2 from the own column of planes p-2..p and the carried slope of p-2
         const float4 qx1 = prim[((p - 2 - P0) & 3) * PSLOT + own], qx2 = prim[((p - 1 - P0) & 3) * PSLOT + own];
@@ -562,7 +675,6 @@ __device__ __forceinline__ void hydro_tile(const HydroLaunch& L, int tile, unsig
         const int si = (i - P0) & 3;
         const float4* q = prim + si * PSLOT;
         const float2* c = cs + ((i - P0) % 3) * PSLOT;
-        const int jj = tj + 2, kk = tk + 2;
         const float4 fyp = face_flux<SOLVER, LIM, 2>(q[(jj - 1) * PW + kk], q[jj * PW + kk], q[(jj + 1) * PW + kk],
                                                      q[(jj + 2) * PW + kk], c[jj * PW + kk], c[(jj + 1) * PW + kk],
                                                      floor_);
@@ -582,6 +694,7 @@ __device__ __forceinline__ void hydro_tile(const HydroLaunch& L, int tile, unsig
         __syncthreads();
         const float4 fym = fy[tj * TK + tk];
         const float4 fzm = fz[tj * (TK + 1) + tk];
+#endif
         const float4 fxp = fx_new, fxm = fx_prev;
         fx_prev = fx_new;
         // div = 0 + (fR-fL)_x, then += (fR-fL)_y, then += (fR-fL)_z  (nebula3d.py:87-109)
