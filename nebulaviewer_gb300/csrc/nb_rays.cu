@@ -188,35 +188,47 @@ __global__ void __launch_bounds__(256, NB_CAST_RAYS_MINB)
 }
 
 // The stars that can change xi or the front distance of the 32-cell segment [kb, kb + 32) of a
-// row, as a mask (nstars <= NB_ROW_STARS; lane s bounds star s).  Over the segment a star's
+// row, as a mask (1 <= nstars <= NB_ROW_STARS).  Over the segment a star's
 // r - rf lies in [LB, UB]: LB = (least distance to the segment) - (largest front radius of the
 // star), UB = (largest distance) - (smallest front radius).  A star with LB at or above both
 // min(1e3, least UB over the stars) and width / 2, plus a margin of one cell for float rounding,
 // gives every cell of the segment val = 0 (no xi) and an r - rf above another star's (no front
 // distance): leaving it out changes no bit.  A NaN bound (NaN radii or positions, whose min /
 // max merges depend on order) keeps every active star.
-__device__ __forceinline__ unsigned segment_stars(const float4* st, const int* act, const float4* tab,
-                                                  const float2* bnd, int nstars, int kb, int nz, float dx,
-                                                  float width) {
+// Computed for per_pass = 32 / nstars consecutive segments [kb0 + 32 g, kb0 + 32 g + 32) at once:
+// lane g * nstars + s bounds star s over segment g, each segment's least upper bound is gathered
+// from its nstars lanes, and lane g returns segment g's mask (bit s: star s).  One warp pass per
+// per_pass segments: the culling costs ~per_pass times fewer instructions per cell.
+__device__ __forceinline__ unsigned segment_masks(const float4* st, const int* act, const float4* tab,
+                                                  const float2* bnd, int nstars, int kb0, int per_pass, int nz,
+                                                  float dx, float width) {
     const int lane = threadIdx.x;
-    const bool on = lane < nstars && act[lane];
-    float lb = __int_as_float(0x7f800000), ub = lb;       // +inf: the lane has no star
+    const int g = lane / nstars, s = lane - g * nstars;
+    const int kb = kb0 + 32 * g;
+    const bool on = g < per_pass && kb < nz && act[s];
+    float lb = __int_as_float(0x7f800000), ub = lb;       // +inf: the lane bounds no star
+    bool bad = false;
     if (on) {
-        const float sz = st[lane].z, d2 = tab[lane].x;
-        const float2 b = bnd[lane];                       // (least, largest) front radius
+        const float sz = st[s].z, d2 = tab[s].x;
+        const float2 b = bnd[s];                          // (least, largest) front radius
         const float z0 = ((float)kb + 0.5f) * dx, z1 = ((float)(min(kb + 31, nz - 1)) + 0.5f) * dx;
         const float en = fmaxf(0.0f, fmaxf(z0 - sz, sz - z1));
         const float ex = fmaxf(fabsf(sz - z0), fabsf(sz - z1));
         lb = sqrtf(d2 + en * en) - b.y;
         ub = sqrtf(d2 + ex * ex) - b.x;
+        bad = isnan(lb) || isnan(ub);
     }
-    const unsigned all = __ballot_sync(0xffffffffu, on);
-    if (__any_sync(0xffffffffu, isnan(lb) || isnan(ub))) return all;
-    float m = ub;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) m = fminf(m, __shfl_xor_sync(0xffffffffu, m, o));
+    const int base = min(g * nstars, 31);
+    float m = __int_as_float(0x7f800000);
+    for (int t = 0; t < nstars; ++t) m = fminf(m, __shfl_sync(0xffffffffu, ub, min(base + t, 31)));
     const float thr = fmaxf(fminf(1e3f, m), 0.5f * width) + dx;
-    return __ballot_sync(0xffffffffu, on && lb < thr);
+    const unsigned keep = __ballot_sync(0xffffffffu, on && lb < thr);
+    const unsigned all = __ballot_sync(0xffffffffu, on);
+    const unsigned nan = __ballot_sync(0xffffffffu, bad);
+    if (lane >= per_pass) return 0u;
+    const int sh = lane * nstars;
+    const unsigned full = nstars == 32 ? 0xffffffffu : ((1u << nstars) - 1u);
+    return ((nan >> sh) & full) ? (all >> sh) & full : (keep >> sh) & full;
 }
 
 // nebula3d.py:273-307 rf_at + apply_front over one row (i, j), fused over the active stars,
@@ -245,8 +257,16 @@ __device__ __forceinline__ void apply_front_row(const NbConst& C, const float4* 
     if (tab) star_row_table(st, act, nstars, px, py, nphi, nu, tab);
     const unsigned row_stars = tab ? __ballot_sync(0xffffffffu, (int)threadIdx.x < nstars && act[threadIdx.x]) : 0u;
     constexpr int SG = 2;                       // stars whose gathers are in flight together
-    for (int kb = 0; kb < nz; kb += 32) {
-        const unsigned seg = bnd ? segment_stars(st, act, tab, bnd, nstars, kb, nz, dx, width) : row_stars;
+    // the culling masks of per_pass segments come from one pass (segment_masks): lane g holds
+    // segment g's, broadcast when that segment's cells are merged
+    if (nstars < 1) bnd = nullptr;
+    const int per_pass = bnd ? 32 / nstars : 1;
+    for (int kb0 = 0; kb0 < nz; kb0 += 32 * per_pass) {
+      const unsigned masks = bnd ? segment_masks(st, act, tab, bnd, nstars, kb0, per_pass, nz, dx, width) : 0u;
+      for (int g = 0; g < per_pass; ++g) {
+        const int kb = kb0 + 32 * g;
+        if (kb >= nz) break;                     // uniform over the warp
+        const unsigned seg = bnd ? __shfl_sync(0xffffffffu, masks, g) : row_stars;
         const int k = kb + (int)threadIdx.x;
         if (k >= nz) continue;
         const long long q = base + k;
@@ -341,6 +361,7 @@ __device__ __forceinline__ void apply_front_row(const NbConst& C, const float4* 
             reinterpret_cast<__half*>(dfront)[q] = __float2half_rn(df);
         else
             reinterpret_cast<float*>(dfront)[q] = df;
+      }
     }
 }
 
