@@ -612,7 +612,7 @@ def served_result(args, requests):
         s = plain_sims[r.snap]
         snaps[r.snap].branch_into(s, r.mod)
         s.step(r.nsteps)
-        serve.result_of(s)
+        serve.result_of(s, keep_state=False)
         plain_cells += s._n * r.nsteps
     plain_s = time.perf_counter() - t0
     for s in plain_sims.values():

@@ -242,8 +242,8 @@ int nb_cast_fuv(nb_handle h, const double star_xyz[3], float* att_out);
  * with its own clock, CFL dt, stars and ionization cadence (it % ion_every, sim.py:1102).
  * A batch step = one control launch for every instance, the ionization of every instance due
  * to ionize (3 launches), and one persistent launch per RK2 stage walking a tile work-list that
- * spans all instances; the step is replayed as a CUDA graph when every instance or none
- * ionizes.  The instances must share solver, limiter and stream and be in the main phase
+ * spans all instances; the step is replayed as a CUDA graph when every slot is active and every
+ * instance or none ionizes.  The instances must share solver, limiter and stream and be in the main phase
  * without stirring (NB_ERR_STATE otherwise: step those alone); the batch works on its own
  * stream, ordered after / before the instances' stream by events.  The instance handles stay
  * valid and usable between batch steps (nb_step, nb_fuv, nb_get_clock ...). */
@@ -254,8 +254,9 @@ int nb_batch_step(nb_batch b, int k);
 /* Slots of a batch (no reference counterpart; a server keeps a pool of instances in one batch): n
  * flags, one per instance in nb_batch_create's order; an idle slot (0) is not stepped -- no weights,
  * clock, rays or tiles -- and is left as it is, so instances can join and leave the stepping set
- * without rebuilding the batch or its graphs.  All slots start active.  Synchronizes the batch's
- * stream. */
+ * without rebuilding the batch or its graphs.  The work list is compacted to the active slots'
+ * tiles; while a slot is idle, steps are launched as they go (on the active and due instances'
+ * work only) rather than replayed.  All slots start active.  Synchronizes the batch's stream. */
 int nb_batch_set_active(nb_batch b, const int* active, int n);
 int nb_batch_set_option(nb_batch b, int key, int value);
 int nb_batch_counters(nb_batch b, long long* launches);

@@ -958,8 +958,9 @@ struct nb_batch_s {
     NbBatchInst* d_inst = nullptr;
     HydroLaunch* d_L1 = nullptr;
     HydroLaunch* d_L2 = nullptr;
-    int2* d_work = nullptr;
-    int n_work = 0;
+    int2* d_work = nullptr;             // the work items of the active instances, in list order
+    int n_work = 0;                     // ... their count
+    std::vector<int2> h_work;           // every instance's items, in list order
     unsigned* d_counters = nullptr;
     NbRayJob* d_jobs_all = nullptr;     // every instance ionizes (the lockstep case)
     long long all_groups = 0, all_blocks = 0;
@@ -1191,6 +1192,7 @@ NB_EXPORT int nb_batch_create(const nb_handle* hs, const int* ion_every, int n, 
         for (int t = 0; t < tiles; ++t) work.push_back(make_int2(i, t));
     }
     b->n_work = (int)work.size();
+    b->h_work = work;
     b->h_all.resize(n);
     for (int i = 0; i < n; ++i) b->h_all[i] = ray_job(b->inst[i]);
     job_prefix(b->h_all, b->inst, b->all_groups, b->all_blocks);
@@ -1269,8 +1271,16 @@ NB_EXPORT int nb_batch_set_active(nb_batch b, const int* active, int n) {
         na += a;
     }
     b->n_active = na;
+    // the work list of the active instances only: an idle instance's tiles are not walked at all
+    std::vector<int2> work;
+    work.reserve(b->h_work.size());
+    for (const int2& w : b->h_work)
+        if (b->active[w.x]) work.push_back(w);
+    b->n_work = (int)work.size();
     // in stream order before the next step; the captured graphs read these arrays when they run
     cudaStream_t s = b->bs;
+    if (!work.empty())
+        BCK(b, cudaMemcpyAsync(b->d_work, work.data(), sizeof(int2) * work.size(), cudaMemcpyHostToDevice, s));
     BCK(b, cudaMemcpyAsync(b->d_inst, b->h_inst.data(), sizeof(NbBatchInst) * n, cudaMemcpyHostToDevice, s));
     BCK(b, cudaMemcpyAsync(b->d_L1, b->h_L1.data(), sizeof(HydroLaunch) * n, cudaMemcpyHostToDevice, s));
     BCK(b, cudaMemcpyAsync(b->d_L2, b->h_L2.data(), sizeof(HydroLaunch) * n, cudaMemcpyHostToDevice, s));
@@ -1308,12 +1318,15 @@ NB_EXPORT int nb_batch_step(nb_batch b, int k) {
         for (int i = 0; i < n; ++i)
             if (b->active[i] && b->inst[i]->host_it % b->ion_every[i] == 0) due.push_back(i);
         int rc = NB_OK;
-        // every active slot or none ionizes: the captured graphs (idle slots skip themselves)
-        const bool all = (int)due.size() == b->n_active, none = due.empty();
-        if (b->use_graphs && (all || none) && (all ? b->warm_ion : b->warm_plain)) {
+        // every slot active and every or no slot ionizing: the captured graphs.  With idle slots the
+        // step is launched as it goes, on the active instances' work list and the due instances'
+        // ray jobs only (a captured step would walk the idle instances' rays and cells too).
+        const bool full = b->n_active == n;
+        const bool all = (int)due.size() == n, none = due.empty();       // all: every slot active and due
+        if (b->use_graphs && full && (all || none) && (all ? b->warm_ion : b->warm_plain)) {
             rc = batch_run_graph(b, all ? &b->g_ion : &b->g_plain, all ? 1 : 0);
         } else {
-            if (all) {                           // every active slot: the whole job list (idle slots skip)
+            if (all) {                           // every slot ionizes: the whole job list
                 rc = batch_ionize(b, b->d_jobs_all, b->h_all.data(), n, b->all_groups, b->all_blocks, due);
                 b->warm_ion = 1;
             } else if (!none) {

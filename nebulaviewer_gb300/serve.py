@@ -23,6 +23,7 @@ import collections
 import time
 
 import numpy as np
+import torch
 
 from .batch import BatchSim
 from .sim import Sim, footprint_bytes
@@ -115,13 +116,16 @@ def poisson_requests(snapshots, n, rate, seed=0, steps=(10, 100), factor=0.5):
     return out
 
 
-def result_of(sim):
-    """what a finished request returns: the clock, FP64 totals and a digest of the fields"""
+def result_of(sim, keep_state=True):
+    """what a finished request returns: the clock, FP64 totals, a digest of the fields and (keep_state)
+    a copy of the state"""
     c = sim._clock()
     tot = sim.conservation()
     xi = sim._xi
-    return dict(t=c.t, it=int(c.it), totals=tot, xi_mean=float(xi.double().mean()),
-                state=[t.clone() for t in (sim._rho, sim._mx, sim._my, sim._mz, sim._xi)])
+    out = dict(t=c.t, it=int(c.it), totals=tot, xi_mean=float(xi.sum(dtype=torch.float64)) / xi.numel())
+    if keep_state:
+        out["state"] = [t.clone() for t in (sim._rho, sim._mx, sim._my, sim._mz, sim._xi)]
+    return out
 
 
 class _Slot:
@@ -186,9 +190,7 @@ class Server:
 
         def finish(slot):            # the result; the instance stays in the pool, idle
             r = slot.req
-            r.result = result_of(slot.sim)
-            if not self.keep_state:
-                r.result.pop("state")
+            r.result = result_of(slot.sim, self.keep_state)
             r.sim = None
             r.t_done = time.perf_counter() - t0
             done.append(r)

@@ -75,7 +75,8 @@ def install(monkeypatch, max_slots=None, budget=None, fail_on_tick=None):
             self.closed = True
 
     monkeypatch.setattr(serve, "BatchSim", FakeBatch)
-    monkeypatch.setattr(serve, "result_of", lambda sim: dict(t=0.0, it=sim.steps, totals=None, xi_mean=0.0, state=[]))
+    monkeypatch.setattr(serve, "result_of", lambda sim, keep_state=True: dict(t=0.0, it=sim.steps, totals=None,
+                                                                              xi_mean=0.0, state=[]))
     return log
 
 
