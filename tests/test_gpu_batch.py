@@ -159,3 +159,34 @@ def test_footprint_is_known_before_allocation_and_matches_the_device(nb):
     assert abs(used - fp) <= 0.03 * fp + (32 << 20), (used, fp)
     assert fp > 40 * s._n + 100e6                     # the FUV and front tables are most of it here
     s.close()
+
+
+def test_batch_beyond_the_parameter_records(nb):
+    """a batch of 130 instances: more than the 128 whose stage records the persistent kernel takes as
+    its parameter, so it reads them from device memory (the other form of the kernel); every
+    instance still ends exactly where stepping it alone ends, with a slot idle for part of it"""
+    batch, ics, S = nb
+    shapes = [(16, 16, 16), (16, 24, 20), (24, 16, 12)]
+    ics_list = [ics.torus(seed=100 + m, device="cuda", shape=shapes[m % 3], nstars=1) if m % 2 == 0 else
+                ics.sheet(res=16, seed=200 + m, nstars=1, device="cuda", shape=shapes[m % 3]) for m in range(130)]
+
+    def mk(ic):
+        return S.Sim.from_state(ic["shape"], ic["dx"], ic["rho"], ic["stars"], ic["kinds"], ic["jets"], ic["jkinds"],
+                                ic["P"], mom=ic["mom"], rays=(16, 32), fuv_grid=(8, 8, 16), arith="exact")
+
+    sims = [mk(ic) for ic in ics_list]
+    B = batch.BatchSim(sims)
+    flags = [1] * 130
+    flags[7] = 0
+    B.set_active(flags)
+    B.step(2)
+    B.set_active([1] * 130)
+    B.step(2)
+    for m, (s, ic) in enumerate(zip(sims, ics_list)):
+        a = mk(ic)
+        a.step(2 if m == 7 else 4)
+        same(state(s), state(a))
+        a.close()
+    B.close()
+    for s in sims:
+        s.close()
