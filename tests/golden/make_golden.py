@@ -375,6 +375,11 @@ BAKE_CASES = {
     "bubbles": dict(overrides=dict(seed=5, min_sep=0.2), t_end=0.16, frames=5,
                     birth=([0.3, 0.6, 0.4], 5.0e-5, 0.05, [0.0, 0.0, 1.0], "none"),
                     events=[[0.03, "wind", 0.8], [0.09, "q_main", 0.7]]),
+    # the cloud wall lit from above: main stars kept wherever they are (above the gas, possibly
+    # outside the box), embedded stars, globules on the wall's face
+    "cliff": dict(overrides=dict(seed=9), t_end=0.1, frames=4,
+                  birth=([0.5, 0.2, 0.5], 1.0e-4, 0.04, [0.0, 1.0, 0.0], "jet"),
+                  events=[[0.02, "wind", 0.6], [0.06, "q_main", 1.3]]),
 }
 
 

@@ -8,7 +8,9 @@ with dt_cap (bake.py:67-114).  tests/golden/bake_<scene>.npz holds a reference `
 constructor left it (the default matched initial conditions, fast=False budgets) and the frames the
 reference wrote running that loop: the bipolar preset (a stirring phase first) and the bubbles
 preset (straight into the main phase, six stars with winds, the preset's triggered star formation
-on at construction -- switched off for the hand-over, as bake.py does).  Here a stand-in object carrying exactly the
+on at construction -- switched off for the hand-over, as bake.py does) and the cliff preset (the
+cloud wall lit from above, a star switching on later, the wind switched on by a live event, a
+later birth with a jet).  Here a stand-in object carrying exactly the
 attributes and get_state_meta() of that reference `Sim` is handed to `Sim.from_reference`, and the
 same loop runs on the drop-in; its frames must match the reference's within the path's tolerances.
 """
@@ -114,7 +116,7 @@ def test_preset_names_point_to_from_reference(S):
 
 
 @pytest.mark.parametrize("arith", ("exact", "fast"))
-@pytest.mark.parametrize("scene,phase", (("bipolar", "pre"), ("bubbles", "main")))
+@pytest.mark.parametrize("scene,phase", (("bipolar", "pre"), ("bubbles", "main"), ("cliff", "main")))
 def test_bake_loop_through_the_dropin_matches_the_reference(S, scene, phase, arith):
     d, m = load_bake(scene)
     ref = reference_standin(d, m)
