@@ -1105,9 +1105,9 @@ int batch_run_graph(nb_batch_s* b, cudaGraphExec_t* g, int ion) {
         e = cudaGraphInstantiate(g, graph, 0);
         cudaGraphDestroy(graph);
         if (e != cudaSuccess) return bfail(b, NB_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
-        b->launches -= ion ? 7 + b->n_plane : 3;       // captured, not launched
+        b->launches -= ion ? 8 + b->n_plane : 3;       // captured, not launched
     }
-    b->launches += ion ? 7 + b->n_plane : 3;
+    b->launches += ion ? 8 + b->n_plane : 3;
     BCK(b, cudaGraphLaunch(*g, b->bs));
     return NB_OK;
 }
