@@ -127,7 +127,9 @@ typedef struct nb_clock {
 } nb_clock;
 
 /* ---------------------------------------------------------------- lifetime */
-/* Replaces Sim.__init__/reset's buffer set-up (sim.py:718-759). */
+/* Replaces Sim.__init__/reset's buffer set-up (sim.py:718-759).  NB_ERR_LIMIT: max_stars outside
+ * [1, 256], ny * nz or fnu * fnphi * fnr at 2^31 or more, or nu * nphi * max_stars or
+ * fnu * fnphi * max_stars at 2^32 or more (ray indices are 32-bit). */
 int nb_create(const nb_desc* desc, nb_handle* out);
 /* Releases library scratch and graphs (never the caller's fields). */
 void nb_destroy(nb_handle h);

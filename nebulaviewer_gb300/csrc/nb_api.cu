@@ -305,6 +305,9 @@ NB_EXPORT int nb_create(const nb_desc* d, nb_handle* out) {
         return fail(nullptr, NB_ERR_ARG, "bad geometry / ray budget");
     if (d->max_stars < 1 || d->max_stars > NB_MAX_STARS)
         return fail(nullptr, NB_ERR_LIMIT, "max_stars must be in [1, 256]");
+    if ((long long)d->nu * d->nphi * d->max_stars >= (1LL << 32) ||
+        (long long)d->fnu * d->fnphi * d->max_stars >= (1LL << 32))    // ray indices in 32 bits
+        return fail(nullptr, NB_ERR_LIMIT, "rays per star times max_stars must stay below 2^32");
     const nb_fields& f = d->f;
     const void* ptrs[] = {f.rho, f.mx, f.my, f.mz, f.xi, f.stage, f.dfront, f.g0};
     for (const void* p : ptrs)

@@ -36,7 +36,8 @@ __global__ void __launch_bounds__(256, 5) cast_fuv_kernel(const NbConst* __restr
     const int lane = threadIdx.x % G;
     const unsigned gmask = G == 32 ? 0xffffffffu : (((1u << G) - 1u) << ((threadIdx.x & 31) / G * G));
     if (gid >= (long long)nray * nstars) return;
-    const int s = (int)(gid / nray), ray = (int)(gid % nray);
+    // below 2^32 (fnu * fnphi * nstars; nb_create checks it): 32-bit division
+    const int s = (int)((unsigned)gid / (unsigned)nray), ray = (int)((unsigned)gid - (unsigned)s * (unsigned)nray);
     float sx, sy, sz;
     if (star_override) {
         sx = star_override[0]; sy = star_override[1]; sz = star_override[2];

@@ -130,7 +130,9 @@ __global__ void __launch_bounds__(256, NB_CAST_RAYS_MINB) cast_rays_kernel(const
     const unsigned gmask = G == 32 ? 0xffffffffu : (((1u << G) - 1u) << ((threadIdx.x & 31) / G * G));
     // no early exit: every lane of a warp reaches cast_ray's warp-uniform loop
     const bool in = gid < (long long)nray * nstars;
-    const int s = in ? (int)(gid / nray) : 0, ray = in ? (int)(gid % nray) : 0;
+    // a group index of one instance stays below 2^32 (nb_create checks it): 32-bit division
+    const unsigned g32 = in ? (unsigned)gid : 0u;
+    const int s = (int)(g32 / (unsigned)nray), ray = (int)(g32 - (unsigned)s * (unsigned)nray);
     if (star_override) {
         cast_ray<G>(*c, dirs, rho, reinterpret_cast<uintptr_t>(rfront + ray), ray, star_override[0], star_override[1],
                     star_override[2], q_override, lane, gmask, in);
@@ -164,7 +166,8 @@ __device__ __forceinline__ void cast_rays_batch_body(const Jobs& J, const NbRayJ
     const NbConst& C = *job.c;
     const int nray = C.nu * C.nphi;
     const long long local = gid - job.ray0;
-    const int s = (int)(local / nray), ray = (int)(local % nray);
+    const unsigned l32 = (unsigned)local;        // below 2^32 within a job (nb_create): 32-bit division
+    const int s = (int)(l32 / (unsigned)nray), ray = (int)(l32 - (unsigned)s * (unsigned)nray);
     const bool star = in && s < job.nstars && Jd[lo].active;
     NbStarW w{};
     if (star) w = job.sw[s];
