@@ -16,7 +16,9 @@ per snapshot, within the budget).  All pooled instances live in one BatchSim (pe
 joins the stepping set when it is admitted and leaves it when it has run its steps, through
 the batch's slot flags, so admissions and retirements rebuild nothing; the batch and its
 graphs are rebuilt only when the pool itself changes.  Every tick advances all busy instances
-one step together, so work that arrives while others run overlaps with them on the device.
+one step together, so work that arrives while others run overlaps with them on the device; a
+host round trip runs as many ticks as no busy request finishes within (and, while arrivals are
+pending, as fit before the next one).
 Each request's result is the same as running it alone (bit-identical with the exact build).
 """
 import collections
@@ -147,6 +149,7 @@ class Server:
         self.max_slots = int(max_slots)
         self.keep_state = keep_state
         self.ticks = 0
+        self.round_trips = 0         # batch.step calls (a call advances one or more ticks)
         self.rebuilds = 0
         self.built = 0               # instances built
         self.reused = 0              # requests branched into a pooled instance
@@ -167,6 +170,7 @@ class Server:
         batch = None
         dirty = False                # the pool changed since the batch was built
         cell_steps = 0
+        tick_s = 0.0                 # wall time per tick of the last round trip
         self.prewarmed = 0
         try:
             for si, n in sorted((warm or {}).items()):
@@ -260,11 +264,20 @@ class Server:
                 flags = [p.req is not None for p in batch_pool]
                 if flags != list(batch.active):
                     batch.set_active(flags)
-                batch.step(1)                          # one tick: every busy instance advances one step
-                self.ticks += 1
+                # ticks: every busy instance advances one step per tick.  As many ticks per host round
+                # trip as no busy request finishes within and, while arrivals are pending, as fit before
+                # the next one is due (at the last round trip's time per tick)
+                k = min(p.req.left for p in busy)
+                if pending and realtime:
+                    k = min(k, max(1, int((pending[0].t_arrive - now) / max(tick_s, 1e-4))))
+                t_tick = time.perf_counter()
+                batch.step(k)
+                tick_s = (time.perf_counter() - t_tick) / k
+                self.ticks += k
+                self.round_trips += 1
                 for p in busy:
-                    p.req.left -= 1
-                    cell_steps += p.sim._n
+                    p.req.left -= k
+                    cell_steps += p.sim._n * k
                     if p.req.left == 0:
                         finish(p)
         finally:
@@ -278,7 +291,8 @@ class Server:
         lat = np.array([r.t_done - r.t_arrive for r in done])
         pct = (lambda q: float(np.percentile(lat, q) * 1e3)) if len(lat) else (lambda q: None)
         return dict(requests=len(done), wall_s=wall, cell_steps=cell_steps, gcells_per_s=cell_steps / wall / 1e9,
-                    p50_ms=pct(50), p99_ms=pct(99), ticks=self.ticks, batch_rebuilds=self.rebuilds,
+                    p50_ms=pct(50), p99_ms=pct(99), ticks=self.ticks, round_trips=self.round_trips,
+                    batch_rebuilds=self.rebuilds,
                     instances_built=self.built, instances_prewarmed=self.prewarmed, branches_in_place=self.reused,
                     evicted=self.evicted, peak_pool_bytes=self.peak_bytes, budget_bytes=self.budget), done
 

@@ -43,7 +43,7 @@ class FakeSnap:
 
 
 def install(monkeypatch, max_slots=None, budget=None, fail_on_tick=None):
-    log = {"batches": [], "ticks": 0, "peak": 0}
+    log = {"batches": [], "ticks": 0, "calls": 0, "peak": 0}
 
     class FakeBatch:
         def __init__(self, sims):
@@ -60,8 +60,9 @@ def install(monkeypatch, max_slots=None, budget=None, fail_on_tick=None):
             self.active = list(flags)
 
         def step(self, k):
-            log["ticks"] += 1
-            if fail_on_tick is not None and log["ticks"] == fail_on_tick:
+            log["calls"] += 1
+            log["ticks"] += k
+            if fail_on_tick is not None and log["ticks"] >= fail_on_tick:
                 raise RuntimeError("injected batch-step failure")
             live = [s for s, a in zip(self.sims, self.active) if a]
             assert live and all(not s.closed for s in live)
@@ -112,6 +113,8 @@ def test_instances_are_reused_and_the_batch_is_not_rebuilt_per_admission(monkeyp
     assert stats["branches_in_place"] == 6 == snaps[0].branched_into
     assert stats["batch_rebuilds"] == len(log["batches"]) <= 2          # only when the pool grew
     assert {r.rid: r.result["it"] for r in done} == {r.rid: r.nsteps for r in reqs}
+    # a round trip runs as many ticks as no busy request finishes within
+    assert stats["ticks"] == log["ticks"] and stats["round_trips"] == log["calls"] < log["ticks"]
 
 
 def test_a_warm_pool_serves_every_request_by_device_copies(monkeypatch):
