@@ -82,8 +82,11 @@ __device__ __forceinline__ void cast_ray(const NbConst& C, const float4* __restr
         const bool cross = valid && (col + inc > Q);
         const unsigned bal = __ballot_sync(0xffffffffu, cross);
         const unsigned mine = G == 32 ? bal : (bal >> ((threadIdx.x & 31) / G * G)) & ((1u << G) - 1u);
-        const float rfl = r - 0.5f * dr + dr * (Q - col) / fmaxr(inc, 1e-20f);
-        const float rfc = __shfl_sync(gmask, rfl, mine ? __ffs(mine) - 1 : 0, G);
+        float rfc = 0.0f;
+        if (bal) {                               // some group of the warp crossed (warp-uniform)
+            const float rfl = r - 0.5f * dr + dr * (Q - col) / fmaxr(inc, 1e-20f);
+            rfc = __shfl_sync(gmask, rfl, mine ? __ffs(mine) - 1 : 0, G);
+        }
         const float total = __shfl_sync(gmask, incl, G - 1, G);
         if (!done) {
             if (mine) {
