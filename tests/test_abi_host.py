@@ -69,6 +69,16 @@ def test_null_handle_errors_without_gpu(lib_built):
     d.abi_version = _lib.NB_ABI_VERSION
     d.nx, d.ny, d.nz = 8, 8, 6           # nz not a multiple of 4
     assert lib.nb_create(C.byref(d), C.byref(h)) == -1
+    # ray indices are 32-bit: rays per star times max_stars must stay below 2^32 (checked before
+    # anything touches the device)
+    d.nz = 8
+    d.dx, d.dr, d.nsteps = 0.125, 0.125, 16
+    d.fnr, d.fnu, d.fnphi = 16, 8, 16
+    d.nu, d.nphi, d.max_stars = 4096, 8192, 128                      # 2^32 ray groups
+    assert lib.nb_create(C.byref(d), C.byref(h)) == -4
+    assert b"2^32" in lib.nb_last_error(None)
+    d.nu, d.nphi, d.fnu, d.fnphi = 8, 16, 4096, 8192                 # the FUV rays likewise
+    assert lib.nb_create(C.byref(d), C.byref(h)) == -4
 
 
 def test_params_defaults_and_sound_speeds():
