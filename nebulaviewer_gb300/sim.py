@@ -426,6 +426,18 @@ class Sim:
     def _chk(self, rc, what):
         _lib.check(rc, self._h, what, self._lib)
 
+    # sim.py:914-925 keys the star-weight upload on _wkey, and bake.py:91 resets it after editing P.
+    # Here P and the star lists are compared at every push; resetting _wkey forces the next push.
+    @property
+    def _wkey(self):
+        return (self._live_key, self._stars_key)
+
+    @_wkey.setter
+    def _wkey(self, value):
+        if value is None:
+            self._live_key = None
+            self._stars_key = None
+
     def _push(self, force=False):
         """upload live parameters / the star table when they changed (P may be edited directly,
         as bake.py does, sim.py:88-93 there)"""
