@@ -212,6 +212,8 @@ class Sim:
         def host(x):
             return np.asarray(x.numpy() if hasattr(x, "numpy") else x)
 
+        if getattr(ref, "L_full", None) is not None:              # sim.py:634: a cropped window
+            raise NotImplementedError("a cropped domain (crop.py) is outside this package")
         P = dict(ref.P)
         P.update(params or {})
         meta = dict(ref.get_state_meta())
@@ -356,6 +358,8 @@ class Sim:
         self._h = h
         self._lib = lib
         self._n = n
+        # the uncropped domain's values of the crop attributes the viewer reads (sim.py:647)
+        self.crop_origin, self.L_full = (0.0, 0.0, 0.0), None
         self._live_key = None
         self._stars_key = None
         self._dt_cap = None

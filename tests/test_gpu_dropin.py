@@ -132,6 +132,7 @@ def test_bake_loop_through_the_dropin_matches_the_reference(S, scene, phase, ari
     assert np.array_equal(sim.xi.numpy(), d["s_xi"]) and np.array_equal(sim.g0.numpy(), d["s_g0"])
     assert sim.noise == {"seed": m["noise"]["seed"], "calls": m["noise"]["calls"], "modes": m["noise"]["K"]}
     assert sim.t == m["meta"]["t"] and sim.it == m["meta"]["it"] and len(sim.stars) == len(m["stars"])
+    assert sim.crop_origin == (0.0, 0.0, 0.0) and sim.L_full is None      # what viewer.py:205-206 reads
     if m["drv_clock"] is not None:
         drv = sim.drv
         assert np.array_equal(np.stack(drv["A"]), d["s_drv_A"]) and np.array_equal(np.stack(drv["B"]), d["s_drv_B"])
