@@ -70,14 +70,25 @@ __device__ __forceinline__ void cast_ray(const NbConst& C, const float4* __restr
         const float r = ((float)n + 0.5f) * dr;
         const float nv = sample_n(rho, nx, ny, nz, sx + d.x * r, sy + d.y * r, sz + d.z * r, dx, inv_dx, pow2);
         const float inc = valid ? nv * nv * r * r * dr : 0.0f;
-        float incl = inc;
+        float incl, excl, total;
+        if (G == 2) {
+            // one exchange gives the pair's scan: lane 1 adds lane 0's term (inc1 + inc0, the
+            // general scan's operation) and both take that sum as the total
+            const float other = __shfl_xor_sync(gmask, inc, 1, 2);
+            incl = lane ? inc + other : inc;
+            excl = lane ? other : 0.0f;
+            total = lane ? incl : other + inc;
+        } else {
+            incl = inc;
 #pragma unroll
-        for (int o = 1; o < G; o <<= 1) {
-            const float v = __shfl_up_sync(gmask, incl, o, G);
-            if (lane >= o) incl = incl + v;
+            for (int o = 1; o < G; o <<= 1) {
+                const float v = __shfl_up_sync(gmask, incl, o, G);
+                if (lane >= o) incl = incl + v;
+            }
+            excl = __shfl_up_sync(gmask, incl, 1, G);
+            if (lane == 0) excl = 0.0f;
+            total = __shfl_sync(gmask, incl, G - 1, G);
         }
-        float excl = __shfl_up_sync(gmask, incl, 1, G);
-        if (lane == 0) excl = 0.0f;
         const float col = hi + (excl - comp);
         const bool cross = valid && (col + inc > Q);
         const unsigned bal = __ballot_sync(0xffffffffu, cross);
@@ -87,7 +98,6 @@ __device__ __forceinline__ void cast_ray(const NbConst& C, const float4* __restr
             const float rfl = r - 0.5f * dr + dr * (Q - col) / fmaxr(inc, 1e-20f);
             rfc = __shfl_sync(gmask, rfl, mine ? __ffs(mine) - 1 : 0, G);
         }
-        const float total = __shfl_sync(gmask, incl, G - 1, G);
         if (!done) {
             if (mine) {
                 rf = rfc;
