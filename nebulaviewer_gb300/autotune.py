@@ -17,7 +17,7 @@ from . import _lib
 CANDIDATES = {
     "chunk_i": (16, 20, 24, 32, 64),
     "tile_order": (0, 1),
-    "ray_group": (2, 4, 8, 16),
+    "ray_group": (1, 2, 4, 8),
     "fuv_group": (8, 16, 32),
     "front_pairs": (0, 1),
     "fuv_pairs": (0, 1),

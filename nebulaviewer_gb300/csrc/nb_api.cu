@@ -37,7 +37,7 @@ struct nb_instance {
     int nstars = 0, star_alloc = 0;
     long long host_it = 0;
     int smax_valid = 0;
-    int chunk_i = 20, ray_group = 2, fuv_group = 16;      // measured best at 192^3-256^3 (nb_set_tuning)
+    int chunk_i = 20, ray_group = 1, fuv_group = 16;      // measured best at 192^3-256^3 (nb_set_tuning)
     int tile_order = 0;
     int front_cull = 1;                 // apply_front skips the stars that cannot change a segment
     int fuv_cut = 1;                    // FUV rays stop where exp(-tau) has reached 0.0f
@@ -956,7 +956,7 @@ struct nb_batch_s {
     cudaStream_t user = nullptr;        // the instances' stream
     cudaStream_t bs = nullptr;          // the batch's own stream (capturable)
     cudaEvent_t ev_in = nullptr, ev_out = nullptr;
-    int solver = 0, limiter = 0, max_stars = 1, grid = 0, ray_group = 2;
+    int solver = 0, limiter = 0, max_stars = 1, grid = 0, ray_group = 1;
     int idx32 = 1;                      // every instance below 2^31 cells: 32-bit cell offsets
     NbBatchInst* d_inst = nullptr;
     HydroLaunch* d_L1 = nullptr;

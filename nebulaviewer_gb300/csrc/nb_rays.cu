@@ -70,11 +70,15 @@ __device__ __forceinline__ void cast_ray(const NbConst& C, const float4* __restr
         const float r = ((float)n + 0.5f) * dr;
         const float nv = sample_n(rho, nx, ny, nz, sx + d.x * r, sy + d.y * r, sz + d.z * r, dx, inv_dx, pow2);
         const float inc = valid ? nv * nv * r * r * dr : 0.0f;
-        float incl, excl, total;
-        if (G == 2) {
+        float incl, excl, total, other = 0.0f;
+        if (G == 1) {
+            incl = inc;
+            excl = 0.0f;
+            total = inc;
+        } else if (G == 2) {
             // one exchange gives the pair's scan: lane 1 adds lane 0's term (inc1 + inc0, the
             // general scan's operation) and both take that sum as the total
-            const float other = __shfl_xor_sync(gmask, inc, 1, 2);
+            other = __shfl_xor_sync(gmask, inc, 1, 2);
             incl = lane ? inc + other : inc;
             excl = lane ? other : 0.0f;
             total = lane ? incl : other + inc;
@@ -95,8 +99,18 @@ __device__ __forceinline__ void cast_ray(const NbConst& C, const float4* __restr
         const unsigned mine = G == 32 ? bal : (bal >> ((threadIdx.x & 31) / G * G)) & ((1u << G) - 1u);
         float rfc = 0.0f;
         if (bal) {                               // some group of the warp crossed (warp-uniform)
-            const float rfl = r - 0.5f * dr + dr * (Q - col) / fmaxr(inc, 1e-20f);
-            rfc = __shfl_sync(gmask, rfl, mine ? __ffs(mine) - 1 : 0, G);
+            if (G <= 2) {
+                // the pair's first crossing lane, from the terms both lanes hold
+                const int p = G == 1 ? 0 : ((mine & 1u) ? 0 : 1);
+                const float inc0 = lane ? other : inc;
+                const float rp = ((float)(base + p) + 0.5f) * dr;
+                const float colp = hi + ((p ? inc0 : 0.0f) - comp);
+                const float incp = p == lane ? inc : other;
+                rfc = rp - 0.5f * dr + dr * (Q - colp) / fmaxr(incp, 1e-20f);
+            } else {
+                const float rfl = r - 0.5f * dr + dr * (Q - col) / fmaxr(inc, 1e-20f);
+                rfc = __shfl_sync(gmask, rfl, mine ? __ffs(mine) - 1 : 0, G);
+            }
         }
         if (!done) {
             if (mine) {
