@@ -517,6 +517,39 @@ def test_ray_lanes_per_ray_agree(nb, arith):
     uni.close()
 
 
+@pytest.mark.parametrize("arith", ARITH)
+def test_fuv_lanes_per_ray_agree(nb, arith):
+    """every lanes-per-ray shape of the FUV rays (8, 16, 32) in both table layouts gives the same G0
+    (float32 fields) up to the rounding of the optical-depth sums, and each shape gives the same bits
+    in both layouts and with the optical-depth cut on and off; a dense 12-star sheet with rays past
+    the cut"""
+    from nebulaviewer_gb300 import autotune as at, ics
+    _, S = nb
+    ic = ics.sheet(res=96, nstars=12)
+    sim = S.Sim.from_state(ic["shape"], ic["dx"], ic["rho"], ic["stars"], ic["kinds"], ic["jets"], ic["jkinds"],
+                           dict(ic["P"], fp32_fields=True), mom=ic["mom"], rays=(64, 128), fuv_grid=(24, 24, 48),
+                           arith=arith)
+    sim.step(3)
+    out = {}
+    for cut in (1, 0):
+        at.put(sim, "fuv_cut", cut)
+        for pairs in (0, 1):
+            at.put(sim, "fuv_pairs", pairs)
+            for g in (8, 16, 32):
+                at.put(sim, "fuv_group", g)
+                sim.fuv_field()
+                torch.cuda.synchronize()
+                out[cut, pairs, g] = sim.g0.numpy().astype(np.float32)
+    assert out[1, 0, 16].dtype == np.float32 and np.isfinite(out[1, 0, 16]).all() and out[1, 0, 16].max() > 0
+    for k, v in out.items():
+        assert rel_linf(v, out[1, 0, 16]) < 1e-5, k
+    for g in (8, 16, 32):
+        for cut in (0, 1):
+            assert np.array_equal(out[cut, 0, g].view(np.int32), out[cut, 1, g].view(np.int32)), (cut, g)
+            assert np.array_equal(out[cut, 0, g].view(np.int32), out[1 - cut, 0, g].view(np.int32)), (cut, g)
+    sim.close()
+
+
 @pytest.mark.parametrize("solver,lim", (("hll", "minmod"), ("hll", "vanleer"), ("hll", "mc"), ("rusanov", "minmod")))
 def test_ragged_grid_many_stars_stage_bit_identical(nb, solver, lim):
     """a 37 x 45 x 100 grid (partial j and k tiles, uneven i-chunks), dx = 0.01 (not a power of
