@@ -570,7 +570,9 @@ def run_batch(args):
 def served_result(args, requests):
     """Served: Poisson arrivals; each request branches from a device snapshot of a 96^3-320^3
     instance, changes one star's photon rate or the wind by +-50% and runs 10-100 steps;
-    admission under a 150 GB HBM budget at 48 B/cell; continuous batching."""
+    admission under a 150 GB HBM budget charging each instance its device footprint; continuous
+    batching of the instances below --solo-cells cells, the larger ones stepped alone in the same
+    ticks (--solo-cells 0: every instance batched)."""
     import torch
     from nebulaviewer_gb300 import build as nb_build
     nb_build.build(verbose=False)
@@ -594,7 +596,8 @@ def served_result(args, requests):
     warm = {}
     for r in reqs:
         warm[r.snap] = warm.get(r.snap, 0) + 1
-    srv = serve.Server(snaps, budget_bytes=150e9, max_slots=64)
+    solo = serve.SOLO_CELLS if args.solo_cells is None else (args.solo_cells if args.solo_cells > 0 else None)
+    srv = serve.Server(snaps, budget_bytes=150e9, max_slots=64, solo_cells=solo)
     clk = ClockSampler(0).start()
     with clk:
         stats, done = srv.run(reqs, realtime=True, warm=warm)
@@ -628,7 +631,9 @@ def served_result(args, requests):
            "config": {"workload": f"{requests} requests, Poisson {args.rate:g}/s, snapshots 96^3/160^3/256^3/320^3, "
                                   "+-50% on a star's Q or the wind, 10-100 steps, 150 GB budget charging each pooled "
                                   "instance its device footprint (fields + library scratch); warm pool of one idle "
-                                  "instance per request of each snapshot, built before the clock starts",
+                                  "instance per request of each snapshot, built before the clock starts; "
+                                  + (f"instances of {solo} cells or more stepped alone, the rest batched" if solo else
+                                     "every instance batched"),
                       "footprint_bytes_per_cell": {f"{s.shape[0]}^3": s.footprint / s.cells for s in snaps}},
            "stats": stats, "clocks": clk.summary(), "arith": snaps[0].arith}
     return res
@@ -820,7 +825,7 @@ def added_forms(args):
         d["workload"] = r["config"]["workload"]
         if key == "served":
             for k in ("requests", "wall_s", "instances_built", "instances_prewarmed", "branches_in_place", "evicted",
-                      "batch_rebuilds", "peak_pool_bytes"):
+                      "batch_rebuilds", "peak_pool_bytes", "solo_ticks", "ticks"):
                 d[k] = r["stats"][k]
             d["footprint_bytes_per_cell"] = r["config"]["footprint_bytes_per_cell"]
         d["run_s"] = time.perf_counter() - t0
@@ -842,6 +847,8 @@ def main():
                     choices=["sheet256", "batch32", "served", "cliff1024", "stirred256", "render256"])
     ap.add_argument("--requests", type=int, default=100)
     ap.add_argument("--rate", type=float, default=200.0)
+    ap.add_argument("--solo-cells", type=int, default=None,
+                    help="served: instances of this many cells or more step alone (default: the server's; 0: none)")
     ap.add_argument("--instances", type=int, default=32)
     ap.add_argument("--arith", default=None, choices=["exact", "fast"],
                     help="library build: exact (bit-identical to the reference's kernel source in float32) or fast (FMA, approximate "

@@ -12,11 +12,14 @@ library's scratch for it (nb_instance_bytes: ray and FUV tables sized for its st
 maps, ...) -- fits the HBM budget next to every instance already pooled, busy or idle; idle
 instances of other snapshots are closed first, least recently used first, when that makes
 room.  A server may also build a warm pool before traffic starts (run's `warm`: idle instances
-per snapshot, within the budget).  All pooled instances live in one BatchSim (persistent kernels, CUDA graphs): a request
-joins the stepping set when it is admitted and leaves it when it has run its steps, through
-the batch's slot flags, so admissions and retirements rebuild nothing; the batch and its
-graphs are rebuilt only when the pool itself changes.  Every tick advances all busy instances
-one step together, so work that arrives while others run overlaps with them on the device; a
+per snapshot, within the budget).  The pooled instances below `solo_cells` cells live in one
+BatchSim (persistent kernels, CUDA graphs): a request joins the stepping set when it is admitted
+and leaves it when it has run its steps, through the batch's slot flags, so admissions and
+retirements rebuild nothing; the batch and its graphs are rebuilt only when the pool itself
+changes.  An instance of `solo_cells` cells or more fills the GPU on its own, where the batched
+kernels would only add their per-cell cost (the instance records they index, the work-list
+walk), so it is stepped through its own Sim.step in the same tick.  Every tick advances all busy
+instances one step, so work that arrives while others run overlaps with them on the device; a
 host round trip runs as many ticks as no busy request finishes within (and, while arrivals are
 pending, as fit before the next one).
 Each request's result is the same as running it alone (bit-identical with the exact build).
@@ -140,16 +143,25 @@ class _Slot:
         self.last = -1
 
 
+# Instances of at least this many cells are stepped alone (Sim.step) rather than in the batch:
+# 8 Mi cells is ~2.7 waves of the stage kernels' resident 32 x 8 x 20-cell tiles on 152 SMs, past
+# which a batch no longer fills idle SMs and its kernels cost ~5% more per cell than the
+# single-instance ones (measured on the served mix: 96^3-320^3 snapshots).
+SOLO_CELLS = 8 * 2 ** 20
+
+
 class Server:
     """Continuous batching over a pool of instances under an HBM budget (see the module text)."""
 
-    def __init__(self, snapshots, budget_bytes=150e9, max_slots=64, keep_state=False):
+    def __init__(self, snapshots, budget_bytes=150e9, max_slots=64, keep_state=False, solo_cells=SOLO_CELLS):
         self.snaps = snapshots
         self.budget = float(budget_bytes)
         self.max_slots = int(max_slots)
         self.keep_state = keep_state
+        self.solo_cells = solo_cells          # None: every instance in the batch
         self.ticks = 0
-        self.round_trips = 0         # batch.step calls (a call advances one or more ticks)
+        self.round_trips = 0         # host round trips (each advances one or more ticks)
+        self.solo_ticks = 0          # instance-ticks stepped alone (instances of solo_cells or more)
         self.rebuilds = 0
         self.built = 0               # instances built
         self.reused = 0              # requests branched into a pooled instance
@@ -167,7 +179,11 @@ class Server:
         pending = collections.deque(sorted(requests, key=lambda r: r.t_arrive))
         queue = collections.deque()
         pool, done = [], []
-        batch = None
+        batch, batch_pool = None, []
+
+        def solo(p):
+            return self.solo_cells is not None and p.sim._n >= self.solo_cells
+
         dirty = False                # the pool changed since the batch was built
         cell_steps = 0
         tick_s = 0.0                 # wall time per tick of the last round trip
@@ -253,17 +269,17 @@ class Server:
                     if pending:
                         time.sleep(max(0.0, min(pending[0].t_arrive - now, 0.01)))
                     continue
-                if dirty or batch is None:
+                if dirty:
                     if batch is not None:
                         batch.close()
                         batch = None
-                    batch = BatchSim([p.sim for p in pool])
-                    batch_pool = list(pool)
-                    self.rebuilds += 1
+                    batch_pool = [p for p in pool if not solo(p)]
+                    if batch_pool:
+                        batch = BatchSim([p.sim for p in batch_pool])
+                        self.rebuilds += 1
                     dirty = False
                 flags = [p.req is not None for p in batch_pool]
-                if flags != list(batch.active):
-                    batch.set_active(flags)
+                alone = [p for p in busy if solo(p)]
                 # ticks: every busy instance advances one step per tick.  As many ticks per host round
                 # trip as no busy request finishes within and, while arrivals are pending, as fit before
                 # the next one is due (at the last round trip's time per tick)
@@ -271,7 +287,15 @@ class Server:
                 if pending and realtime:
                     k = min(k, max(1, int((pending[0].t_arrive - now) / max(tick_s, 1e-4))))
                 t_tick = time.perf_counter()
-                batch.step(k)
+                if any(flags):
+                    if flags != list(batch.active):
+                        batch.set_active(flags)
+                    batch.step(k, sync=not alone)
+                for n, p in enumerate(alone):        # one stream: the last one's sync covers the batch too
+                    p.sim.step(k, sync=n == len(alone) - 1)
+                if alone and any(flags):
+                    batch.check_status()
+                self.solo_ticks += k * len(alone)
                 tick_s = (time.perf_counter() - t_tick) / k
                 self.ticks += k
                 self.round_trips += 1
@@ -292,6 +316,7 @@ class Server:
         pct = (lambda q: float(np.percentile(lat, q) * 1e3)) if len(lat) else (lambda q: None)
         return dict(requests=len(done), wall_s=wall, cell_steps=cell_steps, gcells_per_s=cell_steps / wall / 1e9,
                     p50_ms=pct(50), p99_ms=pct(99), ticks=self.ticks, round_trips=self.round_trips,
+                    solo_ticks=self.solo_ticks,
                     batch_rebuilds=self.rebuilds,
                     instances_built=self.built, instances_prewarmed=self.prewarmed, branches_in_place=self.reused,
                     evicted=self.evicted, peak_pool_bytes=self.peak_bytes, budget_bytes=self.budget), done

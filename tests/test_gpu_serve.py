@@ -33,20 +33,24 @@ def _close(a, b, exact):
     return float((a - b).abs().max()) <= 1e-5 * max(float(b.abs().max()), 1e-30)
 
 
-@pytest.mark.parametrize("slots,tight", ((3, False), (8, True)))
-def test_served_results_equal_alone(env, slots, tight):
+@pytest.mark.parametrize("slots,tight,solo", ((3, False, None), (8, True, None), (4, False, 31000)))
+def test_served_results_equal_alone(env, slots, tight, solo):
     """8 requests over two snapshots: with 3 slots the pool's instances are branched into again by
     later requests; with a budget of one and a half instances (the two snapshots' instances are of
-    about the same size), an idle instance is closed whenever the other snapshot needs room"""
+    about the same size), an idle instance is closed whenever the other snapshot needs room; with
+    solo_cells between the two sizes, the torus instances (32^3 cells) step alone through Sim.step
+    in the same ticks as the batched sheet instances (32 x 40 x 24)"""
     serve, snaps = env
     exact = snaps[0].arith == "exact"
     reqs = serve.poisson_requests(snaps, 8, rate=1000.0, seed=slots, steps=(3, 9))
     budget = max(s.footprint for s in snaps) * 1.5 if tight else 1e12
-    srv = serve.Server(snaps, budget_bytes=budget, max_slots=slots, keep_state=True)
+    srv = serve.Server(snaps, budget_bytes=budget, max_slots=slots, keep_state=True, solo_cells=solo)
     stats, done = srv.run(reqs, realtime=False)
+    assert (stats["solo_ticks"] > 0) == (solo is not None)
     assert stats["requests"] == 8 and stats["ticks"] >= max(r.nsteps for r in done)
     assert stats["peak_pool_bytes"] <= budget
     assert stats["branches_in_place"] > 0 if not tight else stats["evicted"] > 0
+    assert snaps[0].cells > 31000 > snaps[1].cells
     for r in done:
         ref = serve.run_alone(snaps[r.snap], r)
         assert r.result["it"] == ref["it"]

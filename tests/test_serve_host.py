@@ -19,6 +19,11 @@ class FakeSim:
     def footprint(self):
         return self.nbytes
 
+    def step(self, k, sync=True):                # stepped alone (an instance of solo_cells or more)
+        assert not self.closed
+        self.steps += k
+        self.alone = getattr(self, "alone", 0) + k
+
     def close(self):
         self.closed = True
 
@@ -59,7 +64,7 @@ def install(monkeypatch, max_slots=None, budget=None, fail_on_tick=None):
             assert len(flags) == len(self.sims)
             self.active = list(flags)
 
-        def step(self, k):
+        def step(self, k, sync=True):
             log["calls"] += 1
             log["ticks"] += k
             if fail_on_tick is not None and log["ticks"] >= fail_on_tick:
@@ -71,6 +76,9 @@ def install(monkeypatch, max_slots=None, budget=None, fail_on_tick=None):
             log["peak"] = max(log["peak"], sum(s.footprint() for s in self.sims))
             for s in live:
                 s.steps += k
+
+        def check_status(self):
+            assert not self.closed
 
         def close(self):
             self.closed = True
@@ -178,3 +186,31 @@ def test_a_request_beyond_the_budget_is_refused(monkeypatch):
     with pytest.raises(RuntimeError, match="budget"):
         serve.Server(snaps, budget_bytes=snaps[0].footprint * 2).run(requests(snaps, [2, 2]), realtime=False)
     assert all(s.closed for sn in snaps for s in sn.made)
+
+
+def test_instances_of_solo_cells_or_more_step_alone(monkeypatch):
+    """instances that fill the GPU on their own are stepped through their own Sim.step in the same
+    ticks and never enter a batch; the smaller ones are batched; every request runs its steps"""
+    snaps = [FakeSnap(1000), FakeSnap(5000)]
+    log = install(monkeypatch, max_slots=4)
+    reqs = requests(snaps, [5, 2, 7, 1, 4, 3, 6, 2])          # snapshots 0, 1, 0, 1, ...
+    stats, done = serve.Server(snaps, max_slots=4, solo_cells=4000).run(reqs, realtime=False)
+    assert {r.rid: r.result["it"] for r in done} == {r.rid: r.nsteps for r in reqs}
+    big, small = snaps[1].made, snaps[0].made
+    assert big and small and all(s not in b.sims for b in log["batches"] for s in big)
+    assert all(any(s in b.sims for b in log["batches"]) for s in small)
+    assert sum(getattr(s, "alone", 0) for s in big) == stats["solo_ticks"] == sum(r.nsteps for r in reqs if r.snap == 1)
+    assert sum(getattr(s, "alone", 0) for s in small) == 0
+    assert stats["cell_steps"] == sum(r.nsteps * snaps[r.snap].cells for r in reqs)
+    assert all(s.closed for sn in snaps for s in sn.made) and all(b.closed for b in log["batches"])
+    # a pool of large instances only builds no batch at all
+    snaps = [FakeSnap(5000)]
+    log = install(monkeypatch)
+    stats, done = serve.Server(snaps, solo_cells=4000).run(requests(snaps, [3, 4, 2]), realtime=False)
+    assert log["batches"] == [] and stats["batch_rebuilds"] == 0 and log["calls"] == 0
+    assert {r.rid: r.result["it"] for r in done} == {0: 3, 1: 4, 2: 2}
+    # solo_cells=None batches every instance
+    snaps = [FakeSnap(5000)]
+    log = install(monkeypatch)
+    stats, _ = serve.Server(snaps, solo_cells=None).run(requests(snaps, [3, 4]), realtime=False)
+    assert stats["solo_ticks"] == 0 and log["ticks"] >= 4
