@@ -4,12 +4,14 @@
 // apply_front, smooth_xi) as driven by sim.py:927-947 (ionize).
 //
 // GB300 design:
-//  * cast_rays: a group of G lanes (1 to 32; 2 at 256^3) marches one ray, G consecutive
-//    samples at a time; the recombination column sum(n^2 r^2 dr) is an inclusive group scan on
-//    top of a Kahan-compensated carry, and the first sample whose column passes Q is found with
-//    one ballot.  The march is warp-uniform: a warp's groups loop together until all are done,
-//    and the trilinear sampler has no branches, so the lanes never diverge (divergent exits had
-//    made branch resolution the leading stall).  All rays of all active stars are one launch.
+//  * cast_rays: a group of G lanes (1 to 32; 1 by default) marches one ray, G consecutive
+//    samples at a time; the recombination column sum(n^2 r^2 dr) is added to a Kahan-compensated
+//    carry (G > 1: an inclusive group scan; two lanes take it from one exchange; one lane needs
+//    none, which made it the fastest shape once the shuffles' latency led the stalls), and the
+//    first sample whose column passes Q is found with one ballot.  The march is warp-uniform: a
+//    warp's groups loop together until all are done, and the trilinear sampler has no branches,
+//    so the lanes never diverge (divergent exits had made branch resolution the leading stall).
+//    All rays of all active stars are one launch.
 //  * The front table holds, per (star, phi, u), the pair (rf(u), rf(min(u + 1, nu - 1))) as one
 //    float2 (cast_rays writes each front into its own pair and its lower neighbour's), so the
 //    bilinear lookup of apply_front is two 8-byte gathers instead of four 4-byte ones; the values
