@@ -77,10 +77,14 @@ class BatchSim:
             s._it += int(k)
             s.version += int(k)
         if sync:
-            self.sims[0]._sync()
-            self.check_status()
+            self.sync()
         self.prof["step"] = self.prof.get("step", 0.0) + time.perf_counter() - t0
         return time.perf_counter() - t0
+
+    def sync(self):
+        """wait for the batch's steps (the instances' stream follows the batch's), then check_status"""
+        self.sims[0]._sync()
+        self.check_status()
 
     def check_status(self):
         """raise if a batched hydro stage's bounded TMA wait gave up on the device for any instance

@@ -18,13 +18,18 @@ and leaves it when it has run its steps, through the batch's slot flags, so admi
 retirements rebuild nothing; the batch and its graphs are rebuilt only when the pool itself
 changes.  An instance of `solo_cells` cells or more fills the GPU on its own, where the batched
 kernels would only add their per-cell cost (the instance records they index, the work-list
-walk), so it is stepped through its own Sim.step in the same tick.  Every tick advances all busy
-instances one step, so work that arrives while others run overlaps with them on the device; a
-host round trip runs as many ticks as no busy request finishes within (and, while arrivals are
-pending, as fit before the next one).
+walk), so it is stepped through its own Sim.step in the same tick.  The large instances share a
+CUDA stream apart from the batch's: the batch and the large instances are launched together and
+the small instances' kernels fill the large ones' tail waves, while the large instances still
+run one after another (with a stream each, two of them side by side compete for the L2 their
+ray casts and tile marches read from: the served mix then swung between 0.97x and 1.02x of the
+requests run one at a time, from run to run; with one shared stream it stays at 0.99x).  Every tick advances all busy instances one step, so work that arrives while others
+run overlaps with them on the device; a host round trip runs as many ticks as no busy request
+finishes within (and, while arrivals are pending, as fit before the next one).
 Each request's result is the same as running it alone (bit-identical with the exact build).
 """
 import collections
+import contextlib
 import time
 
 import numpy as np
@@ -54,15 +59,17 @@ class Snapshot:
     def cells(self):
         return int(np.prod(self.shape))
 
-    def branch(self, mod=None):
-        """a new Sim resuming from this snapshot; mod = ("q", star_index, factor) | ("wind", factor)"""
+    def branch(self, mod=None, stream=None):
+        """a new Sim resuming from this snapshot; mod = ("q", star_index, factor) | ("wind", factor);
+        stream: the CUDA stream the instance works on (default: the current one)"""
         m = self.meta
         f = self.fields
-        s = Sim.from_state(self.shape, self.dx, f["rho"], m["stars"], m["kinds"], m["jets"], m["jkinds"], m["P"],
-                           mom=[f["mx"], f["my"], f["mz"]], rays=self.rays, fuv_grid=self.fuv,
-                           ion_every=self.ion_every, fast=self.fast, device=self.device, start_main=False,
-                           torus=self.torus, stir_grid=self.stir_grid, arith=self.arith)
-        self._resume(s, mod)
+        with on_stream(stream):
+            s = Sim.from_state(self.shape, self.dx, f["rho"], m["stars"], m["kinds"], m["jets"], m["jkinds"],
+                               m["P"], mom=[f["mx"], f["my"], f["mz"]], rays=self.rays, fuv_grid=self.fuv,
+                               ion_every=self.ion_every, fast=self.fast, device=self.device, start_main=False,
+                               torus=self.torus, stir_grid=self.stir_grid, arith=self.arith)
+            self._resume(s, mod)
         return s
 
     def branch_into(self, sim, mod=None):
@@ -72,7 +79,8 @@ class Snapshot:
         if tuple(sim.shape) != tuple(self.shape) or len(sim.stars) != len(self.meta["stars"]):
             raise ValueError("branch_into needs an instance built from this snapshot")
         sim.events = []
-        self._resume(sim, mod)
+        with on_stream(getattr(sim, "_stream", None)):       # in order with the instance's earlier work
+            self._resume(sim, mod)
         return sim
 
     def _resume(self, s, mod):
@@ -121,15 +129,22 @@ def poisson_requests(snapshots, n, rate, seed=0, steps=(10, 100), factor=0.5):
     return out
 
 
+def on_stream(stream):
+    """a context placing torch's work on `stream` (None: leave the current stream)"""
+    return torch.cuda.stream(stream) if stream is not None else contextlib.nullcontext()
+
+
 def result_of(sim, keep_state=True):
     """what a finished request returns: the clock, FP64 totals, a digest of the fields and (keep_state)
-    a copy of the state"""
-    c = sim._clock()
-    tot = sim.conservation()
-    xi = sim._xi
-    out = dict(t=c.t, it=int(c.it), totals=tot, xi_mean=float(xi.sum(dtype=torch.float64)) / xi.numel())
-    if keep_state:
-        out["state"] = [t.clone() for t in (sim._rho, sim._mx, sim._my, sim._mz, sim._xi)]
+    a copy of the state (complete when this returns, whichever stream the instance works on)"""
+    with on_stream(getattr(sim, "_stream", None)):
+        c = sim._clock()
+        tot = sim.conservation()
+        xi = sim._xi
+        out = dict(t=c.t, it=int(c.it), totals=tot, xi_mean=float(xi.sum(dtype=torch.float64)) / xi.numel())
+        if keep_state:
+            out["state"] = [t.clone() for t in (sim._rho, sim._mx, sim._my, sim._mz, sim._xi)]
+            sim._sync()
     return out
 
 
@@ -153,12 +168,15 @@ SOLO_CELLS = 8 * 2 ** 20
 class Server:
     """Continuous batching over a pool of instances under an HBM budget (see the module text)."""
 
-    def __init__(self, snapshots, budget_bytes=150e9, max_slots=64, keep_state=False, solo_cells=SOLO_CELLS):
+    def __init__(self, snapshots, budget_bytes=150e9, max_slots=64, keep_state=False, solo_cells=SOLO_CELLS,
+                 solo_streams=True):
         self.snaps = snapshots
         self.budget = float(budget_bytes)
         self.max_slots = int(max_slots)
         self.keep_state = keep_state
         self.solo_cells = solo_cells          # None: every instance in the batch
+        self.solo_streams = solo_streams      # the instances stepped alone work on a stream apart from the batch's
+        self._solo_stream = {}                # device -> that stream
         self.ticks = 0
         self.round_trips = 0         # host round trips (each advances one or more ticks)
         self.solo_ticks = 0          # instance-ticks stepped alone (instances of solo_cells or more)
@@ -184,6 +202,17 @@ class Server:
         def solo(p):
             return self.solo_cells is not None and p.sim._n >= self.solo_cells
 
+        def build(snap, mod):
+            """a new instance of snap: one to be stepped alone works on the stream of those"""
+            dev = getattr(snap, "device", None)
+            if (self.solo_streams and self.solo_cells is not None and snap.cells >= self.solo_cells
+                    and dev is not None and torch.device(dev).type == "cuda"):
+                key = str(torch.device(dev))
+                if key not in self._solo_stream:
+                    self._solo_stream[key] = torch.cuda.Stream(device=dev)
+                return snap.branch(mod, stream=self._solo_stream[key])
+            return snap.branch(mod)
+
         dirty = False                # the pool changed since the batch was built
         cell_steps = 0
         tick_s = 0.0                 # wall time per tick of the last round trip
@@ -194,7 +223,7 @@ class Server:
                 for _ in range(int(n)):
                     if sum(p.nbytes for p in pool) + snap.footprint > self.budget:
                         break
-                    sim = snap.branch(None)
+                    sim = build(snap, None)
                     pool.append(_Slot(si, sim, sim.footprint()))
                     self.prewarmed += 1
             self.peak_bytes = max(self.peak_bytes, sum(p.nbytes for p in pool))
@@ -237,7 +266,7 @@ class Server:
                     p.sim.close()
                     self.evicted += 1
                     dirty = True
-                sim = snap.branch(r.mod)
+                sim = build(snap, r.mod)
                 slot = _Slot(r.snap, sim, sim.footprint())
                 pool.append(slot)
                 self.built += 1
@@ -287,14 +316,18 @@ class Server:
                 if pending and realtime:
                     k = min(k, max(1, int((pending[0].t_arrive - now) / max(tick_s, 1e-4))))
                 t_tick = time.perf_counter()
+                # the batch and the instances stepped alone are all launched before any of them is
+                # waited for: on two streams, the batch runs beside the large instances
                 if any(flags):
                     if flags != list(batch.active):
                         batch.set_active(flags)
-                    batch.step(k, sync=not alone)
-                for n, p in enumerate(alone):        # one stream: the last one's sync covers the batch too
-                    p.sim.step(k, sync=n == len(alone) - 1)
-                if alone and any(flags):
-                    batch.check_status()
+                    batch.step(k, sync=False)
+                for p in alone:
+                    p.sim.step(k, sync=False)
+                for p in alone:
+                    p.sim.step(0)                    # its clock mirrored and read: raises if a TMA wait gave up
+                if any(flags):
+                    batch.sync()
                 self.solo_ticks += k * len(alone)
                 tick_s = (time.perf_counter() - t_tick) / k
                 self.ticks += k

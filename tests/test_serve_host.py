@@ -80,6 +80,9 @@ def install(monkeypatch, max_slots=None, budget=None, fail_on_tick=None):
         def check_status(self):
             assert not self.closed
 
+        def sync(self):
+            self.check_status()
+
         def close(self):
             self.closed = True
 
