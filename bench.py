@@ -411,10 +411,12 @@ def run_gb300(args):
         torch.cuda.synchronize(dev)
         return time.perf_counter() - t0
 
-    # three identical passes (each restarts from the same uploaded state); the median is reported:
-    # a single host-timed pass swings with the host's scheduling
-    e2e_runs = [e2e_pass() for _ in range(3)]
-    e2e_s = sorted(e2e_runs)[1]
+    # one untimed pass, then five identical timed passes (each restarts from the same uploaded
+    # state); the median is reported: a host-timed pass swings with the host's scheduling (about one
+    # pass in three lost ~10 ms over 96 steps)
+    e2e_pass()
+    e2e_runs = [e2e_pass() for _ in range(5)]
+    e2e_s = sorted(e2e_runs)[2]
     if dist:
         t = torch.tensor([e2e_s], device=dev, dtype=torch.float64)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
@@ -461,7 +463,7 @@ def run_gb300(args):
                            for k, v in kinds.items()},
             "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "how": "Sim.step(1) + update_render_fields + clock read per step; state upload from pinned "
-                           "host memory and rho/xi read-back inside the timed region; median of 3 passes",
+                           "host memory and rho/xi read-back inside the timed region; median of 5 passes after an untimed one",
                     "passes": [ws * ncell * e2e_steps / t / 1e9 for t in e2e_runs]},
             "gpu_launches": launches,
             "clocks": clocks,
