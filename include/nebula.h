@@ -320,7 +320,8 @@ int nb_profile(nb_handle h, int enable);
 int nb_profile_read(nb_handle h, double ms[NB_PROF_KINDS], long long count[NB_PROF_KINDS]);
 /* Launch-shape knobs picked by the package's autotuner (no reference counterpart): the tile depth
  * along i of the hydro march (i-chunk), the tile sweep order (0: k, j, i-chunk; 1: i-chunk, k, j),
- * and the lanes per ray (1, 2, 4, 8, 16, 32 ionizing; 8, 16, 32 FUV) of the ray kernels.  The hydro
+ * and the lanes per ray (1, 2, 4, 8, 16, 32 ionizing, default 1; 8, 16, 32 FUV, default 16) of the
+ * ray kernels (the defaults: i-chunk 20, order 0).  The hydro
  * result does not depend on them; the ray sums only through their rounding.  NB_TUNE_FRONT_CULL
  * (default 1; up to 32 stars): the front pass first bounds each star's front radius and then
  * leaves out, per 32-cell segment of a row, the stars that cannot change its ionized fraction or
