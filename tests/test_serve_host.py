@@ -29,14 +29,17 @@ class FakeSim:
 
 
 class FakeSnap:
-    def __init__(self, cells, nbytes=None):
+    def __init__(self, cells, nbytes=None, device=None):
         self.cells = cells
         self.footprint = nbytes if nbytes is not None else 40 * cells + 1000     # fields + some scratch
         self.made = []
         self.branched_into = 0
+        if device is not None:
+            self.device = device
 
-    def branch(self, mod):
+    def branch(self, mod, stream=None):
         s = FakeSim(self.cells, self.footprint)
+        s.stream = stream
         self.made.append(s)
         return s
 
@@ -217,3 +220,28 @@ def test_instances_of_solo_cells_or_more_step_alone(monkeypatch):
     log = install(monkeypatch)
     stats, _ = serve.Server(snaps, solo_cells=None).run(requests(snaps, [3, 4]), realtime=False)
     assert stats["solo_ticks"] == 0 and log["ticks"] >= 4
+
+
+def test_instances_stepped_alone_share_one_stream_apart_from_the_batch(monkeypatch):
+    """on a CUDA device every instance of solo_cells or more is built on one stream of the server's
+    (the same for all of them, so two never run side by side), the batched ones on the current
+    stream; solo_streams=False keeps every instance on the current stream"""
+    made = []
+
+    class FakeStream:
+        def __init__(self, device=None):
+            made.append(self)
+
+    monkeypatch.setattr(serve.torch.cuda, "Stream", FakeStream)
+    snaps = [FakeSnap(1000, device="cuda:0"), FakeSnap(5000, device="cuda:0")]
+    install(monkeypatch, max_slots=6)
+    reqs = requests(snaps, [3, 4, 2, 5, 1, 3])
+    stats, done = serve.Server(snaps, max_slots=6, solo_cells=4000).run(reqs, realtime=False)
+    assert {r.rid: r.result["it"] for r in done} == {r.rid: r.nsteps for r in reqs}
+    assert len(made) == 1 and len(snaps[1].made) >= 2
+    assert all(s.stream is made[0] for s in snaps[1].made)
+    assert all(s.stream is None for s in snaps[0].made)
+    snaps = [FakeSnap(1000, device="cuda:0"), FakeSnap(5000, device="cuda:0")]
+    install(monkeypatch, max_slots=6)
+    serve.Server(snaps, max_slots=6, solo_cells=4000, solo_streams=False).run(requests(snaps, [3, 4]), realtime=False)
+    assert len(made) == 1 and all(s.stream is None for sn in snaps for s in sn.made)
