@@ -299,13 +299,17 @@ class Server:
                         time.sleep(max(0.0, min(pending[0].t_arrive - now, 0.01)))
                     continue
                 if dirty:
-                    if batch is not None:
-                        batch.close()
-                        batch = None
-                    batch_pool = [p for p in pool if not solo(p)]
-                    if batch_pool:
-                        batch = BatchSim([p.sim for p in batch_pool])
-                        self.rebuilds += 1
+                    # the batch holds the smaller instances only: a large one joining or leaving the
+                    # pool rebuilds nothing
+                    small = [p for p in pool if not solo(p)]
+                    if [id(p) for p in small] != [id(p) for p in batch_pool] or (small and batch is None):
+                        if batch is not None:
+                            batch.close()
+                            batch = None
+                        batch_pool = small
+                        if batch_pool:
+                            batch = BatchSim([p.sim for p in batch_pool])
+                            self.rebuilds += 1
                     dirty = False
                 flags = [p.req is not None for p in batch_pool]
                 alone = [p for p in busy if solo(p)]

@@ -208,7 +208,18 @@ def test_instances_of_solo_cells_or_more_step_alone(monkeypatch):
     assert sum(getattr(s, "alone", 0) for s in big) == stats["solo_ticks"] == sum(r.nsteps for r in reqs if r.snap == 1)
     assert sum(getattr(s, "alone", 0) for s in small) == 0
     assert stats["cell_steps"] == sum(r.nsteps * snaps[r.snap].cells for r in reqs)
+    # large instances joining the pool rebuilt no batch: every rebuild changed the batched set
+    sets = [tuple(id(s) for s in b.sims) for b in log["batches"]]
+    assert stats["batch_rebuilds"] == len(sets) == len(set(sets)) <= len(small)
     assert all(s.closed for sn in snaps for s in sn.made) and all(b.closed for b in log["batches"])
+    # large instances built (arrivals 1 ms apart) while a small one keeps stepping in its batch:
+    # the batch is built once
+    snaps = [FakeSnap(1000), FakeSnap(5000)]
+    log = install(monkeypatch, max_slots=3)
+    reqs = requests(snaps, [400, 2, 2, 2, 2, 2], pick=lambda i: 0 if i == 0 else 1)
+    stats, done = serve.Server(snaps, max_slots=3, solo_cells=4000).run(reqs, realtime=True)
+    assert {r.rid: r.result["it"] for r in done} == {r.rid: r.nsteps for r in reqs}
+    assert stats["batch_rebuilds"] == 1 == len(log["batches"]) and len(snaps[1].made) >= 1
     # a pool of large instances only builds no batch at all
     snaps = [FakeSnap(5000)]
     log = install(monkeypatch)
