@@ -15,8 +15,8 @@ room.  A server may also build a warm pool before traffic starts (run's `warm`: 
 per snapshot, within the budget).  The pooled instances below `solo_cells` cells live in one
 BatchSim (persistent kernels, CUDA graphs): a request joins the stepping set when it is admitted
 and leaves it when it has run its steps, through the batch's slot flags, so admissions and
-retirements rebuild nothing; the batch and its graphs are rebuilt only when the pool itself
-changes.  An instance of `solo_cells` cells or more fills the GPU on its own, where the batched
+retirements rebuild nothing; the batch and its graphs are rebuilt only when the set of small
+instances in the pool changes.  An instance of `solo_cells` cells or more fills the GPU on its own, where the batched
 kernels would only add their per-cell cost (the instance records they index, the work-list
 walk), so it is stepped through its own Sim.step in the same tick.  The large instances share a
 CUDA stream apart from the batch's: the batch and the large instances are launched together and
